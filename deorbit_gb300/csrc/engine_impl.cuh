@@ -1,0 +1,1363 @@
+// engine_impl.cuh -- host orchestration of the SPH engine, templated on the
+// arithmetic type R of per-particle fields and pair interactions.
+// Instantiated for double (plain form) and float (mixed form).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "engine_kernels.cuh"
+#include "scan_sort.cuh"
+
+namespace dsph {
+
+#define DSPH_CUDA(x)                                                                    \
+    do {                                                                                \
+        cudaError_t e_ = (x);                                                           \
+        if (e_ != cudaSuccess)                                                          \
+            throw SphError(SPH_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ----------------------------------------------------------------- aux kernels
+template <class T>
+static __global__ void k_read_col(const T* col, const int32_t* pos_of_gid, int64_t gid_base, int64_t n,
+                           double* out) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    out[l] = (double)col[pos_of_gid[gid_base + l]];
+}
+template <class T>
+static __global__ void k_write_col(T* col, const int32_t* pos_of_gid, int64_t gid_base, int64_t n,
+                            const double* in) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    col[pos_of_gid[gid_base + l]] = (T)in[l];
+}
+static __global__ void k_read_u8(const uint8_t* col, const int32_t* pos_of_gid, int64_t gid_base,
+                          int64_t n, uint8_t* out) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    out[l] = col[pos_of_gid[gid_base + l]];
+}
+static __global__ void k_write_u8(uint8_t* col, const int32_t* pos_of_gid, int64_t gid_base, int64_t n,
+                           const uint8_t* in) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    col[pos_of_gid[gid_base + l]] = in[l];
+}
+
+template <class R>
+static __global__ void k_eos_eval(const MatT<R>* mats, int mat, int64_t n, const double* rho,
+                           const double* u, double* P, double* cs) {
+    int64_t k = gtid();
+    if (k >= n) return;
+    R p, c;
+    eos_P_cs(mats[mat], (R)rho[k], (R)u[k], p, c);
+    P[k] = (double)p;
+    cs[k] = (double)c;
+}
+
+// Reference cell id (linear, sph.hpp:160) of every particle of an impact, in
+// gid order, for the on-device reference cell sort.
+template <class R>
+static __global__ void k_ref_keys(View<R> v, int b, const int32_t* pos_of_gid, int64_t gid_base,
+                           int64_t n, uint32_t* keys, int32_t* counts) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    const ImpactD& I = v.imps[b];
+    int64_t k = pos_of_gid[gid_base + l];
+    unsigned long long rb = v.refbin[k];
+    int64_t c = ((int64_t)(rb & 0x1fffff) * I.nc[1] + (int64_t)((rb >> 21) & 0x1fffff)) * I.nc[2] +
+                (int64_t)((rb >> 42) & 0x1fffff);
+    const int64_t ncell = (int64_t)I.nc[0] * I.nc[1] * I.nc[2];
+    if (c < 0 || c >= ncell) c = ncell;  // stale bins: parked past the last cell
+    keys[l] = (uint32_t)c;
+    atomicAdd(&counts[c], 1);
+}
+
+// Exact neighbour sets (FP64 criteria) for the parity hook.
+template <class R>
+static __global__ void k_debug_nbr(View<R> v, int b, int kind, int32_t* out, int32_t* cnt_out, int cap) {
+    int64_t idx = gtid();
+    const ImpactD& I = v.imps[b];
+    if (idx >= I.n) return;
+    const int64_t k = I.off + idx;
+    const float4 pi = v.pf[k];
+    const uint32_t ci = v.cpk[k];
+    const unsigned long long bi = v.refbin[k];
+    const float m = 4.0f * I.margin + 1e-6f * (pi.w + I.hmax_f);
+    const float Rs = (kind == 0 ? 2.0f * pi.w : pi.w + I.hmax_f) + 2.0f * m;
+    const double hi = (double)v.hh[k];
+    int cnt = 0;
+    traverse(v, I, pi, ci, Rs, [&](int32_t j, float, float, float) {
+        if (!ref_member(bi, v.refbin[j], I)) return;
+        double dx, dy, dz;
+        double r = sep_exact(v, I, k, j, dx, dy, dz);
+        bool take;
+        if (kind == 0) {
+            take = r < 2.0 * hi;
+        } else {
+            double hsum = __dadd_rn(hi, (double)v.hh[j]);
+            take = !(j == (int32_t)k || r >= hsum || r == 0.0);
+        }
+        if (take) {
+            if (cnt < cap) out[idx * (int64_t)cap + cnt] = v.gid[j] - (int32_t)I.gid_base;
+            cnt++;
+        }
+    });
+    cnt_out[idx] = cnt;
+}
+
+// Compensated FP64 conservation sums of one impact, fixed summation order.
+template <class R>
+static __global__ void k_conservation(View<R> v, int b, double* out) {
+    __shared__ double sh[8][256];
+    const ImpactD& I = v.imps[b];
+    double s[8], c[8];
+    for (int q = 0; q < 8; q++) s[q] = c[q] = 0.0;
+    for (int64_t idx = threadIdx.x; idx < I.n; idx += blockDim.x) {
+        int64_t k = I.off + idx;
+        double m = (double)v.mass[k];
+        double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k];
+        double val[7] = {m, 0.5 * m * (vx * vx + vy * vy + vz * vz), m * v.u[k], m * vx, m * vy, m * vz, 0.0};
+        for (int q = 0; q < 6; q++) {
+            double y = val[q] - c[q];
+            double t = s[q] + y;
+            c[q] = (t - s[q]) - y;
+            s[q] = t;
+        }
+    }
+    for (int q = 0; q < 6; q++) sh[q][threadIdx.x] = s[q] - c[q];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int q = 0; q < 6; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 6; q++) out[q] = sh[q][0];
+}
+
+static __global__ void k_impact_reset_omax(ImpactD* imps, int nimp) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nimp) imps[b].omax_bits = 0u;
+}
+
+static __global__ void k_set_mask_dt(ImpactD* imps, int nimp, const int32_t* mask, const double* dt,
+                              const double* t_end) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nimp) return;
+    imps[b].mask = mask[b];
+    if (dt) imps[b].dt = dt[b];
+    if (t_end) imps[b].t_end = t_end[b];
+}
+
+// ----------------------------------------------------------------- engine
+template <class R>
+class Engine final : public EngineBase {
+public:
+    static constexpr int kNR = 24;   // carried R columns
+    static constexpr int kND = 4;    // carried FP64 columns
+    static constexpr int kNDer = 19; // derived R columns
+    enum { RC_VX, RC_VY, RC_VZ, RC_AX, RC_AY, RC_AZ, RC_DUDT, RC_MASS, RC_HH, RC_D, RC_EPSACT,
+           RC_H0, RC_S0, RC_DS0 = RC_S0 + 6 };
+    enum { DR_RHO, DR_P, DR_CS, DR_CSIG, DR_PF, DR_DSCALE, DR_RART, DR_SIGMAX, DR_EPSW, DR_PFR2,
+           DR_DSR2, DR_VOL, DR_DUDTN, DR_DSN0 };
+
+    struct ImpactH {
+        sph_params prm{};
+        double dlo[3]{}, dhi[3]{};
+        int32_t per[3]{};
+        bool used = false, alive = false, committed = false, initialized = false;
+        int64_t n = 0, gid_base = 0;
+        std::vector<double> sx, sy, sz, svx, svy, svz, smass, su, seps, sh0;
+        std::vector<int32_t> smat;
+        std::vector<uint8_t> sfixed;
+        std::vector<int32_t> mat_host;
+        bool use_h0 = false;
+        double h0max = 0;
+        bool multi = false;
+        std::vector<int64_t> flaw_ptr;
+        std::vector<double> flaw_eps;
+        double t = 0, dt_last = 0;
+        int64_t steps = 0;
+    };
+
+    explicit Engine(int device) : dev_(device) {
+        DSPH_CUDA(cudaSetDevice(dev_));
+        DSPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
+        DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
+        DSPH_CUDA(cudaMallocHost(&flags_h_, sizeof(int32_t) * 4));
+        DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t) * 4, st_));
+        for (int i = 0; i < 6; i++) DSPH_CUDA(cudaEventCreate(&ev_[i]));
+        for (int i = 0; i < 5; i++) phase_ms_[i] = 0;
+    }
+
+    ~Engine() override {
+        cudaSetDevice(dev_);
+        cudaStreamSynchronize(st_);
+        for (void* p : allocs_) cudaFree(p);
+        cudaFree(mats_d_);
+        cudaFree(flags_d_);
+        cudaFreeHost(flags_h_);
+        for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
+        cudaStreamDestroy(st_);
+    }
+
+    int precision() const override { return sizeof(R) == 8 ? SPH_FP64 : SPH_MIXED; }
+
+    // ------------------------------------------------------------- materials
+    int add_material(const sph_material& m) override {
+        if ((int)mats_h_.size() >= kMaxMaterials) throw SphError(SPH_ERR_CAPACITY, "too many materials");
+        mats_h_.push_back(m);
+        upload_materials();
+        return (int)mats_h_.size() - 1;
+    }
+
+    // ------------------------------------------------------------- impacts
+    int impact_create(const sph_params& p, const double dlo[3], const double dhi[3],
+                      const int32_t per[3]) override {
+        int slot = -1;
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (!imp_[b].used) { slot = (int)b; break; }
+        if (slot < 0) {
+            if (imp_.size() >= 65535) throw SphError(SPH_ERR_CAPACITY, "too many impacts");
+            imp_.emplace_back();
+            slot = (int)imp_.size() - 1;
+        }
+        ImpactH& h = imp_[slot];
+        h = ImpactH();
+        h.used = true;
+        h.alive = true;
+        h.prm = p;
+        for (int a = 0; a < 3; a++) {
+            h.dlo[a] = dlo ? dlo[a] : 0.0;
+            h.dhi[a] = dhi ? dhi[a] : 0.0;
+            h.per[a] = per ? (per[a] != 0) : 0;
+        }
+        return slot;
+    }
+
+    ImpactH& imp(int b) {
+        if (b < 0 || b >= (int)imp_.size() || !imp_[b].used) throw SphError(SPH_ERR_ARG, "bad impact id");
+        return imp_[b];
+    }
+
+    void impact_set_domain(int b, const double dlo[3], const double dhi[3], const int32_t per[3]) override {
+        ImpactH& h = imp(b);
+        if (h.committed) throw SphError(SPH_ERR_STATE, "domain is fixed once particles are on the device");
+        for (int a = 0; a < 3; a++) { h.dlo[a] = dlo[a]; h.dhi[a] = dhi[a]; h.per[a] = per ? (per[a] != 0) : 0; }
+    }
+
+    void impact_set_params(int b, const sph_params& p) override {
+        ImpactH& h = imp(b);
+        h.prm = p;
+        if (h.committed) {
+            pull_table();
+            fill_params(tab_[b], h);
+            push_table();
+        }
+    }
+    sph_params impact_get_params(int b) override { return imp(b).prm; }
+
+    void impact_add_particles(int b, int64_t n, const double* x, const double* y, const double* z,
+                              const double* vx, const double* vy, const double* vz,
+                              const double* mass, const double* u, const int32_t* mat,
+                              const uint8_t* fixed) override {
+        ImpactH& h = imp(b);
+        if (h.committed) throw SphError(SPH_ERR_STATE, "particles can only be added before init");
+        if (n < 0 || (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !mass || !u)))
+            throw SphError(SPH_ERR_ARG, "null particle array");
+        for (int64_t i = 0; i < n; i++) {
+            int32_t m = mat ? mat[i] : 0;
+            if (m < 0 || m >= (int)mats_h_.size()) throw SphError(SPH_ERR_ARG, "material id out of range");
+        }
+        auto app = [n](std::vector<double>& v, const double* s) { v.insert(v.end(), s, s + n); };
+        app(h.sx, x); app(h.sy, y); app(h.sz, z);
+        app(h.svx, vx); app(h.svy, vy); app(h.svz, vz);
+        app(h.smass, mass); app(h.su, u);
+        for (int64_t i = 0; i < n; i++) {
+            h.smat.push_back(mat ? mat[i] : 0);
+            h.sfixed.push_back(fixed ? (fixed[i] ? 1 : 0) : 0);
+            h.seps.push_back(1e30);
+            h.sh0.push_back(h.prm.h_init);
+        }
+        h.mat_host.insert(h.mat_host.end(), h.smat.end() - n, h.smat.end());
+        h.n += n;
+    }
+
+    void impact_seed_damage(int b, double dx, uint32_t seed) override {
+        ImpactH& h = imp(b);
+        std::vector<double> eps(h.n);
+        seed_single_flaws(h.n, h.mat_host.data(), mats_h_.data(), (int)mats_h_.size(), dx, seed, eps.data());
+        if (!h.committed) h.seps = eps;
+        else write_field(b, "eps_act", eps.data());
+    }
+
+    int64_t impact_seed_flaws_multi(int b, double dx, uint32_t seed) override {
+        ImpactH& h = imp(b);
+        std::vector<double> eps(h.n);
+        h.flaw_ptr.assign(h.n + 1, 0);
+        double* fe = nullptr;
+        int64_t nf = seed_multi_flaws(h.n, h.mat_host.data(), mats_h_.data(), (int)mats_h_.size(), dx,
+                                      seed, h.flaw_ptr.data(), &fe, eps.data());
+        h.flaw_eps.assign(fe, fe + nf);
+        free(fe);
+        h.multi = true;
+        h.prm.flaw_model = SPH_FLAWS_MULTI;
+        if (!h.committed) {
+            h.seps = eps;
+        } else {
+            write_field(b, "eps_act", eps.data());
+            pull_table();
+            fill_params(tab_[b], h);
+            push_table();
+            upload_flaws();
+        }
+        return nf;
+    }
+
+    void impact_set_h0(int b, const double* h0) override {
+        ImpactH& h = imp(b);
+        h.use_h0 = true;
+        h.h0max = 0;
+        for (int64_t i = 0; i < h.n; i++) h.h0max = std::max(h.h0max, h0[i]);
+        if (!h.committed) {
+            h.sh0.assign(h0, h0 + h.n);
+        } else {
+            write_field(b, "h0", h0);
+            pull_table();
+            fill_params(tab_[b], h);
+            push_table();
+        }
+    }
+
+    void impact_set_time(int b, double t) override {
+        ImpactH& h = imp(b);
+        h.t = t;
+        if (h.committed) {
+            pull_table();
+            tab_[b].t = t;
+            push_table();
+        }
+    }
+
+    void impact_remove(int b) override {
+        ImpactH& h = imp(b);
+        bool was_committed = h.committed;
+        h.alive = false;
+        if (was_committed) {
+            pull_table();
+            tab_[b].alive = 0;
+            tab_[b].mask = 0;
+            push_table();
+            sort_reorder(true);  // purge its particles before the slot can be reused
+            release_gids(h.gid_base, h.n);
+        }
+        h = ImpactH();
+        if (was_committed) {
+            assign_cell_bases();
+            push_table();
+            if (any_multi()) upload_flaws();
+        }
+    }
+
+    int impact_count() override {
+        int c = 0;
+        for (auto& h : imp_) c += h.used ? 1 : 0;
+        return c;
+    }
+
+    sph_impact_info impact_info(int b) override {
+        ImpactH& h = imp(b);
+        sph_impact_info inf{};
+        inf.n = h.n;
+        inf.steps = h.steps;
+        inf.t = h.t;
+        inf.dt = h.dt_last;
+        inf.initialized = h.initialized ? 1 : 0;
+        if (h.committed) {
+            pull_table();
+            const ImpactD& I = tab_[b];
+            inf.h_max = I.h_max;
+            inf.t = I.t;
+            for (int a = 0; a < 3; a++) { inf.nc[a] = I.nc[a]; inf.cw[a] = I.cw[a]; }
+            inf.density_rounds = I.rounds;
+        }
+        return inf;
+    }
+
+    void get_domain(int b, double dlo[3], double dhi[3], int32_t per[3]) override {
+        ImpactH& h = imp(b);
+        for (int a = 0; a < 3; a++) { dlo[a] = h.dlo[a]; dhi[a] = h.dhi[a]; per[a] = h.per[a]; }
+    }
+
+    int64_t impact_n(int b) override { return imp(b).n; }
+
+    // ------------------------------------------------------------- stepping
+    void init() override {
+        commit();
+        std::vector<int32_t> mask(imp_.size(), 0);
+        bool any = false;
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (imp_[b].used && imp_[b].alive && imp_[b].committed && !imp_[b].initialized) {
+                mask[b] = 1;
+                any = true;
+            }
+        if (!any) return;
+        set_masks(mask, nullptr, nullptr);
+        sort_reorder(true);
+        density_rounds(2, true);
+        forces(true);
+        launch_n(k_adopt_derivatives<R>, N_);
+        dt_reduce();
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (mask[b]) imp_[b].initialized = true;
+        check_async();
+    }
+
+    double timestep(int b) override {
+        ImpactH& h = imp(b);
+        if (!h.committed) throw SphError(SPH_ERR_STATE, "impact has no device state yet (call sph_init)");
+        pull_table();
+        return bitsd_host(tab_[b].dt_bits);
+    }
+
+    void step(double dt) override {
+        commit();
+        std::vector<int32_t> mask(imp_.size(), 0);
+        std::vector<double> dts(imp_.size(), dt);
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (imp_[b].used && imp_[b].alive && imp_[b].committed) mask[b] = 1;
+        set_masks(mask, &dts, nullptr);
+        one_step(true);
+        pull_table();
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (mask[b]) {
+                imp_[b].t = tab_[b].t;
+                imp_[b].steps = tab_[b].nsteps;
+                imp_[b].dt_last = dt;
+                imp_[b].initialized = true;
+            }
+        check_async();
+    }
+
+    // One KDK step of the masked impacts (sph.hpp:357-377).  host_sync: the
+    // adaptive-h round loop reads its convergence flag back; otherwise all four
+    // rounds are issued and converged impacts skip them on the device.
+    void one_step(bool host_sync) {
+        const int nimp = (int)imp_.size();
+        if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[0], st_));
+        launch_n(k_kick_drift<R>, N_);
+        sort_reorder(false);
+        if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[1], st_));
+        density_rounds(2, host_sync);
+        if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[2], st_));
+        launch_n(k_eos<R>, N_);
+        if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[3], st_));
+        build_list<kListForce>(true);
+        launch_n(k_force<R>, N_, 128);
+        if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[4], st_));
+        launch_n(k_damage<R>, N_);
+        launch_n(k_finish<R>, N_);
+        dt_reduce();
+        launch_small(k_run_control, nimp, 1);
+        if (profiling_) {
+            DSPH_CUDA(cudaEventRecord(ev_[5], st_));
+            record_phases();
+        }
+    }
+
+    void run(int nsteps, double t_end) override {
+        commit();
+        std::vector<int32_t> mask(imp_.size(), 0);
+        std::vector<double> te(imp_.size(), t_end > 0 ? t_end : 0.0);
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (imp_[b].used && imp_[b].alive && imp_[b].committed && imp_[b].initialized) mask[b] = 1;
+        set_masks(mask, nullptr, &te);
+        const int nimp = (int)imp_.size();
+        for (int s = 0; s < nsteps; s++) {
+            launch_small(k_run_control, nimp, 0);
+            one_step(false);
+        }
+        pull_table();
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (mask[b]) {
+                imp_[b].t = tab_[b].t;
+                imp_[b].steps = tab_[b].nsteps;
+                imp_[b].dt_last = tab_[b].dt;
+            }
+        check_async();
+    }
+
+    void compute_density_h(int iters) override {
+        commit();
+        set_all_masks();
+        sort_reorder(true);
+        density_rounds(iters, true);
+        check_async();
+    }
+
+    void compute_forces() override {
+        commit();
+        set_all_masks();
+        if (!grid_valid_) {
+            sort_reorder(true);
+            final_grid_build();
+        }
+        forces(true);
+        launch_n(k_adopt_derivatives<R>, N_);
+        dt_reduce();
+        check_async();
+    }
+
+    void synchronize() override { DSPH_CUDA(cudaStreamSynchronize(st_)); }
+
+    // ------------------------------------------------------------- fields
+    void read_field(int b, const char* name, double* out) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (h.n == 0) return;
+        ensure_stage(h.n);
+        bool ok = with_column(name, [&](auto* col) {
+            launch_n_raw(k_read_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, stage_d_);
+        });
+        if (!ok) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + name);
+        DSPH_CUDA(cudaMemcpyAsync(out, stage_d_, sizeof(double) * h.n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void write_field(int b, const char* name, const double* in) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (h.n == 0) return;
+        ensure_stage(h.n);
+        DSPH_CUDA(cudaMemcpyAsync(stage_d_, in, sizeof(double) * h.n, cudaMemcpyHostToDevice, st_));
+        bool ok = with_column(name, [&](auto* col) {
+            launch_n_raw(k_write_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, (const double*)stage_d_);
+        });
+        if (!ok) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + name);
+        std::string nm(name);
+        if (nm == "x" || nm == "y" || nm == "z" || nm == "hh") grid_valid_ = false;
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void read_mat(int b, int32_t* out) override {
+        ImpactH& h = imp(b);
+        for (int64_t i = 0; i < h.n; i++) out[i] = h.mat_host[i];
+    }
+
+    void read_fixed(int b, uint8_t* out) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (h.n == 0) return;
+        ensure_stage(h.n);
+        launch_n_raw(k_read_u8, h.n, (const uint8_t*)fixed_[cur_], (const int32_t*)pos_of_gid_, h.gid_base, h.n, (uint8_t*)stage_d_);
+        DSPH_CUDA(cudaMemcpyAsync(out, stage_d_, h.n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void write_fixed(int b, const uint8_t* in) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (h.n == 0) return;
+        ensure_stage(h.n);
+        DSPH_CUDA(cudaMemcpyAsync(stage_d_, in, h.n, cudaMemcpyHostToDevice, st_));
+        launch_n_raw(k_write_u8, h.n, fixed_[cur_], (const int32_t*)pos_of_gid_, h.gid_base, h.n, (const uint8_t*)stage_d_);
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    sph_conservation conservation(int b) override {
+        ImpactH& h = imp(b);
+        commit();
+        sph_conservation c{};
+        if (h.n == 0) return c;
+        ensure_stage(8);
+        if (!grid_valid_) sort_reorder(true);
+        k_conservation<R><<<1, 256, 0, st_>>>(view(), b, stage_d_);
+        launches_++;
+        double out[8];
+        DSPH_CUDA(cudaMemcpyAsync(out, stage_d_, sizeof(double) * 6, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        c.mass = out[0];
+        c.kinetic = out[1];
+        c.internal = out[2];
+        c.energy = out[1] + out[2];
+        c.momentum[0] = out[3];
+        c.momentum[1] = out[4];
+        c.momentum[2] = out[5];
+        return c;
+    }
+
+    void eos_eval(int mat, int64_t n, const double* rho, const double* u, double* P, double* cs) override {
+        if (mat < 0 || mat >= (int)mats_h_.size()) throw SphError(SPH_ERR_ARG, "material id out of range");
+        if (n <= 0) return;
+        ensure_stage(4 * n);
+        double* d = stage_d_;
+        DSPH_CUDA(cudaMemcpyAsync(d, rho, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+        DSPH_CUDA(cudaMemcpyAsync(d + n, u, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+        launch_n_raw(k_eos_eval<R>, n, (const MatT<R>*)mats_d_, mat, n, (const double*)d, (const double*)(d + n), d + 2 * n, d + 3 * n);
+        DSPH_CUDA(cudaMemcpyAsync(P, d + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaMemcpyAsync(cs, d + 3 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    // ------------------------------------------------------------- parity hooks
+    void debug_ref_cells(int b, int32_t nc[3], double cw[3], int32_t* start, int64_t start_len,
+                         int32_t* ids) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (!grid_valid_) {
+            set_all_masks();
+            sort_reorder(true);
+            final_grid_build();
+        }
+        pull_table();
+        const ImpactD& I = tab_[b];
+        int64_t ncell = (int64_t)I.nc[0] * I.nc[1] * I.nc[2];
+        for (int a = 0; a < 3; a++) { nc[a] = I.nc[a]; cw[a] = I.cw[a]; }
+        if (start_len < ncell + 1) throw SphError(SPH_ERR_CAPACITY, "start array too short");
+        int64_t n = h.n;
+        // keys in local-id order -> stable radix sort -> CSR
+        uint32_t* keys = dalloc_tmp<uint32_t>(n + 1);
+        uint32_t* k2 = dalloc_tmp<uint32_t>(n + 1);
+        uint32_t* k3 = dalloc_tmp<uint32_t>(n + 1);
+        int32_t* v2 = dalloc_tmp<int32_t>(n + 1);
+        int32_t* v3 = dalloc_tmp<int32_t>(n + 1);
+        int32_t* cnt = dalloc_tmp<int32_t>(ncell + 2);
+        void* scr = dalloc_tmp<char>(radix_scratch_bytes(std::max(n, ncell + 1)) + scan_scratch_bytes(ncell + 1) + 64);
+        DSPH_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (ncell + 2), st_));
+        if (n > 0) {
+            launch_n_raw(k_ref_keys<R>, n, view(), b, (const int32_t*)pos_of_gid_, h.gid_base, n, keys, cnt);
+            int bits = 1;
+            while ((1ll << bits) <= ncell) bits++;
+            launches_ += radix_sort_pairs(keys, nullptr, k2, v2, k3, v3, n, bits, scr, st_);
+        }
+        launches_ += exclusive_scan_i32(cnt, cnt, ncell + 1, scr, st_);
+        DSPH_CUDA(cudaMemcpyAsync(start, cnt, sizeof(int32_t) * (ncell + 1), cudaMemcpyDeviceToHost, st_));
+        if (n > 0) DSPH_CUDA(cudaMemcpyAsync(ids, v2, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        free_tmp();
+    }
+
+    int64_t debug_neighbors(int b, int kind, int32_t* counts, int32_t* ids, int64_t cap) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (!grid_valid_) {
+            set_all_masks();
+            sort_reorder(true);
+            final_grid_build();
+        }
+        pull_table();
+        const ImpactD& I = tab_[b];
+        int64_t n = I.n;
+        const int pcap = 512;
+        int32_t* out = dalloc_tmp<int32_t>(n * pcap + 1);
+        int32_t* cnt = dalloc_tmp<int32_t>(n + 1);
+        if (n > 0) launch_n_raw(k_debug_nbr<R>, n, view(), b, kind, out, cnt, pcap);
+        std::vector<int32_t> hout((size_t)n * pcap), hcnt(n);
+        if (n > 0) {
+            DSPH_CUDA(cudaMemcpyAsync(hout.data(), out, sizeof(int32_t) * n * pcap, cudaMemcpyDeviceToHost, st_));
+            DSPH_CUDA(cudaMemcpyAsync(hcnt.data(), cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st_));
+        }
+        // local id of each sorted position in this impact
+        std::vector<int32_t> gidv(n);
+        if (n > 0) DSPH_CUDA(cudaMemcpyAsync(gidv.data(), gid_[cur_] + I.off, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        free_tmp();
+        std::vector<int64_t> where(h.n, -1);
+        for (int64_t q = 0; q < n; q++) where[gidv[q] - h.gid_base] = q;
+        int64_t total = 0;
+        for (int64_t l = 0; l < h.n; l++) {
+            int64_t q = where[l];
+            int c = q >= 0 ? hcnt[q] : 0;
+            if (c > pcap) throw SphError(SPH_ERR_CAPACITY, "debug neighbour set larger than 512");
+            counts[l] = c;
+            if (ids && total + c <= cap) {
+                int32_t* dst = ids + total;
+                std::copy(hout.begin() + q * pcap, hout.begin() + q * pcap + c, dst);
+                std::sort(dst, dst + c);
+            }
+            total += c;
+        }
+        if (total > cap && ids) throw SphError(SPH_ERR_CAPACITY, "neighbour id buffer too small");
+        return total;
+    }
+
+    // ------------------------------------------------------------- tuning
+    void set_tuning(int block, double cell_factor) override {
+        if (block > 0) {
+            if (block % 32 != 0 || block > 1024) throw SphError(SPH_ERR_ARG, "block must be a multiple of 32 <= 1024");
+            block_ = block;
+        }
+        if (cell_factor > 0) {
+            bool any_committed = false;
+            for (auto& h : imp_) any_committed |= h.committed;
+            if (any_committed) throw SphError(SPH_ERR_STATE, "cell factor must be set before particles are committed");
+            cell_factor_ = cell_factor;
+        }
+    }
+    int64_t launches() override { return launches_; }
+    void phase_times(double ms[5]) override { for (int i = 0; i < 5; i++) ms[i] = phase_ms_[i]; }
+    void set_profiling(int on) override { profiling_ = on != 0; }
+
+private:
+    // ------------------------------------------------------------- helpers
+    static double bitsd_host(unsigned long long b) {
+        double d;
+        std::memcpy(&d, &b, 8);
+        return d;
+    }
+
+    template <class T>
+    T* dalloc(size_t n) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw SphError(SPH_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        allocs_.push_back(p);
+        return static_cast<T*>(p);
+    }
+    void dfree(void* p) {
+        if (!p) return;
+        auto it = std::find(allocs_.begin(), allocs_.end(), p);
+        if (it != allocs_.end()) allocs_.erase(it);
+        cudaFree(p);
+    }
+    template <class T>
+    T* dalloc_tmp(size_t n) {
+        T* p = dalloc<T>(n);
+        tmp_.push_back(p);
+        return p;
+    }
+    void free_tmp() {
+        for (void* p : tmp_) dfree(p);
+        tmp_.clear();
+    }
+
+    void check_async() {
+        cudaError_t e = cudaPeekAtLastError();
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw SphError(SPH_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+        }
+    }
+
+    template <class Kern, class... Args>
+    void launch_n_raw(Kern k, int64_t n, Args... args) {
+        if (n <= 0) return;
+        int bs = 256;
+        k<<<(unsigned)((n + bs - 1) / bs), bs, 0, st_>>>(args...);
+        launches_++;
+    }
+    template <class Kern>
+    void launch_n(Kern k, int64_t n, int bs = 0) {
+        if (n <= 0) return;
+        if (bs <= 0) bs = 256;
+        k<<<(unsigned)((n + bs - 1) / bs), bs, 0, st_>>>(view());
+        launches_++;
+    }
+    template <class Kern, class... Args>
+    void launch_small(Kern k, int nimp, Args... args) {
+        if (nimp <= 0) return;
+        k<<<(nimp + 127) / 128, 128, 0, st_>>>(tab_d_, nimp, args...);
+        launches_++;
+    }
+
+    void ensure_stage(int64_t n) {
+        if (n <= stage_cap_) return;
+        dfree(stage_d_);
+        stage_cap_ = std::max<int64_t>(n, 1024);
+        stage_d_ = dalloc<double>(stage_cap_);
+    }
+
+    View<R> view() {
+        View<R> v{};
+        v.n = N_;
+        v.stride = nbr_stride_;
+        v.cap = cap_nbr_;
+        v.x = dcol_[cur_][0]; v.y = dcol_[cur_][1]; v.z = dcol_[cur_][2]; v.u = dcol_[cur_][3];
+        R** r = rcol_[cur_];
+        v.vx = r[RC_VX]; v.vy = r[RC_VY]; v.vz = r[RC_VZ];
+        v.ax = r[RC_AX]; v.ay = r[RC_AY]; v.az = r[RC_AZ];
+        v.dudt = r[RC_DUDT]; v.mass = r[RC_MASS]; v.hh = r[RC_HH]; v.D = r[RC_D];
+        v.eps_act = r[RC_EPSACT]; v.h0 = r[RC_H0];
+        for (int c = 0; c < 6; c++) { v.S[c] = r[RC_S0 + c]; v.dS[c] = r[RC_DS0 + c]; }
+        v.mat = mat_[cur_]; v.fixed = fixed_[cur_]; v.imp = impc_[cur_]; v.gid = gid_[cur_];
+        v.rho = der_[DR_RHO]; v.P = der_[DR_P]; v.cs = der_[DR_CS]; v.csig = der_[DR_CSIG];
+        v.Pf = der_[DR_PF]; v.dscale = der_[DR_DSCALE]; v.Rart = der_[DR_RART];
+        v.sigmax = der_[DR_SIGMAX]; v.epsw = der_[DR_EPSW]; v.pfr2 = der_[DR_PFR2];
+        v.dsr2 = der_[DR_DSR2]; v.vol = der_[DR_VOL]; v.dudt_new = der_[DR_DUDTN];
+        for (int c = 0; c < 6; c++) v.dS_new[c] = der_[DR_DSN0 + c];
+        v.pf = pf_; v.cpk = cpk_; v.refbin = refbin_;
+        v.cell_ptr = cell_cnt_;
+        v.nbr = nbr_; v.nbr_cnt = nbr_cnt_;
+        v.flags = flags_d_;
+        v.imps = tab_d_;
+        v.mats = mats_d_;
+        v.flaw_ptr = flaw_ptr_d_;
+        v.flaw_eps = flaw_eps_d_;
+        return v;
+    }
+
+    template <class F>
+    bool with_column(const char* name, F f) {
+        std::string s(name);
+        static const char* dn[] = {"x", "y", "z", "u"};
+        for (int c = 0; c < 4; c++) if (s == dn[c]) { f(dcol_[cur_][c]); return true; }
+        static const char* rn[] = {"vx", "vy", "vz", "ax", "ay", "az", "dudt", "mass", "hh", "D",
+                                   "eps_act", "h0", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
+                                   "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz"};
+        for (int c = 0; c < kNR; c++) if (s == rn[c]) { f(rcol_[cur_][c]); return true; }
+        static const char* en[] = {"rho", "P", "cs", "csig", "Pf", "dscale", "Rart", "sigmax", "eps_work"};
+        for (int c = 0; c < 9; c++) if (s == en[c]) { f(der_[c]); return true; }
+        return false;
+    }
+
+    void upload_materials() {
+        std::vector<MatT<R>> m(kMaxMaterials);
+        std::memset(m.data(), 0, sizeof(MatT<R>) * kMaxMaterials);
+        for (size_t i = 0; i < mats_h_.size(); i++) {
+            const sph_material& s = mats_h_[i];
+            MatT<R>& d = m[i];
+            d.type = s.type; d.yield_model = s.yield_model;
+            d.gamma = (R)s.gamma; d.rho0 = (R)s.rho0; d.a = (R)s.a; d.b = (R)s.b; d.A = (R)s.A; d.B = (R)s.B;
+            d.alpha = (R)s.alpha; d.beta = (R)s.beta; d.u0 = (R)s.u0; d.uiv = (R)s.uiv; d.ucv = (R)s.ucv;
+            d.G = (R)s.G; d.Y = (R)s.Y; d.Emod = (R)s.Emod; d.wm = (R)s.wm; d.wk = (R)s.wk;
+            d.Y0 = (R)s.Y0; d.mu_i = (R)s.mu_i; d.Ylim = (R)s.Ylim; d.Yd0 = (R)s.Yd0; d.mu_d = (R)s.mu_d;
+        }
+        DSPH_CUDA(cudaMemcpyAsync(mats_d_, m.data(), sizeof(MatT<R>) * kMaxMaterials, cudaMemcpyHostToDevice, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    // Impact table: host mirror <-> device (only at configuration changes).
+    void pull_table() {
+        if (tab_.empty() || !tab_d_) return;
+        DSPH_CUDA(cudaMemcpyAsync(tab_.data(), tab_d_, sizeof(ImpactD) * tab_.size(), cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+    void push_table() {
+        if (tab_.empty()) return;
+        if ((int)tab_.size() > tab_cap_) {
+            dfree(tab_d_);
+            tab_cap_ = (int)tab_.size() * 2;
+            tab_d_ = dalloc<ImpactD>(tab_cap_);
+        }
+        DSPH_CUDA(cudaMemcpyAsync(tab_d_, tab_.data(), sizeof(ImpactD) * tab_.size(), cudaMemcpyHostToDevice, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void fill_params(ImpactD& I, const ImpactH& h) {
+        const sph_params& p = h.prm;
+        I.eta = p.eta; I.h_init = p.h_init; I.alpha = p.alpha; I.beta = p.beta; I.eps = p.eps;
+        I.alpha_u = p.alpha_u; I.cfl = p.cfl; I.eps_as = p.eps_as;
+        I.damage_on = p.damage_on != 0;
+        I.multi_flaw = (p.flaw_model == SPH_FLAWS_MULTI && h.multi) ? 1 : 0;
+        I.use_h0 = h.use_h0 ? 1 : 0;
+        double h0m = h.use_h0 ? h.h0max : p.h_init;
+        I.hcap = (float)(2.0 * h0m);
+        // W polynomial at q = 1/eta, for the artificial-stress ratio W(r)/W(dp)
+        double q = 1.0 / p.eta, poly;
+        if (q < 1.0) poly = 1.0 - 1.5 * q * q + 0.75 * q * q * q;
+        else if (q < 2.0) { double t = 2.0 - q; poly = 0.25 * t * t * t; }
+        else poly = 0.0;
+        I.inv_poly_eta = poly > 0 ? 1.0 / poly : 0.0;
+        for (int a = 0; a < 3; a++) {
+            I.dlo[a] = h.dlo[a]; I.dhi[a] = h.dhi[a]; I.per[a] = h.per[a];
+        }
+    }
+
+    // Fine traversal grid of an impact: cells of ~cell_factor * h_init over the
+    // domain (padded on open axes), exact period on periodic axes.
+    void make_fine_grid(ImpactD& I, const ImpactH& h) {
+        double w0 = cell_factor_ * h.prm.h_init;
+        if (!(w0 > 0)) w0 = 1.0;
+        double bblo[3], bbhi[3];
+        for (int a = 0; a < 3; a++) { bblo[a] = 1e300; bbhi[a] = -1e300; }
+        const std::vector<double>* P[3] = {&h.sx, &h.sy, &h.sz};
+        for (int a = 0; a < 3; a++)
+            for (double c : *P[a]) { bblo[a] = std::min(bblo[a], c); bbhi[a] = std::max(bbhi[a], c); }
+        const int lim[3] = {2047, 2047, 1023};
+        int64_t cells = 1;
+        for (int a = 0; a < 3; a++) {
+            double lo = h.dlo[a], ext = h.dhi[a] - h.dlo[a];
+            if (!(ext > 0)) {  // no domain on this axis: cover the particles
+                lo = (bblo[a] <= bbhi[a] ? bblo[a] : 0.0) - 2 * w0;
+                ext = (bblo[a] <= bbhi[a] ? bbhi[a] - bblo[a] : 0.0) + 4 * w0;
+            }
+            if (h.per[a] && h.dhi[a] > h.dlo[a]) {
+                int nf = std::max(1, (int)std::floor(ext / w0));
+                nf = std::min(nf, lim[a]);
+                I.glo[a] = h.dlo[a];
+                I.nf[a] = nf;
+                I.w[a] = ext / nf;
+            } else {
+                double pad = 0.1 * ext + 2 * w0;
+                double span = ext + 2 * pad;
+                int nf = (int)std::ceil(span / w0);
+                double w = w0;
+                if (nf > lim[a]) { nf = lim[a]; w = span / nf; }
+                I.glo[a] = lo - pad;
+                I.nf[a] = std::max(nf, 1);
+                I.w[a] = w;
+            }
+            cells *= I.nf[a];
+        }
+        // keep the empty-cell overhead bounded
+        int64_t budget = std::max<int64_t>(64 * std::max<int64_t>(h.n, 1), 1 << 20);
+        while (cells > budget) {
+            cells = 1;
+            for (int a = 0; a < 3; a++) {
+                if (h.per[a] && h.dhi[a] > h.dlo[a]) {
+                    int nf = std::max(1, I.nf[a] / 2);
+                    I.w[a] = (h.dhi[a] - h.dlo[a]) / nf;
+                    I.nf[a] = nf;
+                } else {
+                    double span = I.nf[a] * I.w[a];
+                    I.w[a] *= 1.26;
+                    I.nf[a] = std::max(1, (int)std::ceil(span / I.w[a]));
+                }
+                cells *= I.nf[a];
+            }
+        }
+        for (int a = 0; a < 3; a++) {
+            I.iw[a] = 1.0 / I.w[a];
+            I.wf[a] = (float)I.w[a];
+            I.Lf[a] = (float)(h.dhi[a] - h.dlo[a]);
+        }
+        I.ncells = cells;
+    }
+
+    void assign_cell_bases() {
+        int64_t base = 0;
+        for (size_t b = 0; b < imp_.size(); b++) {
+            ImpactD& I = tab_[b];
+            if (imp_[b].used && imp_[b].alive && imp_[b].committed) {
+                I.cell_base = base;
+                base += I.ncells;
+            } else {
+                I.cell_base = 0;
+                I.alive = 0;
+                I.mask = 0;
+            }
+        }
+        if (base >= (int64_t)0xfffffff0ll) throw SphError(SPH_ERR_CAPACITY, "too many traversal cells");
+        C_ = base;
+        if (C_ + 1 > Ccap_) {
+            dfree(cell_cnt_);
+            Ccap_ = std::max<int64_t>(C_ + 1, (int64_t)(Ccap_ * 1.5));
+            cell_cnt_ = dalloc<int32_t>(Ccap_);
+        }
+        ensure_scratch();
+    }
+
+    void ensure_scratch() {
+        size_t need = std::max(radix_scratch_bytes(std::max<int64_t>(Gcap_, 1)),
+                               scan_scratch_bytes(std::max<int64_t>(Ccap_, 1))) + 256;
+        if (need > scratch_bytes_) {
+            dfree(scratch_);
+            scratch_bytes_ = need;
+            scratch_ = dalloc<char>(need);
+        }
+    }
+
+    // gid ranges: first fit in a free list
+    int64_t alloc_gids(int64_t n) {
+        for (size_t i = 0; i < free_gids_.size(); i++) {
+            if (free_gids_[i].second >= n) {
+                int64_t base = free_gids_[i].first;
+                free_gids_[i].first += n;
+                free_gids_[i].second -= n;
+                if (free_gids_[i].second == 0) free_gids_.erase(free_gids_.begin() + i);
+                return base;
+            }
+        }
+        int64_t base = G_;
+        G_ += n;
+        return base;
+    }
+    void release_gids(int64_t base, int64_t n) {
+        if (n <= 0) return;
+        free_gids_.push_back({base, n});
+        std::sort(free_gids_.begin(), free_gids_.end());
+        std::vector<std::pair<int64_t, int64_t>> merged;
+        for (auto& r : free_gids_) {
+            if (!merged.empty() && merged.back().first + merged.back().second == r.first)
+                merged.back().second += r.second;
+            else
+                merged.push_back(r);
+        }
+        free_gids_ = merged;
+        // trailing free range shrinks the id space
+        if (!free_gids_.empty() && free_gids_.back().first + free_gids_.back().second == G_) {
+            G_ = free_gids_.back().first;
+            free_gids_.pop_back();
+        }
+    }
+
+    void ensure_gid_capacity(int64_t need) {
+        if (need <= Gcap_) return;
+        int64_t nc = std::max<int64_t>(need, (int64_t)(Gcap_ * 1.5) + 1024);
+        int32_t* npos = dalloc<int32_t>(nc);
+        if (pos_of_gid_ && Gcap_ > 0)
+            DSPH_CUDA(cudaMemcpyAsync(npos, pos_of_gid_, sizeof(int32_t) * Gcap_, cudaMemcpyDeviceToDevice, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        dfree(pos_of_gid_);
+        pos_of_gid_ = npos;
+        for (uint32_t** p : {&keys_by_gid_, &skeys_, &tkeys_}) { dfree(*p); *p = dalloc<uint32_t>(nc); }
+        for (int32_t** p : {&sgid_, &tgid_}) { dfree(*p); *p = dalloc<int32_t>(nc); }
+        Gcap_ = nc;
+        ensure_scratch();
+    }
+
+    void ensure_particle_capacity(int64_t need) {
+        if (need <= cap_) return;
+        int64_t nc = std::max<int64_t>(need, (int64_t)(cap_ * 1.5) + 1024);
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        for (int side = 0; side < 2; side++) {
+            bool keep = side == cur_;
+            auto grow = [&](auto*& p, size_t esz) {
+                using T = std::remove_reference_t<decltype(*p)>;
+                T* q = dalloc<T>(nc);
+                if (keep && p && N_ > 0)
+                    DSPH_CUDA(cudaMemcpyAsync(q, p, esz * N_, cudaMemcpyDeviceToDevice, st_));
+                DSPH_CUDA(cudaStreamSynchronize(st_));
+                dfree(p);
+                p = q;
+            };
+            for (int c = 0; c < kND; c++) grow(dcol_[side][c], sizeof(double));
+            for (int c = 0; c < kNR; c++) grow(rcol_[side][c], sizeof(R));
+            grow(mat_[side], 1);
+            grow(fixed_[side], 1);
+            grow(impc_[side], 2);
+            grow(gid_[side], 4);
+        }
+        for (int c = 0; c < kNDer; c++) { dfree(der_[c]); der_[c] = dalloc<R>(nc); }
+        dfree(pf_); pf_ = dalloc<float4>(nc);
+        dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
+        dfree(refbin_); refbin_ = dalloc<unsigned long long>(nc);
+        dfree(src_); src_ = dalloc<int32_t>(nc);
+        dfree(nbr_cnt_); nbr_cnt_ = dalloc<int32_t>(nc);
+        // derived columns start at zero so reads before the first force pass are defined
+        for (int c = 0; c < kNDer; c++) DSPH_CUDA(cudaMemsetAsync(der_[c], 0, sizeof(R) * nc, st_));
+        cap_ = nc;
+        alloc_lists();
+    }
+
+    void alloc_lists() {
+        dfree(nbr_);
+        nbr_stride_ = cap_;
+        nbr_ = dalloc<int32_t>((size_t)cap_ * cap_nbr_);
+    }
+
+    // Moves staged impacts onto the device.
+    void commit() {
+        bool any = false;
+        for (auto& h : imp_) any |= (h.used && h.alive && !h.committed);
+        if (!any) return;
+        pull_table();
+        if (tab_.size() < imp_.size()) tab_.resize(imp_.size());
+        int64_t add = 0;
+        for (auto& h : imp_) if (h.used && h.alive && !h.committed) add += h.n;
+        ensure_particle_capacity(N_ + add);
+        for (size_t b = 0; b < imp_.size(); b++) {
+            ImpactH& h = imp_[b];
+            if (!(h.used && h.alive && !h.committed)) continue;
+            ImpactD& I = tab_[b];
+            std::memset(&I, 0, sizeof(ImpactD));
+            fill_params(I, h);
+            make_fine_grid(I, h);
+            I.alive = 1;
+            I.t = h.t;
+            I.dt_bits = 0x7ff0000000000000ull;
+            I.nc[0] = I.nc[1] = I.nc[2] = 1;
+            I.cw[0] = I.cw[1] = I.cw[2] = 1;
+            h.gid_base = alloc_gids(h.n);
+            I.gid_base = h.gid_base;
+            ensure_gid_capacity(G_);
+            upload_impact(b, h);
+            h.committed = true;
+            // staging no longer needed except materials (seeding) and flaws
+            h.sx.clear(); h.sy.clear(); h.sz.clear(); h.svx.clear(); h.svy.clear(); h.svz.clear();
+            h.smass.clear(); h.su.clear(); h.seps.clear(); h.sh0.clear(); h.smat.clear(); h.sfixed.clear();
+            h.sx.shrink_to_fit(); h.sy.shrink_to_fit(); h.sz.shrink_to_fit();
+        }
+        assign_cell_bases();
+        push_table();
+        if (any_multi()) upload_flaws();
+        grid_valid_ = false;
+    }
+
+    bool any_multi() {
+        for (auto& h : imp_) if (h.used && h.alive && h.multi) return true;
+        return false;
+    }
+
+    void upload_impact(size_t b, ImpactH& h) {
+        int64_t n = h.n, at = N_;
+        if (n == 0) return;
+        auto up = [&](auto* dst, const auto& src) {
+            using T = std::remove_pointer_t<decltype(dst)>;
+            std::vector<T> tmp(src.begin(), src.end());
+            DSPH_CUDA(cudaMemcpyAsync(dst + at, tmp.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st_));
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+        };
+        int c = cur_;
+        up(dcol_[c][0], h.sx); up(dcol_[c][1], h.sy); up(dcol_[c][2], h.sz); up(dcol_[c][3], h.su);
+        up(rcol_[c][RC_VX], h.svx); up(rcol_[c][RC_VY], h.svy); up(rcol_[c][RC_VZ], h.svz);
+        up(rcol_[c][RC_MASS], h.smass);
+        up(rcol_[c][RC_EPSACT], h.seps);
+        up(rcol_[c][RC_H0], h.sh0);
+        std::vector<double> hinit(n, h.prm.h_init);
+        up(rcol_[c][RC_HH], hinit);
+        for (int col : {RC_AX, RC_AY, RC_AZ, RC_DUDT, RC_D})
+            DSPH_CUDA(cudaMemsetAsync(rcol_[c][col] + at, 0, sizeof(R) * n, st_));
+        for (int q = 0; q < 6; q++) {
+            DSPH_CUDA(cudaMemsetAsync(rcol_[c][RC_S0 + q] + at, 0, sizeof(R) * n, st_));
+            DSPH_CUDA(cudaMemsetAsync(rcol_[c][RC_DS0 + q] + at, 0, sizeof(R) * n, st_));
+        }
+        std::vector<uint8_t> m8(n);
+        for (int64_t i = 0; i < n; i++) m8[i] = (uint8_t)h.smat[i];
+        up(mat_[c], m8);
+        up(fixed_[c], h.sfixed);
+        std::vector<uint16_t> im(n, (uint16_t)b);
+        up(impc_[c], im);
+        std::vector<int32_t> g(n), pos(n);
+        for (int64_t i = 0; i < n; i++) { g[i] = (int32_t)(h.gid_base + i); pos[i] = (int32_t)(at + i); }
+        up(gid_[c], g);
+        DSPH_CUDA(cudaMemcpyAsync(pos_of_gid_ + h.gid_base, pos.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        N_ += n;
+    }
+
+    void upload_flaws() {
+        std::vector<int64_t> ptr(G_ + 1, 0);
+        std::vector<R> eps;
+        // per gid counts
+        std::vector<int64_t> cnt(G_, 0);
+        for (auto& h : imp_) {
+            if (!(h.used && h.alive && h.committed && h.multi)) continue;
+            for (int64_t l = 0; l < h.n; l++) cnt[h.gid_base + l] = h.flaw_ptr[l + 1] - h.flaw_ptr[l];
+        }
+        for (int64_t g = 0; g < G_; g++) ptr[g + 1] = ptr[g] + cnt[g];
+        eps.resize(std::max<int64_t>(ptr[G_], 1));
+        for (auto& h : imp_) {
+            if (!(h.used && h.alive && h.committed && h.multi)) continue;
+            for (int64_t l = 0; l < h.n; l++) {
+                int64_t o = ptr[h.gid_base + l];
+                for (int64_t q = h.flaw_ptr[l]; q < h.flaw_ptr[l + 1]; q++) eps[o++] = (R)h.flaw_eps[q];
+            }
+        }
+        dfree(flaw_ptr_d_);
+        dfree(flaw_eps_d_);
+        flaw_ptr_d_ = dalloc<int64_t>(ptr.size());
+        flaw_eps_d_ = dalloc<R>(eps.size());
+        DSPH_CUDA(cudaMemcpyAsync(flaw_ptr_d_, ptr.data(), sizeof(int64_t) * ptr.size(), cudaMemcpyHostToDevice, st_));
+        DSPH_CUDA(cudaMemcpyAsync(flaw_eps_d_, eps.data(), sizeof(R) * eps.size(), cudaMemcpyHostToDevice, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void set_masks(const std::vector<int32_t>& mask, const std::vector<double>* dt,
+                   const std::vector<double>* t_end) {
+        int nimp = (int)imp_.size();
+        if (nimp == 0) return;
+        size_t bytes = sizeof(int32_t) * nimp + sizeof(double) * 2 * nimp + 64;
+        if (mask_buf_bytes_ < bytes) {
+            dfree(mask_buf_);
+            mask_buf_bytes_ = bytes * 2;
+            mask_buf_ = dalloc<char>(mask_buf_bytes_);
+        }
+        char* p = mask_buf_;
+        int32_t* dm = (int32_t*)p;
+        double* ddt = (double*)(p + ((sizeof(int32_t) * nimp + 15) / 16) * 16);
+        double* dte = ddt + nimp;
+        DSPH_CUDA(cudaMemcpyAsync(dm, mask.data(), sizeof(int32_t) * nimp, cudaMemcpyHostToDevice, st_));
+        if (dt) DSPH_CUDA(cudaMemcpyAsync(ddt, dt->data(), sizeof(double) * nimp, cudaMemcpyHostToDevice, st_));
+        if (t_end) DSPH_CUDA(cudaMemcpyAsync(dte, t_end->data(), sizeof(double) * nimp, cudaMemcpyHostToDevice, st_));
+        launch_small(k_set_mask_dt, nimp, (const int32_t*)dm, dt ? (const double*)ddt : nullptr,
+                     t_end ? (const double*)dte : nullptr);
+        DSPH_CUDA(cudaStreamSynchronize(st_));  // host vectors are temporaries
+    }
+
+    void set_all_masks() {
+        std::vector<int32_t> mask(imp_.size(), 0);
+        for (size_t b = 0; b < imp_.size(); b++)
+            if (imp_[b].used && imp_[b].alive && imp_[b].committed) mask[b] = 1;
+        set_masks(mask, nullptr, nullptr);
+    }
+
+    int key_bits() const {
+        int bits = 1;
+        while ((1ll << bits) <= C_) bits++;
+        return bits;
+    }
+
+    // Cell sort of all resident particles and gather of the carried state.
+    void sort_reorder(bool count_changes) {
+        if (N_ == 0 && !count_changes) return;
+        const int nimp = (int)imp_.size();
+        DSPH_CUDA(cudaMemsetAsync(keys_by_gid_, 0xff, sizeof(uint32_t) * std::max<int64_t>(G_, 1), st_));
+        DSPH_CUDA(cudaMemsetAsync(cell_cnt_, 0, sizeof(int32_t) * (C_ + 1), st_));
+        launch_n_raw(k_fine_keys<R>, N_, view(), keys_by_gid_, cell_cnt_);
+        launches_ += radix_sort_pairs(keys_by_gid_, nullptr, skeys_, sgid_, tkeys_, tgid_, G_,
+                                      key_bits(), scratch_, st_);
+        launches_ += exclusive_scan_i32(cell_cnt_, cell_cnt_, C_ + 1, scratch_, st_);
+        int64_t n_new = N_;
+        if (count_changes) {
+            DSPH_CUDA(cudaMemcpyAsync(flags_h_ + 2, cell_cnt_ + C_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+            n_new = flags_h_[2];
+        }
+        const int alt = cur_ ^ 1;
+        if (n_new > 0) {
+            launch_n_raw(k_make_src, n_new, n_new, (const int32_t*)sgid_, (const int32_t*)pos_of_gid_, src_);
+            GatherCols g{};
+            for (int c = 0; c < kND; c++) { g.din[c] = dcol_[cur_][c]; g.dout[c] = dcol_[alt][c]; }
+            g.nr = kNR;
+            for (int c = 0; c < kNR; c++) { g.rin[c] = rcol_[cur_][c]; g.rout[c] = rcol_[alt][c]; }
+            g.b_in[0] = mat_[cur_]; g.b_out[0] = mat_[alt];
+            g.b_in[1] = fixed_[cur_]; g.b_out[1] = fixed_[alt];
+            g.imp_in = impc_[cur_]; g.imp_out = impc_[alt];
+            g.gid_in = gid_[cur_]; g.gid_out = gid_[alt];
+            launch_n_raw(k_gather<R>, n_new, n_new, (const int32_t*)src_, g);
+        }
+        cur_ = alt;
+        N_ = n_new;
+        launch_small(k_impact_reset_omax, nimp);
+        launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_);
+        launch_small(k_impact_ranges, nimp, (const int32_t*)cell_cnt_);
+        grid_valid_ = true;
+    }
+
+    template <int KIND>
+    void build_list(bool host_check) {
+        for (int attempt = 0; attempt < 8; attempt++) {
+            DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t), st_));
+            launch_n(k_list<R, KIND>, N_, block_);
+            if (!host_check) return;
+            DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+            if (flags_h_[0] <= cap_nbr_) return;
+            cap_nbr_ = (int)(flags_h_[0] * 1.25) + 8;
+            alloc_lists();
+        }
+        throw SphError(SPH_ERR_CAPACITY, "neighbour list capacity could not be satisfied");
+    }
+
+    void hmax_pass(int which) {
+        int64_t n = N_;
+        if (n <= 0) return;
+        k_hmax<R><<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(view(), which);
+        launches_++;
+    }
+
+    void density_rounds(int iters, bool host_sync) {
+        const int nimp = (int)imp_.size();
+        launch_small(k_impact_begin_round, nimp, 2);
+        for (int round = 0; round < 4; round++) {
+            if (round > 0) launch_small(k_impact_begin_round, nimp, 0);
+            hmax_pass(0);
+            launch_small(k_ref_grid, nimp);
+            launch_n(k_ref_bins<R>, N_);
+            for (int it = 0; it < iters; it++) {
+                build_list<kListDensity>(true);
+                launch_n(k_density<R>, N_);
+            }
+            hmax_pass(1);
+            DSPH_CUDA(cudaMemsetAsync(flags_d_ + 1, 0, sizeof(int32_t), st_));
+            launch_small(k_round_check, nimp, flags_d_);
+            if (host_sync) {
+                DSPH_CUDA(cudaMemcpyAsync(flags_h_ + 1, flags_d_ + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+                DSPH_CUDA(cudaStreamSynchronize(st_));
+                if (!flags_h_[1]) break;
+            }
+        }
+        final_grid_build();
+    }
+
+    void final_grid_build() {
+        const int nimp = (int)imp_.size();
+        launch_small(k_impact_begin_round, nimp, 1);
+        hmax_pass(0);
+        launch_small(k_ref_grid, nimp);
+        launch_n(k_ref_bins<R>, N_);
+    }
+
+    void forces(bool host_check) {
+        launch_n(k_eos<R>, N_);
+        build_list<kListForce>(host_check);
+        launch_n(k_force<R>, N_, 128);
+    }
+
+    void dt_reduce() {
+        launch_small(k_dt_begin, (int)imp_.size());
+        launch_n(k_dt<R>, N_);
+    }
+
+    void record_phases() {
+        DSPH_CUDA(cudaEventSynchronize(ev_[5]));
+        for (int i = 0; i < 5; i++) {
+            float ms = 0;
+            DSPH_CUDA(cudaEventElapsedTime(&ms, ev_[i], ev_[i + 1]));
+            phase_ms_[i] = ms;
+        }
+    }
+
+    // ------------------------------------------------------------- members
+    int dev_;
+    cudaStream_t st_{};
+    std::vector<void*> allocs_, tmp_;
+    std::vector<sph_material> mats_h_;
+    MatT<R>* mats_d_ = nullptr;
+    std::vector<ImpactH> imp_;
+    std::vector<ImpactD> tab_;
+    ImpactD* tab_d_ = nullptr;
+    int tab_cap_ = 0;
+    int64_t N_ = 0, cap_ = 0, G_ = 0, Gcap_ = 0, C_ = 0, Ccap_ = 0;
+    std::vector<std::pair<int64_t, int64_t>> free_gids_;
+    int cur_ = 0;
+    double* dcol_[2][kND] = {};
+    R* rcol_[2][kNR] = {};
+    uint8_t* mat_[2] = {};
+    uint8_t* fixed_[2] = {};
+    uint16_t* impc_[2] = {};
+    int32_t* gid_[2] = {};
+    R* der_[kNDer] = {};
+    float4* pf_ = nullptr;
+    uint32_t* cpk_ = nullptr;
+    unsigned long long* refbin_ = nullptr;
+    int32_t* src_ = nullptr;
+    uint32_t *keys_by_gid_ = nullptr, *skeys_ = nullptr, *tkeys_ = nullptr;
+    int32_t *sgid_ = nullptr, *tgid_ = nullptr, *pos_of_gid_ = nullptr;
+    int32_t* cell_cnt_ = nullptr;
+    int32_t* nbr_ = nullptr;
+    int32_t* nbr_cnt_ = nullptr;
+    int64_t nbr_stride_ = 0;
+    int cap_nbr_ = 160;
+    int32_t* flags_d_ = nullptr;
+    int32_t* flags_h_ = nullptr;
+    void* scratch_ = nullptr;
+    size_t scratch_bytes_ = 0;
+    double* stage_d_ = nullptr;
+    int64_t stage_cap_ = 0;
+    char* mask_buf_ = nullptr;
+    size_t mask_buf_bytes_ = 0;
+    int64_t* flaw_ptr_d_ = nullptr;
+    R* flaw_eps_d_ = nullptr;
+    int block_ = 128;
+    double cell_factor_ = 1.0;
+    int64_t launches_ = 0;
+    bool profiling_ = false;
+    cudaEvent_t ev_[6]{};
+    double phase_ms_[5];
+    bool grid_valid_ = false;
+};
+
+}  // namespace dsph

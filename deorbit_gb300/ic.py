@@ -1,0 +1,313 @@
+"""Seeded synthetic initial conditions for the impact workloads.
+
+Every workload is a `Scenario`: particle arrays in the reference's IC layout
+(x y z vx vy vz mass u mat fixed, run_ic.cpp:4-6), a domain, the System
+parameters (sph.hpp:86-92) and a material list.  The same Scenario feeds the
+CUDA solver and the CPU oracle, so both see bit-identical inputs.
+
+Workloads (sizes as named; all from numpy's seeded PCG64 generator):
+  impact_halfspace  granite half-space lattice + iron sphere, hydro only
+                    (48x48x24 + r = 8 dx sphere, 45 deg, 8 km/s, CFL 0.3)
+  grazing           iron sphere of 1 km into a granite slab at a shallow angle,
+                    strength (von Mises iron, Collins granite) + multi-flaw
+                    damage; total particle count chosen exactly
+  sheared_cube      the reference oracle-dump scenario (cpu_dump.cpp:12-40):
+                    sheared, compressed basalt cube with an iron core, frac on
+  batch             many independent impacts with log-uniform sizes
+Materials: granite = the Tillotson set named for these workloads; its shear
+modulus (24 GPa), Collins parameters (Y0 10 MPa, mu_i 1.5, Ylim 3.5 GPa, mu_d
+0.6) and Weibull constants (m 9, k 4e35 m^-3) are this build's choices, as is
+using the reference iron set (eos.hpp:42-43) for the impactor.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+MAT_FIELDS = "type yield_model gamma rho0 a b A B alpha beta u0 uiv ucv G Y Emod wm wk Y0 mu_i Ylim Yd0 mu_d".split()
+
+
+def tillotson(rho0, A, B, a, b, alpha, beta, u0, uiv, ucv, G=0.0, Y=0.0, wm=0.0, wk=0.0, **ext):
+    """Material dict with the fields of eos.hpp:15-27 (Emod = 9AG/(3A+G), eos.hpp:37)."""
+    m = dict(type=1, yield_model=0, gamma=1.4, rho0=rho0, a=a, b=b, A=A, B=B, alpha=alpha, beta=beta,
+             u0=u0, uiv=uiv, ucv=ucv, G=G, Y=Y, Emod=(9.0 * A * G / (3.0 * A + G) if G > 0 else 0.0),
+             wm=wm, wk=wk, Y0=0.0, mu_i=0.0, Ylim=0.0, Yd0=0.0, mu_d=0.0)
+    m.update(ext)
+    return m
+
+
+def iron(strength=True):
+    """Reference iron set (eos.hpp:42-43); strength=False drops G and Y (hydro only)."""
+    return tillotson(7800, 1.28e11, 1.05e11, 0.5, 1.5, 5, 5, 9.5e6, 2.4e6, 8.67e6,
+                     *((7.75e10, 1.0e9) if strength else (0.0, 0.0)))
+
+
+def basalt():
+    return tillotson(2700, 2.67e10, 2.67e10, 0.5, 1.5, 5, 5, 4.87e8, 4.72e6, 1.82e7, 2.27e10, 3.5e8, 16.0, 1.0e61)
+
+
+def granite(strength=True):
+    """Granite Tillotson set (rho0 2680, A = B = 18 GPa, E0 16, Eiv 3.5, Ecv 18 MJ/kg,
+    a 0.5, b 1.3, alpha = beta = 5) with this build's strength / flaw constants."""
+    if not strength:
+        return tillotson(2680, 1.8e10, 1.8e10, 0.5, 1.3, 5, 5, 1.6e7, 3.5e6, 1.8e7)
+    return tillotson(2680, 1.8e10, 1.8e10, 0.5, 1.3, 5, 5, 1.6e7, 3.5e6, 1.8e7,
+                     G=2.4e10, Y=3.5e9, wm=9.0, wk=4.0e35,
+                     yield_model=1, Y0=1.0e7, mu_i=1.5, Ylim=3.5e9, Yd0=0.0, mu_d=0.6)
+
+
+@dataclasses.dataclass
+class Scenario:
+    name: str
+    pos: np.ndarray
+    vel: np.ndarray
+    mass: np.ndarray
+    u: np.ndarray
+    mat: np.ndarray
+    fixed: np.ndarray
+    lo: np.ndarray
+    hi: np.ndarray
+    periodic: np.ndarray
+    params: dict
+    materials: list
+    dx: float
+    flaws: tuple | None = None      # ("single" | "multi", seed)
+    h0: np.ndarray | None = None
+
+    @property
+    def n(self):
+        return int(self.pos.shape[0])
+
+
+def lattice(nx, ny, nz, dx, origin=(0.0, 0.0, 0.0)):
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    p = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float64)
+    return np.asarray(origin, float) + (p + 0.5) * dx
+
+
+def sphere(R, dx, center):
+    m = int(math.ceil(R / dx)) + 1
+    g = (np.arange(-m, m) + 0.5) * dx
+    i, j, k = np.meshgrid(g, g, g, indexing="ij")
+    p = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1)
+    p = p[(p * p).sum(1) < R * R]
+    return p + np.asarray(center, float)
+
+
+def _jitter(p, dx, frac, rng):
+    return p + rng.uniform(-frac * dx, frac * dx, size=p.shape)
+
+
+def impact_halfspace(nx=48, ny=48, nz=24, dx=10.0, r_cells=8.0, angle_deg=45.0, speed=8000.0,
+                     jitter=0.01, cfl=0.3, seed=20261203):
+    """Hydro-only iron sphere into a granite half-space (FP64 plain workload)."""
+    rng = np.random.default_rng(seed)
+    tgt = _jitter(lattice(nx, ny, nz, dx, (0.0, 0.0, -nz * dx)), dx, jitter, rng)
+    R = r_cells * dx
+    th = math.radians(angle_deg)
+    cx = 0.5 * nx * dx - (R + dx) / math.tan(th) if angle_deg < 89 else 0.5 * nx * dx
+    imp = _jitter(sphere(R, dx, (cx, 0.5 * ny * dx, R + dx)), dx, jitter, rng)
+    pos = np.concatenate([tgt, imp])
+    n_t = tgt.shape[0]
+    vel = np.zeros_like(pos)
+    vel[n_t:, 0] = speed * math.cos(th)
+    vel[n_t:, 2] = -speed * math.sin(th)
+    mat = np.r_[np.zeros(n_t, np.int32), np.ones(imp.shape[0], np.int32)]
+    mats = [granite(strength=False), iron(strength=False)]
+    mass = np.where(mat == 1, mats[1]["rho0"], mats[0]["rho0"]) * dx ** 3
+    L = np.array([nx, ny, nz]) * dx
+    lo = np.array([-0.25 * L[0], -0.25 * L[1], -L[2] - 0.25 * L[2]])
+    hi = np.array([1.25 * L[0], 1.25 * L[1], 0.75 * L[2]])
+    return Scenario("impact_halfspace", pos, vel, mass, np.zeros(pos.shape[0]), mat,
+                    np.zeros(pos.shape[0], np.uint8), lo, hi, np.zeros(3, np.int32),
+                    dict(eta=1.3, h_init=1.3 * dx, alpha=1.0, beta=2.0, eps=0.01, cfl=cfl,
+                         eps_as=0.0, damage_on=0), mats, dx)
+
+
+def grazing(n_total=1 << 20, radius=500.0, dx=None, angle_deg=3.0, speed=8000.0, jitter=0.01,
+            aspect=(8.0, 4.0, 1.0), seed=20261203, flaws="multi", eps_as=0.3, cfl=0.2):
+    """Strength + damage grazing impact: iron sphere (von Mises, 1 GPa) into a
+    granite slab (Collins yield, multi-flaw Weibull), exactly n_total particles."""
+    rng = np.random.default_rng(seed)
+    if dx is None:  # slab of aspect ax:ay:az (in sphere diameters) holding n_total
+        vol = (n_total * 1.0) / 1.0
+        D = 2 * radius
+        ax, ay, az = aspect
+        dx = (ax * ay * az * D ** 3 / vol) ** (1.0 / 3.0)
+    R = radius
+    imp = sphere(R, dx, (0.0, 0.0, 0.0))
+    n_imp = imp.shape[0]
+    n_slab = n_total - n_imp
+    ax, ay, az = aspect
+    D = 2 * R
+    nz = max(2, int(round(az * D / dx)))
+    ny = max(2, int(round(ay * D / dx)))
+    nx = int(math.ceil(n_slab / (ny * nz)))
+    slab = lattice(nx, ny, nz, dx, (0.0, -0.5 * ny * dx, -nz * dx))
+    # drop surplus particles from the bottom of the far end (away from the track)
+    order = np.lexsort((slab[:, 2], -slab[:, 0]))  # far x first, bottom first
+    keep = np.ones(slab.shape[0], bool)
+    keep[order[: slab.shape[0] - n_slab]] = False
+    slab = slab[keep]
+    th = math.radians(angle_deg)
+    x0 = 0.15 * nx * dx
+    cen = np.array([x0, 0.0, R + dx])
+    imp = imp + cen
+    slab = _jitter(slab, dx, jitter, rng)
+    imp = _jitter(imp, dx, jitter, rng)
+    pos = np.concatenate([slab, imp])
+    vel = np.zeros_like(pos)
+    vel[n_slab:, 0] = speed * math.cos(th)
+    vel[n_slab:, 2] = -speed * math.sin(th)
+    mat = np.r_[np.zeros(n_slab, np.int32), np.ones(n_imp, np.int32)]
+    mats = [granite(strength=True), iron(strength=True)]
+    mass = np.where(mat == 1, mats[1]["rho0"], mats[0]["rho0"]) * dx ** 3
+    Lx, Ly, Lz = nx * dx, ny * dx, nz * dx
+    lo = np.array([-0.1 * Lx - 2 * R, -0.5 * Ly - 0.5 * Ly, -Lz - 0.5 * Lz])
+    hi = np.array([1.1 * Lx, 0.5 * Ly + 0.5 * Ly, 4 * R + 0.5 * Lz])
+    return Scenario("grazing", pos, vel, mass, np.zeros(pos.shape[0]), mat,
+                    np.zeros(pos.shape[0], np.uint8), lo, hi, np.zeros(3, np.int32),
+                    dict(eta=1.3, h_init=1.3 * dx, alpha=1.0, beta=2.0, eps=0.01, cfl=cfl,
+                         eps_as=eps_as, damage_on=1, flaw_model=1 if flaws == "multi" else 0),
+                    mats, dx, flaws=(flaws, 12345))
+
+
+def sheared_cube(L=22, dx=30.0):
+    """The reference's oracle-dump state builder (cpu_dump.cpp:12-31)."""
+    lo = -L * dx / 2.0
+    hi = L * dx / 2.0
+    p = lattice(L, L, L, dx, (lo, lo, lo))
+    x, y, z = p[:, 0], p[:, 1], p[:, 2]
+    R = 5.0 * dx
+    ir = (x * x + y * y + z * z) < R * R
+    vel = np.stack([80.0 * (y / hi), np.zeros_like(x), -40.0 * (z / hi)], axis=1)
+    u = 2.0e5 * (1.0 + x / hi)
+    mats = [basalt(), iron()]
+    mass = np.where(ir, 7800.0, 2700.0) * dx ** 3
+    return Scenario("sheared_cube", p, vel, mass, u, ir.astype(np.int32), np.zeros(p.shape[0], np.uint8),
+                    np.full(3, lo - dx), np.full(3, hi + dx), np.zeros(3, np.int32),
+                    dict(eta=1.3, h_init=1.3 * dx, eps_as=0.3, damage_on=1), mats, dx, flaws=("single", 12345))
+
+
+def periodic_bar(nx=24, ny=6, dx=0.01, seed=7):
+    """Basalt bar, periodic in y and z, Gaussian velocity pulse, frozen ends
+    (the wave-speed gate's geometry, strength_test.cpp:95-110, scaled down)."""
+    x0, x1, Lyz = -nx * dx / 2, nx * dx / 2, ny * dx
+    p = lattice(nx, ny, ny, dx, (x0, 0.0, 0.0))
+    rng = np.random.default_rng(seed)
+    p = _jitter(p, dx, 0.05, rng)
+    vel = np.zeros_like(p)
+    vel[:, 0] = np.exp(-(p[:, 0] ** 2) / (0.06 * nx * dx / 1.2) ** 2)
+    fixed = (np.abs(p[:, 0]) > 0.45 * nx * dx).astype(np.uint8)
+    mats = [basalt()]
+    mass = np.full(p.shape[0], mats[0]["rho0"] * dx ** 3)
+    return Scenario("periodic_bar", p, vel, mass, np.zeros(p.shape[0]), np.zeros(p.shape[0], np.int32), fixed,
+                    np.array([x0, 0.0, 0.0]), np.array([x1, Lyz, Lyz]), np.array([0, 1, 1], np.int32),
+                    dict(eta=1.3, h_init=1.3 * dx), mats, dx)
+
+
+def batch_sizes(count=256, lo=5000, hi=80000, seed=20261203):
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
+
+
+def sized_impact(n_target, seed, angle_deg, speed, ratio, strength=True, flaws="multi", jitter=0.01):
+    """One impact of roughly n_target particles: iron sphere of radius ratio x
+    the slab half-depth into a granite slab (batched / served workloads)."""
+    rng = np.random.default_rng(seed)
+    # slab 4:2:1 in units of its depth T with lattice dx; sphere radius ratio * T
+    frac_sphere = (4.0 / 3.0) * math.pi * ratio ** 3 / 8.0
+    dx_cells = (n_target / (8.0 * (1.0 + frac_sphere))) ** (1.0 / 3.0)  # cells per depth
+    nz = max(4, int(round(dx_cells)))
+    dx = 1.0
+    nx, ny = 4 * nz, 2 * nz
+    slab = _jitter(lattice(nx, ny, nz, dx, (0.0, -0.5 * ny * dx, -nz * dx)), dx, jitter, rng)
+    R = max(2.0, ratio * nz) * dx
+    th = math.radians(angle_deg)
+    imp = _jitter(sphere(R, dx, (0.2 * nx * dx, 0.0, R + dx)), dx, jitter, rng)
+    pos = np.concatenate([slab, imp])
+    vel = np.zeros_like(pos)
+    vel[slab.shape[0]:, 0] = speed * math.cos(th)
+    vel[slab.shape[0]:, 2] = -speed * math.sin(th)
+    mat = np.r_[np.zeros(slab.shape[0], np.int32), np.ones(imp.shape[0], np.int32)]
+    mats = [granite(strength), iron(strength)]
+    mass = np.where(mat == 1, mats[1]["rho0"], mats[0]["rho0"]) * dx ** 3
+    L = np.array([nx, ny, nz]) * dx
+    lo = np.array([-0.2 * L[0], -L[1], -1.5 * L[2]])
+    hi = np.array([1.2 * L[0], L[1], 1.5 * L[2] + 2 * R])
+    prm = dict(eta=1.3, h_init=1.3 * dx, alpha=1.0, beta=2.0, eps=0.01, cfl=0.2,
+               eps_as=0.3 if strength else 0.0, damage_on=1 if strength else 0,
+               flaw_model=1 if (strength and flaws == "multi") else 0)
+    return Scenario(f"impact_{n_target}", pos, vel, mass, np.zeros(pos.shape[0]), mat,
+                    np.zeros(pos.shape[0], np.uint8), lo, hi, np.zeros(3, np.int32), prm, mats, dx,
+                    flaws=(flaws, int(seed) & 0xffffffff) if strength else None)
+
+
+# ------------------------------------------------------------ loaders
+def _material_struct(cls, d):
+    m = cls()
+    for k in MAT_FIELDS:
+        setattr(m, k, int(d[k]) if k in ("type", "yield_model") else float(d[k]))
+    return m
+
+
+def to_context(ctx, sc: Scenario, prm_overrides=None):
+    """Create one impact of `sc` in a deorbit_gb300.sph.Context; returns its id.
+    Material ids of the scenario are offset by the materials already present."""
+    from . import sph
+
+    base = None
+    for d in sc.materials:
+        i = ctx.add_material(_material_struct(sph.Material, d))
+        base = i if base is None else base
+    base = 0 if base is None else base
+    p = dict(sc.params)
+    if prm_overrides:
+        p.update(prm_overrides)
+    b = ctx.impact_create(sph.params(**p), sc.lo, sc.hi, sc.periodic)
+    ctx.add_particles(b, sc.pos, sc.vel, sc.mass, sc.u, sc.mat + base, sc.fixed)
+    if sc.flaws is not None:
+        kind, seed = sc.flaws
+        if kind == "multi":
+            ctx.seed_flaws_multi(b, sc.dx, seed)
+        else:
+            ctx.seed_damage(b, sc.dx, seed)
+    if sc.h0 is not None:
+        ctx.set_h0(b, sc.h0)
+    return b
+
+
+def to_oracle(sc: Scenario, threads=0):
+    """The same scenario in the CPU oracle (test infrastructure)."""
+    from oracle import oracle as O
+
+    S = O.OracleSystem()
+    if threads:
+        S.set_threads(threads)
+    for d in sc.materials:
+        S.add_material(_material_struct(O.Material, d))
+    p = dict(sc.params)
+    S.set_params(**p)
+    S.set_domain(sc.lo, sc.hi, tuple(bool(x) for x in sc.periodic))
+    S.add_many(sc.pos, sc.vel, sc.mass, sc.u, sc.mat, sc.fixed)
+    if sc.flaws is not None:
+        kind, seed = sc.flaws
+        if kind == "multi":
+            S.seed_flaws_multi(sc.dx, seed)
+        else:
+            S.seed_damage(sc.dx, seed)
+    if sc.h0 is not None:
+        S.set_h0(sc.h0)
+    return S
+
+
+def write_ic(sc: Scenario, path):
+    """Reference IC file (run_ic.cpp:4-6): f8 [xlo xhi ylo yhi zlo zhi n] + n x 10 f8."""
+    hdr = np.array([sc.lo[0], sc.hi[0], sc.lo[1], sc.hi[1], sc.lo[2], sc.hi[2], sc.n], np.float64)
+    rec = np.concatenate([sc.pos, sc.vel, sc.mass[:, None], sc.u[:, None], sc.mat[:, None].astype(float),
+                          sc.fixed[:, None].astype(float)], axis=1)
+    with open(path, "wb") as f:
+        f.write(hdr.tobytes())
+        f.write(np.ascontiguousarray(rec, np.float64).tobytes())

@@ -1,0 +1,245 @@
+/*
+ * deorbit_sph.h -- C ABI of the GB300 SPH impact solver (libdeorbit_sph.so).
+ *
+ * Drop-in boundary for the step loop of the reference's SPH hydrocode:
+ * the in-process `struct System` of hydrocodes/sph/sph.hpp:72-380 (init /
+ * timestep / step over public particle arrays) and the Tillotson `Material`
+ * of hydrocodes/common/eos.hpp:15-113.  Plain C types only: host pointers,
+ * sizes and integer status codes; no CUDA or C++ types cross the boundary.
+ *
+ * Work is organised in IMPACTS: independent particle systems, each with its
+ * own domain, parameters, cell grid and time step.  A context holds one or
+ * many impacts and advances them together on one GPU (single-instance use =
+ * one impact).  Particle fields are read and written in the caller's original
+ * particle order.
+ *
+ * Threading: one host thread per context; calls on a context are not
+ * re-entrant.  Each context owns its CUDA stream and device buffers; there is
+ * no global mutable state apart from the per-thread error string.
+ * Errors: every call returns SPH_OK (0) or a negative SPH_ERR_* code;
+ * sph_last_error() describes the last failure on the calling thread.
+ */
+#ifndef DEORBIT_SPH_H
+#define DEORBIT_SPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_ARG = -1,      /* invalid argument (null pointer, bad id, bad size) */
+    SPH_ERR_CUDA = -2,     /* a CUDA call failed (message has the CUDA error)   */
+    SPH_ERR_STATE = -3,    /* call not valid in the current state               */
+    SPH_ERR_NOMEM = -4,    /* device or host allocation failed                  */
+    SPH_ERR_IO = -5,       /* file could not be read / written, short read      */
+    SPH_ERR_CAPACITY = -6, /* a fixed capacity (materials, impacts) exceeded    */
+    SPH_ERR_TIMEOUT = -7   /* a bounded device wait ran out                     */
+};
+
+enum sph_precision {
+    SPH_FP64 = 0,  /* plain form: every field and pair interaction in FP64      */
+    SPH_MIXED = 1  /* FP32 pairs / EOS / stress, FP64 positions and energies    */
+};
+
+enum sph_eos_type { SPH_EOS_IDEAL = 0, SPH_EOS_TILLOTSON = 1 };
+enum sph_yield_model { SPH_YIELD_VON_MISES = 0, SPH_YIELD_COLLINS = 1 };
+enum sph_flaw_model { SPH_FLAWS_SINGLE = 0, SPH_FLAWS_MULTI = 1 };
+enum sph_neighbor_kind { SPH_NBR_DENSITY = 0, SPH_NBR_FORCE = 1 };
+
+/* Replaces `struct Material` (hydrocodes/common/eos.hpp:15-39).  Emod is
+ * derived by sph_material_tillotson as 9AG/(3A+G) (eos.hpp:37).  The Collins
+ * fields are used only when yield_model == SPH_YIELD_COLLINS (no counterpart in
+ * the reference SPH; pressure-dependent yield as in
+ * hydrocodes/euler/hydro_cpu.cpp:229-252). */
+typedef struct sph_material {
+    int32_t type;        /* sph_eos_type */
+    int32_t yield_model; /* sph_yield_model */
+    double gamma;
+    double rho0, a, b, A, B, alpha, beta, u0, uiv, ucv;
+    double G, Y, Emod, wm, wk;
+    double Y0, mu_i, Ylim, Yd0, mu_d;
+} sph_material;
+
+/* Replaces the public parameter members of `System`
+ * (hydrocodes/sph/sph.hpp:86-92).  flaw_model selects single-flaw seeding
+ * (reference) or Benz-Asphaug multi-flaw damage (extension). */
+typedef struct sph_params {
+    double eta, h_init, alpha, beta, eps, alpha_u, cfl, eps_as;
+    int32_t as_n, damage_on;
+    int32_t flaw_model;
+    int32_t reserved;
+} sph_params;
+
+/* Per-impact status. */
+typedef struct sph_impact_info {
+    int64_t n;          /* particles */
+    int64_t steps;      /* steps taken */
+    double t;           /* simulated time */
+    double dt;          /* last step size used */
+    double h_max;       /* max smoothing length at the last cell build */
+    int32_t nc[3];      /* reference cell grid (sph.hpp:147-157) */
+    double cw[3];
+    int32_t density_rounds; /* adaptive-h rounds in the last step (sph.hpp:185) */
+    int32_t initialized;
+} sph_impact_info;
+
+/* Conservation record of one impact, from compensated FP64 device sums. */
+typedef struct sph_conservation {
+    double mass, kinetic, internal, energy;
+    double momentum[3];
+} sph_conservation;
+
+typedef struct sph_ctx sph_ctx;
+
+/* ---- library -------------------------------------------------------------- */
+int sph_abi_version(void);
+const char* sph_last_error(void);
+/* Fills a Tillotson material exactly like Material::tillotson (eos.hpp:30-39). */
+void sph_material_tillotson(sph_material* out, double rho0, double A, double B, double a,
+                            double b, double alpha, double beta, double u0, double uiv,
+                            double ucv, double G, double Y, double wm, double wk);
+/* Ideal gas, Material::ideal (eos.hpp:29). */
+void sph_material_ideal(sph_material* out, double gamma);
+/* Standard sets of eos.hpp:42-50: 0 iron, 1 basalt, 2 water, 3 aluminum. */
+int sph_material_standard(int which, sph_material* out);
+/* Reference parameter defaults (sph.hpp:86-92). */
+void sph_params_default(sph_params* out);
+/* Host-only flaw thresholds of System::seed_damage (sph.hpp:117-128) for n
+ * particles with material ids mat[] (no GPU needed). */
+int sph_seed_flaws_single(int64_t n, const int32_t* mat, const sph_material* mats, int32_t nmat,
+                          double dx, uint32_t seed, double* eps_act);
+/* Host-only Benz-Asphaug multi-flaw seeding (extension, no reference
+ * counterpart): ptr[n+1] CSR over particles, eps[cap] activation strains,
+ * *total the flaw count (SPH_ERR_CAPACITY when cap is too small), eps_act[n]
+ * each particle's weakest flaw. */
+int sph_seed_flaws_multi_host(int64_t n, const int32_t* mat, const sph_material* mats,
+                              int32_t nmat, double dx, uint32_t seed, int64_t* ptr, double* eps,
+                              int64_t cap, int64_t* total, double* eps_act);
+
+/* ---- context -------------------------------------------------------------- */
+/* Replaces constructing a `System` (sph.hpp:72).  device: CUDA ordinal. */
+int sph_create(sph_ctx** out, int precision, int device);
+int sph_destroy(sph_ctx* ctx);
+/* Replaces `materials.push_back(...)` (sph.hpp:82); materials are shared by all
+ * impacts of the context.  *id receives the material index. */
+int sph_add_material(sph_ctx* ctx, const sph_material* m, int32_t* id);
+
+/* ---- impacts (one System each) ------------------------------------------- */
+/* Creates an impact with parameters (sph.hpp:86-92) and domain
+ * (set_domain, sph.hpp:96-101; periodic[a] != 0 for a periodic axis). */
+int sph_impact_create(sph_ctx* ctx, const sph_params* p, const double dlo[3],
+                      const double dhi[3], const int32_t periodic[3], int32_t* impact);
+/* Replaces System::set_domain (sph.hpp:96-101) before sph_init. */
+int sph_impact_set_domain(sph_ctx* ctx, int32_t impact, const double dlo[3],
+                          const double dhi[3], const int32_t periodic[3]);
+int sph_impact_set_params(sph_ctx* ctx, int32_t impact, const sph_params* p);
+int sph_impact_get_params(sph_ctx* ctx, int32_t impact, sph_params* p);
+/* Replaces System::add (sph.hpp:103-111) for n particles at once: hh starts at
+ * h_init, derived fields at zero, eps_act 1e30, dscale 1.  mat may be NULL
+ * (material 0); fixed may be NULL (none fixed). */
+int sph_impact_add_particles(sph_ctx* ctx, int32_t impact, int64_t n, const double* x,
+                             const double* y, const double* z, const double* vx,
+                             const double* vy, const double* vz, const double* mass,
+                             const double* u, const int32_t* mat, const uint8_t* fixed);
+/* Replaces System::seed_damage (sph.hpp:117-128): one Weibull flaw per brittle
+ * particle from mt19937(seed), eps = (U(1e-9,1] / (k dx^3))^(1/m). */
+int sph_impact_seed_damage(sph_ctx* ctx, int32_t impact, double dx, uint32_t seed);
+/* Extension (no reference counterpart): Benz & Asphaug (1995) multi-flaw
+ * seeding, ceil(N ln N) flaws per brittle material; sets flaw_model MULTI.
+ * *nflaws (may be NULL) receives the total. */
+int sph_impact_seed_flaws_multi(sph_ctx* ctx, int32_t impact, double dx, uint32_t seed,
+                                int64_t* nflaws);
+/* Extension: per-particle reference smoothing length (graded lattices). */
+int sph_impact_set_h0(sph_ctx* ctx, int32_t impact, const double* h0);
+/* Releases an impact's particles and slot (serving). */
+int sph_impact_remove(sph_ctx* ctx, int32_t impact);
+int sph_impact_count(sph_ctx* ctx, int32_t* count);
+int sph_impact_info_get(sph_ctx* ctx, int32_t impact, sph_impact_info* info);
+
+/* ---- stepping (System::init / timestep / step) ---------------------------- */
+/* Replaces System::init (sph.hpp:379) for every impact not yet initialised. */
+int sph_init(sph_ctx* ctx);
+/* Replaces System::timestep (sph.hpp:350-355): CFL step of one impact. */
+int sph_timestep(sph_ctx* ctx, int32_t impact, double* dt);
+/* Replaces System::step(dt) (sph.hpp:357-377): one KDK step of EVERY impact
+ * with the caller's dt. */
+int sph_step(sph_ctx* ctx, double dt);
+/* Batched run: nsteps KDK steps in which each impact uses its own CFL dt
+ * (device-side, as run_ic.cpp:328-329), clipped at its t_end when t_end > 0.
+ * Impacts that reached t_end stop advancing. */
+int sph_run(sph_ctx* ctx, int32_t nsteps, double t_end);
+/* Individual phases (for parity checks, as cpu_dump.cpp:171 uses them). */
+int sph_compute_density_h(sph_ctx* ctx, int32_t iters);   /* sph.hpp:184-208 */
+int sph_compute_forces(sph_ctx* ctx);                     /* sph.hpp:260-318 */
+int sph_synchronize(sph_ctx* ctx);
+
+/* ---- particle fields, original order --------------------------------------
+ * name: x y z vx vy vz ax ay az mass rho u dudt P cs csig hh eps_work D eps_act
+ * sigmax Pf Rart dscale Sxx Syy Szz Sxy Sxz Syz dSxx dSyy dSzz dSxy dSxz dSyz h0
+ * (replaces reading / writing System's public vectors, sph.hpp:73-81). */
+int sph_read_field(sph_ctx* ctx, int32_t impact, const char* name, double* out);
+int sph_write_field(sph_ctx* ctx, int32_t impact, const char* name, const double* in);
+int sph_read_mat(sph_ctx* ctx, int32_t impact, int32_t* out);
+int sph_read_fixed(sph_ctx* ctx, int32_t impact, uint8_t* out);
+int sph_write_fixed(sph_ctx* ctx, int32_t impact, const uint8_t* in);
+
+/* ---- diagnostics ----------------------------------------------------------- */
+int sph_conservation_get(sph_ctx* ctx, int32_t impact, sph_conservation* out);
+/* Tillotson / ideal EOS on the device in the context precision
+ * (eos.hpp:65-113): n (rho, u) pairs of material mat -> P, cs. */
+int sph_eos_eval(sph_ctx* ctx, int32_t mat, int64_t n, const double* rho, const double* u,
+                 double* P, double* cs);
+
+/* ---- parity hooks: integer outputs of the last cell build ------------------
+ * Reference cell grid (sph.hpp:147-162) of one impact: nc, cw, and its cell
+ * list as CSR in original particle ids, each cell ascending (bit-exact with
+ * System::cells).  start has nc0*nc1*nc2+1 entries, ids n entries. */
+int sph_debug_ref_cells(sph_ctx* ctx, int32_t impact, int32_t nc[3], double cw[3],
+                        int32_t* start, int64_t start_len, int32_t* ids);
+/* Neighbour sets of the current state as System::for_neighbors sees them
+ * (sph.hpp:163-182): kind SPH_NBR_DENSITY = {j : r < 2 h_i} (self included),
+ * SPH_NBR_FORCE = {j != i : r < 2 hbar, r != 0}.  counts[n] per particle (original
+ * order), ids: each set ascending in original ids, concatenated in original
+ * particle order.  *total receives the number of entries; returns
+ * SPH_ERR_CAPACITY when cap is too small. */
+int sph_debug_neighbors(sph_ctx* ctx, int32_t impact, int32_t kind, int32_t* counts,
+                        int32_t* ids, int64_t cap, int64_t* total);
+
+/* ---- files (formats of run_ic.cpp / gpu_ic.cpp) ----------------------------
+ * IC: f8 header [xlo xhi ylo yhi zlo zhi n], then n x [x y z vx vy vz mass u mat
+ * fixed] (run_ic.cpp:4-6).  Creates an impact with the given parameters and
+ * the IC's domain; *impact receives its id. */
+int sph_load_ic(sph_ctx* ctx, const char* path, const sph_params* p, int32_t* impact);
+/* Snapshot: int64 n, then n x f8 [x y z vx vy vz u rho h mat] (run_ic.cpp:15-30). */
+int sph_write_snapshot(sph_ctx* ctx, int32_t impact, const char* path);
+/* Lossless checkpoint, write-then-rename: f8 header [xlo xhi ylo yhi zlo zhi n t dx]
+ * then n x 18 f8 [x y z vx vy vz mass u mat fixed D eps_act Sxx Sxy Sxz Syy Syz Szz]
+ * (run_ic.cpp:32-55). */
+int sph_write_checkpoint(sph_ctx* ctx, int32_t impact, const char* path, double dx);
+/* Restart from a checkpoint (run_ic.cpp:76-102): new impact, t and D / eps_act /
+ * S restored; *dx_out (may be NULL) receives dx. */
+int sph_load_checkpoint(sph_ctx* ctx, const char* path, const sph_params* p, int32_t* impact,
+                        double* dx_out);
+
+/* ---- tuning ---------------------------------------------------------------- */
+/* Launch shape of the neighbour kernels and the traversal cell width as a
+ * multiple of h_init.  Zero keeps the current value. */
+int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor);
+/* Number of kernel launches issued by this context since creation. */
+int sph_launch_count(sph_ctx* ctx, int64_t* launches);
+/* CUDA-event phase times of the last step in ms: [kick+sort, density, eos,
+ * force, damage+finish+dt] (mirrors gpu_ic's PROFILE line, gpu_ic.cpp:147). */
+int sph_phase_times(sph_ctx* ctx, double ms[5]);
+/* Opt-in CUDA-event timing of the phases (off by default). */
+int sph_set_profiling(sph_ctx* ctx, int32_t on);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
