@@ -1,0 +1,374 @@
+"""Benchmark of the SPH step loop on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload grazing|halfspace] [--n PARTICLES]
+
+Workload (default): the grazing strength + damage impact, 1,048,576 particles
+(1 km iron sphere at 3 deg, 8 km/s into a granite slab; von Mises iron, Collins
+granite, multi-flaw damage), seeded synthetic inputs.  A step is one KDK step
+of the whole workload (sph.hpp:357-377) with the CFL dt computed on the device.
+
+value   particle-steps/s of the mixed form (FP32 pairs / EOS / stress, FP64
+        positions and energies), state resident in HBM, CUDA events on the
+        engine stream around exactly K steps.
+e2e     the same metric through the C ABI with host buffers: every step
+        writes the carried state from pinned host memory, steps, and reads it
+        back (a drop-in caller that keeps System's vectors on the host).
+plain_fp64  the FP64 plain form on the same workload (the 4x comparison).
+cpu_baseline  the FP64 CPU oracle on host cores (reference thread cap of 16)
+        over a cropped sample of the same workload.
+--impl reference  times that CPU oracle as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s batched vs plain GPU at ≤1e-4 FP64 rel err; p50/p99 latency"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per particle of one launch (compulsory reads of the
+# particle's own state and writes of its results; neighbour re-reads, lists
+# and sort scratch excluded).  See the design doc for the derivation.
+ALG_BYTES = {
+    # k_force: reads pf 16, cpk 4, imp 2, mat 1, list count 4, h, rho, csig,
+    # Pf/rho^2, dscale/rho^2, dscale, Rart, P, m/rho, mass (10 R), vel 3R, S 6R,
+    # u 8, (FP64 form also x y z 24); writes acc 3R, dudt R, dSdt 6R, eps_work R
+    ("force", 4): 16 + 4 + 2 + 1 + 4 + 10 * 4 + 3 * 4 + 6 * 4 + 8 + (3 + 1 + 6 + 1) * 4,
+    ("force", 8): 16 + 4 + 2 + 1 + 4 + 24 + 10 * 8 + 3 * 8 + 6 * 8 + 8 + (3 + 1 + 6 + 1) * 8,
+    # k_list (force): reads pf 16, cpk 4, refbin 8, imp 2; writes count 4
+    ("list_force", 4): 34, ("list_force", 8): 34,
+    ("list_density", 4): 34, ("list_density", 8): 34,
+    # k_density: reads pf 16, cpk 4, h R, mass R, imp 2, count 4 (+x y z FP64); writes rho R, h R, pf.w 4
+    ("density", 4): 16 + 4 + 2 + 4 + 4 * 4 + 4, ("density", 8): 16 + 4 + 2 + 4 + 24 + 4 * 8 + 4,
+}
+# whole step, per particle-step: FP64 strength+damage 429 B, mixed 241 B
+STEP_BYTES = {8: 429, 4: 241}
+
+
+def rank_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(name, n):
+    from deorbit_gb300 import ic
+    if name == "halfspace":
+        return ic.impact_halfspace()
+    return ic.grazing(n_total=n)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out, _ = self.p.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_form(sph, ic, sc, precision, steps, warmup, device, profile=True):
+    """Init (untimed), W warm-up steps, then exactly K timed steps."""
+    ctx = sph.Context(precision, device)
+    b = ic.to_context(ctx, sc)
+    ctx.init()
+    for _ in range(warmup):
+        ctx.run(1)
+    ctx.synchronize()
+    ctx.set_profiling(profile)
+    ctx.kernel_stats_reset()
+    l0 = ctx.launches()
+    ctx.event_record(0)
+    ctx.run(steps)
+    ctx.event_record(1)
+    ms = ctx.event_elapsed(0, 1)
+    ctx.synchronize()
+    l1 = ctx.launches()
+    ctx.set_profiling(False)
+    return ctx, b, ms, ctx.kernel_stats(), l1 - l0
+
+
+def mixed_error(sph, ic, sc, steps, device):
+    """rel-L2 of the mixed form against the FP64 form after `steps` steps with
+    the same dt sequence (taken from the FP64 form)."""
+    c64 = sph.Context(sph.FP64, device)
+    b64 = ic.to_context(c64, sc)
+    c32 = sph.Context(sph.MIXED, device)
+    b32 = ic.to_context(c32, sc)
+    c64.init()
+    c32.init()
+    for _ in range(steps):
+        dt = c64.timestep(b64)
+        c64.step(dt)
+        c32.step(dt)
+    out = {}
+    for grp, names in (("pos", ["x", "y", "z"]), ("vel", ["vx", "vy", "vz"]), ("u", ["u"]), ("rho", ["rho"]),
+                       ("P", ["P"]), ("S", ["Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"]), ("D", ["D"])):
+        a = np.concatenate([c32.read(b32, k) for k in names])
+        r = np.concatenate([c64.read(b64, k) for k in names])
+        nr = np.linalg.norm(r)
+        out[grp] = float(np.linalg.norm(a - r) / nr) if nr > 0 else float(np.linalg.norm(a - r))
+    c64.close()
+    c32.close()
+    return out
+
+
+def e2e_rate(sph, ctx, b, n, steps, warmup):
+    """Steps through the C ABI with the carried state crossing the boundary
+    from / to pinned host buffers every step."""
+    names = ["x", "y", "z", "vx", "vy", "vz", "u", "hh", "D", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"]
+    pinned = True
+    try:
+        import torch
+        bufs = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in names}
+    except Exception:
+        pinned = False
+        bufs = {k: np.empty(n) for k in names}
+    for k in names:
+        bufs[k][:] = ctx.read(b, k)
+
+    def one():
+        for k in names:
+            ctx.write(b, k, bufs[k])
+        dt = ctx.timestep(b)
+        ctx.step(dt)
+        for k in names:
+            bufs[k][:] = ctx.read(b, k)
+
+    for _ in range(warmup):
+        one()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    ctx.synchronize()
+    el = time.perf_counter() - t0
+    nbytes = 8 * n * len(names)
+    return n * steps / el, el, nbytes, pinned
+
+
+def cpu_rate(ic, sc, steps, threads=0):
+    S = ic.to_oracle(sc, threads=threads)
+    S.init()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        S.step(S.timestep())
+    el = time.perf_counter() - t0
+    return sc.n * steps / el, el, S.threads()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="grazing", choices=["grazing", "halfspace"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+
+    from deorbit_gb300 import ic
+
+    sc = workload(args.workload, args.n)
+    sample_n = min(args.cpu_sample, sc.n)
+    wl = {"workload": f"{args.workload} impact, strength+damage" if args.workload == "grazing"
+          else "halfspace impact, hydro only", "n_particles": sc.n, "dx_m": sc.dx,
+          "materials": "granite (Collins, multi-flaw) + iron (von Mises)" if args.workload == "grazing"
+          else "granite + iron, hydro only", "l2": "working set > 129 MB L2 (no flush needed)"}
+
+    if args.impl == "reference":
+        # the reference's own CPU path is the oracle port here (the reference
+        # tree is not on this machine); rank 0 only
+        if rank != 0:
+            return
+        from oracle import oracle  # noqa: F401
+        sample = ic.crop(sc, sample_n)
+        S = ic.to_oracle(sample, threads=min(os.cpu_count() or 1, 16))
+        S.init()
+        for _ in range(args.warmup):
+            S.step(S.timestep())
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            S.step(S.timestep())
+        el = time.perf_counter() - t0
+        v = sample.n * args.steps / el
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": dict(wl, sample=sample.n),
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": S.threads(), "kind": "port",
+                                 "sample": f"{sample.n} particles cropped from the {sc.n}-particle workload "
+                                           f"around the impact point, {args.steps} KDK steps after init"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    from deorbit_gb300 import sph
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- mixed form (headline)
+    barrier()
+    with ClockSampler(device) as clk:
+        ctx, b, ms, kst, launches = time_form(sph, ic, sc, sph.MIXED, args.steps, args.warmup, device)
+    barrier()
+    ms = max_over_ranks(ms)
+    value = world * sc.n * args.steps / (ms / 1000.0)
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        r, el, nbytes, pinned = e2e_rate(sph, ctx, b, sc.n, args.steps, min(args.warmup, 2))
+        el = max_over_ranks(el)
+        e2e = {"value": world * sc.n * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes + 8, "pinned_host": pinned}
+    ctx.close()
+
+    # ---- plain FP64 form
+    c64, b64, ms64, kst64, _ = time_form(sph, ic, sc, sph.FP64, args.steps, args.warmup, device)
+    c64.close()
+    ms64 = max_over_ranks(ms64)
+    value64 = world * sc.n * args.steps / (ms64 / 1000.0)
+
+    # ---- accuracy of the mixed form against FP64 (same dt sequence)
+    err = mixed_error(sph, ic, sc, args.steps, device) if rank == 0 else None
+
+    # ---- roofline of the dominant mixed-form kernel
+    hbm, hbm_kind = peaks()
+    dom = max(kst, key=lambda k: kst[k][0])
+    tot_ms, nl = kst[dom]
+    avg_ms = tot_ms / max(nl, 1)
+    alg = ALG_BYTES.get((dom, 4))
+    achieved = (alg * sc.n / (avg_ms / 1000.0) / 1e9) if alg else None
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if os.path.exists(tfile):
+        for line in open(tfile):
+            f = line.split()
+            if len(f) >= 4 and f[0] == f"{dom}_mixed":
+                traffic = (float(f[2]) + float(f[3])) * sc.n / float(f[1])
+    roof = {"kernel": f"k_{dom}", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+            "peak_kind": f"{hbm_kind} copy bandwidth", "alg_bytes_per_particle": alg,
+            "avg_launch_ms": avg_ms, "launches": nl}
+    step_bytes = STEP_BYTES[4] * sc.n
+    step_roof = {"alg_bytes_per_particle_step": STEP_BYTES[4],
+                 "achieved_gbs": step_bytes / (ms / args.steps / 1000.0) / 1e9}
+    step_roof["frac"] = step_roof["achieved_gbs"] / hbm
+
+    # ---- CPU baseline (rank 0, N = 1): oracle on a cropped sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sample = ic.crop(sc, sample_n)
+        v, el, thr = cpu_rate(ic, sample, 2, threads=min(os.cpu_count() or 1, 16))
+        cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{sample.n} particles cropped from the {sc.n}-particle workload around the "
+                         f"impact point, 2 KDK steps after init ({el:.1f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": dict(wl, form="mixed (FP32 pairs/EOS/stress, FP64 positions/energies)",
+                               parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+                "roofline": roof, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk.summary(),
+                "plain_fp64": {"value": value64, "ms_per_step": ms64 / args.steps,
+                               "kernel_ms": {k: v[0] for k, v in kst64.items()}},
+                "speedup_vs_plain_fp64": value / value64,
+                "mixed_vs_fp64_rel_l2": err,
+                "kernel_ms": {k: v[0] for k, v in kst.items()}}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

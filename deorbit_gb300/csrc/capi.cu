@@ -670,4 +670,31 @@ int sph_set_profiling(sph_ctx* ctx, int32_t on) {
     return guard([&] { E(ctx).set_profiling(on); });
 }
 
+int sph_kernel_stats(sph_ctx* ctx, int32_t kernel_class, double* total_ms, int64_t* launches) {
+    return guard([&] {
+        need(total_ms, "total_ms");
+        need(launches, "launches");
+        E(ctx).kernel_stats(kernel_class, total_ms, launches);
+    });
+}
+
+int sph_kernel_stats_reset(sph_ctx* ctx) {
+    return guard([&] { E(ctx).kernel_stats_reset(); });
+}
+
+int sph_event_record(sph_ctx* ctx, int32_t slot) {
+    return guard([&] {
+        CTX_SET();
+        E(ctx).event_record(slot);
+    });
+}
+
+int sph_event_elapsed(sph_ctx* ctx, int32_t slot_a, int32_t slot_b, double* ms) {
+    return guard([&] {
+        need(ms, "ms");
+        CTX_SET();
+        *ms = E(ctx).event_elapsed(slot_a, slot_b);
+    });
+}
+
 }  // extern "C"

@@ -62,6 +62,10 @@ public:
     virtual int64_t launches() = 0;
     virtual void phase_times(double ms[5]) = 0;
     virtual void set_profiling(int on) = 0;
+    virtual void kernel_stats(int cls, double* ms, int64_t* n) = 0;
+    virtual void kernel_stats_reset() = 0;
+    virtual void event_record(int slot) = 0;
+    virtual double event_elapsed(int a, int b) = 0;
 };
 
 std::unique_ptr<EngineBase> make_engine_fp64(int device);

@@ -206,6 +206,8 @@ public:
         cudaFree(flags_d_);
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
+        for (auto& e : prof_pool_) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        for (int i = 0; i < 16; i++) if (user_ev_[i]) cudaEventDestroy(user_ev_[i]);
         cudaStreamDestroy(st_);
     }
 
@@ -453,24 +455,55 @@ public:
     void one_step(bool host_sync) {
         const int nimp = (int)imp_.size();
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[0], st_));
+        cls(KC_KICK);
         launch_n(k_kick_drift<R>, N_);
         sort_reorder(false);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[1], st_));
         density_rounds(2, host_sync);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[2], st_));
+        cls(KC_EOS);
         launch_n(k_eos<R>, N_);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[3], st_));
+        cls(KC_LIST_FORCE);
         build_list<kListForce>(true);
+        cls(KC_FORCE);
         launch_n(k_force<R>, N_, 128);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[4], st_));
+        cls(KC_DAMAGE);
         launch_n(k_damage<R>, N_);
+        cls(KC_FINISH);
         launch_n(k_finish<R>, N_);
+        cls(KC_DT);
         dt_reduce();
         launch_small(k_run_control, nimp, 1);
+        cls(KC_OTHER);
         if (profiling_) {
             DSPH_CUDA(cudaEventRecord(ev_[5], st_));
             record_phases();
+            prof_flush();
         }
+    }
+
+    void kernel_stats(int c, double* ms, int64_t* n) override {
+        if (c < 0 || c >= KC_N) throw SphError(SPH_ERR_ARG, "bad kernel class");
+        *ms = kstat_ms_[c];
+        *n = kstat_n_[c];
+    }
+    void kernel_stats_reset() override {
+        for (int c = 0; c < KC_N; c++) { kstat_ms_[c] = 0; kstat_n_[c] = 0; }
+    }
+    void event_record(int slot) override {
+        if (slot < 0 || slot >= 16) throw SphError(SPH_ERR_ARG, "event slot out of range");
+        if (!user_ev_[slot]) DSPH_CUDA(cudaEventCreate(&user_ev_[slot]));
+        DSPH_CUDA(cudaEventRecord(user_ev_[slot], st_));
+    }
+    double event_elapsed(int a, int b) override {
+        if (a < 0 || a >= 16 || b < 0 || b >= 16 || !user_ev_[a] || !user_ev_[b])
+            throw SphError(SPH_ERR_ARG, "event slot not recorded");
+        DSPH_CUDA(cudaEventSynchronize(user_ev_[b]));
+        float ms = 0;
+        DSPH_CUDA(cudaEventElapsedTime(&ms, user_ev_[a], user_ev_[b]));
+        return ms;
     }
 
     void run(int nsteps, double t_end) override {
@@ -754,22 +787,66 @@ private:
     void launch_n_raw(Kern k, int64_t n, Args... args) {
         if (n <= 0) return;
         int bs = 256;
+        prof_begin();
         k<<<(unsigned)((n + bs - 1) / bs), bs, 0, st_>>>(args...);
+        prof_end();
         launches_++;
     }
     template <class Kern>
     void launch_n(Kern k, int64_t n, int bs = 0) {
         if (n <= 0) return;
         if (bs <= 0) bs = 256;
+        prof_begin();
         k<<<(unsigned)((n + bs - 1) / bs), bs, 0, st_>>>(view());
+        prof_end();
         launches_++;
     }
     template <class Kern, class... Args>
     void launch_small(Kern k, int nimp, Args... args) {
         if (nimp <= 0) return;
+        prof_begin();
         k<<<(nimp + 127) / 128, 128, 0, st_>>>(tab_d_, nimp, args...);
+        prof_end();
         launches_++;
     }
+
+    // ---- per-kernel-class CUDA-event timing on the engine stream
+public:
+    enum KClass { KC_KICK, KC_SORT, KC_GRID, KC_LIST_DENSITY, KC_DENSITY, KC_EOS, KC_LIST_FORCE,
+                  KC_FORCE, KC_DAMAGE, KC_FINISH, KC_DT, KC_OTHER, KC_N };
+
+private:
+    void prof_begin() {
+        if (!profiling_) return;
+        if (np_ >= prof_pool_.size()) {
+            cudaEvent_t a, b;
+            DSPH_CUDA(cudaEventCreate(&a));
+            DSPH_CUDA(cudaEventCreate(&b));
+            prof_pool_.push_back({a, b});
+            prof_cls_.push_back(0);
+        }
+        DSPH_CUDA(cudaEventRecord(prof_pool_[np_].first, st_));
+    }
+    void prof_end() {
+        if (!profiling_) return;
+        DSPH_CUDA(cudaEventRecord(prof_pool_[np_].second, st_));
+        prof_cls_[np_] = cur_cls_;
+        np_++;
+    }
+    void prof_flush() {
+        if (!profiling_ || np_ == 0) return;
+        DSPH_CUDA(cudaEventSynchronize(prof_pool_[np_ - 1].second));
+        for (size_t i = 0; i < np_; i++) {
+            float ms = 0;
+            DSPH_CUDA(cudaEventElapsedTime(&ms, prof_pool_[i].first, prof_pool_[i].second));
+            kstat_ms_[prof_cls_[i]] += ms;
+            kstat_n_[prof_cls_[i]] += 1;
+        }
+        np_ = 0;
+    }
+    void cls(int c) { cur_cls_ = c; }
+
+public:
 
     void ensure_stage(int64_t n) {
         if (n <= stage_cap_) return;
@@ -1205,10 +1282,14 @@ private:
         const int nimp = (int)imp_.size();
         DSPH_CUDA(cudaMemsetAsync(keys_by_gid_, 0xff, sizeof(uint32_t) * std::max<int64_t>(G_, 1), st_));
         DSPH_CUDA(cudaMemsetAsync(cell_cnt_, 0, sizeof(int32_t) * (C_ + 1), st_));
+        const int keep_cls = cur_cls_;
+        cls(KC_SORT);
         launch_n_raw(k_fine_keys<R>, N_, view(), keys_by_gid_, cell_cnt_);
+        prof_begin();
         launches_ += radix_sort_pairs(keys_by_gid_, nullptr, skeys_, sgid_, tkeys_, tgid_, G_,
                                       key_bits(), scratch_, st_);
         launches_ += exclusive_scan_i32(cell_cnt_, cell_cnt_, C_ + 1, scratch_, st_);
+        prof_end();
         int64_t n_new = N_;
         if (count_changes) {
             DSPH_CUDA(cudaMemcpyAsync(flags_h_ + 2, cell_cnt_ + C_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
@@ -1233,6 +1314,7 @@ private:
         launch_small(k_impact_reset_omax, nimp);
         launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_);
         launch_small(k_impact_ranges, nimp, (const int32_t*)cell_cnt_);
+        cls(keep_cls);
         grid_valid_ = true;
     }
 
@@ -1254,7 +1336,9 @@ private:
     void hmax_pass(int which) {
         int64_t n = N_;
         if (n <= 0) return;
+        prof_begin();
         k_hmax<R><<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(view(), which);
+        prof_end();
         launches_++;
     }
 
@@ -1262,14 +1346,18 @@ private:
         const int nimp = (int)imp_.size();
         launch_small(k_impact_begin_round, nimp, 2);
         for (int round = 0; round < 4; round++) {
+            cls(KC_GRID);
             if (round > 0) launch_small(k_impact_begin_round, nimp, 0);
             hmax_pass(0);
             launch_small(k_ref_grid, nimp);
             launch_n(k_ref_bins<R>, N_);
             for (int it = 0; it < iters; it++) {
+                cls(KC_LIST_DENSITY);
                 build_list<kListDensity>(true);
+                cls(KC_DENSITY);
                 launch_n(k_density<R>, N_);
             }
+            cls(KC_GRID);
             hmax_pass(1);
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 1, 0, sizeof(int32_t), st_));
             launch_small(k_round_check, nimp, flags_d_);
@@ -1284,6 +1372,7 @@ private:
 
     void final_grid_build() {
         const int nimp = (int)imp_.size();
+        cls(KC_GRID);
         launch_small(k_impact_begin_round, nimp, 1);
         hmax_pass(0);
         launch_small(k_ref_grid, nimp);
@@ -1357,6 +1446,13 @@ private:
     bool profiling_ = false;
     cudaEvent_t ev_[6]{};
     double phase_ms_[5];
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_pool_;
+    std::vector<int> prof_cls_;
+    size_t np_ = 0;
+    int cur_cls_ = 0;
+    double kstat_ms_[KC_N] = {};
+    int64_t kstat_n_[KC_N] = {};
+    cudaEvent_t user_ev_[16]{};
     bool grid_valid_ = false;
 };
 

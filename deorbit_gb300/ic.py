@@ -311,3 +311,21 @@ def write_ic(sc: Scenario, path):
     with open(path, "wb") as f:
         f.write(hdr.tobytes())
         f.write(np.ascontiguousarray(rec, np.float64).tobytes())
+
+
+def crop(sc: Scenario, n_keep: int, center=None) -> Scenario:
+    """A bounded sample of a workload: all impactor particles plus the target
+    particles nearest the impact point, n_keep in total (same dx, materials,
+    parameters and domain)."""
+    if n_keep >= sc.n:
+        return sc
+    imp = np.nonzero(sc.mat != 0)[0]
+    tgt = np.nonzero(sc.mat == 0)[0]
+    if center is None:
+        center = sc.pos[imp].mean(0) if imp.size else sc.pos.mean(0)
+    d = ((sc.pos[tgt] - center) ** 2).sum(1)
+    keep_t = tgt[np.argsort(d, kind="stable")[: max(0, n_keep - imp.size)]]
+    keep = np.sort(np.r_[keep_t, imp])[:n_keep]
+    return dataclasses.replace(sc, name=sc.name + f"_crop{n_keep}", pos=sc.pos[keep], vel=sc.vel[keep],
+                               mass=sc.mass[keep], u=sc.u[keep], mat=sc.mat[keep], fixed=sc.fixed[keep],
+                               h0=None if sc.h0 is None else sc.h0[keep])

@@ -113,7 +113,14 @@ _SIGS = {
     "sph_launch_count": (C.c_int, [_P, _I64]),
     "sph_phase_times": (C.c_int, [_P, _D]),
     "sph_set_profiling": (C.c_int, [_P, C.c_int32]),
+    "sph_kernel_stats": (C.c_int, [_P, C.c_int32, _D, _I64]),
+    "sph_kernel_stats_reset": (C.c_int, [_P]),
+    "sph_event_record": (C.c_int, [_P, C.c_int32]),
+    "sph_event_elapsed": (C.c_int, [_P, C.c_int32, C.c_int32, _D]),
 }
+
+KERNEL_CLASSES = ["kick", "sort", "grid", "list_density", "density", "eos", "list_force", "force",
+                  "damage", "finish", "dt", "other"]
 
 _lib = None
 
@@ -435,6 +442,27 @@ class Context:
         ms = np.zeros(5)
         check(lib().sph_phase_times(self.h, _dp(ms)))
         return ms
+
+    def kernel_stats(self):
+        """{class name: (total device ms, launches)} accumulated while profiling."""
+        out = {}
+        for i, nm in enumerate(KERNEL_CLASSES):
+            ms = C.c_double()
+            n = C.c_int64()
+            check(lib().sph_kernel_stats(self.h, i, C.byref(ms), C.byref(n)))
+            out[nm] = (ms.value, n.value)
+        return out
+
+    def kernel_stats_reset(self):
+        check(lib().sph_kernel_stats_reset(self.h))
+
+    def event_record(self, slot):
+        check(lib().sph_event_record(self.h, slot))
+
+    def event_elapsed(self, a, b) -> float:
+        ms = C.c_double()
+        check(lib().sph_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
 
 
 # ------------------------------------------------------------------ System

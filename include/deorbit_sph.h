@@ -236,8 +236,22 @@ int sph_launch_count(sph_ctx* ctx, int64_t* launches);
 /* CUDA-event phase times of the last step in ms: [kick+sort, density, eos,
  * force, damage+finish+dt] (mirrors gpu_ic's PROFILE line, gpu_ic.cpp:147). */
 int sph_phase_times(sph_ctx* ctx, double ms[5]);
-/* Opt-in CUDA-event timing of the phases (off by default). */
+/* Opt-in CUDA-event timing of the phases and kernel classes (off by default;
+ * adds one host wait per step while on). */
 int sph_set_profiling(sph_ctx* ctx, int32_t on);
+/* Kernel classes for sph_kernel_stats. */
+enum sph_kernel_class {
+    SPH_K_KICK = 0, SPH_K_SORT, SPH_K_GRID, SPH_K_LIST_DENSITY, SPH_K_DENSITY, SPH_K_EOS,
+    SPH_K_LIST_FORCE, SPH_K_FORCE, SPH_K_DAMAGE, SPH_K_FINISH, SPH_K_DT, SPH_K_OTHER, SPH_K_COUNT
+};
+/* Accumulated device time (CUDA events on the context stream) and launch count
+ * of one kernel class while profiling was on. */
+int sph_kernel_stats(sph_ctx* ctx, int32_t kernel_class, double* total_ms, int64_t* launches);
+int sph_kernel_stats_reset(sph_ctx* ctx);
+/* CUDA events on the context's stream, slots 0..15, for device-side timing of
+ * any span of calls; elapsed waits for the later event. */
+int sph_event_record(sph_ctx* ctx, int32_t slot);
+int sph_event_elapsed(sph_ctx* ctx, int32_t slot_a, int32_t slot_b, double* ms);
 
 #ifdef __cplusplus
 }
