@@ -1,0 +1,124 @@
+"""Autotuner for the neighbour-search shape of the SPH engine.
+
+Chooses, per (GPU, precision, workload class), the traversal cell width (as a
+multiple of h_init), the neighbour-list builder (one thread per particle or one
+warp per target cell) and the thread-block size, by timing a few KDK steps of
+a representative workload with CUDA events on the engine stream.  Results are
+cached in a JSON file so a run pays for the search once per class.
+
+A workload class is (strength on/off, particles per impact rounded to a power
+of two); classes share a configuration because the cost drivers -- particles
+per cell and neighbours per particle -- depend on those and not on geometry.
+"""
+from __future__ import annotations
+
+import itertools
+import json
+import math
+import os
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CACHE = os.environ.get("DEORBIT_SPH_TUNE_CACHE", os.path.join(HERE, "_tune", "autotune.json"))
+
+CELL_FACTORS = (0.75, 1.0, 1.5)
+SLACKS = (0.05, 0.1)
+BLOCKS = (128, 256)
+
+
+def gpu_name(device=0) -> str:
+    try:
+        import torch
+        return torch.cuda.get_device_name(device)
+    except Exception:
+        return "unknown-gpu"
+
+
+def workload_class(sc, per_impact_n=None) -> str:
+    n = per_impact_n if per_impact_n is not None else sc.n
+    strength = int(bool(sc.params.get("damage_on", 0)) or any(m.get("G", 0) > 0 for m in sc.materials))
+    return f"s{strength}_n2^{int(round(math.log2(max(n, 2))))}"
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _save(d):
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    tmp = CACHE + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(d, f, indent=1, sort_keys=True)
+    os.replace(tmp, CACHE)
+
+
+def key(precision, cls, device=0) -> str:
+    return f"{gpu_name(device)}|p{precision}|{cls}"
+
+
+def measure(sc, precision, cfg, device=0, steps=3, warmup=2) -> float:
+    """ms per KDK step of `sc` under configuration cfg (dict of engine options)."""
+    from . import ic, sph
+
+    ctx = sph.Context(precision, device)
+    try:
+        ctx.set_tuning(cfg.get("block", 0), cfg.get("cell_factor", 0.0))
+        ctx.set_option("slack", cfg.get("slack", 0.08))
+        ic.to_context(ctx, sc)
+        ctx.init()
+        for _ in range(warmup):
+            ctx.run(1)
+        ctx.event_record(0)
+        ctx.run(steps)
+        ctx.event_record(1)
+        return ctx.event_elapsed(0, 1) / steps
+    finally:
+        ctx.close()
+
+
+def tune(sc, precision, device=0, steps=3, warmup=2, candidates=None, force=False, verbose=False):
+    """Search the candidates on `sc`, cache and return (best_cfg, table)."""
+    cls = workload_class(sc)
+    k = key(precision, cls, device)
+    cache = _load()
+    if not force and k in cache:
+        return cache[k]["best"], cache[k]["table"]
+    if candidates is None:
+        candidates = [dict(slack=sl, cell_factor=f, block=b)
+                      for sl, f, b in itertools.product(SLACKS, CELL_FACTORS, BLOCKS)]
+    table = []
+    for cfg in candidates:
+        t0 = time.perf_counter()
+        try:
+            ms = measure(sc, precision, cfg, device, steps, warmup)
+        except Exception as e:  # a shape that cannot run is skipped, not fatal
+            ms = float("inf")
+            cfg = dict(cfg, error=str(e))
+        table.append(dict(cfg, ms_per_step=ms))
+        if verbose:
+            print(f"  {cfg} -> {ms:.3f} ms/step ({time.perf_counter() - t0:.1f} s)", flush=True)
+    best = min(table, key=lambda r: r["ms_per_step"])
+    best = {k2: best[k2] for k2 in ("slack", "cell_factor", "block")}
+    cache[k] = {"best": best, "table": table, "n": sc.n, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
+    _save(cache)
+    return best, table
+
+
+def lookup(sc, precision, device=0, per_impact_n=None):
+    """Cached best configuration for this workload class, or None."""
+    cache = _load()
+    e = cache.get(key(precision, workload_class(sc, per_impact_n), device))
+    return None if e is None else e["best"]
+
+
+def apply(ctx, sc, precision, device=0, per_impact_n=None, default=None):
+    """Configure a fresh context from the cache (or `default`)."""
+    cfg = lookup(sc, precision, device, per_impact_n) or default
+    if cfg:
+        ctx.set_tuning(int(cfg.get("block", 0)), float(cfg.get("cell_factor", 0.0)))
+        ctx.set_option("slack", cfg.get("slack", 0.08))
+    return cfg

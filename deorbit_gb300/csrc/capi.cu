@@ -652,6 +652,21 @@ int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor) {
     return guard([&] { E(ctx).set_tuning(block_threads, cell_factor); });
 }
 
+int sph_set_option(sph_ctx* ctx, const char* key, double value) {
+    return guard([&] {
+        need(key, "key");
+        E(ctx).set_option(key, value);
+    });
+}
+
+int sph_get_option(sph_ctx* ctx, const char* key, double* value) {
+    return guard([&] {
+        need(key, "key");
+        need(value, "value");
+        *value = E(ctx).get_option(key);
+    });
+}
+
 int sph_launch_count(sph_ctx* ctx, int64_t* launches) {
     return guard([&] {
         need(launches, "launches");

@@ -59,6 +59,8 @@ public:
     virtual int64_t debug_neighbors(int b, int kind, int32_t* counts, int32_t* ids,
                                     int64_t cap) = 0;
     virtual void set_tuning(int block, double cell_factor) = 0;
+    virtual void set_option(const char* key, double value) = 0;
+    virtual double get_option(const char* key) = 0;
     virtual int64_t launches() = 0;
     virtual void phase_times(double ms[5]) = 0;
     virtual void set_profiling(int on) = 0;

@@ -160,10 +160,10 @@ static __global__ void k_set_mask_dt(ImpactD* imps, int nimp, const int32_t* mas
 template <class R>
 class Engine final : public EngineBase {
 public:
-    static constexpr int kNR = 24;   // carried R columns
-    static constexpr int kND = 4;    // carried FP64 columns
+    static constexpr int kNR = 21;   // carried R columns
+    static constexpr int kND = 7;    // carried FP64 columns: x y z u vx vy vz
     static constexpr int kNDer = 19; // derived R columns
-    enum { RC_VX, RC_VY, RC_VZ, RC_AX, RC_AY, RC_AZ, RC_DUDT, RC_MASS, RC_HH, RC_D, RC_EPSACT,
+    enum { RC_AX, RC_AY, RC_AZ, RC_DUDT, RC_MASS, RC_HH, RC_D, RC_EPSACT,
            RC_H0, RC_S0, RC_DS0 = RC_S0 + 6 };
     enum { DR_RHO, DR_P, DR_CS, DR_CSIG, DR_PF, DR_DSCALE, DR_RART, DR_SIGMAX, DR_EPSW, DR_PFR2,
            DR_DSR2, DR_VOL, DR_DUDTN, DR_DSN0 };
@@ -192,6 +192,8 @@ public:
         DSPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
         DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
+        DSPH_CUDA(cudaMalloc(&ne_count_, sizeof(int32_t)));
+        DSPH_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
         DSPH_CUDA(cudaMallocHost(&flags_h_, sizeof(int32_t) * 4));
         DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t) * 4, st_));
         for (int i = 0; i < 6; i++) DSPH_CUDA(cudaEventCreate(&ev_[i]));
@@ -204,6 +206,7 @@ public:
         for (void* p : allocs_) cudaFree(p);
         cudaFree(mats_d_);
         cudaFree(flags_d_);
+        cudaFree(ne_count_);
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
         for (auto& e : prof_pool_) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -414,6 +417,7 @@ public:
         if (!any) return;
         set_masks(mask, nullptr, nullptr);
         sort_reorder(true);
+        build_list<kListSuperset>(true);
         density_rounds(2, true);
         forces(true);
         launch_n(k_adopt_derivatives<R>, N_);
@@ -438,6 +442,7 @@ public:
             if (imp_[b].used && imp_[b].alive && imp_[b].committed) mask[b] = 1;
         set_masks(mask, &dts, nullptr);
         one_step(true);
+        grow_lists_after_overflow();
         pull_table();
         for (size_t b = 0; b < imp_.size(); b++)
             if (mask[b]) {
@@ -458,14 +463,15 @@ public:
         cls(KC_KICK);
         launch_n(k_kick_drift<R>, N_);
         sort_reorder(false);
+        cls(KC_LIST_DENSITY);
+        build_list<kListSuperset>(false);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[1], st_));
         density_rounds(2, host_sync);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[2], st_));
+        if (host_sync) refresh_list_if_needed();
         cls(KC_EOS);
         launch_n(k_eos<R>, N_);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[3], st_));
-        cls(KC_LIST_FORCE);
-        build_list<kListForce>(true);
         cls(KC_FORCE);
         launch_n(k_force<R>, N_, 128);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[4], st_));
@@ -516,7 +522,8 @@ public:
         const int nimp = (int)imp_.size();
         for (int s = 0; s < nsteps; s++) {
             launch_small(k_run_control, nimp, 0);
-            one_step(false);
+            one_step(true);
+            grow_lists_after_overflow();
         }
         pull_table();
         for (size_t b = 0; b < imp_.size(); b++)
@@ -532,6 +539,7 @@ public:
         commit();
         set_all_masks();
         sort_reorder(true);
+        build_list<kListSuperset>(true);
         density_rounds(iters, true);
         check_async();
     }
@@ -541,6 +549,7 @@ public:
         set_all_masks();
         if (!grid_valid_) {
             sort_reorder(true);
+            build_list<kListSuperset>(true);
             final_grid_build();
         }
         forces(true);
@@ -735,6 +744,36 @@ public:
             cell_factor_ = cell_factor;
         }
     }
+    void set_option(const char* key, double value) override {
+        std::string k(key);
+        if (k == "list_mode") {
+            if (value != 0) throw SphError(SPH_ERR_ARG, "list_mode 0 (thread per particle) is the only builder");
+            list_mode_ = 0;
+        } else if (k == "slack") {
+            if (!(value >= 0.0 && value <= 1.0)) throw SphError(SPH_ERR_ARG, "slack must be in [0, 1]");
+            slack_ = value;
+            if (!tab_.empty()) {
+                pull_table();
+                for (auto& I : tab_) I.slack = (float)slack_;
+                push_table();
+            }
+        } else if (k == "cell_factor") {
+            set_tuning(0, value);
+        } else if (k == "block") {
+            set_tuning((int)value, 0);
+        } else {
+            throw SphError(SPH_ERR_ARG, "unknown option " + k);
+        }
+    }
+    double get_option(const char* key) override {
+        std::string k(key);
+        if (k == "list_mode") return list_mode_;
+        if (k == "slack") return slack_;
+        if (k == "cell_factor") return cell_factor_;
+        if (k == "block") return block_;
+        if (k == "list_capacity") return cap_nbr_;
+        throw SphError(SPH_ERR_ARG, "unknown option " + k);
+    }
     int64_t launches() override { return launches_; }
     void phase_times(double ms[5]) override { for (int i = 0; i < 5; i++) ms[i] = phase_ms_[i]; }
     void set_profiling(int on) override { profiling_ = on != 0; }
@@ -861,8 +900,8 @@ public:
         v.stride = nbr_stride_;
         v.cap = cap_nbr_;
         v.x = dcol_[cur_][0]; v.y = dcol_[cur_][1]; v.z = dcol_[cur_][2]; v.u = dcol_[cur_][3];
+        v.vx = dcol_[cur_][4]; v.vy = dcol_[cur_][5]; v.vz = dcol_[cur_][6];
         R** r = rcol_[cur_];
-        v.vx = r[RC_VX]; v.vy = r[RC_VY]; v.vz = r[RC_VZ];
         v.ax = r[RC_AX]; v.ay = r[RC_AY]; v.az = r[RC_AZ];
         v.dudt = r[RC_DUDT]; v.mass = r[RC_MASS]; v.hh = r[RC_HH]; v.D = r[RC_D];
         v.eps_act = r[RC_EPSACT]; v.h0 = r[RC_H0];
@@ -874,8 +913,9 @@ public:
         v.dsr2 = der_[DR_DSR2]; v.vol = der_[DR_VOL]; v.dudt_new = der_[DR_DUDTN];
         for (int c = 0; c < 6; c++) v.dS_new[c] = der_[DR_DSN0 + c];
         v.pf = pf_; v.cpk = cpk_; v.refbin = refbin_;
+        v.vh = vh_; v.vl = vl_;
         v.cell_ptr = cell_cnt_;
-        v.nbr = nbr_; v.nbr_cnt = nbr_cnt_;
+        v.nbr = nbr_; v.nbr_cnt = nbr_cnt_; v.hlist = hlist_;
         v.flags = flags_d_;
         v.imps = tab_d_;
         v.mats = mats_d_;
@@ -887,9 +927,9 @@ public:
     template <class F>
     bool with_column(const char* name, F f) {
         std::string s(name);
-        static const char* dn[] = {"x", "y", "z", "u"};
-        for (int c = 0; c < 4; c++) if (s == dn[c]) { f(dcol_[cur_][c]); return true; }
-        static const char* rn[] = {"vx", "vy", "vz", "ax", "ay", "az", "dudt", "mass", "hh", "D",
+        static const char* dn[] = {"x", "y", "z", "u", "vx", "vy", "vz"};
+        for (int c = 0; c < kND; c++) if (s == dn[c]) { f(dcol_[cur_][c]); return true; }
+        static const char* rn[] = {"ax", "ay", "az", "dudt", "mass", "hh", "D",
                                    "eps_act", "h0", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
                                    "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz"};
         for (int c = 0; c < kNR; c++) if (s == rn[c]) { f(rcol_[cur_][c]); return true; }
@@ -940,6 +980,7 @@ public:
         I.use_h0 = h.use_h0 ? 1 : 0;
         double h0m = h.use_h0 ? h.h0max : p.h_init;
         I.hcap = (float)(2.0 * h0m);
+        I.slack = (float)slack_;
         // W polynomial at q = 1/eta, for the artificial-stress ratio W(r)/W(dp)
         double q = 1.0 / p.eta, poly;
         if (q < 1.0) poly = 1.0 - 1.5 * q * q + 0.75 * q * q * q;
@@ -1029,8 +1070,10 @@ public:
         C_ = base;
         if (C_ + 1 > Ccap_) {
             dfree(cell_cnt_);
+            dfree(cell_hmax_);
             Ccap_ = std::max<int64_t>(C_ + 1, (int64_t)(Ccap_ * 1.5));
             cell_cnt_ = dalloc<int32_t>(Ccap_);
+            cell_hmax_ = dalloc<unsigned int>(Ccap_);
         }
         ensure_scratch();
     }
@@ -1118,10 +1161,14 @@ public:
         }
         for (int c = 0; c < kNDer; c++) { dfree(der_[c]); der_[c] = dalloc<R>(nc); }
         dfree(pf_); pf_ = dalloc<float4>(nc);
+        dfree(vh_); vh_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
+        dfree(vl_); vl_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
+        dfree(ne_cells_); ne_cells_ = dalloc<int32_t>(nc);
         dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
         dfree(refbin_); refbin_ = dalloc<unsigned long long>(nc);
         dfree(src_); src_ = dalloc<int32_t>(nc);
         dfree(nbr_cnt_); nbr_cnt_ = dalloc<int32_t>(nc);
+        dfree(hlist_); hlist_ = dalloc<float>(nc);
         // derived columns start at zero so reads before the first force pass are defined
         for (int c = 0; c < kNDer; c++) DSPH_CUDA(cudaMemsetAsync(der_[c], 0, sizeof(R) * nc, st_));
         cap_ = nc;
@@ -1130,7 +1177,7 @@ public:
 
     void alloc_lists() {
         dfree(nbr_);
-        nbr_stride_ = cap_;
+        nbr_stride_ = cap_nbr_;
         nbr_ = dalloc<int32_t>((size_t)cap_ * cap_nbr_);
     }
 
@@ -1188,7 +1235,7 @@ public:
         };
         int c = cur_;
         up(dcol_[c][0], h.sx); up(dcol_[c][1], h.sy); up(dcol_[c][2], h.sz); up(dcol_[c][3], h.su);
-        up(rcol_[c][RC_VX], h.svx); up(rcol_[c][RC_VY], h.svy); up(rcol_[c][RC_VZ], h.svz);
+        up(dcol_[c][4], h.svx); up(dcol_[c][5], h.svy); up(dcol_[c][6], h.svz);
         up(rcol_[c][RC_MASS], h.smass);
         up(rcol_[c][RC_EPSACT], h.seps);
         up(rcol_[c][RC_H0], h.sh0);
@@ -1312,17 +1359,25 @@ public:
         cur_ = alt;
         N_ = n_new;
         launch_small(k_impact_reset_omax, nimp);
-        launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_);
+        DSPH_CUDA(cudaMemsetAsync(ne_count_, 0, sizeof(int32_t), st_));
+        launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_, (const uint32_t*)skeys_, ne_cells_, ne_count_);
         launch_small(k_impact_ranges, nimp, (const int32_t*)cell_cnt_);
         cls(keep_cls);
         grid_valid_ = true;
     }
 
+    // Neighbour lists.  The step uses one superset list (see k_list_thread);
+    // capacity overflow is handled by the consumers' traversal fallback, and
+    // the capacity grows for later steps when host_check reads the overflow.
     template <int KIND>
     void build_list(bool host_check) {
+        if (N_ <= 0) return;
+        const int nimp = (int)imp_.size();
+        if (KIND == kListSuperset) launch_small(k_impact_reset_slack, nimp);
         for (int attempt = 0; attempt < 8; attempt++) {
             DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t), st_));
-            launch_n(k_list<R, KIND>, N_, block_);
+            if (KIND == kListSuperset) DSPH_CUDA(cudaMemsetAsync(flags_d_ + 2, 0, sizeof(int32_t), st_));
+            launch_n(k_list_thread<R, KIND>, N_, block_);
             if (!host_check) return;
             DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
             DSPH_CUDA(cudaStreamSynchronize(st_));
@@ -1331,6 +1386,19 @@ public:
             alloc_lists();
         }
         throw SphError(SPH_ERR_CAPACITY, "neighbour list capacity could not be satisfied");
+    }
+
+    // Rebuild the superset list when some h outgrew its slack (avoids the
+    // consumers' slower traversal fallback).
+    void refresh_list_if_needed() {
+        DSPH_CUDA(cudaMemcpyAsync(flags_h_ + 3, flags_d_ + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        if (flags_h_[3]) {
+            const int keep = cur_cls_;
+            cls(KC_LIST_FORCE);
+            build_list<kListSuperset>(false);
+            cls(keep);
+        }
     }
 
     void hmax_pass(int which) {
@@ -1352,8 +1420,6 @@ public:
             launch_small(k_ref_grid, nimp);
             launch_n(k_ref_bins<R>, N_);
             for (int it = 0; it < iters; it++) {
-                cls(KC_LIST_DENSITY);
-                build_list<kListDensity>(true);
                 cls(KC_DENSITY);
                 launch_n(k_density<R>, N_);
             }
@@ -1380,14 +1446,25 @@ public:
     }
 
     void forces(bool host_check) {
+        if (host_check) refresh_list_if_needed();
+        cls(KC_EOS);
         launch_n(k_eos<R>, N_);
-        build_list<kListForce>(host_check);
+        cls(KC_FORCE);
         launch_n(k_force<R>, N_, 128);
     }
 
     void dt_reduce() {
         launch_small(k_dt_begin, (int)imp_.size());
         launch_n(k_dt<R>, N_);
+    }
+
+    void grow_lists_after_overflow() {
+        DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        if (flags_h_[0] > cap_nbr_) {
+            cap_nbr_ = (int)(flags_h_[0] * 1.25) + 8;
+            alloc_lists();
+        }
     }
 
     void record_phases() {
@@ -1420,6 +1497,12 @@ public:
     int32_t* gid_[2] = {};
     R* der_[kNDer] = {};
     float4* pf_ = nullptr;
+    float4* vh_ = nullptr;
+    float4* vl_ = nullptr;
+    int32_t* ne_cells_ = nullptr;
+    int32_t* ne_count_ = nullptr;
+    unsigned int* cell_hmax_ = nullptr;
+    int nsm_ = 148;
     uint32_t* cpk_ = nullptr;
     unsigned long long* refbin_ = nullptr;
     int32_t* src_ = nullptr;
@@ -1428,8 +1511,10 @@ public:
     int32_t* cell_cnt_ = nullptr;
     int32_t* nbr_ = nullptr;
     int32_t* nbr_cnt_ = nullptr;
+    float* hlist_ = nullptr;
+    double slack_ = 0.08;
     int64_t nbr_stride_ = 0;
-    int cap_nbr_ = 160;
+    int cap_nbr_ = 192;
     int32_t* flags_d_ = nullptr;
     int32_t* flags_h_ = nullptr;
     void* scratch_ = nullptr;
@@ -1442,6 +1527,7 @@ public:
     R* flaw_eps_d_ = nullptr;
     int block_ = 128;
     double cell_factor_ = 1.0;
+    int list_mode_ = 0;   // 0: thread per particle, 1: warp per target cell
     int64_t launches_ = 0;
     bool profiling_ = false;
     cudaEvent_t ev_[6]{};

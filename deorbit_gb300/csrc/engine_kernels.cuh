@@ -2,14 +2,14 @@
 //
 // Data layout (HBM, structure of arrays, sorted by (impact, traversal cell,
 // original id) at every step):
-//   carried state      x y z u (FP64); vel, acc, dudt, mass, h, D, eps_act, h0,
-//                      S[6], dSdt[6] (type R); mat, fixed (u8); impact (u16); gid (i32)
+//   carried state      x y z u vx vy vz (FP64); acc, dudt, mass, h, D, eps_act,
+//                      h0, S[6], dSdt[6] (type R); mat, fixed (u8); impact (u16); gid (i32)
 //   derived per step   rho P cs csig Pf dscale Rart sigmax eps_work,
 //                      Pf/rho^2, dscale/rho^2, m/rho, new dudt, new dSdt[6]
 //   geometry           pf = float4(offset from own traversal-cell origin, h),
 //                      cpk = packed traversal-cell coordinates,
 //                      refbin = packed reference-grid bins (sph.hpp:142-146)
-//   neighbour lists    column-major nbr[t * stride + k], count per particle
+//   neighbour lists    row-major nbr[k * cap + t], count per particle
 //
 // Reference semantics kept exactly: the neighbour criteria r < 2 h_i (density,
 // self included, sph.hpp:193) and j != i, r < 2 hbar, r != 0 (sph.hpp:222,287),
@@ -30,6 +30,7 @@ namespace dsph {
 constexpr uint32_t kInvalidKey = 0xffffffffu;
 constexpr int kListDensity = 0;
 constexpr int kListForce = 1;
+constexpr int kListSuperset = 2;
 
 // Per-impact parameters and per-step scalars, resident on the device.
 struct ImpactD {
@@ -49,7 +50,9 @@ struct ImpactD {
     float hmax_f, margin;
     double inv_poly_eta;                           // 1 / W-polynomial at q = 1/eta
     float hcap;                                    // upper bound of h (2 max h0)
-    int32_t pad0;
+    float cwmin;                                   // smallest reference cell width (nc > 1)
+    float slack;                                   // superset-list radius slack
+    int32_t slack_flag;                            // some h outgrew the list slack
     // step scalars
     double dt, t, t_end;
     int64_t nsteps;
@@ -65,8 +68,8 @@ struct View {
     int64_t stride;     // neighbour list column stride
     int32_t cap;        // neighbour list capacity per particle
     int32_t pad;
-    double *x, *y, *z, *u;
-    R *vx, *vy, *vz, *ax, *ay, *az, *dudt, *mass, *hh, *D, *eps_act, *h0;
+    double *x, *y, *z, *u, *vx, *vy, *vz;
+    R *ax, *ay, *az, *dudt, *mass, *hh, *D, *eps_act, *h0;
     R* S[6];
     R* dS[6];
     uint8_t *mat, *fixed;
@@ -75,11 +78,13 @@ struct View {
     R *rho, *P, *cs, *csig, *Pf, *dscale, *Rart, *sigmax, *epsw, *pfr2, *dsr2, *vol, *dudt_new;
     R* dS_new[6];
     float4* pf;
+    float4 *vh, *vl;     // mixed form: FP64 velocity split into FP32 hi + lo
     uint32_t* cpk;
     unsigned long long* refbin;
     const int32_t* cell_ptr;
     int32_t* nbr;
     int32_t* nbr_cnt;
+    float* hlist;       // h of each particle when its list was built
     int32_t* flags;     // [0] list overflow max, [1] any impact still in a density round
     ImpactD* imps;
     const MatT<R>* mats;
@@ -282,16 +287,16 @@ static __global__ void k_kick_drift(View<R> v) {
     const ImpactD& I = v.imps[v.imp[k]];
     if (!I.mask || v.fixed[k]) return;
     const double dt = I.dt;
-    const R hd = (R)(0.5 * dt);
-    R vx = v.vx[k] + v.ax[k] * hd;
-    R vy = v.vy[k] + v.ay[k] * hd;
-    R vz = v.vz[k] + v.az[k] * hd;
+    const double hd = 0.5 * dt;
+    double vx = v.vx[k] + (double)v.ax[k] * hd;
+    double vy = v.vy[k] + (double)v.ay[k] * hd;
+    double vz = v.vz[k] + (double)v.az[k] * hd;
     v.vx[k] = vx;
     v.vy[k] = vy;
     v.vz[k] = vz;
-    v.x[k] += (double)vx * dt;
-    v.y[k] += (double)vy * dt;
-    v.z[k] += (double)vz * dt;
+    v.x[k] += vx * dt;
+    v.y[k] += vy * dt;
+    v.z[k] += vz * dt;
 }
 
 __device__ __forceinline__ int fine_cell(const ImpactD& I, int a, double c, double& frac) {
@@ -330,8 +335,8 @@ static __global__ void k_make_src(int64_t n, const int32_t* sorted_gid, const in
 
 // Gather of all carried columns into sorted order.
 struct GatherCols {
-    const double* din[4];
-    double* dout[4];
+    const double* din[7];
+    double* dout[7];
     const void* rin[24];
     void* rout[24];
     int nr;
@@ -349,7 +354,7 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
     if (k >= n) return;
     int64_t s = src[k];
 #pragma unroll
-    for (int c = 0; c < 4; c++) g.dout[c][k] = g.din[c][s];
+    for (int c = 0; c < 7; c++) g.dout[c][k] = g.din[c][s];
     for (int c = 0; c < g.nr; c++) static_cast<R*>(g.rout[c])[k] = static_cast<const R*>(g.rin[c])[s];
     g.b_out[0][k] = g.b_in[0][s];
     g.b_out[1][k] = g.b_in[1][s];
@@ -360,10 +365,12 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
 // After the gather: inverse permutation, traversal-cell coordinates and FP32
 // offsets from the cell origin, largest |offset| per impact.
 template <class R>
-static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid) {
+static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid, const uint32_t* skey,
+                                   int32_t* ne_cells, int32_t* ne_count) {
     int64_t k = gtid();
     if (k >= v.n) return;
     pos_of_gid[v.gid[k]] = (int32_t)k;
+    if (k == 0 || skey[k] != skey[k - 1]) ne_cells[atomicAdd(ne_count, 1)] = (int32_t)skey[k];
     ImpactD& I = v.imps[v.imp[k]];
     double fx, fy, fz;
     int cx = fine_cell(I, 0, v.x[k], fx);
@@ -392,6 +399,11 @@ static __global__ void k_impact_ranges(ImpactD* imps, int nimp, const int32_t* c
 }
 
 // Phase flags: 0 = clear reductions for masked impacts.
+static __global__ void k_impact_reset_slack(ImpactD* imps, int nimp) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nimp && imps[b].mask) imps[b].slack_flag = 0;
+}
+
 static __global__ void k_impact_begin_round(ImpactD* imps, int nimp, int set_active) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nimp) return;
@@ -434,6 +446,10 @@ static __global__ void k_ref_grid(ImpactD* imps, int nimp) {
         I.nc[a] = m;
         I.cw[a] = __ddiv_rn(ext, (double)m);
     }
+    float cwm = 3.0e38f;
+    for (int a = 0; a < 3; a++)
+        if (I.nc[a] > 1) cwm = fminf(cwm, (float)I.cw[a]);
+    I.cwmin = cwm;
     I.hm_bits = 0x3bc79ca10c924223ull;
 }
 
@@ -465,10 +481,17 @@ static __global__ void k_round_check(ImpactD* imps, int nimp, int32_t* flags) {
     }
 }
 
-// Neighbour-list build (FP32 filter; exact criteria applied by the consumer in
-// the FP64 form, or as the criterion itself in the mixed form).
+// Neighbour-list build, one thread per target particle: each thread walks the
+// cell columns of its own search sphere with an FP32 distance test.
+//   kListSuperset (used by the step): one list per step holding every j with
+//     r < max(2 h_i, h_i + h_j) (1 + slack) -- a superset of the density sets
+//     {r < 2 h_i} and the force sets {r < h_i + h_j} for as long as no h grows
+//     by more than the slack; the consumers apply the exact criteria and the
+//     reference-stencil restriction, and fall back to a direct traversal when
+//     a particle outgrows the slack.
+//   kListDensity / kListForce: the exact sets (with the FP64 form's margin).
 template <class R, int KIND>
-static __global__ void k_list(View<R> v) {
+static __global__ void k_list_thread(View<R> v) {
     int64_t k = gtid();
     if (k >= v.n) return;
     const ImpactD& I = v.imps[v.imp[k]];
@@ -478,10 +501,15 @@ static __global__ void k_list(View<R> v) {
     const unsigned long long bi = v.refbin[k];
     const bool exact = sizeof(R) == 8;
     const float m = exact ? I.margin : 0.0f;
-    const float Rs = (KIND == kListDensity ? 2.0f * pi.w : pi.w + I.hmax_f) + m + (exact ? m : 0.0f);
+    const float sl = 1.0f + I.slack;
+    float Rs;
+    if (KIND == kListSuperset) Rs = fmaxf(2.0f * pi.w, pi.w + I.hmax_f) * sl + 2.0f * I.margin + 1e-6f * pi.w;
+    else Rs = (KIND == kListDensity ? 2.0f * pi.w : pi.w + I.hmax_f) + 2.0f * m;
+    const bool need_member = KIND != kListSuperset && Rs >= I.cwmin * 0.999f;
     const float lim_d = 2.0f * pi.w + m;
     int cnt = 0;
     const int cap = v.cap;
+    int32_t* out = v.nbr + (int64_t)k * cap;
     traverse(v, I, pi, ci, Rs, [&](int32_t j, float dxc, float dyc, float dzc) {
         float4 pj = v.pf[j];
         float dx = (pi.x - pj.x) + dxc;
@@ -491,54 +519,103 @@ static __global__ void k_list(View<R> v) {
         if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
         if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
         float r2 = dx * dx + dy * dy + dz * dz;
-        float lim = KIND == kListDensity ? lim_d : (pi.w + pj.w + m);
+        float lim;
+        if (KIND == kListSuperset) lim = fmaxf(2.0f * pi.w, pi.w + pj.w) * sl + I.margin + 1e-6f * pi.w;
+        else lim = KIND == kListDensity ? lim_d : (pi.w + pj.w + m);
         bool take = r2 < lim * lim;
         if (KIND == kListForce) take = take && (j != (int32_t)k) && (exact || r2 > 0.0f);
-        if (take && ref_member(bi, v.refbin[j], I)) {
-            if (cnt < cap) v.nbr[(int64_t)cnt * v.stride + k] = j;
+        if (take && (!need_member || ref_member(bi, v.refbin[j], I))) {
+            if (cnt < cap) out[cnt] = j;
             cnt++;
         }
     });
     v.nbr_cnt[k] = cnt;
+    if (KIND == kListSuperset) v.hlist[k] = pi.w;
     if (cnt > cap) atomicMax(&v.flags[0], cnt);
 }
 
-// Density sum and h update (sph.hpp:189-201).
+template <class R>
+struct Kahan {
+    R s, c;
+    __device__ __forceinline__ void init() { s = R(0); c = R(0); }
+    __device__ __forceinline__ void add(R x) {
+        R y = x - c;
+        R t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ R value() const { return s; }
+};
+template <class R>
+struct Plain {
+    R s;
+    __device__ __forceinline__ void init() { s = R(0); }
+    __device__ __forceinline__ void add(R x) { s += x; }
+    __device__ __forceinline__ R value() const { return s; }
+};
+template <class R>
+using AccT = typename std::conditional<sizeof(R) == 4, Kahan<R>, Plain<R>>::type;
+
+// Does particle k's superset list still cover it (count within capacity and h
+// within the slack, with an allowance for the FP32 distance)?
+template <class R>
+__device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, int64_t k, float h_now) {
+    return v.nbr_cnt[k] <= v.cap && h_now <= v.hlist[k] * (1.0f + I.slack) * 0.99999f;
+}
+
+// Density sum and h update (sph.hpp:189-201).  Criterion r < 2 h_i (self
+// included) within the reference stencil; compensated sum in the mixed form.
 template <class R>
 static __global__ void k_density(View<R> v) {
     int64_t k = gtid();
     if (k >= v.n) return;
-    const ImpactD& I = v.imps[v.imp[k]];
+    ImpactD& I = v.imps[v.imp[k]];
     if (!(I.mask && I.active)) return;
     const R hi = v.hh[k];
     const R ihi = R(1) / hi;
-    const int cnt = min(v.nbr_cnt[k], v.cap);
-    R sum = R(0);
-    if (sizeof(R) == 8) {
-        const double two_h = 2.0 * (double)hi;
-        for (int t = 0; t < cnt; t++) {
-            int32_t j = v.nbr[(int64_t)t * v.stride + k];
+    const float4 pi = v.pf[k];
+    const uint32_t ci = v.cpk[k];
+    const unsigned long long bi = v.refbin[k];
+    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const bool need_member = 2.0f * (float)hi + 2.0f * m >= I.cwmin * 0.999f;
+    AccT<R> sum;
+    sum.init();
+    auto body = [&](int32_t j) {
+        R r;
+        if (sizeof(R) == 8) {
             double dx, dy, dz;
-            double r = sep_exact(v, I, k, j, dx, dy, dz);
-            if (r < two_h) sum += v.mass[j] * kernel_W_ih<R>((R)r, ihi);
-        }
-    } else {
-        const float4 pi = v.pf[k];
-        const uint32_t ci = v.cpk[k];
-        for (int t = 0; t < cnt; t++) {
-            int32_t j = v.nbr[(int64_t)t * v.stride + k];
+            double rr = sep_exact(v, I, k, j, dx, dy, dz);
+            if (!(rr < 2.0 * (double)hi)) return;
+            r = (R)rr;
+        } else {
             float dx, dy, dz;
             sep_f32(I, pi, ci, v.pf[j], v.cpk[j], dx, dy, dz);
-            float r = sqrtf(dx * dx + dy * dy + dz * dz);
-            sum += v.mass[j] * kernel_W_ih<R>((R)r, ihi);
+            float r2 = dx * dx + dy * dy + dz * dz;
+            float th = 2.0f * (float)hi;
+            if (!(r2 < th * th)) return;
+            r = (R)sqrtf(r2);
         }
+        if (need_member && !ref_member(bi, v.refbin[j], I)) return;
+        sum.add(v.mass[j] * kernel_W_ih<R>(r, ihi));
+    };
+    if (list_covers(v, I, k, (float)hi)) {
+        const int cnt = v.nbr_cnt[k];
+        const int32_t* lst = v.nbr + (int64_t)k * v.cap;
+        for (int t = 0; t < cnt; t++) body(lst[t]);
+    } else {
+        traverse(v, I, pi, ci, 2.0f * pi.w * 1.0001f + 2.0f * I.margin + 1e-6f * pi.w,
+                 [&](int32_t j, float, float, float) { body(j); });
     }
-    R rho = rmax(sum, R(1e-30));
+    R rho = rmax(sum.value(), R(1e-30));
     v.rho[k] = rho;
     R h0 = I.use_h0 ? v.h0[k] : (R)I.h_init;
     R hn = rmin(R(2) * h0, rmax(R(0.5) * h0, (R)I.eta * rcbrt(v.mass[k] / rho)));
     v.hh[k] = hn;
     v.pf[k].w = (float)hn;
+    if (!((float)hn <= v.hlist[k] * (1.0f + I.slack) * 0.99999f)) {
+        atomicOr(&I.slack_flag, 1);
+        atomicOr(&v.flags[2], 1);
+    }
 }
 
 // EOS + damage pre-pass (sph.hpp:261-275) and per-particle factors reused by
@@ -570,34 +647,20 @@ static __global__ void k_eos(View<R> v) {
     v.pfr2[k] = pf * irho2;
     v.dsr2[k] = irho2 * dsc;
     v.vol[k] = v.mass[k] / rho;
-}
-
-template <class R>
-struct Kahan {
-    R s, c;
-    __device__ __forceinline__ void init() { s = R(0); c = R(0); }
-    __device__ __forceinline__ void add(R x) {
-        R y = x - c;
-        R t = s + y;
-        c = (t - s) - y;
-        s = t;
+    if (sizeof(R) == 4) {
+        const double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k];
+        const float hx = (float)vx, hy = (float)vy, hz = (float)vz;
+        v.vh[k] = make_float4(hx, hy, hz, 0.0f);
+        v.vl[k] = make_float4((float)(vx - (double)hx), (float)(vy - (double)hy), (float)(vz - (double)hz), 0.0f);
     }
-    __device__ __forceinline__ R value() const { return s; }
-};
-template <class R>
-struct Plain {
-    R s;
-    __device__ __forceinline__ void init() { s = R(0); }
-    __device__ __forceinline__ void add(R x) { s += x; }
-    __device__ __forceinline__ R value() const { return s; }
-};
+}
 
 // Velocity gradient -> Jaumann dS/dt and deviatoric power (sph.hpp:212-258)
 // fused with the momentum / energy pair loop (sph.hpp:277-317).  Writes acc,
 // the new dudt and dSdt, eps_work.
 template <class R>
 static __global__ void __launch_bounds__(128) k_force(View<R> v) {
-    using Acc = typename std::conditional<sizeof(R) == 4, Kahan<R>, Plain<R>>::type;
+    using Acc = AccT<R>;
     int64_t k = gtid();
     if (k >= v.n) return;
     const ImpactD& I = v.imps[v.imp[k]];
@@ -608,40 +671,55 @@ static __global__ void __launch_bounds__(128) k_force(View<R> v) {
     const R alpha_u = (R)I.alpha_u;
     const R hi = v.hh[k], rhoi = v.rho[k], csi = v.csig[k], Pi_over = v.pfr2[k];
     const R dsri = v.dsr2[k], di = v.dscale[k], Rai = v.Rart[k];
-    const R vxi = v.vx[k], vyi = v.vy[k], vzi = v.vz[k];
+    const double vxi = v.vx[k], vyi = v.vy[k], vzi = v.vz[k];
+    float4 vhi = make_float4(0, 0, 0, 0), vli = vhi;
+    if (sizeof(R) == 4) { vhi = v.vh[k]; vli = v.vl[k]; }
     const R sxx = v.S[0][k], syy = v.S[1][k], szz = v.S[2][k];
     const R sxy = v.S[3][k], sxz = v.S[4][k], syz = v.S[5][k];
     const R Pi = v.P[k], ui = (R)v.u[k];
     R L00 = 0, L01 = 0, L02 = 0, L10 = 0, L11 = 0, L12 = 0, L20 = 0, L21 = 0, L22 = 0;
     Acc ax, ay, az, du;
     ax.init(); ay.init(); az.init(); du.init();
-    const int cnt = min(v.nbr_cnt[k], v.cap);
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
-    for (int t = 0; t < cnt; t++) {
-        const int32_t j = v.nbr[(int64_t)t * v.stride + k];
+    const unsigned long long bi = v.refbin[k];
+    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const bool need_member = (float)hi + I.hmax_f + 2.0f * m >= I.cwmin * 0.999f;
+    auto body = [&](int32_t j) {
+        if (j == (int32_t)k) return;
         const R hj = v.hh[j];
         R rx, ry, rz, r;
         if (sizeof(R) == 8) {
             double dx, dy, dz;
             double rr = sep_exact(v, I, k, j, dx, dy, dz);
             double hsum = __dadd_rn((double)hi, (double)hj);
-            if (rr >= hsum || rr == 0.0 || j == (int32_t)k) continue;
+            if (rr >= hsum || rr == 0.0) return;
             rx = (R)dx; ry = (R)dy; rz = (R)dz; r = (R)rr;
         } else {
             float dx, dy, dz;
             sep_f32(I, pi, ci, v.pf[j], v.cpk[j], dx, dy, dz);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float hs = (float)hi + (float)hj;
+            if (!(r2 < hs * hs) || r2 == 0.0f) return;
             rx = (R)dx; ry = (R)dy; rz = (R)dz;
-            r = (R)sqrtf(dx * dx + dy * dy + dz * dz);
+            r = (R)sqrtf(r2);
         }
+        if (need_member && !ref_member(bi, v.refbin[j], I)) return;
         const R hbar = R(0.5) * (hi + hj);
         const R ihb = R(1) / hbar;
         const R ir = R(1) / r;
         const R dW = kernel_dW<R>(r, ihb);
         const R wg = dW * ir;
         const R gx = rx * wg, gy = ry * wg, gz = rz * wg;
-        const R vxj = v.vx[j], vyj = v.vy[j], vzj = v.vz[j];
-        const R vx = vxi - vxj, vy = vyi - vyj, vz = vzi - vzj;
+        R vx, vy, vz;  // v_i - v_j
+        if (sizeof(R) == 8) {
+            vx = (R)(vxi - v.vx[j]); vy = (R)(vyi - v.vy[j]); vz = (R)(vzi - v.vz[j]);
+        } else {  // hi parts nearly cancel exactly; lo parts restore the FP64 difference
+            const float4 vhj = v.vh[j], vlj = v.vl[j];
+            vx = (R)((vhi.x - vhj.x) + (vli.x - vlj.x));
+            vy = (R)((vhi.y - vhj.y) + (vli.y - vlj.y));
+            vz = (R)((vhi.z - vhj.z) + (vli.z - vlj.z));
+        }
         if (strength) {
             const R Vj = v.vol[j];
             const R ex = -vx * Vj, ey = -vy * Vj, ez = -vz * Vj;  // Vj (v_j - v_i)
@@ -687,6 +765,14 @@ static __global__ void __launch_bounds__(128) k_force(View<R> v) {
             const R vsig = rsqrt_(rabs(Pi - v.P[j]) / rbar);
             du.add(alpha_u * mj * vsig * (ui - (R)v.u[j]) * dW / rbar);
         }
+    };
+    if (!I.slack_flag && v.nbr_cnt[k] <= v.cap) {
+        const int cnt = v.nbr_cnt[k];
+        const int32_t* lst = v.nbr + (int64_t)k * v.cap;
+        for (int t = 0; t < cnt; t++) body(lst[t]);
+    } else {
+        traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
+                 [&](int32_t j, float, float, float) { body(j); });
     }
     R epsw = R(0);
     if (strength) {
@@ -768,9 +854,9 @@ static __global__ void k_finish(View<R> v) {
     if (!v.fixed[k]) {
         const double dt = I.dt;
         const R hd = (R)(0.5 * dt);
-        v.vx[k] += v.ax[k] * hd;
-        v.vy[k] += v.ay[k] * hd;
-        v.vz[k] += v.az[k] * hd;
+        v.vx[k] += (double)v.ax[k] * (0.5 * dt);
+        v.vy[k] += (double)v.ay[k] * (0.5 * dt);
+        v.vz[k] += (double)v.az[k] * (0.5 * dt);
         double u = v.u[k] + (0.5 * dt) * ((double)v.dudt[k] + (double)dn);
         if (u < 1e-12) u = 1e-12;
         v.u[k] = u;

@@ -111,6 +111,8 @@ _SIGS = {
     "sph_load_checkpoint": (C.c_int, [_P, C.c_char_p, C.POINTER(Params), _I32, _D]),
     "sph_set_tuning": (C.c_int, [_P, C.c_int32, C.c_double]),
     "sph_launch_count": (C.c_int, [_P, _I64]),
+    "sph_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),
+    "sph_get_option": (C.c_int, [_P, C.c_char_p, _D]),
     "sph_phase_times": (C.c_int, [_P, _D]),
     "sph_set_profiling": (C.c_int, [_P, C.c_int32]),
     "sph_kernel_stats": (C.c_int, [_P, C.c_int32, _D, _I64]),
@@ -429,6 +431,14 @@ class Context:
 
     def set_tuning(self, block=0, cell_factor=0.0):
         check(lib().sph_set_tuning(self.h, block, cell_factor))
+
+    def set_option(self, key, value):
+        check(lib().sph_set_option(self.h, key.encode(), float(value)))
+
+    def get_option(self, key) -> float:
+        v = C.c_double()
+        check(lib().sph_get_option(self.h, key.encode(), C.byref(v)))
+        return v.value
 
     def launches(self) -> int:
         v = C.c_int64()

@@ -231,6 +231,11 @@ int sph_load_checkpoint(sph_ctx* ctx, const char* path, const sph_params* p, int
 /* Launch shape of the neighbour kernels and the traversal cell width as a
  * multiple of h_init.  Zero keeps the current value. */
 int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor);
+/* Named engine options: "list_mode" (0 thread-per-particle or 1
+ * warp-per-cell neighbour-list build), "cell_factor", "block"; read-only
+ * "list_capacity" (entries per particle). */
+int sph_set_option(sph_ctx* ctx, const char* key, double value);
+int sph_get_option(sph_ctx* ctx, const char* key, double* value);
 /* Number of kernel launches issued by this context since creation. */
 int sph_launch_count(sph_ctx* ctx, int64_t* launches);
 /* CUDA-event phase times of the last step in ms: [kick+sort, density, eos,
