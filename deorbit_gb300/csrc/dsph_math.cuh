@@ -81,6 +81,22 @@ __device__ __forceinline__ R kernel_W_ih(R r, R ih) {
     return R(0);
 }
 
+// Branch-free forms of the same spline: with t = max(2 - q, 0) and
+// a = max(1 - q, 0), W = s (t^3 / 4 - a^3) and dW/dr = s / h (3 a^2 - 3 t^2 / 4)
+// reproduce both pieces and the zero tail (no divergence inside warps).
+template <class R>
+__device__ __forceinline__ R kernel_W_bf(R r, R ih) {
+    R q = r * ih;
+    R t = rmax(R(2) - q, R(0)), a = rmax(R(1) - q, R(0));
+    return K<R>::inv_pi * ih * ih * ih * (R(0.25) * t * t * t - a * a * a);
+}
+template <class R>
+__device__ __forceinline__ R kernel_dW_bf(R r, R ih) {
+    R q = r * ih;
+    R t = rmax(R(2) - q, R(0)), a = rmax(R(1) - q, R(0));
+    return K<R>::inv_pi * ih * ih * ih * ih * (R(3) * a * a - R(0.75) * t * t);
+}
+
 // Largest eigenvalue of the symmetric tensor {xx,yy,zz,xy,xz,yz} by Smith's
 // trigonometric method (sph.hpp:41-54).
 template <class R>

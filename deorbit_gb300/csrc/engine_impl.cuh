@@ -914,8 +914,10 @@ public:
         for (int c = 0; c < 6; c++) v.dS_new[c] = der_[DR_DSN0 + c];
         v.pf = pf_; v.cpk = cpk_; v.refbin = refbin_;
         v.vh = vh_; v.vl = vl_;
+        v.pk = pk_; v.fa = fa_; v.fb = fb_; v.fc = fc_;
         v.cell_ptr = cell_cnt_;
         v.nbr = nbr_; v.nbr_cnt = nbr_cnt_; v.hlist = hlist_;
+        v.xnbr = xnbr_; v.xcnt = xcnt_;
         v.flags = flags_d_;
         v.imps = tab_d_;
         v.mats = mats_d_;
@@ -1163,12 +1165,18 @@ public:
         dfree(pf_); pf_ = dalloc<float4>(nc);
         dfree(vh_); vh_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(vl_); vl_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
+        dfree(pk_); pk_ = dalloc<float2>(sizeof(R) == 4 ? nc : 1);
+        dfree(fa_); fa_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
+        dfree(fb_); fb_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
+        dfree(fc_); fc_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(ne_cells_); ne_cells_ = dalloc<int32_t>(nc);
         dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
         dfree(refbin_); refbin_ = dalloc<unsigned long long>(nc);
         dfree(src_); src_ = dalloc<int32_t>(nc);
         dfree(nbr_cnt_); nbr_cnt_ = dalloc<int32_t>(nc);
         dfree(hlist_); hlist_ = dalloc<float>(nc);
+        dfree(xcnt_); xcnt_ = dalloc<int32_t>(nc);
+        dfree(xnbr_); xnbr_ = dalloc<int32_t>((size_t)nc * kExtraCap);
         // derived columns start at zero so reads before the first force pass are defined
         for (int c = 0; c < kNDer; c++) DSPH_CUDA(cudaMemsetAsync(der_[c], 0, sizeof(R) * nc, st_));
         cap_ = nc;
@@ -1373,11 +1381,13 @@ public:
     void build_list(bool host_check) {
         if (N_ <= 0) return;
         const int nimp = (int)imp_.size();
-        if (KIND == kListSuperset) launch_small(k_impact_reset_slack, nimp);
+        launch_small(k_impact_reset_slack, nimp);
         for (int attempt = 0; attempt < 8; attempt++) {
             DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t), st_));
-            if (KIND == kListSuperset) DSPH_CUDA(cudaMemsetAsync(flags_d_ + 2, 0, sizeof(int32_t), st_));
-            launch_n(k_list_thread<R, KIND>, N_, block_);
+            DSPH_CUDA(cudaMemsetAsync(flags_d_ + 2, 0, sizeof(int32_t), st_));
+            DSPH_CUDA(cudaMemsetAsync(xcnt_, 0, sizeof(int32_t) * N_, st_));
+            launch_n(k_list_thread<R>, N_, block_);
+            launch_n(k_sort_extra<R>, N_);
             if (!host_check) return;
             DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
             DSPH_CUDA(cudaStreamSynchronize(st_));
@@ -1499,6 +1509,8 @@ public:
     float4* pf_ = nullptr;
     float4* vh_ = nullptr;
     float4* vl_ = nullptr;
+    float2* pk_ = nullptr;
+    float4 *fa_ = nullptr, *fb_ = nullptr, *fc_ = nullptr;
     int32_t* ne_cells_ = nullptr;
     int32_t* ne_count_ = nullptr;
     unsigned int* cell_hmax_ = nullptr;
@@ -1512,9 +1524,11 @@ public:
     int32_t* nbr_ = nullptr;
     int32_t* nbr_cnt_ = nullptr;
     float* hlist_ = nullptr;
+    int32_t* xnbr_ = nullptr;
+    int32_t* xcnt_ = nullptr;
     double slack_ = 0.08;
     int64_t nbr_stride_ = 0;
-    int cap_nbr_ = 192;
+    int cap_nbr_ = 160;
     int32_t* flags_d_ = nullptr;
     int32_t* flags_h_ = nullptr;
     void* scratch_ = nullptr;

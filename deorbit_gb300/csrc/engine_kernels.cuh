@@ -31,6 +31,7 @@ constexpr uint32_t kInvalidKey = 0xffffffffu;
 constexpr int kListDensity = 0;
 constexpr int kListForce = 1;
 constexpr int kListSuperset = 2;
+constexpr int kExtraCap = 32;   // reverse-pair entries per particle
 
 // Per-impact parameters and per-step scalars, resident on the device.
 struct ImpactD {
@@ -79,12 +80,17 @@ struct View {
     R* dS_new[6];
     float4* pf;
     float4 *vh, *vl;     // mixed form: FP64 velocity split into FP32 hi + lo
+    float2* pk;          // mixed form: (mass, packed cell) per particle, for density gathers
+    float4 *fa, *fb, *fc; // mixed form: packed force-source records (m/rho, rho, csig,
+                          // Pf/rho^2), (dscale/rho^2, Rart, S4, S5), (S0..S3)
     uint32_t* cpk;
     unsigned long long* refbin;
     const int32_t* cell_ptr;
     int32_t* nbr;
     int32_t* nbr_cnt;
     float* hlist;       // h of each particle when its list was built
+    int32_t* xnbr;      // extra (reverse) list, row-major [k * kExtraCap + t]
+    int32_t* xcnt;
     int32_t* flags;     // [0] list overflow max, [1] any impact still in a density round
     ImpactD* imps;
     const MatT<R>* mats;
@@ -277,6 +283,68 @@ __device__ __forceinline__ void traverse(const View<R>& v, const ImpactD& I, flo
     }
 }
 
+// Like traverse(), but visits only the cell columns whose footprint meets the
+// sphere and, per column, only the z-cells within the sphere's chord there
+// (non-periodic impacts; periodic ones use the full box).  Border columns are
+// never pruned by x / y because clamped particles may lie outside their cell.
+template <class R, class F>
+__device__ __forceinline__ void traverse_sphere(const View<R>& v, const ImpactD& I, float4 pi,
+                                                uint32_t ci, float Rs, F&& f) {
+    if (I.per[0] | I.per[1] | I.per[2]) {
+        traverse(v, I, pi, ci, Rs, f);
+        return;
+    }
+    int c[3];
+    unpack_cell(ci, c[0], c[1], c[2]);
+    const float o[3] = {pi.x, pi.y, pi.z};
+    int lo[2], hi[2];
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const float w = I.wf[a];
+        const int nf = I.nf[a];
+        int l = c[a] + (int)floorf((o[a] - Rs) / w);
+        int h = c[a] + (int)floorf((o[a] + Rs) / w);
+        lo[a] = l < 0 ? 0 : (l > nf - 1 ? nf - 1 : l);
+        hi[a] = h < 0 ? 0 : (h > nf - 1 ? nf - 1 : h);
+    }
+    const float R2 = Rs * Rs;
+    const float w0 = I.wf[0], w1 = I.wf[1], w2 = I.wf[2];
+    const int nf2 = I.nf[2];
+    for (int ix = lo[0]; ix <= hi[0]; ix++) {
+        const float xa = (float)(ix - c[0]) * w0 - o[0];   // column x-interval [xa, xa + w0) rel. to i
+        float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
+        if (ix == 0 || ix == I.nf[0] - 1) bx = 0.0f;
+        const float dxc = (float)(c[0] - ix) * w0;
+        for (int iy = lo[1]; iy <= hi[1]; iy++) {
+            const float ya = (float)(iy - c[1]) * w1 - o[1];
+            float by = ya > 0.0f ? ya : (ya + w1 < 0.0f ? -(ya + w1) : 0.0f);
+            if (iy == 0 || iy == I.nf[1] - 1) by = 0.0f;
+            const float d2 = bx * bx + by * by;
+            if (d2 >= R2) continue;
+            const float hz = sqrtf(R2 - d2);
+            int zl = c[2] + (int)floorf((o[2] - hz) / w2);
+            int zh = c[2] + (int)floorf((o[2] + hz) / w2);
+            zl = zl < 0 ? 0 : (zl > nf2 - 1 ? nf2 - 1 : zl);
+            zh = zh < 0 ? 0 : (zh > nf2 - 1 ? nf2 - 1 : zh);
+            const float dyc = (float)(c[1] - iy) * w1;
+            const int64_t colbase = I.cell_base + ((int64_t)ix * I.nf[1] + iy) * nf2;
+            int cz = zl;
+            const int32_t s = v.cell_ptr[colbase + zl];
+            const int32_t e = v.cell_ptr[colbase + zh + 1];
+            int32_t next = v.cell_ptr[colbase + cz + 1];
+            float dzc = (float)(c[2] - cz) * w2;
+            for (int32_t j = s; j < e; j++) {
+                while (j >= next) {
+                    cz++;
+                    next = v.cell_ptr[colbase + cz + 1];
+                    dzc = (float)(c[2] - cz) * w2;
+                }
+                f(j, dxc, dyc, dzc);
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------- kernels
 
 // Kick (half step with the old acceleration) and drift (sph.hpp:360-361).
@@ -379,6 +447,7 @@ static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid, const uint32_
     float ox = (float)(fx * I.w[0]), oy = (float)(fy * I.w[1]), oz = (float)(fz * I.w[2]);
     v.pf[k] = make_float4(ox, oy, oz, (float)v.hh[k]);
     v.cpk[k] = (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22);
+    if (sizeof(R) == 4) v.pk[k] = make_float2((float)v.mass[k], __uint_as_float(v.cpk[k]));
     float om = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
     impact_atomic_max_u32(&I.omax_bits, __float_as_uint(om));
 }
@@ -481,57 +550,77 @@ static __global__ void k_round_check(ImpactD* imps, int nimp, int32_t* flags) {
     }
 }
 
-// Neighbour-list build, one thread per target particle: each thread walks the
-// cell columns of its own search sphere with an FP32 distance test.
-//   kListSuperset (used by the step): one list per step holding every j with
-//     r < max(2 h_i, h_i + h_j) (1 + slack) -- a superset of the density sets
-//     {r < 2 h_i} and the force sets {r < h_i + h_j} for as long as no h grows
-//     by more than the slack; the consumers apply the exact criteria and the
-//     reference-stencil restriction, and fall back to a direct traversal when
-//     a particle outgrows the slack.
-//   kListDensity / kListForce: the exact sets (with the FP64 form's margin).
-template <class R, int KIND>
+// Neighbour-list build, one thread per particle k.  Each particle searches only
+// its own sphere of radius 2 h_k (1 + slack) and records
+//   own list   every j with r < 2 h_k (1 + s)  -- a superset of the density set
+//              {r < 2 h_k} and of the force pairs with h_j <= h_k;
+//   extra list of j: k itself, when j's own search misses k (r >= 2 h_j (1 + s))
+//              but the pair can interact (r < (h_j + h_k)(1 + s)); such a k is
+//              always inside k's own sphere, so every force pair is found once.
+// The FP32 pair distance is computed bit-symmetrically from either side, so the
+// two tests partition the pairs exactly; the FP64 form adds its margin m to
+// both radii.  Extra lists are appended with atomics and sorted afterwards, so
+// list contents and order depend only on the state.  Consumers apply the exact
+// criteria, the reference-stencil restriction, and fall back to a traversal
+// for a particle whose h outgrew the slack or whose list overflowed.
+template <class R>
 static __global__ void k_list_thread(View<R> v) {
     int64_t k = gtid();
     if (k >= v.n) return;
     const ImpactD& I = v.imps[v.imp[k]];
-    if (!I.mask || (KIND == kListDensity && !I.active)) return;
+    if (!I.mask) return;
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
-    const unsigned long long bi = v.refbin[k];
-    const bool exact = sizeof(R) == 8;
-    const float m = exact ? I.margin : 0.0f;
+    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
     const float sl = 1.0f + I.slack;
-    float Rs;
-    if (KIND == kListSuperset) Rs = fmaxf(2.0f * pi.w, pi.w + I.hmax_f) * sl + 2.0f * I.margin + 1e-6f * pi.w;
-    else Rs = (KIND == kListDensity ? 2.0f * pi.w : pi.w + I.hmax_f) + 2.0f * m;
-    const bool need_member = KIND != kListSuperset && Rs >= I.cwmin * 0.999f;
-    const float lim_d = 2.0f * pi.w + m;
+    const float ri = 2.0f * pi.w * sl + m;
+    const float ri2 = ri * ri;
     int cnt = 0;
     const int cap = v.cap;
     int32_t* out = v.nbr + (int64_t)k * cap;
-    traverse(v, I, pi, ci, Rs, [&](int32_t j, float dxc, float dyc, float dzc) {
-        float4 pj = v.pf[j];
+    traverse_sphere(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
+        const float4 pj = v.pf[j];
         float dx = (pi.x - pj.x) + dxc;
         float dy = (pi.y - pj.y) + dyc;
         float dz = (pi.z - pj.z) + dzc;
         if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
         if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
         if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
-        float r2 = dx * dx + dy * dy + dz * dz;
-        float lim;
-        if (KIND == kListSuperset) lim = fmaxf(2.0f * pi.w, pi.w + pj.w) * sl + I.margin + 1e-6f * pi.w;
-        else lim = KIND == kListDensity ? lim_d : (pi.w + pj.w + m);
-        bool take = r2 < lim * lim;
-        if (KIND == kListForce) take = take && (j != (int32_t)k) && (exact || r2 > 0.0f);
-        if (take && (!need_member || ref_member(bi, v.refbin[j], I))) {
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < ri2) {
             if (cnt < cap) out[cnt] = j;
             cnt++;
+            // does j's own search miss k although the pair can interact?
+            const float rj = 2.0f * pj.w * sl + m;
+            const float rb = (pi.w + pj.w) * sl + m;
+            if (!(r2 < rj * rj) && r2 < rb * rb) {
+                const int slot = atomicAdd(&v.xcnt[j], 1);
+                if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+            }
         }
     });
     v.nbr_cnt[k] = cnt;
-    if (KIND == kListSuperset) v.hlist[k] = pi.w;
+    v.hlist[k] = pi.w;
     if (cnt > cap) atomicMax(&v.flags[0], cnt);
+}
+
+// Sort each particle's extra list (filled by atomics) into ascending order.
+template <class R>
+static __global__ void k_sort_extra(View<R> v) {
+    int64_t k = gtid();
+    if (k >= v.n) return;
+    const int c = min(v.xcnt[k], kExtraCap);
+    if (c < 2) return;
+    int32_t* a = v.xnbr + (int64_t)k * kExtraCap;
+    for (int i = 1; i < c; i++) {
+        int32_t x = a[i];
+        int j = i - 1;
+        while (j >= 0 && a[j] > x) {
+            a[j + 1] = a[j];
+            j--;
+        }
+        a[j + 1] = x;
+    }
 }
 
 template <class R>
@@ -566,7 +655,7 @@ __device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, 
 // Density sum and h update (sph.hpp:189-201).  Criterion r < 2 h_i (self
 // included) within the reference stencil; compensated sum in the mixed form.
 template <class R>
-static __global__ void k_density(View<R> v) {
+static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_density(View<R> v) {
     int64_t k = gtid();
     if (k >= v.n) return;
     ImpactD& I = v.imps[v.imp[k]];
@@ -580,23 +669,28 @@ static __global__ void k_density(View<R> v) {
     const bool need_member = 2.0f * (float)hi + 2.0f * m >= I.cwmin * 0.999f;
     AccT<R> sum;
     sum.init();
+    const float th2 = (2.0f * (float)hi + m) * (2.0f * (float)hi + m);
     auto body = [&](int32_t j) {
-        R r;
         if (sizeof(R) == 8) {
+            float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
+            sep_f32(I, pi, ci, v.pf[j], v.cpk[j], fx, fy, fz);
+            if (!(fx * fx + fy * fy + fz * fz < th2)) return;
             double dx, dy, dz;
             double rr = sep_exact(v, I, k, j, dx, dy, dz);
             if (!(rr < 2.0 * (double)hi)) return;
-            r = (R)rr;
+            if (need_member && !ref_member(bi, v.refbin[j], I)) return;
+            sum.add(v.mass[j] * kernel_W_ih<R>((R)rr, ihi));
         } else {
+            const float4 pj = v.pf[j];
+            const float2 mk = v.pk[j];
             float dx, dy, dz;
-            sep_f32(I, pi, ci, v.pf[j], v.cpk[j], dx, dy, dz);
-            float r2 = dx * dx + dy * dy + dz * dz;
-            float th = 2.0f * (float)hi;
-            if (!(r2 < th * th)) return;
-            r = (R)sqrtf(r2);
+            sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            // the kernel vanishes at q >= 2; only the stencil restriction needs a test
+            float w = mk.x * kernel_W_bf<float>(sqrtf(r2), (float)ihi);
+            if (need_member && !ref_member(bi, v.refbin[j], I)) w = 0.0f;
+            sum.add((R)w);
         }
-        if (need_member && !ref_member(bi, v.refbin[j], I)) return;
-        sum.add(v.mass[j] * kernel_W_ih<R>(r, ihi));
     };
     if (list_covers(v, I, k, (float)hi)) {
         const int cnt = v.nbr_cnt[k];
@@ -648,6 +742,9 @@ static __global__ void k_eos(View<R> v) {
     v.dsr2[k] = irho2 * dsc;
     v.vol[k] = v.mass[k] / rho;
     if (sizeof(R) == 4) {
+        v.fa[k] = make_float4((float)v.vol[k], (float)rho, (float)v.csig[k], (float)v.pfr2[k]);
+        v.fb[k] = make_float4((float)v.dsr2[k], (float)v.Rart[k], (float)v.S[4][k], (float)v.S[5][k]);
+        v.fc[k] = make_float4((float)v.S[0][k], (float)v.S[1][k], (float)v.S[2][k], (float)v.S[3][k]);
         const double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k];
         const float hx = (float)vx, hy = (float)vy, hz = (float)vz;
         v.vh[k] = make_float4(hx, hy, hz, 0.0f);
@@ -685,78 +782,38 @@ static __global__ void __launch_bounds__(128) k_force(View<R> v) {
     const unsigned long long bi = v.refbin[k];
     const float m = sizeof(R) == 8 ? I.margin : 0.0f;
     const bool need_member = (float)hi + I.hmax_f + 2.0f * m >= I.cwmin * 0.999f;
-    auto body = [&](int32_t j) {
-        if (j == (int32_t)k) return;
-        const R hj = v.hh[j];
-        R rx, ry, rz, r;
-        if (sizeof(R) == 8) {
-            double dx, dy, dz;
-            double rr = sep_exact(v, I, k, j, dx, dy, dz);
-            double hsum = __dadd_rn((double)hi, (double)hj);
-            if (rr >= hsum || rr == 0.0) return;
-            rx = (R)dx; ry = (R)dy; rz = (R)dz; r = (R)rr;
-        } else {
-            float dx, dy, dz;
-            sep_f32(I, pi, ci, v.pf[j], v.cpk[j], dx, dy, dz);
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const float hs = (float)hi + (float)hj;
-            if (!(r2 < hs * hs) || r2 == 0.0f) return;
-            rx = (R)dx; ry = (R)dy; rz = (R)dz;
-            r = (R)sqrtf(r2);
-        }
-        if (need_member && !ref_member(bi, v.refbin[j], I)) return;
-        const R hbar = R(0.5) * (hi + hj);
-        const R ihb = R(1) / hbar;
-        const R ir = R(1) / r;
-        const R dW = kernel_dW<R>(r, ihb);
-        const R wg = dW * ir;
-        const R gx = rx * wg, gy = ry * wg, gz = rz * wg;
-        R vx, vy, vz;  // v_i - v_j
-        if (sizeof(R) == 8) {
-            vx = (R)(vxi - v.vx[j]); vy = (R)(vyi - v.vy[j]); vz = (R)(vzi - v.vz[j]);
-        } else {  // hi parts nearly cancel exactly; lo parts restore the FP64 difference
-            const float4 vhj = v.vh[j], vlj = v.vl[j];
-            vx = (R)((vhi.x - vhj.x) + (vli.x - vlj.x));
-            vy = (R)((vhi.y - vhj.y) + (vli.y - vlj.y));
-            vz = (R)((vhi.z - vhj.z) + (vli.z - vlj.z));
-        }
+    // one pair's contributions: strain-rate tensor, momentum, energy
+    auto pair_math = [&](R rx, R ry, R rz, R r, R hbar, R ihb, R dW, R gx, R gy, R gz, R vx, R vy, R vz,
+                         R Vj, R rhoj, R csj, R pfj, R dsj, R Raj, R mj, R tjxx, R tjyy, R tjzz, R tjxy,
+                         R tjxz, R tjyz, int32_t j) {
         if (strength) {
-            const R Vj = v.vol[j];
             const R ex = -vx * Vj, ey = -vy * Vj, ez = -vz * Vj;  // Vj (v_j - v_i)
             L00 += ex * gx; L01 += ex * gy; L02 += ex * gz;
             L10 += ey * gx; L11 += ey * gy; L12 += ey * gz;
             L20 += ez * gx; L21 += ez * gy; L22 += ez * gz;
         }
-        const R rhoj = v.rho[j];
         const R dvr = vx * rx + vy * ry + vz * rz;
         R Pij = R(0);
         if (dvr < R(0)) {
             const R mu = hbar * dvr / (r * r + eps * hbar * hbar);
-            const R cbar = R(0.5) * (csi + v.csig[j]);
+            const R cbar = R(0.5) * (csi + csj);
             Pij = (-alpha * cbar * mu + beta * mu * mu) / (R(0.5) * (rhoi + rhoj));
         }
-        const R mj = v.mass[j];
-        const R term = Pi_over + v.pfr2[j] + Pij;
+        const R term = Pi_over + pfj + Pij;
         du.add(R(0.5) * mj * term * (vx * gx + vy * gy + vz * gz));
         R mterm = term;
         if (eps_as > R(0)) {
             const R q = r * ihb;
-            R poly;
-            if (q < R(1)) poly = R(1) - R(1.5) * q * q + R(0.75) * q * q * q;
-            else if (q < R(2)) { R tt = R(2) - q; poly = R(0.25) * tt * tt * tt; }
-            else poly = R(0);
-            R fr = poly * (R)I.inv_poly_eta;
+            const R t = rmax(R(2) - q, R(0)), a = rmax(R(1) - q, R(0));
+            const R fr = (R(0.25) * t * t * t - a * a * a) * (R)I.inv_poly_eta;
             R fn = fr * fr;
             fn *= fn;
-            mterm += (Rai + v.Rart[j]) * fn;
+            mterm += (Rai + Raj) * fn;
         }
         const R mm = mj * mterm;
-        const R tjxx = v.S[0][j], tjyy = v.S[1][j], tjzz = v.S[2][j];
-        const R tjxy = v.S[3][j], tjxz = v.S[4][j], tjyz = v.S[5][j];
-        const R ci_ = dsri, cj_ = v.dsr2[j];
-        const R stx = (sxx * gx + sxy * gy + sxz * gz) * ci_ + (tjxx * gx + tjxy * gy + tjxz * gz) * cj_;
-        const R sty = (sxy * gx + syy * gy + syz * gz) * ci_ + (tjxy * gx + tjyy * gy + tjyz * gz) * cj_;
-        const R stz = (sxz * gx + syz * gy + szz * gz) * ci_ + (tjxz * gx + tjyz * gy + tjzz * gz) * cj_;
+        const R stx = (sxx * gx + sxy * gy + sxz * gz) * dsri + (tjxx * gx + tjxy * gy + tjxz * gz) * dsj;
+        const R sty = (sxy * gx + syy * gy + syz * gz) * dsri + (tjxy * gx + tjyy * gy + tjyz * gz) * dsj;
+        const R stz = (sxz * gx + syz * gy + szz * gz) * dsri + (tjxz * gx + tjyz * gy + tjzz * gz) * dsj;
         ax.add(stx * mj - gx * mm);
         ay.add(sty * mj - gy * mm);
         az.add(stz * mj - gz * mm);
@@ -766,10 +823,66 @@ static __global__ void __launch_bounds__(128) k_force(View<R> v) {
             du.add(alpha_u * mj * vsig * (ui - (R)v.u[j]) * dW / rbar);
         }
     };
-    if (!I.slack_flag && v.nbr_cnt[k] <= v.cap) {
+    const float hs_pad = 2.0f * m;
+    auto body = [&](int32_t j) {
+        if (j == (int32_t)k) return;
+        if (sizeof(R) == 8) {
+            const float4 pjf = v.pf[j];
+            float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
+            sep_f32(I, pi, ci, pjf, v.cpk[j], fx, fy, fz);
+            const float lim = pi.w + pjf.w + hs_pad;
+            if (!(fx * fx + fy * fy + fz * fz < lim * lim)) return;
+            const R hj = v.hh[j];
+            double dx, dy, dz;
+            double rr = sep_exact(v, I, k, j, dx, dy, dz);
+            double hsum = __dadd_rn((double)hi, (double)hj);
+            if (rr >= hsum || rr == 0.0) return;
+            if (need_member && !ref_member(bi, v.refbin[j], I)) return;
+            const R rx = (R)dx, ry = (R)dy, rz = (R)dz, r = (R)rr;
+            const R hbar = R(0.5) * (hi + hj);
+            const R ihb = R(1) / hbar;
+            const R dW = kernel_dW_bf<R>(r, ihb);
+            const R wg = dW / r;
+            const R gx = rx * wg, gy = ry * wg, gz = rz * wg;
+            const R vx = (R)(vxi - v.vx[j]), vy = (R)(vyi - v.vy[j]), vz = (R)(vzi - v.vz[j]);
+            const R Vj = v.vol[j], rhoj = v.rho[j], csj = v.csig[j], pfj = v.pfr2[j];
+            const R dsj = v.dsr2[j], Raj = v.Rart[j], mj = v.mass[j];
+            const R tj0 = v.S[0][j], tj1 = v.S[1][j], tj2 = v.S[2][j];
+            const R tj3 = v.S[3][j], tj4 = v.S[4][j], tj5 = v.S[5][j];
+            pair_math(rx, ry, rz, r, hbar, ihb, dW, gx, gy, gz, vx, vy, vz, Vj, rhoj, csj, pfj, dsj, Raj, mj,
+                      tj0, tj1, tj2, tj3, tj4, tj5, j);
+        } else {
+            const float4 pj = v.pf[j];
+            const float2 mk = v.pk[j];
+            float dx, dy, dz;
+            sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float hs = (float)hi + pj.w;
+            if (!(r2 < hs * hs) || r2 == 0.0f) return;
+            if (need_member && !ref_member(bi, v.refbin[j], I)) return;
+            const float4 fa = v.fa[j], fb = v.fb[j], fc = v.fc[j];
+            const float4 vhj = v.vh[j], vlj = v.vl[j];
+            const R r = (R)sqrtf(r2);
+            const R hbar = R(0.5) * (hi + (R)pj.w);
+            const R ihb = R(1) / hbar;
+            const R dW = kernel_dW_bf<R>(r, ihb);
+            const R wg = dW / r;
+            const R gx = (R)dx * wg, gy = (R)dy * wg, gz = (R)dz * wg;
+            // hi parts nearly cancel exactly; lo parts restore the FP64 difference
+            const R vx = (R)((vhi.x - vhj.x) + (vli.x - vlj.x));
+            const R vy = (R)((vhi.y - vhj.y) + (vli.y - vlj.y));
+            const R vz = (R)((vhi.z - vhj.z) + (vli.z - vlj.z));
+            pair_math((R)dx, (R)dy, (R)dz, r, hbar, ihb, dW, gx, gy, gz, vx, vy, vz, (R)fa.x, (R)fa.y, (R)fa.z,
+                      (R)fa.w, (R)fb.x, (R)fb.y, (R)mk.x, (R)fc.x, (R)fc.y, (R)fc.z, (R)fc.w, (R)fb.z, (R)fb.w, j);
+        }
+    };
+    if (!I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap) {
         const int cnt = v.nbr_cnt[k];
         const int32_t* lst = v.nbr + (int64_t)k * v.cap;
         for (int t = 0; t < cnt; t++) body(lst[t]);
+        const int xc = v.xcnt[k];
+        const int32_t* xl = v.xnbr + (int64_t)k * kExtraCap;
+        for (int t = 0; t < xc; t++) body(xl[t]);
     } else {
         traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
                  [&](int32_t j, float, float, float) { body(j); });
