@@ -134,7 +134,9 @@ class ClockSampler:
 
 def time_form(sph, ic, sc, precision, steps, warmup, device, profile=True):
     """Init (untimed), W warm-up steps, then exactly K timed steps."""
+    from deorbit_gb300 import autotune
     ctx = sph.Context(precision, device)
+    autotune.apply(ctx, sc, precision, device)
     b = ic.to_context(ctx, sc)
     ctx.init()
     for _ in range(warmup):

@@ -193,6 +193,7 @@ public:
         DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
         DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
         DSPH_CUDA(cudaMalloc(&ne_count_, sizeof(int32_t)));
+        DSPH_CUDA(cudaMalloc(&ntask_, sizeof(int32_t)));
         DSPH_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
         DSPH_CUDA(cudaMallocHost(&flags_h_, sizeof(int32_t) * 4));
         DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t) * 4, st_));
@@ -207,6 +208,7 @@ public:
         cudaFree(mats_d_);
         cudaFree(flags_d_);
         cudaFree(ne_count_);
+        cudaFree(ntask_);
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
         for (auto& e : prof_pool_) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -747,8 +749,8 @@ public:
     void set_option(const char* key, double value) override {
         std::string k(key);
         if (k == "list_mode") {
-            if (value != 0) throw SphError(SPH_ERR_ARG, "list_mode 0 (thread per particle) is the only builder");
-            list_mode_ = 0;
+            if (value != 0 && value != 1) throw SphError(SPH_ERR_ARG, "list_mode is 0 (thread) or 1 (warp per column run)");
+            list_mode_ = (int)value;
         } else if (k == "slack") {
             if (!(value >= 0.0 && value <= 1.0)) throw SphError(SPH_ERR_ARG, "slack must be in [0, 1]");
             slack_ = value;
@@ -1170,6 +1172,7 @@ public:
         dfree(fb_); fb_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(fc_); fc_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(ne_cells_); ne_cells_ = dalloc<int32_t>(nc);
+        dfree(tasks_); tasks_ = dalloc<int32_t>(nc);
         dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
         dfree(refbin_); refbin_ = dalloc<unsigned long long>(nc);
         dfree(src_); src_ = dalloc<int32_t>(nc);
@@ -1386,7 +1389,17 @@ public:
             DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t), st_));
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 2, 0, sizeof(int32_t), st_));
             DSPH_CUDA(cudaMemsetAsync(xcnt_, 0, sizeof(int32_t) * N_, st_));
-            launch_n(k_list_thread<R>, N_, block_);
+            if (list_mode_ == 1) {
+                DSPH_CUDA(cudaMemsetAsync(ntask_, 0, sizeof(int32_t), st_));
+                launch_n_raw(k_column_tasks<R>, N_, view(), tasks_, ntask_);
+                const int grid = std::max(1, std::min<int>(nsm_ * 8, (int)((N_ / 16 + 255) / 256) + 1));
+                prof_begin();
+                k_list_warp<R><<<grid, 256, 0, st_>>>(view(), (const int32_t*)tasks_, (const int32_t*)ntask_);
+                prof_end();
+                launches_++;
+            } else {
+                launch_n(k_list_thread<R>, N_, block_);
+            }
             launch_n(k_sort_extra<R>, N_);
             if (!host_check) return;
             DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
@@ -1513,6 +1526,8 @@ public:
     float4 *fa_ = nullptr, *fb_ = nullptr, *fc_ = nullptr;
     int32_t* ne_cells_ = nullptr;
     int32_t* ne_count_ = nullptr;
+    int32_t* tasks_ = nullptr;
+    int32_t* ntask_ = nullptr;
     unsigned int* cell_hmax_ = nullptr;
     int nsm_ = 148;
     uint32_t* cpk_ = nullptr;
@@ -1526,7 +1541,7 @@ public:
     float* hlist_ = nullptr;
     int32_t* xnbr_ = nullptr;
     int32_t* xcnt_ = nullptr;
-    double slack_ = 0.08;
+    double slack_ = 0.03;
     int64_t nbr_stride_ = 0;
     int cap_nbr_ = 160;
     int32_t* flags_d_ = nullptr;
@@ -1540,8 +1555,8 @@ public:
     int64_t* flaw_ptr_d_ = nullptr;
     R* flaw_eps_d_ = nullptr;
     int block_ = 128;
-    double cell_factor_ = 1.0;
-    int list_mode_ = 0;   // 0: thread per particle, 1: warp per target cell
+    double cell_factor_ = 0.75;
+    int list_mode_ = 0;   // 0: thread per particle, 1: warp per column run
     int64_t launches_ = 0;
     bool profiling_ = false;
     cudaEvent_t ev_[6]{};

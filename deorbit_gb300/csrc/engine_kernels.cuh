@@ -604,6 +604,155 @@ static __global__ void k_list_thread(View<R> v) {
     if (cnt > cap) atomicMax(&v.flags[0], cnt);
 }
 
+// Work list for the warp-converged list build: one task per run of up to 32
+// consecutive sorted particles inside one traversal-cell column of one impact.
+template <class R>
+static __global__ void k_column_tasks(View<R> v, int32_t* tasks, int32_t* ntask) {
+    int64_t k = gtid();
+    if (k >= v.n) return;
+    const ImpactD& I = v.imps[v.imp[k]];
+    if (!I.mask) return;
+    int cx, cy, cz;
+    unpack_cell(v.cpk[k], cx, cy, cz);
+    const int64_t colbase = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2];
+    const int32_t cs = v.cell_ptr[colbase];
+    if (((int32_t)k - cs) % 32 == 0) tasks[atomicAdd(ntask, 1)] = (int32_t)k;
+}
+
+__device__ __forceinline__ float warp_min(float x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+__device__ __forceinline__ float warp_max(float x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+
+// Neighbour-list build, one warp per column task (same lists as k_list_thread,
+// bit for bit: each lane appends its candidates in ascending sorted index).
+// The warp walks the union of its lanes' sphere chords column by column; every
+// candidate is loaded once (broadcast) and tested by all lanes, so the loops
+// are warp-uniform.  Periodic impacts take the per-lane path.
+template <class R>
+static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32_t* tasks, const int32_t* ntask) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    const int nt_all = *ntask;
+    for (int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < nt_all; q += nwarps) {
+        const int32_t t0 = tasks[q];
+        const ImpactD& I = v.imps[v.imp[t0]];
+        int cx, cy, cz0;
+        unpack_cell(v.cpk[t0], cx, cy, cz0);
+        const int64_t colbase0 = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2];
+        const int32_t cend = v.cell_ptr[colbase0 + I.nf[2]];
+        const int nt = min(32, (int)(cend - t0));
+        const bool active = lane < nt;
+        const int64_t k = t0 + (active ? lane : 0);
+        const float4 pi = v.pf[k];
+        const uint32_t ci = v.cpk[k];
+        const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+        const float sl = 1.0f + I.slack;
+        const float ri = 2.0f * pi.w * sl + m;
+        const float ri2 = ri * ri;
+        const float Rs = ri + m;
+        int cnt = 0;
+        const int cap = v.cap;
+        int32_t* out = v.nbr + k * cap;
+        int icx, icy, icz;
+        unpack_cell(ci, icx, icy, icz);
+        if (I.per[0] | I.per[1] | I.per[2]) {
+            if (active) {
+                traverse(v, I, pi, ci, Rs, [&](int32_t j, float dxc, float dyc, float dzc) {
+                    const float4 pj = v.pf[j];
+                    float dx = (pi.x - pj.x) + dxc, dy = (pi.y - pj.y) + dyc, dz = (pi.z - pj.z) + dzc;
+                    if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
+                    if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
+                    if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 < ri2) {
+                        if (cnt < cap) out[cnt] = j;
+                        cnt++;
+                        const float rj = 2.0f * pj.w * sl + m, rb = (pi.w + pj.w) * sl + m;
+                        if (!(r2 < rj * rj) && r2 < rb * rb) {
+                            const int slot = atomicAdd(&v.xcnt[j], 1);
+                            if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                        }
+                    }
+                });
+            }
+        } else {
+            const float w0 = I.wf[0], w1 = I.wf[1], w2 = I.wf[2];
+            // union x / y column range of the warp (positions relative to the shared column)
+            const float xl = warp_min(active ? pi.x - Rs : 3e38f), xh = warp_max(active ? pi.x + Rs : -3e38f);
+            const float yl = warp_min(active ? pi.y - Rs : 3e38f), yh = warp_max(active ? pi.y + Rs : -3e38f);
+            int lox = cx + (int)floorf(xl / w0), hix = cx + (int)floorf(xh / w0);
+            int loy = cy + (int)floorf(yl / w1), hiy = cy + (int)floorf(yh / w1);
+            lox = max(0, min(I.nf[0] - 1, lox)); hix = max(0, min(I.nf[0] - 1, hix));
+            loy = max(0, min(I.nf[1] - 1, loy)); hiy = max(0, min(I.nf[1] - 1, hiy));
+            const float zi = (float)icz * w2 + pi.z;   // lane z in the column frame (range use only)
+            const int nf2 = I.nf[2];
+            for (int ix = lox; ix <= hix; ix++) {
+                const float xa = (float)(ix - icx) * w0 - pi.x;
+                float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
+                if (ix == 0 || ix == I.nf[0] - 1) bx = 0.0f;
+                const float dxc = (float)(icx - ix) * w0;
+                for (int iy = loy; iy <= hiy; iy++) {
+                    const float ya = (float)(iy - icy) * w1 - pi.y;
+                    float by = ya > 0.0f ? ya : (ya + w1 < 0.0f ? -(ya + w1) : 0.0f);
+                    if (iy == 0 || iy == I.nf[1] - 1) by = 0.0f;
+                    const float d2 = bx * bx + by * by;
+                    float zlo = 3e38f, zhi = -3e38f;
+                    if (active && d2 < Rs * Rs) {
+                        const float hz = sqrtf(Rs * Rs - d2);
+                        zlo = zi - hz;
+                        zhi = zi + hz;
+                    }
+                    zlo = warp_min(zlo);
+                    zhi = warp_max(zhi);
+                    if (zlo > zhi) continue;
+                    zlo -= 1e-3f * w2;  // covers rounding of the column-frame z
+                    zhi += 1e-3f * w2;
+                    int zl = (int)floorf(zlo / w2), zh = (int)floorf(zhi / w2);
+                    zl = max(0, min(nf2 - 1, zl));
+                    zh = max(0, min(nf2 - 1, zh));
+                    const float dyc = (float)(icy - iy) * w1;
+                    const int64_t colbase = I.cell_base + ((int64_t)ix * I.nf[1] + iy) * nf2;
+                    int cz = zl;
+                    const int32_t s = v.cell_ptr[colbase + zl];
+                    const int32_t e = v.cell_ptr[colbase + zh + 1];
+                    int32_t next = v.cell_ptr[colbase + cz + 1];
+                    for (int32_t j = s; j < e; j++) {
+                        while (j >= next) {
+                            cz++;
+                            next = v.cell_ptr[colbase + cz + 1];
+                        }
+                        const float4 pj = v.pf[j];
+                        const float dzc = (float)(icz - cz) * w2;
+                        const float dx = (pi.x - pj.x) + dxc, dy = (pi.y - pj.y) + dyc, dz = (pi.z - pj.z) + dzc;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        if (active && r2 < ri2) {
+                            if (cnt < cap) out[cnt] = j;
+                            cnt++;
+                            const float rj = 2.0f * pj.w * sl + m, rb = (pi.w + pj.w) * sl + m;
+                            if (!(r2 < rj * rj) && r2 < rb * rb) {
+                                const int slot = atomicAdd(&v.xcnt[j], 1);
+                                if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (active) {
+            v.nbr_cnt[k] = cnt;
+            v.hlist[k] = pi.w;
+            if (cnt > cap) atomicMax(&v.flags[0], cnt);
+        }
+    }
+}
+
 // Sort each particle's extra list (filled by atomics) into ascending order.
 template <class R>
 static __global__ void k_sort_extra(View<R> v) {

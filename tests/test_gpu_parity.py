@@ -175,3 +175,21 @@ def test_batch_equals_alone(sph_mod):
             for k in alone:
                 assert np.array_equal(alone[k], m[k]), (precision, k)
             c1.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_list_builders_agree(sph_mod, precision):
+    """The per-thread and warp-per-column list builders give identical lists,
+    hence bit-identical trajectories."""
+    sc = small_impact()
+    out = []
+    for mode in (0, 1):
+        ctx = sph_mod.Context(precision)
+        ctx.set_option("list_mode", mode)
+        b = ic.to_context(ctx, sc)
+        ctx.init()
+        ctx.run(4)
+        out.append(read_all(ctx, b, ["x", "vx", "u", "rho", "P"]))
+        ctx.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
