@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdeorbit_sph.so")
 
-SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu"]
+SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
 

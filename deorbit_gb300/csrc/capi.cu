@@ -22,6 +22,14 @@ namespace {
 
 thread_local std::string g_err;
 
+}  // namespace
+
+namespace dsph {
+void set_error_message(const std::string& m) { g_err = m; }
+}  // namespace dsph
+
+namespace {
+
 int fail(int code, const std::string& msg) {
     g_err = msg;
     return code;

@@ -112,6 +112,7 @@ _SIGS = {
     "sph_set_tuning": (C.c_int, [_P, C.c_int32, C.c_double]),
     "sph_launch_count": (C.c_int, [_P, _I64]),
     "sph_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),
+    "sph_cell_sort": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sph_get_option": (C.c_int, [_P, C.c_char_p, _D]),
     "sph_phase_times": (C.c_int, [_P, _D]),
     "sph_set_profiling": (C.c_int, [_P, C.c_int32]),

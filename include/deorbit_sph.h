@@ -211,6 +211,18 @@ int sph_debug_ref_cells(sph_ctx* ctx, int32_t impact, int32_t nc[3], double cw[3
 int sph_debug_neighbors(sph_ctx* ctx, int32_t impact, int32_t kind, int32_t* counts,
                         int32_t* ids, int64_t cap, int64_t* total);
 
+/* ---- primitives on caller-owned device memory ------------------------------
+ * Stable radix cell sort (the cell-list build of sph.hpp:147-162 as a
+ * device primitive): keys[n] (device, uint32 cell ids in [0, ncells)) ->
+ * perm[n] (device): particle indices ordered by (cell, index); cell_start
+ * [ncells+1] (device): first sorted position of each cell, cell_start[ncells]
+ * = n.  stream is a cudaStream_t (NULL: the legacy default stream); the call
+ * returns when the result is complete.  Scratch is taken with
+ * cudaMallocAsync on the stream and released before returning.
+ * SPH_ERR_ARG when a key is out of range (outputs then undefined). */
+int sph_cell_sort(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm,
+                  int32_t* cell_start, void* stream);
+
 /* ---- files (formats of run_ic.cpp / gpu_ic.cpp) ----------------------------
  * IC: f8 header [xlo xhi ylo yhi zlo zhi n], then n x [x y z vx vy vz mass u mat
  * fixed] (run_ic.cpp:4-6).  Creates an impact with the given parameters and
