@@ -31,4 +31,4 @@ def test_cell_sort_rejects_bad_keys(cuda_lib):
     perm = torch.empty(3, dtype=torch.int32, device="cuda")
     start = torch.empty(5, dtype=torch.int32, device="cuda")
     rc = sph.lib().sph_cell_sort(dk.data_ptr(), 3, 4, perm.data_ptr(), start.data_ptr(), None)
-    assert rc == -1 and b"out of range" in sph.lib().sph_last_error()
+    assert rc == -1 and b"outside" in sph.lib().sph_last_error()
