@@ -114,3 +114,77 @@ extern "C" int sph_cell_sort(const uint32_t* keys, int64_t n, int64_t ncells, in
     cudaStreamSynchronize(st);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant.  Its scratch is this file-scope device array: every
+// GPU that loads the library reserves it (3.5 MiB) until the process exits,
+// and all calls share it.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr int64_t kStaticMaxKeys = 1 << 18;    // 262,144 keys per call
+constexpr int64_t kStaticMaxCells = 1 << 24;   // 16,777,216 cells per call
+constexpr size_t kStaticScratchBytes = 3670016;
+
+__device__ __align__(256) unsigned char g_cell_sort_scratch[kStaticScratchBytes];
+
+std::mutex g_static_mu;
+void* g_static_addr[256] = {};
+
+// Device address of the scratch array on the current device.  The host-side
+// name g_cell_sort_scratch is only a stand-in for the symbol, not a device
+// address, so the address is looked up once per device (with that device
+// current) and cached.
+int static_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 256) {
+        cudaGetLastError();
+        dsph::set_error_message("sph_cell_sort_static: no current CUDA device");
+        return SPH_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_cell_sort_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            dsph::set_error_message(std::string("sph_cell_sort_static: cudaGetSymbolAddress: ") +
+                                    cudaGetErrorString(e));
+            return SPH_ERR_CUDA;
+        }
+        g_static_addr[dev] = p;
+    }
+    *out = g_static_addr[dev];
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" int sph_cell_sort_static(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm,
+                                    int32_t* cell_start, void* stream) {
+    if (n < 0 || ncells < 1) {
+        dsph::set_error_message("sph_cell_sort_static: n must be >= 0 and ncells >= 1");
+        return SPH_ERR_ARG;
+    }
+    if (n > kStaticMaxKeys || ncells > kStaticMaxCells) {
+        dsph::set_error_message("sph_cell_sort_static: at most 262144 keys and 16777216 cells per call "
+                                "(use sph_cell_sort for larger inputs)");
+        return SPH_ERR_CAPACITY;
+    }
+    if (!cell_start || (n > 0 && (!keys || !perm))) {
+        dsph::set_error_message("sph_cell_sort_static: null pointer");
+        return SPH_ERR_ARG;
+    }
+    if (dsph::cell_sort_scratch_bytes(n, ncells) > kStaticScratchBytes) {
+        dsph::set_error_message("sph_cell_sort_static: scratch layout exceeds the static array");
+        return SPH_ERR_CAPACITY;
+    }
+    void* scratch = nullptr;
+    int rc = static_scratch(&scratch);
+    if (rc != SPH_OK) return rc;
+    return dsph::cell_sort_with_scratch(keys, n, ncells, perm, cell_start,
+                                        static_cast<cudaStream_t>(stream), scratch);
+}

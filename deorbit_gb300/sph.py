@@ -113,6 +113,7 @@ _SIGS = {
     "sph_launch_count": (C.c_int, [_P, _I64]),
     "sph_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),
     "sph_cell_sort": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sph_cell_sort_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sph_get_option": (C.c_int, [_P, C.c_char_p, _D]),
     "sph_phase_times": (C.c_int, [_P, _D]),
     "sph_set_profiling": (C.c_int, [_P, C.c_int32]),

@@ -222,6 +222,20 @@ int sph_debug_neighbors(sph_ctx* ctx, int32_t impact, int32_t kind, int32_t* cou
  * SPH_ERR_ARG when a key is out of range (outputs then undefined). */
 int sph_cell_sort(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm,
                   int32_t* cell_start, void* stream);
+/* The same cell sort without any device allocation (no counterpart in the
+ * reference).  For callers that must not allocate device memory once they are
+ * running: hosts with a fixed device-memory budget or their own pool allocator
+ * that accounts for every byte, and latency-critical loops that cannot take an
+ * allocation's cost or implicit synchronization.  They pass inputs and outputs
+ * as above; the scratch is a 3.5 MiB array inside the library that every GPU
+ * loading it reserves until the process exits.  Limits: n <= 262144 keys and
+ * ncells <= 16777216 per call (SPH_ERR_CAPACITY beyond).  The first call on a
+ * device looks up the array's device address (once per device, with that
+ * device current); make that first call before any stream capture.  All calls
+ * share the one array, so calls that overlap on the GPU (other streams or
+ * threads) race; serialize them.  Returns when the result is complete. */
+int sph_cell_sort_static(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm,
+                         int32_t* cell_start, void* stream);
 
 /* ---- files (formats of run_ic.cpp / gpu_ic.cpp) ----------------------------
  * IC: f8 header [xlo xhi ylo yhi zlo zhi n], then n x [x y z vx vy vz mass u mat
