@@ -40,19 +40,29 @@ UNIT = "particle-steps/s"
 # Algorithmic bytes per particle of one launch (compulsory reads of the
 # particle's own state and writes of its results; neighbour re-reads, lists
 # and sort scratch excluded).  See the design doc for the derivation.
+# Kernel of each single-kernel class and its algorithmic bytes per particle
+# in the mixed form: (fixed bytes, list bytes per list entry).  The neighbour
+# list is written once per step by k_list_thread and read by every k_density
+# and k_force launch; its length (own + reverse entries per particle) is read
+# from the engine after the profiled steps.
+KERNEL_OF_CLASS = {"list_density": "k_list_thread", "density": "k_density", "force": "k_force",
+                   "eos": "k_eos", "damage": "k_damage", "finish": "k_finish"}
 ALG_BYTES = {
-    # k_force: reads pf 16, cpk 4, imp 2, mat 1, list count 4, h, rho, csig,
-    # Pf/rho^2, dscale/rho^2, dscale, Rart, P, m/rho, mass (10 R), vel 3R, S 6R,
-    # u 8, (FP64 form also x y z 24); writes acc 3R, dudt R, dSdt 6R, eps_work R
-    ("force", 4): 16 + 4 + 2 + 1 + 4 + 10 * 4 + 3 * 4 + 6 * 4 + 8 + (3 + 1 + 6 + 1) * 4,
-    ("force", 8): 16 + 4 + 2 + 1 + 4 + 24 + 10 * 8 + 3 * 8 + 6 * 8 + 8 + (3 + 1 + 6 + 1) * 8,
-    # k_list (force): reads pf 16, cpk 4, refbin 8, imp 2; writes count 4
-    ("list_force", 4): 34, ("list_force", 8): 34,
-    ("list_density", 4): 34, ("list_density", 8): 34,
-    # k_density: reads pf 16, cpk 4, h R, mass R, imp 2, count 4 (+x y z FP64); writes rho R, h R, pf.w 4
-    ("density", 4): 16 + 4 + 2 + 4 + 4 * 4 + 4, ("density", 8): 16 + 4 + 2 + 4 + 24 + 4 * 8 + 4,
+    # k_list_thread: reads pf 16, cpk 4, refbin 8, imp 2; writes count 4 and 4 B per entry
+    "list_density": (34, 4),
+    # k_density: reads pf 16, cpk 4, imp 2, count 4, h, mass; writes rho, h, pf.w 4; reads 4 B per entry
+    "density": (16 + 4 + 2 + 4 + 2 * 4 + 2 * 4 + 4, 4),
+    # k_force: reads pf 16, cpk 4, imp 2, mat 1, count 4, the packed record
+    # (h, rho, csig, P/rho^2, dscale/rho^2, dscale, Rart, P, m/rho, mass: 10 x 4),
+    # vel 3 x 4, S 6 x 4, u 8; writes acc 3, dudt 1, dSdt 6, eps_work 1 (x 4); reads 4 B per entry
+    "force": (16 + 4 + 2 + 1 + 4 + 10 * 4 + 3 * 4 + 6 * 4 + 8 + (3 + 1 + 6 + 1) * 4, 4),
+    # k_eos: reads rho, u 8, mat 1, D, S 6; writes P, cs, packed record 40
+    "eos": (4 + 8 + 1 + 4 + 24 + 8 + 40, 0),
+    "damage": (4 + 4 + 4 + 8 + 4 + 4, 0),
+    "finish": (8 * 4 + 6 * 4 + 6 * 4, 0),
 }
-# whole step, per particle-step: FP64 strength+damage 429 B, mixed 241 B
+# whole step, per particle-step (carried state read + written, derived fields,
+# lists excluded): FP64 strength+damage 429 B, mixed 241 B
 STEP_BYTES = {8: 429, 4: 241}
 
 
@@ -132,18 +142,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def time_form(sph, ic, sc, precision, steps, warmup, device, profile=True):
-    """Init (untimed), W warm-up steps, then exactly K timed steps."""
+def time_form(sph, ic, sc, precision, steps, warmup, device):
+    """Init (untimed), W warm-up steps, then exactly K timed steps in the
+    production mode (captured CUDA graphs, no per-kernel events); then K more
+    steps with per-kernel CUDA events for the kernel breakdown (not timed)."""
     from deorbit_gb300 import autotune
     ctx = sph.Context(precision, device)
     autotune.apply(ctx, sc, precision, device)
     b = ic.to_context(ctx, sc)
     ctx.init()
-    for _ in range(warmup):
-        ctx.run(1)
+    ctx.run(max(warmup, 3))  # also captures the step graphs
     ctx.synchronize()
-    ctx.set_profiling(profile)
-    ctx.kernel_stats_reset()
     l0 = ctx.launches()
     ctx.event_record(0)
     ctx.run(steps)
@@ -151,8 +160,13 @@ def time_form(sph, ic, sc, precision, steps, warmup, device, profile=True):
     ms = ctx.event_elapsed(0, 1)
     ctx.synchronize()
     l1 = ctx.launches()
+    ctx.set_profiling(True)
+    ctx.kernel_stats_reset()
+    ctx.run(steps)
+    ctx.synchronize()
+    kst = ctx.kernel_stats()
     ctx.set_profiling(False)
-    return ctx, b, ms, ctx.kernel_stats(), l1 - l0
+    return ctx, b, ms, kst, l1 - l0
 
 
 def mixed_error(sph, ic, sc, steps, device):
@@ -300,6 +314,7 @@ def main():
     barrier()
     with ClockSampler(device) as clk:
         ctx, b, ms, kst, launches = time_form(sph, ic, sc, sph.MIXED, args.steps, args.warmup, device)
+    list_entries = ctx.get_option("list_entries")
     barrier()
     ms = max_over_ranks(ms)
     value = world * sc.n * args.steps / (ms / 1000.0)
@@ -322,23 +337,27 @@ def main():
     # ---- accuracy of the mixed form against FP64 (same dt sequence)
     err = mixed_error(sph, ic, sc, args.steps, device) if rank == 0 else None
 
-    # ---- roofline of the dominant mixed-form kernel
+    # ---- roofline of the dominant mixed-form kernel (largest total time of
+    # the classes that hold one kernel; per-launch time from CUDA events)
     hbm, hbm_kind = peaks()
-    dom = max(kst, key=lambda k: kst[k][0])
+    dom = max((k for k in kst if k in KERNEL_OF_CLASS), key=lambda k: kst[k][0])
     tot_ms, nl = kst[dom]
     avg_ms = tot_ms / max(nl, 1)
-    alg = ALG_BYTES.get((dom, 4))
-    achieved = (alg * sc.n / (avg_ms / 1000.0) / 1e9) if alg else None
+    fixed, per_entry = ALG_BYTES[dom]
+    alg = fixed + per_entry * list_entries / sc.n
+    achieved = alg * sc.n / (avg_ms / 1000.0) / 1e9
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if os.path.exists(tfile):
         for line in open(tfile):
             f = line.split()
-            if len(f) >= 4 and f[0] == f"{dom}_mixed":
+            if len(f) >= 4 and not line.startswith("#") and f[0] == KERNEL_OF_CLASS[dom] + "_mixed":
+                # bytes per particle measured on a smaller case, scaled to this launch
                 traffic = (float(f[2]) + float(f[3])) * sc.n / float(f[1])
-    roof = {"kernel": f"k_{dom}", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-            "peak_kind": f"{hbm_kind} copy bandwidth", "alg_bytes_per_particle": alg,
+    roof = {"kernel": KERNEL_OF_CLASS[dom] + "<float>", "bound": "hbm", "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+            "peak_kind": f"{hbm_kind} copy bandwidth", "alg_bytes_per_launch": alg * sc.n,
+            "alg_bytes_per_particle": alg, "list_entries_per_particle": list_entries / sc.n,
             "avg_launch_ms": avg_ms, "launches": nl}
     step_bytes = STEP_BYTES[4] * sc.n
     step_roof = {"alg_bytes_per_particle_step": STEP_BYTES[4],

@@ -321,6 +321,14 @@ int sph_impact_set_h0(sph_ctx* ctx, int32_t impact, const double* h0) {
     });
 }
 
+int sph_impact_set_step_limit(sph_ctx* ctx, int32_t impact, int64_t steps) {
+    return guard([&] {
+        if (steps < 0) throw SphError(SPH_ERR_ARG, "steps < 0");
+        CTX_SET();
+        E(ctx).impact_set_step_limit(impact, steps);
+    });
+}
+
 int sph_impact_remove(sph_ctx* ctx, int32_t impact) {
     return guard([&] {
         CTX_SET();

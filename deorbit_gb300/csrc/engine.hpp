@@ -34,6 +34,7 @@ public:
     virtual int64_t impact_seed_flaws_multi(int b, double dx, uint32_t seed) = 0;
     virtual void impact_set_h0(int b, const double* h0) = 0;
     virtual void impact_set_time(int b, double t) = 0;
+    virtual void impact_set_step_limit(int b, int64_t steps) = 0;
     virtual void impact_remove(int b) = 0;
     virtual int impact_count() = 0;
     virtual sph_impact_info impact_info(int b) = 0;

@@ -185,6 +185,7 @@ public:
         std::vector<double> flaw_eps;
         double t = 0, dt_last = 0;
         int64_t steps = 0;
+        int64_t step_limit = 0;
     };
 
     explicit Engine(int device) : dev_(device) {
@@ -212,6 +213,8 @@ public:
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
         for (auto& e : prof_pool_) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        for (int p = 0; p < 2; p++)
+            if (graph_exec_[p]) cudaGraphExecDestroy(graph_exec_[p]);
         for (int i = 0; i < 16; i++) if (user_ev_[i]) cudaEventDestroy(user_ev_[i]);
         cudaStreamDestroy(st_);
     }
@@ -340,6 +343,16 @@ public:
             write_field(b, "h0", h0);
             pull_table();
             fill_params(tab_[b], h);
+            push_table();
+        }
+    }
+
+    void impact_set_step_limit(int b, int64_t steps) override {
+        ImpactH& h = imp(b);
+        h.step_limit = steps;
+        if (h.committed) {
+            pull_table();
+            tab_[b].max_steps = steps;
             push_table();
         }
     }
@@ -522,7 +535,23 @@ public:
             if (imp_[b].used && imp_[b].alive && imp_[b].committed && imp_[b].initialized) mask[b] = 1;
         set_masks(mask, nullptr, &te);
         const int nimp = (int)imp_.size();
-        for (int s = 0; s < nsteps; s++) {
+        int s = 0;
+        if (use_graphs_ && !profiling_ && nsteps >= 2 && N_ > 0) {
+            // two captured steps per launch (the gather alternates the carried
+            // buffers, so one graph covers both parities); an odd step first
+            if (nsteps % 2) {
+                launch_small(k_run_control, nimp, 0);
+                one_step(false);
+                s = 1;
+            }
+            cudaGraphExec_t ge = ensure_graph();
+            for (; s + 1 < nsteps; s += 2) {
+                DSPH_CUDA(cudaGraphLaunch(ge, st_));
+                launches_ += graph_launches_[cur_];
+            }
+            grow_lists_after_overflow();
+        }
+        for (; s < nsteps; s++) {
             launch_small(k_run_control, nimp, 0);
             one_step(true);
             grow_lists_after_overflow();
@@ -535,6 +564,36 @@ public:
                 imp_[b].dt_last = tab_[b].dt;
             }
         check_async();
+    }
+
+    // Captures two device-controlled steps (no host round trips: all four
+    // adaptive-h rounds are issued and converged impacts skip them; list
+    // overflow and slack are handled by the consumers' fallback) into one
+    // executable graph; re-captured whenever buffers, sizes or options change.
+    cudaGraphExec_t ensure_graph() {
+        const int p = cur_;
+        const int64_t shape = N_ * 65536 + (int64_t)imp_.size();
+        if (graph_exec_[p] && graph_key_[p] == layout_epoch_ && graph_n_[p] == shape) return graph_exec_[p];
+        if (graph_exec_[p]) { cudaGraphExecDestroy(graph_exec_[p]); graph_exec_[p] = nullptr; }
+        const int nimp = (int)imp_.size();
+        const int64_t l0 = launches_;
+        const uint64_t epoch0 = layout_epoch_;
+        DSPH_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < 2; k++) {
+            launch_small(k_run_control, nimp, 0);
+            one_step(false);
+        }
+        cudaGraph_t g = nullptr;
+        DSPH_CUDA(cudaStreamEndCapture(st_, &g));
+        DSPH_CUDA(cudaGraphInstantiate(&graph_exec_[p], g, 0));
+        cudaGraphDestroy(g);
+        graph_launches_[p] = launches_ - l0;
+        launches_ = l0;
+        if (cur_ != p || layout_epoch_ != epoch0)
+            throw SphError(SPH_ERR_STATE, "graph capture changed the buffer layout");
+        graph_key_[p] = layout_epoch_;
+        graph_n_[p] = shape;
+        return graph_exec_[p];
     }
 
     void compute_density_h(int iters) override {
@@ -748,6 +807,11 @@ public:
     }
     void set_option(const char* key, double value) override {
         std::string k(key);
+        layout_epoch_++;
+        if (k == "graphs") {
+            use_graphs_ = value != 0;
+            return;
+        }
         if (k == "list_mode") {
             if (value != 0 && value != 1) throw SphError(SPH_ERR_ARG, "list_mode is 0 (thread) or 1 (warp per column run)");
             list_mode_ = (int)value;
@@ -770,10 +834,12 @@ public:
     double get_option(const char* key) override {
         std::string k(key);
         if (k == "list_mode") return list_mode_;
+        if (k == "graphs") return use_graphs_ ? 1 : 0;
         if (k == "slack") return slack_;
         if (k == "cell_factor") return cell_factor_;
         if (k == "block") return block_;
         if (k == "list_capacity") return cap_nbr_;
+        if (k == "list_entries") return (double)list_entries();
         throw SphError(SPH_ERR_ARG, "unknown option " + k);
     }
     int64_t launches() override { return launches_; }
@@ -781,6 +847,24 @@ public:
     void set_profiling(int on) override { profiling_ = on != 0; }
 
 private:
+    // entries of the current neighbour lists (0 before the first build)
+    unsigned long long list_entries() {
+        if (N_ <= 0 || !nbr_cnt_ || !xcnt_) return 0;
+        // a plain allocation: the engine's own allocator would invalidate
+        // the captured step graphs
+        unsigned long long* d = nullptr;
+        DSPH_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+        unsigned long long h = 0;
+        DSPH_CUDA(cudaMemsetAsync(d, 0, sizeof(h), st_));
+        k_sum_list_entries<<<std::max(1, std::min(nsm_ * 4, (int)((N_ + 255) / 256))), 256, 0, st_>>>(
+            nbr_cnt_, xcnt_, N_, cap_nbr_, d);
+        DSPH_CUDA(cudaGetLastError());
+        DSPH_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        cudaFree(d);
+        return h;
+    }
+
     // ------------------------------------------------------------- helpers
     static double bitsd_host(unsigned long long b) {
         double d;
@@ -797,6 +881,7 @@ private:
             throw SphError(SPH_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         }
         allocs_.push_back(p);
+        layout_epoch_++;
         return static_cast<T*>(p);
     }
     void dfree(void* p) {
@@ -1211,6 +1296,7 @@ public:
             make_fine_grid(I, h);
             I.alive = 1;
             I.t = h.t;
+            I.max_steps = h.step_limit;
             I.dt_bits = 0x7ff0000000000000ull;
             I.nc[0] = I.nc[1] = I.nc[2] = 1;
             I.cw[0] = I.cw[1] = I.cw[2] = 1;
@@ -1384,7 +1470,10 @@ public:
     void build_list(bool host_check) {
         if (N_ <= 0) return;
         const int nimp = (int)imp_.size();
+        const int keep = cur_cls_;
+        cls(KC_OTHER);
         launch_small(k_impact_reset_slack, nimp);
+        cls(keep);
         for (int attempt = 0; attempt < 8; attempt++) {
             DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t), st_));
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 2, 0, sizeof(int32_t), st_));
@@ -1400,7 +1489,9 @@ public:
             } else {
                 launch_n(k_list_thread<R>, N_, block_);
             }
+            cls(KC_OTHER);
             launch_n(k_sort_extra<R>, N_);
+            cls(keep);
             if (!host_check) return;
             DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
             DSPH_CUDA(cudaStreamSynchronize(st_));
@@ -1435,6 +1526,7 @@ public:
 
     void density_rounds(int iters, bool host_sync) {
         const int nimp = (int)imp_.size();
+        cls(KC_GRID);
         launch_small(k_impact_begin_round, nimp, 2);
         for (int round = 0; round < 4; round++) {
             cls(KC_GRID);
@@ -1557,6 +1649,12 @@ public:
     int block_ = 128;
     double cell_factor_ = 0.75;
     int list_mode_ = 0;   // 0: thread per particle, 1: warp per column run
+    bool use_graphs_ = true;
+    uint64_t layout_epoch_ = 1;
+    cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+    uint64_t graph_key_[2] = {0, 0};
+    int64_t graph_n_[2] = {-1, -1};
+    int64_t graph_launches_[2] = {0, 0};
     int64_t launches_ = 0;
     bool profiling_ = false;
     cudaEvent_t ev_[6]{};

@@ -56,7 +56,7 @@ struct ImpactD {
     int32_t slack_flag;                            // some h outgrew the list slack
     // step scalars
     double dt, t, t_end;
-    int64_t nsteps;
+    int64_t nsteps, max_steps;   // max_steps > 0: the impact stops after that many steps
     int64_t off, n;                                // sorted particle range
     int64_t gid_base;
     unsigned long long hmax_bits, hm_bits, dt_bits;
@@ -1185,6 +1185,7 @@ static __global__ void k_run_control(ImpactD* imps, int nimp, int phase) {
     if (!I.alive) { I.mask = 0; return; }
     if (phase == 0) {  // before a step
         if (I.t_end > 0 && I.t >= I.t_end) { I.mask = 0; return; }
+        if (I.max_steps > 0 && I.nsteps >= I.max_steps) { I.mask = 0; return; }
         double dt = bitsd(I.dt_bits);
         if (I.t_end > 0 && I.t + dt > I.t_end) dt = I.t_end - I.t;
         I.dt = dt;
@@ -1194,6 +1195,17 @@ static __global__ void k_run_control(ImpactD* imps, int nimp, int phase) {
             I.nsteps++;
         }
     }
+}
+
+// Total entries of the current neighbour lists (own list + reverse extras,
+// each clipped to its capacity): the list bytes every list consumer reads.
+static __global__ void k_sum_list_entries(const int32_t* cnt, const int32_t* xcnt, int64_t n, int32_t cap,
+                                   unsigned long long* out) {
+    unsigned long long s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (unsigned long long)min(cnt[i], cap) + (unsigned long long)min(xcnt[i], kExtraCap);
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
 }  // namespace dsph

@@ -87,6 +87,7 @@ _SIGS = {
     "sph_impact_seed_flaws_multi": (C.c_int, [_P, C.c_int32, C.c_double, C.c_uint32, _I64]),
     "sph_impact_set_h0": (C.c_int, [_P, C.c_int32, _D]),
     "sph_impact_remove": (C.c_int, [_P, C.c_int32]),
+    "sph_impact_set_step_limit": (C.c_int, [_P, C.c_int32, C.c_int64]),
     "sph_impact_count": (C.c_int, [_P, _I32]),
     "sph_impact_info_get": (C.c_int, [_P, C.c_int32, C.POINTER(ImpactInfo)]),
     "sph_init": (C.c_int, [_P]),
@@ -315,6 +316,9 @@ class Context:
         p = Params()
         check(lib().sph_impact_get_params(self.h, b, C.byref(p)))
         return p
+
+    def set_step_limit(self, b, steps):
+        check(lib().sph_impact_set_step_limit(self.h, b, int(steps)))
 
     def remove(self, b):
         check(lib().sph_impact_remove(self.h, b))

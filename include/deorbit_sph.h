@@ -157,6 +157,9 @@ int sph_impact_seed_flaws_multi(sph_ctx* ctx, int32_t impact, double dx, uint32_
                                 int64_t* nflaws);
 /* Extension: per-particle reference smoothing length (graded lattices). */
 int sph_impact_set_h0(sph_ctx* ctx, int32_t impact, const double* h0);
+/* Batched runs stop advancing an impact once it has taken `steps` steps in
+ * total (0: no limit). */
+int sph_impact_set_step_limit(sph_ctx* ctx, int32_t impact, int64_t steps);
 /* Releases an impact's particles and slot (serving). */
 int sph_impact_remove(sph_ctx* ctx, int32_t impact);
 int sph_impact_count(sph_ctx* ctx, int32_t* count);
@@ -172,7 +175,9 @@ int sph_timestep(sph_ctx* ctx, int32_t impact, double* dt);
 int sph_step(sph_ctx* ctx, double dt);
 /* Batched run: nsteps KDK steps in which each impact uses its own CFL dt
  * (device-side, as run_ic.cpp:328-329), clipped at its t_end when t_end > 0.
- * Impacts that reached t_end stop advancing. */
+ * Impacts that reached t_end or their step limit stop advancing.  Unless the
+ * "graphs" option is 0, steps run as a captured CUDA graph of two
+ * device-controlled steps (no host round trips inside). */
 int sph_run(sph_ctx* ctx, int32_t nsteps, double t_end);
 /* Individual phases (for parity checks, as cpu_dump.cpp:171 uses them). */
 int sph_compute_density_h(sph_ctx* ctx, int32_t iters);   /* sph.hpp:184-208 */
@@ -258,8 +263,9 @@ int sph_load_checkpoint(sph_ctx* ctx, const char* path, const sph_params* p, int
  * multiple of h_init.  Zero keeps the current value. */
 int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor);
 /* Named engine options: "list_mode" (0 thread-per-particle or 1
- * warp-per-cell neighbour-list build), "cell_factor", "block"; read-only
- * "list_capacity" (entries per particle). */
+ * warp-per-column neighbour-list build), "cell_factor", "block", "slack"
+ * (neighbour-list radius slack), "graphs" (1: sph_run uses CUDA graphs);
+ * read-only "list_capacity" (entries per particle). */
 int sph_set_option(sph_ctx* ctx, const char* key, double value);
 int sph_get_option(sph_ctx* ctx, const char* key, double* value);
 /* Number of kernel launches issued by this context since creation. */

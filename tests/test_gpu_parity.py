@@ -193,3 +193,38 @@ def test_list_builders_agree(sph_mod, precision):
         ctx.close()
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]), k
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_run_matches_stepwise(sph_mod, precision):
+    """sph_run through captured CUDA graphs (device-controlled rounds and list
+    fallbacks) gives the same trajectory as host-driven stepping."""
+    scs = [ic.sized_impact(3000 + 2000 * i, seed=40 + i, angle_deg=15 + 10 * i, speed=7000, ratio=0.2)
+           for i in range(2)]
+    out = []
+    for graphs in (0, 1):
+        ctx = sph_mod.Context(precision)
+        ctx.set_option("graphs", graphs)
+        ids = [ic.to_context(ctx, s) for s in scs]
+        ctx.init()
+        ctx.run(1)
+        ctx.run(6)   # odd + even: exercises both buffer parities
+        out.append([read_all(ctx, b, ["x", "vz", "u", "rho", "Sxz", "D"]) for b in ids])
+        infos = [ctx.info(b) for b in ids]
+        assert all(i.steps == 7 for i in infos)
+        ctx.close()
+    for a, b in zip(out[0], out[1]):
+        for k in a:
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-12 if precision == 0 else 1e-5,
+                                       atol=1e-12 * (np.abs(b[k]).max() + 1e-300), err_msg=k)
+
+
+def test_step_limit_stops_impacts(sph_mod):
+    ctx = sph_mod.Context(1)
+    ids = [ic.to_context(ctx, ic.sized_impact(3000, seed=5 + i, angle_deg=20, speed=6000, ratio=0.2))
+           for i in range(2)]
+    ctx.init()
+    ctx.set_step_limit(ids[0], 3)
+    ctx.run(8)
+    assert ctx.info(ids[0]).steps == 3 and ctx.info(ids[1]).steps == 8
+    ctx.close()
