@@ -1,8 +1,8 @@
 """Autotuner for the neighbour-search shape of the SPH engine.
 
 Chooses, per (GPU, precision, workload class), the traversal cell width (as a
-multiple of h_init), the neighbour-list builder (one thread per particle or one
-warp per target cell) and the thread-block size, by timing a few KDK steps of
+multiple of h_init), the neighbour-list builder (one thread per particle, one
+warp per column run or one warp per particle) and the thread-block size, by timing a few KDK steps of
 a representative workload with CUDA events on the engine stream.  Results are
 cached in a JSON file so a run pays for the search once per class.
 
@@ -24,7 +24,7 @@ CACHE = os.environ.get("DEORBIT_SPH_TUNE_CACHE", os.path.join(HERE, "_tune", "au
 CELL_FACTORS = (0.75, 1.0, 1.5)
 SLACKS = (0.03, 0.06)
 BLOCKS = (128, 256)
-LIST_MODES = (1, 0)
+LIST_MODES = (2, 1, 0)
 
 
 def gpu_name(device=0) -> str:

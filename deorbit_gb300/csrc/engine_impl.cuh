@@ -813,7 +813,8 @@ public:
             return;
         }
         if (k == "list_mode") {
-            if (value != 0 && value != 1) throw SphError(SPH_ERR_ARG, "list_mode is 0 (thread) or 1 (warp per column run)");
+            if (value != 0 && value != 1 && value != 2)
+                throw SphError(SPH_ERR_ARG, "list_mode is 0 (thread), 1 (warp per column run) or 2 (warp per particle)");
             list_mode_ = (int)value;
         } else if (k == "slack") {
             if (!(value >= 0.0 && value <= 1.0)) throw SphError(SPH_ERR_ARG, "slack must be in [0, 1]");
@@ -1486,6 +1487,11 @@ public:
                 k_list_warp<R><<<grid, 256, 0, st_>>>(view(), (const int32_t*)tasks_, (const int32_t*)ntask_);
                 prof_end();
                 launches_++;
+            } else if (list_mode_ == 2) {
+                prof_begin();
+                k_list_wpp<R><<<(unsigned)((N_ + 7) / 8), 256, 0, st_>>>(view());
+                prof_end();
+                launches_++;
             } else {
                 launch_n(k_list_thread<R>, N_, block_);
             }
@@ -1534,10 +1540,8 @@ public:
             hmax_pass(0);
             launch_small(k_ref_grid, nimp);
             launch_n(k_ref_bins<R>, N_);
-            for (int it = 0; it < iters; it++) {
-                cls(KC_DENSITY);
-                launch_n(k_density<R>, N_);
-            }
+            cls(KC_DENSITY);
+            if (iters > 0) launch_n_raw(k_density<R>, N_, view(), iters);
             cls(KC_GRID);
             hmax_pass(1);
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 1, 0, sizeof(int32_t), st_));

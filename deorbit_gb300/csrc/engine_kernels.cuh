@@ -19,6 +19,7 @@
 // that intersect its search sphere.
 #pragma once
 
+#include <climits>
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -550,25 +551,10 @@ static __global__ void k_round_check(ImpactD* imps, int nimp, int32_t* flags) {
     }
 }
 
-// Neighbour-list build, one thread per particle k.  Each particle searches only
-// its own sphere of radius 2 h_k (1 + slack) and records
-//   own list   every j with r < 2 h_k (1 + s)  -- a superset of the density set
-//              {r < 2 h_k} and of the force pairs with h_j <= h_k;
-//   extra list of j: k itself, when j's own search misses k (r >= 2 h_j (1 + s))
-//              but the pair can interact (r < (h_j + h_k)(1 + s)); such a k is
-//              always inside k's own sphere, so every force pair is found once.
-// The FP32 pair distance is computed bit-symmetrically from either side, so the
-// two tests partition the pairs exactly; the FP64 form adds its margin m to
-// both radii.  Extra lists are appended with atomics and sorted afterwards, so
-// list contents and order depend only on the state.  Consumers apply the exact
-// criteria, the reference-stencil restriction, and fall back to a traversal
-// for a particle whose h outgrew the slack or whose list overflowed.
+// One particle's list by its own traversal (periodic impacts, and warps that
+// straddle two impacts).
 template <class R>
-static __global__ void k_list_thread(View<R> v) {
-    int64_t k = gtid();
-    if (k >= v.n) return;
-    const ImpactD& I = v.imps[v.imp[k]];
-    if (!I.mask) return;
+__device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int64_t k) {
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
     const float m = sizeof(R) == 8 ? I.margin : 0.0f;
@@ -602,6 +588,120 @@ static __global__ void k_list_thread(View<R> v) {
     v.nbr_cnt[k] = cnt;
     v.hlist[k] = pi.w;
     if (cnt > cap) atomicMax(&v.flags[0], cnt);
+}
+
+// Neighbour-list build, one thread per particle k.  Each particle searches only
+// its own sphere of radius 2 h_k (1 + slack) and records
+//   own list   every j with r < 2 h_k (1 + s)  -- a superset of the density set
+//              {r < 2 h_k} and of the force pairs with h_j <= h_k;
+//   extra list of j: k itself, when j's own search misses k (r >= 2 h_j (1 + s))
+//              but the pair can interact (r < (h_j + h_k)(1 + s)); such a k is
+//              always inside k's own sphere, so every force pair is found once.
+// The FP32 pair distance is computed bit-symmetrically from either side, so the
+// two tests partition the pairs exactly; the FP64 form adds its margin m to
+// both radii.  Extra lists are appended with atomics and sorted afterwards, so
+// list contents and order depend only on the state.  Consumers apply the exact
+// criteria, the reference-stencil restriction, and fall back to a traversal
+// for a particle whose h outgrew the slack or whose list overflowed.
+//
+// Loop shape: the 32 particles of a warp are consecutive in sorted order, so
+// they sit in one or two cell columns and search nearly the same columns.  The
+// warp walks the union of its lanes' column boxes in a fixed order; each lane
+// takes the columns of its own box that meet its sphere, over the z-range of
+// its own chord, and the candidate loop runs to the longest chord of the warp
+// with the other lanes predicated off.  A candidate's z-cell comes from its
+// packed cell word instead of a walk over the cell boundaries.  Every lane
+// visits the same candidates in the same order as traverse_sphere(), so the
+// lists equal those of a per-thread traversal entry for entry.
+template <class R>
+static __global__ void k_list_thread(View<R> v) {
+    const unsigned full = 0xffffffffu;
+    const int64_t k0 = gtid();
+    const bool inb = k0 < v.n;
+    const int64_t k = inb ? k0 : v.n - 1;
+    const int ib = v.imp[k];
+    const ImpactD& I = v.imps[ib];
+    const bool one_impact = __all_sync(full, ib == __shfl_sync(full, ib, 0));
+    if (!one_impact || (I.per[0] | I.per[1] | I.per[2])) {
+        if (inb && I.mask) list_one(v, I, k);
+        return;
+    }
+    if (!I.mask) return;  // warp-uniform: one impact
+    const bool act = inb;
+    const float4 pi = v.pf[k];
+    const uint32_t ci = v.cpk[k];
+    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const float sl = 1.0f + I.slack;
+    const float ri = 2.0f * pi.w * sl + m;
+    const float ri2 = ri * ri;
+    const float Rs = ri + m;
+    const float R2 = Rs * Rs;
+    int c[3];
+    unpack_cell(ci, c[0], c[1], c[2]);
+    const float w0 = I.wf[0], w1 = I.wf[1], w2 = I.wf[2];
+    const int nf0 = I.nf[0], nf1 = I.nf[1], nf2 = I.nf[2];
+    int lo0 = c[0] + (int)floorf((pi.x - Rs) / w0), hi0 = c[0] + (int)floorf((pi.x + Rs) / w0);
+    int lo1 = c[1] + (int)floorf((pi.y - Rs) / w1), hi1 = c[1] + (int)floorf((pi.y + Rs) / w1);
+    lo0 = lo0 < 0 ? 0 : (lo0 > nf0 - 1 ? nf0 - 1 : lo0);
+    hi0 = hi0 < 0 ? 0 : (hi0 > nf0 - 1 ? nf0 - 1 : hi0);
+    lo1 = lo1 < 0 ? 0 : (lo1 > nf1 - 1 ? nf1 - 1 : lo1);
+    hi1 = hi1 < 0 ? 0 : (hi1 > nf1 - 1 ? nf1 - 1 : hi1);
+    const int ulo0 = __reduce_min_sync(full, act ? lo0 : INT_MAX), uhi0 = __reduce_max_sync(full, act ? hi0 : INT_MIN);
+    const int ulo1 = __reduce_min_sync(full, act ? lo1 : INT_MAX), uhi1 = __reduce_max_sync(full, act ? hi1 : INT_MIN);
+    int cnt = 0;
+    const int cap = v.cap;
+    int32_t* out = v.nbr + k * cap;
+    for (int ix = ulo0; ix <= uhi0; ix++) {
+        const float xa = (float)(ix - c[0]) * w0 - pi.x;
+        float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
+        if (ix == 0 || ix == nf0 - 1) bx = 0.0f;
+        const float dxc = (float)(c[0] - ix) * w0;
+        const bool in_x = act && ix >= lo0 && ix <= hi0;
+        for (int iy = ulo1; iy <= uhi1; iy++) {
+            const float ya = (float)(iy - c[1]) * w1 - pi.y;
+            float by = ya > 0.0f ? ya : (ya + w1 < 0.0f ? -(ya + w1) : 0.0f);
+            if (iy == 0 || iy == nf1 - 1) by = 0.0f;
+            const float d2 = bx * bx + by * by;
+            int32_t s = 0, len = 0;
+            if (in_x && iy >= lo1 && iy <= hi1 && d2 < R2) {
+                const float hz = sqrtf(R2 - d2);
+                int zl = c[2] + (int)floorf((pi.z - hz) / w2);
+                int zh = c[2] + (int)floorf((pi.z + hz) / w2);
+                zl = zl < 0 ? 0 : (zl > nf2 - 1 ? nf2 - 1 : zl);
+                zh = zh < 0 ? 0 : (zh > nf2 - 1 ? nf2 - 1 : zh);
+                const int64_t colbase = I.cell_base + ((int64_t)ix * nf1 + iy) * nf2;
+                s = v.cell_ptr[colbase + zl];
+                len = v.cell_ptr[colbase + zh + 1] - s;
+            }
+            const int maxlen = __reduce_max_sync(full, len);
+            const float dyc = (float)(c[1] - iy) * w1;
+            for (int t = 0; t < maxlen; t++) {
+                const bool ok = t < len;
+                const int32_t j = ok ? s + t : (int32_t)k;
+                const float4 pj = v.pf[j];
+                const float dzc = (float)(c[2] - (int)(v.cpk[j] >> 22)) * w2;
+                const float dx = (pi.x - pj.x) + dxc;
+                const float dy = (pi.y - pj.y) + dyc;
+                const float dz = (pi.z - pj.z) + dzc;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (ok && r2 < ri2) {
+                    if (cnt < cap) out[cnt] = j;
+                    cnt++;
+                    const float rj = 2.0f * pj.w * sl + m;
+                    const float rb = (pi.w + pj.w) * sl + m;
+                    if (!(r2 < rj * rj) && r2 < rb * rb) {
+                        const int slot = atomicAdd(&v.xcnt[j], 1);
+                        if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                    }
+                }
+            }
+        }
+    }
+    if (act) {
+        v.nbr_cnt[k] = cnt;
+        v.hlist[k] = pi.w;
+        if (cnt > cap) atomicMax(&v.flags[0], cnt);
+    }
 }
 
 // Work list for the warp-converged list build: one task per run of up to 32
@@ -753,6 +853,143 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
     }
 }
 
+// Neighbour-list build, one warp per particle.  The lanes take the cell
+// columns that meet the particle's search sphere, 32 at a time, and walk them
+// cell by cell in step; the hits of a step are compacted with a ballot, so the
+// list is written in coalesced runs and the loops stay converged.  Same sets
+// and the same extra-list entries as k_list_thread (the pair test is the same
+// expression); entries are ordered by step, then by column.
+__device__ __forceinline__ int wrap_cell(int i, int nf, int per) {
+    return per ? ((i % nf) + nf) % nf : i;
+}
+
+template <class R>
+static __global__ void __launch_bounds__(256) k_list_wpp(View<R> v) {
+    const int lane = threadIdx.x & 31;
+    const int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= v.n) return;  // warp-uniform
+    const ImpactD& I = v.imps[v.imp[k]];
+    if (!I.mask) return;
+    const float4 pi = v.pf[k];
+    const uint32_t ci = v.cpk[k];
+    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const float sl = 1.0f + I.slack;
+    const float ri = 2.0f * pi.w * sl + m;
+    const float ri2 = ri * ri;
+    const float Rs = ri + m;
+    const int cap = v.cap;
+    int32_t* out = v.nbr + k * cap;
+    int c[3];
+    unpack_cell(ci, c[0], c[1], c[2]);
+    const float o[3] = {pi.x, pi.y, pi.z};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {  // the cell box of traverse()
+        const float w = I.wf[a];
+        int l = c[a] + (int)floorf((o[a] - Rs) / w);
+        int h = c[a] + (int)floorf((o[a] + Rs) / w);
+        const int nf = I.nf[a];
+        if (I.per[a]) {
+            if (h - l + 1 > nf) { l = c[a] - nf / 2; h = l + nf - 1; }
+        } else {
+            l = l < 0 ? 0 : (l > nf - 1 ? nf - 1 : l);
+            h = h < 0 ? 0 : (h > nf - 1 ? nf - 1 : h);
+        }
+        lo[a] = l;
+        hi[a] = h;
+    }
+    const bool sphere = !(I.per[0] | I.per[1] | I.per[2]);
+    const float w0 = I.wf[0], w1 = I.wf[1], w2 = I.wf[2];
+    const int nf0 = I.nf[0], nf1 = I.nf[1], nf2 = I.nf[2];
+    const int ncy = hi[1] - lo[1] + 1;
+    const int ncol = (hi[0] - lo[0] + 1) * ncy;
+    const float R2 = Rs * Rs;
+    const unsigned below = (1u << lane) - 1u;
+    int cnt = 0;
+    for (int base = 0; base < ncol; base += 32) {
+        const int q = base + lane;
+        int iz = 0, izh = -1;
+        int32_t j = 0, e = 0;
+        float dxc = 0.0f, dyc = 0.0f, dzc = 0.0f;
+        int64_t colbase = 0;
+        if (q < ncol) {
+            const int ix = lo[0] + q / ncy, iy = lo[1] + q % ncy;
+            dxc = (float)(c[0] - ix) * w0;
+            dyc = (float)(c[1] - iy) * w1;
+            colbase = I.cell_base + ((int64_t)wrap_cell(ix, nf0, I.per[0]) * nf1 + wrap_cell(iy, nf1, I.per[1])) * nf2;
+            iz = lo[2];
+            izh = hi[2];
+            if (sphere) {  // the column pruning and z chord of traverse_sphere()
+                const float xa = (float)(ix - c[0]) * w0 - o[0];
+                float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
+                if (ix == 0 || ix == nf0 - 1) bx = 0.0f;
+                const float ya = (float)(iy - c[1]) * w1 - o[1];
+                float by = ya > 0.0f ? ya : (ya + w1 < 0.0f ? -(ya + w1) : 0.0f);
+                if (iy == 0 || iy == nf1 - 1) by = 0.0f;
+                const float d2 = bx * bx + by * by;
+                if (d2 < R2) {
+                    const float hz = sqrtf(R2 - d2);
+                    int zl = c[2] + (int)floorf((o[2] - hz) / w2);
+                    int zh = c[2] + (int)floorf((o[2] + hz) / w2);
+                    iz = zl < 0 ? 0 : (zl > nf2 - 1 ? nf2 - 1 : zl);
+                    izh = zh < 0 ? 0 : (zh > nf2 - 1 ? nf2 - 1 : zh);
+                } else {
+                    izh = iz - 1;
+                }
+            }
+            if (iz <= izh) {
+                const int wz = wrap_cell(iz, nf2, I.per[2]);
+                j = v.cell_ptr[colbase + wz];
+                e = v.cell_ptr[colbase + wz + 1];
+                dzc = (float)(c[2] - iz) * w2;
+            }
+        }
+        while (true) {
+            while (j >= e && iz < izh) {  // next non-empty cell of this lane's column
+                iz++;
+                const int wz = wrap_cell(iz, nf2, I.per[2]);
+                j = v.cell_ptr[colbase + wz];
+                e = v.cell_ptr[colbase + wz + 1];
+                dzc = (float)(c[2] - iz) * w2;
+            }
+            const bool have = j < e;
+            if (!__any_sync(0xffffffffu, have)) break;
+            bool hit = false;
+            if (have) {
+                const float4 pj = v.pf[j];
+                float dx = (pi.x - pj.x) + dxc;
+                float dy = (pi.y - pj.y) + dyc;
+                float dz = (pi.z - pj.z) + dzc;
+                if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
+                if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
+                if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                hit = r2 < ri2;
+                if (hit) {
+                    const float rj = 2.0f * pj.w * sl + m;
+                    const float rb = (pi.w + pj.w) * sl + m;
+                    if (!(r2 < rj * rj) && r2 < rb * rb) {
+                        const int slot = atomicAdd(&v.xcnt[j], 1);
+                        if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                    }
+                }
+            }
+            const unsigned bm = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int pos = cnt + __popc(bm & below);
+                if (pos < cap) out[pos] = j;
+            }
+            cnt += __popc(bm);
+            if (have) j++;
+        }
+    }
+    if (lane == 0) {
+        v.nbr_cnt[k] = cnt;
+        v.hlist[k] = pi.w;
+        if (cnt > cap) atomicMax(&v.flags[0], cnt);
+    }
+}
+
 // Sort each particle's extra list (filled by atomics) into ascending order.
 template <class R>
 static __global__ void k_sort_extra(View<R> v) {
@@ -801,61 +1038,69 @@ __device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, 
     return v.nbr_cnt[k] <= v.cap && h_now <= v.hlist[k] * (1.0f + I.slack) * 0.99999f;
 }
 
-// Density sum and h update (sph.hpp:189-201).  Criterion r < 2 h_i (self
-// included) within the reference stencil; compensated sum in the mixed form.
+// Density sum and h update (sph.hpp:189-201), `iters` iterations in one
+// launch.  Criterion r < 2 h_i (self included) within the reference stencil;
+// compensated sum in the mixed form.  An iteration reads only the particle's
+// own h and the neighbours' positions and masses, so running the iterations
+// back to back per particle gives the same result as one launch per iteration.
 template <class R>
-static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_density(View<R> v) {
+static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_density(View<R> v, int iters) {
     int64_t k = gtid();
     if (k >= v.n) return;
     ImpactD& I = v.imps[v.imp[k]];
     if (!(I.mask && I.active)) return;
-    const R hi = v.hh[k];
-    const R ihi = R(1) / hi;
+    R hi = v.hh[k];
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
     const unsigned long long bi = v.refbin[k];
     const float m = sizeof(R) == 8 ? I.margin : 0.0f;
-    const bool need_member = 2.0f * (float)hi + 2.0f * m >= I.cwmin * 0.999f;
-    AccT<R> sum;
-    sum.init();
-    const float th2 = (2.0f * (float)hi + m) * (2.0f * (float)hi + m);
-    auto body = [&](int32_t j) {
-        if (sizeof(R) == 8) {
-            float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
-            sep_f32(I, pi, ci, v.pf[j], v.cpk[j], fx, fy, fz);
-            if (!(fx * fx + fy * fy + fz * fz < th2)) return;
-            double dx, dy, dz;
-            double rr = sep_exact(v, I, k, j, dx, dy, dz);
-            if (!(rr < 2.0 * (double)hi)) return;
-            if (need_member && !ref_member(bi, v.refbin[j], I)) return;
-            sum.add(v.mass[j] * kernel_W_ih<R>((R)rr, ihi));
+    const R mass_k = v.mass[k];
+    const R h0 = I.use_h0 ? v.h0[k] : (R)I.h_init;
+    R rho = R(1e-30);
+    for (int it = 0; it < iters; it++) {
+        const R ihi = R(1) / hi;
+        const bool need_member = 2.0f * (float)hi + 2.0f * m >= I.cwmin * 0.999f;
+        AccT<R> sum;
+        sum.init();
+        const float th2 = (2.0f * (float)hi + m) * (2.0f * (float)hi + m);
+        auto body = [&](int32_t j) {
+            if (sizeof(R) == 8) {
+                float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
+                sep_f32(I, pi, ci, v.pf[j], v.cpk[j], fx, fy, fz);
+                if (!(fx * fx + fy * fy + fz * fz < th2)) return;
+                double dx, dy, dz;
+                double rr = sep_exact(v, I, k, j, dx, dy, dz);
+                if (!(rr < 2.0 * (double)hi)) return;
+                if (need_member && !ref_member(bi, v.refbin[j], I)) return;
+                sum.add(v.mass[j] * kernel_W_ih<R>((R)rr, ihi));
+            } else {
+                const float4 pj = v.pf[j];
+                const float2 mk = v.pk[j];
+                float dx, dy, dz;
+                sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                // the kernel vanishes at q >= 2; only the stencil restriction needs a test
+                float w = mk.x * kernel_W_bf<float>(sqrtf(r2), (float)ihi);
+                if (need_member && !ref_member(bi, v.refbin[j], I)) w = 0.0f;
+                sum.add((R)w);
+            }
+        };
+        if (list_covers(v, I, k, (float)hi)) {
+            const int cnt = v.nbr_cnt[k];
+            const int32_t* lst = v.nbr + (int64_t)k * v.cap;
+            for (int t = 0; t < cnt; t++) body(lst[t]);
         } else {
-            const float4 pj = v.pf[j];
-            const float2 mk = v.pk[j];
-            float dx, dy, dz;
-            sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            // the kernel vanishes at q >= 2; only the stencil restriction needs a test
-            float w = mk.x * kernel_W_bf<float>(sqrtf(r2), (float)ihi);
-            if (need_member && !ref_member(bi, v.refbin[j], I)) w = 0.0f;
-            sum.add((R)w);
+            const float hf = (float)hi;
+            traverse(v, I, pi, ci, 2.0f * hf * 1.0001f + 2.0f * I.margin + 1e-6f * hf,
+                     [&](int32_t j, float, float, float) { body(j); });
         }
-    };
-    if (list_covers(v, I, k, (float)hi)) {
-        const int cnt = v.nbr_cnt[k];
-        const int32_t* lst = v.nbr + (int64_t)k * v.cap;
-        for (int t = 0; t < cnt; t++) body(lst[t]);
-    } else {
-        traverse(v, I, pi, ci, 2.0f * pi.w * 1.0001f + 2.0f * I.margin + 1e-6f * pi.w,
-                 [&](int32_t j, float, float, float) { body(j); });
+        rho = rmax(sum.value(), R(1e-30));
+        hi = rmin(R(2) * h0, rmax(R(0.5) * h0, (R)I.eta * rcbrt(mass_k / rho)));
     }
-    R rho = rmax(sum.value(), R(1e-30));
     v.rho[k] = rho;
-    R h0 = I.use_h0 ? v.h0[k] : (R)I.h_init;
-    R hn = rmin(R(2) * h0, rmax(R(0.5) * h0, (R)I.eta * rcbrt(v.mass[k] / rho)));
-    v.hh[k] = hn;
-    v.pf[k].w = (float)hn;
-    if (!((float)hn <= v.hlist[k] * (1.0f + I.slack) * 0.99999f)) {
+    v.hh[k] = hi;
+    v.pf[k].w = (float)hi;
+    if (!((float)hi <= v.hlist[k] * (1.0f + I.slack) * 0.99999f)) {
         atomicOr(&I.slack_flag, 1);
         atomicOr(&v.flags[2], 1);
     }

@@ -262,10 +262,11 @@ int sph_load_checkpoint(sph_ctx* ctx, const char* path, const sph_params* p, int
 /* Launch shape of the neighbour kernels and the traversal cell width as a
  * multiple of h_init.  Zero keeps the current value. */
 int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor);
-/* Named engine options: "list_mode" (0 thread-per-particle or 1
- * warp-per-column neighbour-list build), "cell_factor", "block", "slack"
- * (neighbour-list radius slack), "graphs" (1: sph_run uses CUDA graphs);
- * read-only "list_capacity" (entries per particle). */
+/* Named engine options: "list_mode" (neighbour-list build: 0 thread per
+ * particle, 1 warp per column run, 2 warp per particle), "cell_factor",
+ * "block", "slack" (neighbour-list radius slack), "graphs" (1: sph_run uses
+ * CUDA graphs); read-only "list_capacity" (entries per particle) and
+ * "list_entries" (entries of the current lists, own plus reverse). */
 int sph_set_option(sph_ctx* ctx, const char* key, double value);
 int sph_get_option(sph_ctx* ctx, const char* key, double* value);
 /* Number of kernel launches issued by this context since creation. */
