@@ -19,7 +19,10 @@ LIB = os.path.join(LIBDIR, "libdeorbit_sph.so")
 
 SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+# -ffp-contract=off: host code (flaw seeding, file formats) gives the same
+# results on x86 and on Arm, where g++ would otherwise fuse a*b+c.
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I", os.path.join(ROOT, "include")]
 
 
 def nvcc() -> str:

@@ -1044,7 +1044,7 @@ __device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, 
 // own h and the neighbours' positions and masses, so running the iterations
 // back to back per particle gives the same result as one launch per iteration.
 template <class R>
-static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_density(View<R> v, int iters) {
+static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(View<R> v, int iters) {
     int64_t k = gtid();
     if (k >= v.n) return;
     ImpactD& I = v.imps[v.imp[k]];
@@ -1150,7 +1150,7 @@ static __global__ void k_eos(View<R> v) {
 // fused with the momentum / energy pair loop (sph.hpp:277-317).  Writes acc,
 // the new dudt and dSdt, eps_work.
 template <class R>
-static __global__ void __launch_bounds__(128) k_force(View<R> v) {
+static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(View<R> v) {
     using Acc = AccT<R>;
     int64_t k = gtid();
     if (k >= v.n) return;
@@ -1219,8 +1219,8 @@ static __global__ void __launch_bounds__(128) k_force(View<R> v) {
     };
     const float hs_pad = 2.0f * m;
     auto body = [&](int32_t j) {
-        if (j == (int32_t)k) return;
         if (sizeof(R) == 8) {
+            if (j == (int32_t)k) return;
             const float4 pjf = v.pf[j];
             float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
             sep_f32(I, pi, ci, pjf, v.cpk[j], fx, fy, fz);
@@ -1246,20 +1246,23 @@ static __global__ void __launch_bounds__(128) k_force(View<R> v) {
             pair_math(rx, ry, rz, r, hbar, ihb, dW, gx, gy, gz, vx, vy, vz, Vj, rhoj, csj, pfj, dsj, Raj, mj,
                       tj0, tj1, tj2, tj3, tj4, tj5, j);
         } else {
+            // Branch-free: every record of the entry is loaded up front (most
+            // entries interact), and a pair that fails the criterion -- or the
+            // particle itself (r = 0) -- contributes exact zeros through dW = 0.
             const float4 pj = v.pf[j];
             const float2 mk = v.pk[j];
+            const float4 fa = v.fa[j], fb = v.fb[j], fc = v.fc[j];
+            const float4 vhj = v.vh[j], vlj = v.vl[j];
             float dx, dy, dz;
             sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
             const float r2 = dx * dx + dy * dy + dz * dz;
             const float hs = (float)hi + pj.w;
-            if (!(r2 < hs * hs) || r2 == 0.0f) return;
-            if (need_member && !ref_member(bi, v.refbin[j], I)) return;
-            const float4 fa = v.fa[j], fb = v.fb[j], fc = v.fc[j];
-            const float4 vhj = v.vh[j], vlj = v.vl[j];
-            const R r = (R)sqrtf(r2);
+            bool ok = r2 < hs * hs && r2 != 0.0f;
+            if (need_member) ok = ok && ref_member(bi, v.refbin[j], I);
+            const R r = ok ? (R)sqrtf(r2) : R(1);
             const R hbar = R(0.5) * (hi + (R)pj.w);
             const R ihb = R(1) / hbar;
-            const R dW = kernel_dW_bf<R>(r, ihb);
+            const R dW = ok ? kernel_dW_bf<R>(r, ihb) : R(0);
             const R wg = dW / r;
             const R gx = (R)dx * wg, gy = (R)dy * wg, gz = (R)dz * wg;
             // hi parts nearly cancel exactly; lo parts restore the FP64 difference
