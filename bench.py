@@ -238,6 +238,81 @@ def cpu_rate(ic, sc, steps, threads=0):
     return sc.n * steps / el, el, S.threads()
 
 
+def plain_single_rate(sph, ic, scs, steps, device):
+    """The plain form: one impact per context, FP64, host-driven
+    timestep()/step() (the reference's System loop), impacts one after the
+    other.  Returns particle-steps/s over the sample."""
+    tot_ps, tot_s = 0, 0.0
+    for sc in scs:
+        ctx = sph.Context(sph.FP64, device)
+        b = ic.to_context(ctx, sc)
+        ctx.init()
+        ctx.step(ctx.timestep(b))  # warm-up
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.step(ctx.timestep(b))
+        ctx.synchronize()
+        tot_s += time.perf_counter() - t0
+        tot_ps += sc.n * steps
+        ctx.close()
+    return tot_ps / tot_s
+
+
+def batched_section(sph, ic, device, steps, warmup, count=256):
+    """The batched sweep: `count` impacts of uneven size in one context, every
+    step one launch sequence over all of them (captured CUDA graphs), each
+    impact with its own CFL dt."""
+    from deorbit_gb300 import autotune
+    scs = ic.batch_impacts(count)
+    n_tot = sum(sc.n for sc in scs)
+    out = {"workload": f"{count} impacts, iron into granite, strength + damage, N log-uniform 5k-80k",
+           "n_particles": n_tot, "steps": steps}
+    for prec, name in ((sph.MIXED, "mixed"), (sph.FP64, "fp64_batched")):
+        ctx = sph.Context(prec, device)
+        autotune.apply(ctx, scs[0], prec, device, per_impact_n=n_tot // count)
+        mids = {}
+        for sc in scs:
+            ic.to_context(ctx, sc, material_ids=mids)
+        ctx.init()
+        ctx.run(max(warmup, 3))
+        ctx.synchronize()
+        l0 = ctx.launches()
+        ctx.event_record(0)
+        ctx.run(steps)
+        ctx.event_record(1)
+        ms = ctx.event_elapsed(0, 1)
+        out[name] = {"value": n_tot * steps / (ms / 1000.0), "ms_per_step": ms / steps,
+                     "gpu_launches": ctx.launches() - l0}
+        ctx.close()
+    sample = scs[:: max(1, count // 8)][:8]
+    out["plain_fp64_single"] = {"value": plain_single_rate(sph, ic, sample, steps, device),
+                                "sample": f"{len(sample)} of the impacts, one at a time, {steps} steps each"}
+    out["speedup_vs_plain_fp64_single"] = out["mixed"]["value"] / out["plain_fp64_single"]["value"]
+    out["speedup_vs_fp64_batched"] = out["mixed"]["value"] / out["fp64_batched"]["value"]
+    out["value"] = out["mixed"]["value"]
+    return out
+
+
+def serving_section(device, rates=(2.0, 4.0, 8.0), count=24, steps=300):
+    """Poisson request streams through the continuous-batching server."""
+    from deorbit_gb300 import serve, sph
+    out = {"workload": f"{count} requests per rate, N log-uniform 10k-500k, half strength + damage, "
+                       f"{steps} steps each, 160 GB admission budget", "rates": []}
+    for rate in rates:
+        reqs = serve.poisson_requests(count, rate, steps=steps)
+        srv = serve.Server(sph.MIXED, device, hbm_budget_bytes=160e9, chunk=4)
+        base = srv.now()
+        for t, sc, st in reqs:
+            srv.submit(sc, st, arrival=base + t)
+        srv.serve(timeout=900)
+        rep = srv.report()
+        srv.close()
+        rep["rate_per_s"] = rate
+        out["rates"].append(rep)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -249,6 +324,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=256)
     args = ap.parse_args()
     rank, world, local = rank_info()
 
@@ -334,6 +412,13 @@ def main():
     ms64 = max_over_ranks(ms64)
     value64 = world * sc.n * args.steps / (ms64 / 1000.0)
 
+    # ---- batched sweep and serving streams (rank 0 of a replica run)
+    batched = serving = None
+    if rank == 0 and not args.no_batch:
+        batched = batched_section(sph, ic, device, args.steps, args.warmup, args.batch_count)
+    if rank == 0 and not args.no_serve:
+        serving = serving_section(device)
+
     # ---- accuracy of the mixed form against FP64 (same dt sequence)
     err = mixed_error(sph, ic, sc, args.steps, device) if rank == 0 else None
 
@@ -385,7 +470,8 @@ def main():
                                "kernel_ms": {k: v[0] for k, v in kst64.items()}},
                 "speedup_vs_plain_fp64": value / value64,
                 "mixed_vs_fp64_rel_l2": err,
-                "kernel_ms": {k: v[0] for k, v in kst.items()}}
+                "kernel_ms": {k: v[0] for k, v in kst.items()},
+                "batched": batched, "serving": serving}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -75,7 +75,27 @@ def build(verbose: bool = False, force: bool = False) -> str:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError("link failed")
+    build_cli(verbose, force)
     return LIB
+
+
+CLI = os.path.join(LIBDIR, "gpu_ic")
+
+
+def build_cli(verbose: bool = False, force: bool = False) -> str:
+    """The gpu_ic command-line driver (host C++ over the C ABI)."""
+    src = os.path.join(CSRC, "gpu_ic.cpp")
+    if not force and _newer(CLI, [src, LIB, os.path.join(ROOT, "include", "deorbit_sph.h")]):
+        return CLI
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include"), src,
+           "-o", CLI, "-L", LIBDIR, "-ldeorbit_sph", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if verbose or r.returncode != 0:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+    if r.returncode != 0:
+        raise RuntimeError("gpu_ic build failed")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -453,6 +453,26 @@ int sph_conservation_get(sph_ctx* ctx, int32_t impact, sph_conservation* out) {
     });
 }
 
+int sph_impact_diagnostics(sph_ctx* ctx, int32_t impact, int32_t mat_lo, int32_t mat_hi, double u_melt,
+                           sph_diagnostics* out) {
+    return guard([&] {
+        need(out, "out");
+        if (mat_lo > mat_hi) throw SphError(SPH_ERR_ARG, "mat_lo > mat_hi");
+        CTX_SET();
+        double r[11];
+        E(ctx).diagnostics(impact, mat_lo, mat_hi, u_melt, r);
+        out->count = (int64_t)r[0];
+        out->melted = (int64_t)r[1];
+        for (int a = 0; a < 3; a++) {
+            out->mean_pos[a] = r[2 + a];
+            out->mean_vel[a] = r[5 + a];
+        }
+        out->mean_speed = r[8];
+        out->dispersion = r[9];
+        out->u_max = r[10];
+    });
+}
+
 int sph_eos_eval(sph_ctx* ctx, int32_t mat, int64_t n, const double* rho, const double* u,
                  double* P, double* cs) {
     return guard([&] {

@@ -53,6 +53,7 @@ public:
     virtual void read_fixed(int b, uint8_t* out) = 0;
     virtual void write_fixed(int b, const uint8_t* in) = 0;
     virtual sph_conservation conservation(int b) = 0;
+    virtual void diagnostics(int b, int mat_lo, int mat_hi, double u_melt, double out[11]) = 0;
     virtual void eos_eval(int mat, int64_t n, const double* rho, const double* u, double* P,
                           double* cs) = 0;
     virtual void debug_ref_cells(int b, int32_t nc[3], double cw[3], int32_t* start,

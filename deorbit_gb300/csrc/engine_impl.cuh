@@ -142,6 +142,84 @@ static __global__ void k_conservation(View<R> v, int b, double* out) {
         for (int q = 0; q < 6; q++) out[q] = sh[q][0];
 }
 
+// Projectile diagnostics of one impact (the quantities gpu_ic's progress line
+// and the campaign's regime classifier derive from a snapshot,
+// gpu_ic.cpp:112-117, boundary_daemon.py:181-212), over the particles with
+// mat_lo <= mat <= mat_hi: count, melted count (u > u_melt), position and
+// velocity means, mean speed, velocity dispersion, u max.  One block, fixed
+// summation order, compensated FP64 sums; the dispersion takes a second pass
+// about the mean.  out: [count, melted, mx, my, mz, mvx, mvy, mvz, mspeed,
+// dispersion, umax].
+__device__ __forceinline__ double block_sum(double x, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) sh[w] = x;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < nw; i++) t += sh[i];  // same order in every thread
+    return t;
+}
+
+template <class R>
+static __global__ void __launch_bounds__(512) k_diagnostics(View<R> v, int b, int mat_lo, int mat_hi,
+                                                            double u_melt, double* out) {
+    __shared__ double sh[32];
+    const ImpactD& I = v.imps[b];
+    double s[9], c[9];
+    for (int q = 0; q < 9; q++) s[q] = c[q] = 0.0;
+    double umax = -1e300;
+    auto kadd = [&](int q, double x) {
+        const double y = x - c[q];
+        const double t = s[q] + y;
+        c[q] = (t - s[q]) - y;
+        s[q] = t;
+    };
+    for (int64_t idx = threadIdx.x; idx < I.n; idx += blockDim.x) {
+        const int64_t k = I.off + idx;
+        const int m = v.mat[k];
+        if (m < mat_lo || m > mat_hi) continue;
+        const double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k], u = v.u[k];
+        kadd(0, 1.0);
+        kadd(1, u > u_melt ? 1.0 : 0.0);
+        kadd(2, v.x[k]); kadd(3, v.y[k]); kadd(4, v.z[k]);
+        kadd(5, vx); kadd(6, vy); kadd(7, vz);
+        kadd(8, sqrt(vx * vx + vy * vy + vz * vz));
+        umax = fmax(umax, u);
+    }
+    double tot[9];
+    for (int q = 0; q < 9; q++) tot[q] = block_sum(s[q] - c[q], sh);
+    for (int o = 16; o > 0; o >>= 1) umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = umax;
+    __syncthreads();
+    double um = -1e300;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) um = fmax(um, sh[i]);
+    const double n = tot[0] > 0.0 ? tot[0] : 1.0;
+    const double mvx = tot[5] / n, mvy = tot[6] / n, mvz = tot[7] / n;
+    double sd = 0.0, cd = 0.0;
+    for (int64_t idx = threadIdx.x; idx < I.n; idx += blockDim.x) {
+        const int64_t k = I.off + idx;
+        const int m = v.mat[k];
+        if (m < mat_lo || m > mat_hi) continue;
+        const double dx = v.vx[k] - mvx, dy = v.vy[k] - mvy, dz = v.vz[k] - mvz;
+        const double y = (dx * dx + dy * dy + dz * dz) - cd;
+        const double t = sd + y;
+        cd = (t - sd) - y;
+        sd = t;
+    }
+    const double var = block_sum(sd - cd, sh);
+    if (threadIdx.x == 0) {
+        out[0] = tot[0];
+        out[1] = tot[1];
+        out[2] = tot[2] / n; out[3] = tot[3] / n; out[4] = tot[4] / n;
+        out[5] = mvx; out[6] = mvy; out[7] = mvz;
+        out[8] = tot[8] / n;
+        out[9] = sqrt(var / n);
+        out[10] = tot[0] > 0.0 ? um : 0.0;
+    }
+}
+
 static __global__ void k_impact_reset_omax(ImpactD* imps, int nimp) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nimp) imps[b].omax_bits = 0u;
@@ -695,6 +773,20 @@ public:
         c.momentum[1] = out[4];
         c.momentum[2] = out[5];
         return c;
+    }
+
+    void diagnostics(int b, int mat_lo, int mat_hi, double u_melt, double out[11]) override {
+        ImpactH& h = imp(b);
+        commit();
+        for (int q = 0; q < 11; q++) out[q] = 0.0;
+        if (h.n == 0) return;
+        ensure_stage(16);
+        if (!grid_valid_) sort_reorder(true);
+        k_diagnostics<R><<<1, 512, 0, st_>>>(view(), b, mat_lo, mat_hi, u_melt, stage_d_);
+        DSPH_CUDA(cudaGetLastError());
+        launches_++;
+        DSPH_CUDA(cudaMemcpyAsync(out, stage_d_, sizeof(double) * 11, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
     }
 
     void eos_eval(int mat, int64_t n, const double* rho, const double* u, double* P, double* cs) override {

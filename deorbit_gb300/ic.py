@@ -213,6 +213,19 @@ def batch_sizes(count=256, lo=5000, hi=80000, seed=20261203):
     return np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
 
 
+def batch_impacts(count=256, lo=5000, hi=80000, seed=20261203):
+    """The batched sweep: `count` iron-into-granite impacts with strength and
+    damage, particle counts log-uniform in [lo, hi], angle U[1, 45] deg, speed
+    U[4, 12] km/s, impactor / target radius ratio U[0.1, 0.3], from one seed."""
+    sizes = batch_sizes(count, lo, hi, seed)
+    rng = np.random.default_rng(seed + 1)
+    out = []
+    for i, n in enumerate(sizes):
+        out.append(sized_impact(int(n), seed=seed + 7 * i, angle_deg=float(rng.uniform(1.0, 45.0)),
+                                speed=float(rng.uniform(4000.0, 12000.0)), ratio=float(rng.uniform(0.1, 0.3))))
+    return out
+
+
 def sized_impact(n_target, seed, angle_deg, speed, ratio, strength=True, flaws="multi", jitter=0.01):
     """One impact of roughly n_target particles: iron sphere of radius ratio x
     the slab half-depth into a granite slab (batched / served workloads)."""
@@ -253,21 +266,29 @@ def _material_struct(cls, d):
     return m
 
 
-def to_context(ctx, sc: Scenario, prm_overrides=None):
+def to_context(ctx, sc: Scenario, prm_overrides=None, material_ids=None):
     """Create one impact of `sc` in a deorbit_gb300.sph.Context; returns its id.
-    Material ids of the scenario are offset by the materials already present."""
+    Material ids of the scenario are offset by the materials already present.
+    With a dict `material_ids`, equal materials are added once and shared by
+    the impacts created through the same dict (a context holds a few dozen)."""
     from . import sph
 
-    base = None
+    ids = []
     for d in sc.materials:
+        key = tuple(sorted(d.items()))
+        if material_ids is not None and key in material_ids:
+            ids.append(material_ids[key])
+            continue
         i = ctx.add_material(_material_struct(sph.Material, d))
-        base = i if base is None else base
-    base = 0 if base is None else base
+        if material_ids is not None:
+            material_ids[key] = i
+        ids.append(i)
+    ids = np.asarray(ids if ids else [0], np.int32)
     p = dict(sc.params)
     if prm_overrides:
         p.update(prm_overrides)
     b = ctx.impact_create(sph.params(**p), sc.lo, sc.hi, sc.periodic)
-    ctx.add_particles(b, sc.pos, sc.vel, sc.mass, sc.u, sc.mat + base, sc.fixed)
+    ctx.add_particles(b, sc.pos, sc.vel, sc.mass, sc.u, ids[sc.mat], sc.fixed)
     if sc.flaws is not None:
         kind, seed = sc.flaws
         if kind == "multi":

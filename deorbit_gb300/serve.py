@@ -79,15 +79,6 @@ class Server:
     def resident_particles(self):
         return sum(r.scenario.n for r in self.active.values())
 
-    def _materials(self, sc):
-        ids = []
-        for d in sc.materials:
-            key = tuple(sorted(d.items()))
-            if key not in self.mat_ids:
-                self.mat_ids[key] = self.ctx.add_material(ic._material_struct(sph.Material, d))
-            ids.append(self.mat_ids[key])
-        return np.asarray(ids, np.int32)
-
     def _admit(self, now):
         admitted = []
         while self.pending and self.pending[0].arrival <= now:
@@ -96,15 +87,7 @@ class Server:
             if self.active and need > self.budget:
                 break  # wait for memory to free up (FIFO admission)
             self.pending.popleft()
-            sc = r.scenario
-            ids = self._materials(sc)
-            b = self.ctx.impact_create(sph.params(**sc.params), sc.lo, sc.hi, sc.periodic)
-            self.ctx.add_particles(b, sc.pos, sc.vel, sc.mass, sc.u, ids[sc.mat], sc.fixed)
-            if sc.flaws is not None:
-                kind, seed = sc.flaws
-                (self.ctx.seed_flaws_multi if kind == "multi" else self.ctx.seed_damage)(b, sc.dx, seed)
-            if sc.h0 is not None:
-                self.ctx.set_h0(b, sc.h0)
+            b = ic.to_context(self.ctx, r.scenario, material_ids=self.mat_ids)
             self.ctx.set_step_limit(b, r.steps)
             r.impact = b
             r.admitted = now

@@ -59,6 +59,12 @@ class Conservation(C.Structure):
                 ("energy", C.c_double), ("momentum", C.c_double * 3)]
 
 
+class Diagnostics(C.Structure):
+    _fields_ = [("count", C.c_int64), ("melted", C.c_int64), ("mean_pos", C.c_double * 3),
+                ("mean_vel", C.c_double * 3), ("mean_speed", C.c_double), ("dispersion", C.c_double),
+                ("u_max", C.c_double)]
+
+
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
 _I64 = C.POINTER(C.c_int64)
@@ -103,6 +109,8 @@ _SIGS = {
     "sph_read_fixed": (C.c_int, [_P, C.c_int32, _U8]),
     "sph_write_fixed": (C.c_int, [_P, C.c_int32, _U8]),
     "sph_conservation_get": (C.c_int, [_P, C.c_int32, C.POINTER(Conservation)]),
+    "sph_impact_diagnostics": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                         C.POINTER(Diagnostics)]),
     "sph_eos_eval": (C.c_int, [_P, C.c_int32, C.c_int64, _D, _D, _D, _D]),
     "sph_debug_ref_cells": (C.c_int, [_P, C.c_int32, _I32, _D, _I32, C.c_int64, _I32]),
     "sph_debug_neighbors": (C.c_int, [_P, C.c_int32, C.c_int32, _I32, _I32, C.c_int64, _I64]),
@@ -381,6 +389,13 @@ class Context:
         c = Conservation()
         check(lib().sph_conservation_get(self.h, b, C.byref(c)))
         return c
+
+    def diagnostics(self, b, mat_lo, mat_hi, u_melt=1.0e6) -> Diagnostics:
+        """Projectile centroid, bulk velocity, speed, dispersion and melt count
+        over materials mat_lo..mat_hi, reduced on the device."""
+        d = Diagnostics()
+        check(lib().sph_impact_diagnostics(self.h, b, mat_lo, mat_hi, u_melt, C.byref(d)))
+        return d
 
     def eos(self, mat, rho, u):
         rho = _f64(rho)

@@ -196,6 +196,22 @@ int sph_write_fixed(sph_ctx* ctx, int32_t impact, const uint8_t* in);
 
 /* ---- diagnostics ----------------------------------------------------------- */
 int sph_conservation_get(sph_ctx* ctx, int32_t impact, sph_conservation* out);
+/* Projectile diagnostics reduced on the device over the particles with
+ * mat_lo <= material id <= mat_hi: what gpu_ic's progress line
+ * (gpu_ic.cpp:112-117: centroid, |v|, vz, melt=%, umax) and the campaign's
+ * regime classifier (boundary_daemon.py:181-212: bulk velocity, dispersion,
+ * melt fraction) compute from host copies of every particle. */
+typedef struct sph_diagnostics {
+    int64_t count;       /* selected particles */
+    int64_t melted;      /* of those with u > u_melt */
+    double mean_pos[3];
+    double mean_vel[3];  /* bulk velocity (unweighted mean) */
+    double mean_speed;   /* mean |v| */
+    double dispersion;   /* sqrt(mean |v - bulk|^2) */
+    double u_max;
+} sph_diagnostics;
+int sph_impact_diagnostics(sph_ctx* ctx, int32_t impact, int32_t mat_lo, int32_t mat_hi, double u_melt,
+                           sph_diagnostics* out);
 /* Tillotson / ideal EOS on the device in the context precision
  * (eos.hpp:65-113): n (rho, u) pairs of material mat -> P, cs. */
 int sph_eos_eval(sph_ctx* ctx, int32_t mat, int64_t n, const double* rho, const double* u,

@@ -256,3 +256,28 @@ def test_step_limit_stops_impacts(sph_mod):
     ctx.run(8)
     assert ctx.info(ids[0]).steps == 3 and ctx.info(ids[1]).steps == 8
     ctx.close()
+
+
+def test_diagnostics_match_host_reduction(sph_mod):
+    """On-device projectile diagnostics equal the host reduction of the fields
+    (what gpu_ic's progress line and the campaign's classifier compute)."""
+    sc = small_impact()
+    ctx = sph_mod.Context(0)
+    b = ic.to_context(ctx, sc)
+    ctx.init()
+    ctx.run(5)
+    f = read_all(ctx, b, ["x", "y", "z", "vx", "vy", "vz", "u"])
+    mat = ctx.mat(b)
+    for lo, hi in ((1, 255), (0, 0), (0, 255)):
+        sel = (mat >= lo) & (mat <= hi)
+        d = ctx.diagnostics(b, lo, hi, u_melt=1e3)
+        assert d.count == sel.sum()
+        assert d.melted == (sel & (f["u"] > 1e3)).sum()
+        v = np.stack([f["vx"][sel], f["vy"][sel], f["vz"][sel]], axis=1)
+        p = np.stack([f["x"][sel], f["y"][sel], f["z"][sel]], axis=1)
+        np.testing.assert_allclose(list(d.mean_pos), p.mean(0), rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(list(d.mean_vel), v.mean(0), rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(d.mean_speed, np.linalg.norm(v, axis=1).mean(), rtol=1e-12)
+        np.testing.assert_allclose(d.dispersion, np.sqrt(((v - v.mean(0)) ** 2).sum(1).mean()), rtol=1e-10)
+        assert d.u_max == f["u"][sel].max()
+    ctx.close()
