@@ -294,6 +294,33 @@ def batched_section(sph, ic, device, steps, warmup, count=256):
     return out
 
 
+def large_section(sph, ic, device, steps, warmup, n_total=1 << 24):
+    """The large graded run (mixed form), plus the mixed-vs-FP64 error on its
+    1/64-particle replica (same geometry, 4x the spacing)."""
+    from deorbit_gb300 import autotune
+    t0 = time.perf_counter()
+    sc = ic.large_graded(n_total)
+    t_ic = time.perf_counter() - t0
+    ctx = sph.Context(sph.MIXED, device)
+    autotune.apply(ctx, sc, sph.MIXED, device)
+    ic.to_context(ctx, sc)
+    ctx.init()
+    ctx.run(max(warmup, 3))
+    ctx.synchronize()
+    ctx.event_record(0)
+    ctx.run(steps)
+    ctx.event_record(1)
+    ms = ctx.event_elapsed(0, 1)
+    ctx.close()
+    rep = ic.large_graded(n_total // 64)
+    return {"workload": f"graded grazing slab 40x20x5 km, iron sphere r=500 m at 2 deg, 8 km/s, "
+                        f"{sc.n} particles, surface spacing {sc.dx:.1f} m growing 6% per layer",
+            "n_particles": sc.n, "value": sc.n * steps / (ms / 1000.0), "ms_per_step": ms / steps,
+            "ic_build_s": t_ic,
+            "replica_mixed_vs_fp64_rel_l2": mixed_error(sph, ic, rep, steps, device),
+            "replica_particles": rep.n}
+
+
 def serving_section(device, rates=(2.0, 4.0, 8.0), count=24, steps=300):
     """Poisson request streams through the continuous-batching server."""
     from deorbit_gb300 import serve, sph
@@ -327,6 +354,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--no-large", action="store_true")
     args = ap.parse_args()
     rank, world, local = rank_info()
 
@@ -418,6 +446,9 @@ def main():
         batched = batched_section(sph, ic, device, args.steps, args.warmup, args.batch_count)
     if rank == 0 and not args.no_serve:
         serving = serving_section(device)
+    large = None
+    if rank == 0 and not args.no_large:
+        large = large_section(sph, ic, device, args.steps, args.warmup)
 
     # ---- accuracy of the mixed form against FP64 (same dt sequence)
     err = mixed_error(sph, ic, sc, args.steps, device) if rank == 0 else None
@@ -471,7 +502,7 @@ def main():
                 "speedup_vs_plain_fp64": value / value64,
                 "mixed_vs_fp64_rel_l2": err,
                 "kernel_ms": {k: v[0] for k, v in kst.items()},
-                "batched": batched, "serving": serving}
+                "batched": batched, "serving": serving, "large": large}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

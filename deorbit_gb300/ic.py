@@ -208,6 +208,79 @@ def periodic_bar(nx=24, ny=6, dx=0.01, seed=7):
                     dict(eta=1.3, h_init=1.3 * dx), mats, dx)
 
 
+def _graded_layers(dx0, growth, L):
+    """Depth layers of a slab graded in z: spacing dx0 * growth^k from the
+    surface down; returns [(spacing, z_center, nx, ny)]."""
+    Lx, Ly, Lz = L
+    out, ztop, s = [], 0.0, dx0
+    while ztop < Lz:
+        nx, ny = int(Lx // s), int(Ly // s)
+        out.append((s, -(ztop + 0.5 * s), nx, ny))
+        ztop += s
+        s *= growth
+    return out
+
+
+def large_graded(n_total=1 << 24, L=(40.0e3, 20.0e3, 5.0e3), radius=500.0, angle_deg=2.0, speed=8000.0,
+                 growth=1.06, jitter=0.01, seed=20261203):
+    """Large grazing run: iron sphere (radius 500 m) at 2 deg, 8 km/s into a
+    40 x 20 x 5 km granite slab whose lattice spacing grows with depth by
+    `growth` per layer (fine at the surface where the impactor runs, coarse at
+    depth).  Exactly n_total particles; per-particle reference smoothing length
+    h0 = 1.3 x the local spacing, mass = rho0 x spacing^3.  Strength + damage
+    (Collins granite, multi-flaw with the surface spacing as flaw volume)."""
+    rng = np.random.default_rng(seed)
+
+    def count(dx0):
+        n_imp = sphere(radius, dx0, (0.0, 0.0, 0.0)).shape[0]
+        return n_imp + sum(nx * ny for _, _, nx, ny in _graded_layers(dx0, growth, L)), n_imp
+
+    lo_dx, hi_dx = 1.0, 1000.0  # count decreases with dx0
+    for _ in range(60):
+        mid = math.sqrt(lo_dx * hi_dx)
+        if count(mid)[0] >= n_total:
+            lo_dx = mid
+        else:
+            hi_dx = mid
+    dx0 = lo_dx
+    layers = _graded_layers(dx0, growth, L)
+    Lx, Ly, Lz = L
+    slab, hsp = [], []
+    for s, zc, nx, ny in layers:
+        i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+        xy = np.stack([(i.ravel() + 0.5) * s, (j.ravel() + 0.5) * s - 0.5 * ny * s], axis=1)
+        p = np.concatenate([xy, np.full((xy.shape[0], 1), zc)], axis=1)
+        slab.append(_jitter(p, s, jitter, rng))
+        hsp.append(np.full(p.shape[0], s))
+    slab = np.concatenate(slab)
+    sp = np.concatenate(hsp)
+    imp = sphere(radius, dx0, (0.0, 0.0, 0.0))
+    n_imp = imp.shape[0]
+    n_slab = n_total - n_imp
+    # drop the surplus from the bottom of the far end (away from the track)
+    order = np.lexsort((slab[:, 2], -slab[:, 0]))
+    keep = np.ones(slab.shape[0], bool)
+    keep[order[: slab.shape[0] - n_slab]] = False
+    slab, sp = slab[keep], sp[keep]
+    th = math.radians(angle_deg)
+    imp = _jitter(imp + np.array([0.1 * Lx, 0.0, radius + dx0]), dx0, jitter, rng)
+    pos = np.concatenate([slab, imp])
+    spacing = np.r_[sp, np.full(n_imp, dx0)]
+    vel = np.zeros_like(pos)
+    vel[n_slab:, 0] = speed * math.cos(th)
+    vel[n_slab:, 2] = -speed * math.sin(th)
+    mat = np.r_[np.zeros(n_slab, np.int32), np.ones(n_imp, np.int32)]
+    mats = [granite(strength=True), iron(strength=True)]
+    mass = np.where(mat == 1, mats[1]["rho0"], mats[0]["rho0"]) * spacing ** 3
+    lo = np.array([-0.05 * Lx - 2 * radius, -0.6 * Ly, -1.2 * Lz])
+    hi = np.array([1.05 * Lx, 0.6 * Ly, 4 * radius + 0.2 * Lz])
+    return Scenario(f"large_graded_{n_total}", pos, vel, mass, np.zeros(pos.shape[0]), mat,
+                    np.zeros(pos.shape[0], np.uint8), lo, hi, np.zeros(3, np.int32),
+                    dict(eta=1.3, h_init=1.3 * dx0, alpha=1.0, beta=2.0, eps=0.01, cfl=0.2,
+                         eps_as=0.3, damage_on=1, flaw_model=1),
+                    mats, dx0, flaws=("multi", 12345), h0=1.3 * spacing)
+
+
 def batch_sizes(count=256, lo=5000, hi=80000, seed=20261203):
     rng = np.random.default_rng(seed)
     return np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)

@@ -34,3 +34,18 @@ def test_served_results_equal_alone(cuda_lib):
         for k in serve.RESULT_FIELDS:
             assert np.array_equal(ctx.read(b, k), by_id[i].result[k]), (i, k)
         ctx.close()
+
+
+def test_replica_shards_equal_one_context(cuda_lib):
+    """Splitting a batch across replicas changes nothing: each shard run in its
+    own context gives bit-identical results to the whole batch in one."""
+    from deorbit_gb300 import replicas
+    scs = ic.batch_impacts(count=6, lo=1500, hi=4000)
+    whole = replicas.gpu_runner(scs, 4)
+    merged = {}
+    for rank in range(2):
+        merged.update(replicas.run_shard(scs, 4, rank, 2))
+    assert sorted(merged) == list(range(len(scs)))
+    for i, w in enumerate(whole):
+        for k in w:
+            assert np.array_equal(w[k], merged[i][k]), (i, k)
