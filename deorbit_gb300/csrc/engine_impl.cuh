@@ -1077,8 +1077,8 @@ public:
     View<R> view() {
         View<R> v{};
         v.n = N_;
-        v.stride = nbr_stride_;
         v.cap = cap_nbr_;
+        v.ls = cap_;
         v.x = dcol_[cur_][0]; v.y = dcol_[cur_][1]; v.z = dcol_[cur_][2]; v.u = dcol_[cur_][3];
         v.vx = dcol_[cur_][4]; v.vy = dcol_[cur_][5]; v.vz = dcol_[cur_][6];
         R** r = rcol_[cur_];
@@ -1366,8 +1366,8 @@ public:
 
     void alloc_lists() {
         dfree(nbr_);
-        nbr_stride_ = cap_nbr_;
-        nbr_ = dalloc<int32_t>((size_t)cap_ * cap_nbr_);
+        const size_t blocks = (size_t)(cap_nbr_ + 3) / 4;  // lists are stored in 4-entry blocks
+        nbr_ = dalloc<int32_t>((size_t)cap_ * blocks * 4);
     }
 
     // Moves staged impacts onto the device.
@@ -1730,7 +1730,6 @@ public:
     int32_t* xnbr_ = nullptr;
     int32_t* xcnt_ = nullptr;
     double slack_ = 0.03;
-    int64_t nbr_stride_ = 0;
     int cap_nbr_ = 160;
     int32_t* flags_d_ = nullptr;
     int32_t* flags_h_ = nullptr;

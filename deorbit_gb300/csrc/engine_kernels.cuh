@@ -9,7 +9,8 @@
 //   geometry           pf = float4(offset from own traversal-cell origin, h),
 //                      cpk = packed traversal-cell coordinates,
 //                      refbin = packed reference-grid bins (sph.hpp:142-146)
-//   neighbour lists    row-major nbr[k * cap + t], count per particle
+//   neighbour lists    4-entry blocks, entry-major: entries 4b..4b+3 of particle k are
+//                      the int4 at nbr[(b * ls + k) * 4] (ls = particle capacity)
 //
 // Reference semantics kept exactly: the neighbour criteria r < 2 h_i (density,
 // self included, sph.hpp:193) and j != i, r < 2 hbar, r != 0 (sph.hpp:222,287),
@@ -67,7 +68,6 @@ struct ImpactD {
 template <class R>
 struct View {
     int64_t n;          // resident particles
-    int64_t stride;     // neighbour list column stride
     int32_t cap;        // neighbour list capacity per particle
     int32_t pad;
     double *x, *y, *z, *u, *vx, *vy, *vz;
@@ -87,10 +87,12 @@ struct View {
     uint32_t* cpk;
     unsigned long long* refbin;
     const int32_t* cell_ptr;
-    int32_t* nbr;
+    int32_t* nbr;       // own list, 4-entry blocks: entry t of k at nbr_slot(t, ls) + 4k
+    int64_t ls;         // list stride (particle capacity): a warp reads a block of 32
+                        // consecutive particles as one contiguous 512-byte run
     int32_t* nbr_cnt;
     float* hlist;       // h of each particle when its list was built
-    int32_t* xnbr;      // extra (reverse) list, row-major [k * kExtraCap + t]
+    int32_t* xnbr;      // extra (reverse) list, entry-major [t * ls + k], t < kExtraCap
     int32_t* xcnt;
     int32_t* flags;     // [0] list overflow max, [1] any impact still in a density round
     ImpactD* imps;
@@ -346,6 +348,25 @@ __device__ __forceinline__ void traverse_sphere(const View<R>& v, const ImpactD&
     }
 }
 
+// Own-list addressing: entry t of particle k lives at nbr[4k + nbr_slot(t, ls)],
+// i.e. 4-entry blocks stored block-major, so one int4 load brings a lane four
+// entries and a warp's block loads are contiguous.
+__device__ __forceinline__ int64_t nbr_slot(int t, int64_t ls) {
+    return (((int64_t)(t >> 2) * ls) << 2) + (t & 3);
+}
+
+// f(j) for entries 0..cnt-1 of particle k's own list, in list order.
+template <class F>
+__device__ __forceinline__ void walk_list(const int32_t* nbr, int64_t ls, int64_t k, int cnt, F&& f) {
+    const int4* p = reinterpret_cast<const int4*>(nbr) + k;
+    for (int t = 0; t < cnt; t += 4, p += ls) {
+        const int4 q = *p;
+        const int m = min(4, cnt - t);
+#pragma unroll 1
+        for (int i = 0; i < m; i++) f(i == 0 ? q.x : i == 1 ? q.y : i == 2 ? q.z : q.w);
+    }
+}
+
 // ---------------------------------------------------------------- kernels
 
 // Kick (half step with the old acceleration) and drift (sph.hpp:360-361).
@@ -563,7 +584,7 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
     const float ri2 = ri * ri;
     int cnt = 0;
     const int cap = v.cap;
-    int32_t* out = v.nbr + (int64_t)k * cap;
+    int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
     traverse_sphere(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
         const float4 pj = v.pf[j];
         float dx = (pi.x - pj.x) + dxc;
@@ -574,14 +595,14 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
         if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < ri2) {
-            if (cnt < cap) out[cnt] = j;
+            if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
             cnt++;
             // does j's own search miss k although the pair can interact?
             const float rj = 2.0f * pj.w * sl + m;
             const float rb = (pi.w + pj.w) * sl + m;
             if (!(r2 < rj * rj) && r2 < rb * rb) {
                 const int slot = atomicAdd(&v.xcnt[j], 1);
-                if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
             }
         }
     });
@@ -650,7 +671,7 @@ static __global__ void k_list_thread(View<R> v) {
     const int ulo1 = __reduce_min_sync(full, act ? lo1 : INT_MAX), uhi1 = __reduce_max_sync(full, act ? hi1 : INT_MIN);
     int cnt = 0;
     const int cap = v.cap;
-    int32_t* out = v.nbr + k * cap;
+    int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
     for (int ix = ulo0; ix <= uhi0; ix++) {
         const float xa = (float)(ix - c[0]) * w0 - pi.x;
         float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
@@ -685,13 +706,13 @@ static __global__ void k_list_thread(View<R> v) {
                 const float dz = (pi.z - pj.z) + dzc;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (ok && r2 < ri2) {
-                    if (cnt < cap) out[cnt] = j;
+                    if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
                     cnt++;
                     const float rj = 2.0f * pj.w * sl + m;
                     const float rb = (pi.w + pj.w) * sl + m;
                     if (!(r2 < rj * rj) && r2 < rb * rb) {
                         const int slot = atomicAdd(&v.xcnt[j], 1);
-                        if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                        if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
                     }
                 }
             }
@@ -759,7 +780,7 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
         const float Rs = ri + m;
         int cnt = 0;
         const int cap = v.cap;
-        int32_t* out = v.nbr + k * cap;
+        int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
         int icx, icy, icz;
         unpack_cell(ci, icx, icy, icz);
         if (I.per[0] | I.per[1] | I.per[2]) {
@@ -772,12 +793,12 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
                     if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     if (r2 < ri2) {
-                        if (cnt < cap) out[cnt] = j;
+                        if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
                         cnt++;
                         const float rj = 2.0f * pj.w * sl + m, rb = (pi.w + pj.w) * sl + m;
                         if (!(r2 < rj * rj) && r2 < rb * rb) {
                             const int slot = atomicAdd(&v.xcnt[j], 1);
-                            if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                            if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
                         }
                     }
                 });
@@ -833,12 +854,12 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
                         const float dx = (pi.x - pj.x) + dxc, dy = (pi.y - pj.y) + dyc, dz = (pi.z - pj.z) + dzc;
                         const float r2 = dx * dx + dy * dy + dz * dz;
                         if (active && r2 < ri2) {
-                            if (cnt < cap) out[cnt] = j;
+                            if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
                             cnt++;
                             const float rj = 2.0f * pj.w * sl + m, rb = (pi.w + pj.w) * sl + m;
                             if (!(r2 < rj * rj) && r2 < rb * rb) {
                                 const int slot = atomicAdd(&v.xcnt[j], 1);
-                                if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                                if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
                             }
                         }
                     }
@@ -878,7 +899,7 @@ static __global__ void __launch_bounds__(256) k_list_wpp(View<R> v) {
     const float ri2 = ri * ri;
     const float Rs = ri + m;
     const int cap = v.cap;
-    int32_t* out = v.nbr + k * cap;
+    int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
     int c[3];
     unpack_cell(ci, c[0], c[1], c[2]);
     const float o[3] = {pi.x, pi.y, pi.z};
@@ -970,14 +991,14 @@ static __global__ void __launch_bounds__(256) k_list_wpp(View<R> v) {
                     const float rb = (pi.w + pj.w) * sl + m;
                     if (!(r2 < rj * rj) && r2 < rb * rb) {
                         const int slot = atomicAdd(&v.xcnt[j], 1);
-                        if (slot < kExtraCap) v.xnbr[(int64_t)j * kExtraCap + slot] = (int32_t)k;
+                        if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
                     }
                 }
             }
             const unsigned bm = __ballot_sync(0xffffffffu, hit);
             if (hit) {
                 const int pos = cnt + __popc(bm & below);
-                if (pos < cap) out[pos] = j;
+                if (pos < cap) out[nbr_slot(pos, v.ls)] = j;
             }
             cnt += __popc(bm);
             if (have) j++;
@@ -997,15 +1018,16 @@ static __global__ void k_sort_extra(View<R> v) {
     if (k >= v.n) return;
     const int c = min(v.xcnt[k], kExtraCap);
     if (c < 2) return;
-    int32_t* a = v.xnbr + (int64_t)k * kExtraCap;
+    int32_t* a = v.xnbr + k;  // entry t at a[t * ls]
+    const int64_t ls = v.ls;
     for (int i = 1; i < c; i++) {
-        int32_t x = a[i];
+        int32_t x = a[i * ls];
         int j = i - 1;
-        while (j >= 0 && a[j] > x) {
-            a[j + 1] = a[j];
+        while (j >= 0 && a[j * ls] > x) {
+            a[(j + 1) * ls] = a[j * ls];
             j--;
         }
-        a[j + 1] = x;
+        a[(j + 1) * ls] = x;
     }
 }
 
@@ -1087,8 +1109,7 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
         };
         if (list_covers(v, I, k, (float)hi)) {
             const int cnt = v.nbr_cnt[k];
-            const int32_t* lst = v.nbr + (int64_t)k * v.cap;
-            for (int t = 0; t < cnt; t++) body(lst[t]);
+            walk_list(v.nbr, v.ls, k, cnt, body);
         } else {
             const float hf = (float)hi;
             traverse(v, I, pi, ci, 2.0f * hf * 1.0001f + 2.0f * I.margin + 1e-6f * hf,
@@ -1141,8 +1162,11 @@ static __global__ void k_eos(View<R> v) {
         v.fc[k] = make_float4((float)v.S[0][k], (float)v.S[1][k], (float)v.S[2][k], (float)v.S[3][k]);
         const double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k];
         const float hx = (float)vx, hy = (float)vy, hz = (float)vz;
-        v.vh[k] = make_float4(hx, hy, hz, 0.0f);
-        v.vl[k] = make_float4((float)(vx - (double)hx), (float)(vy - (double)hy), (float)(vz - (double)hz), 0.0f);
+        // .w lanes carry the mass and packed cell of the particle, so the force
+        // pass gathers six records per neighbour instead of seven
+        v.vh[k] = make_float4(hx, hy, hz, (float)v.mass[k]);
+        v.vl[k] = make_float4((float)(vx - (double)hx), (float)(vy - (double)hy), (float)(vz - (double)hz),
+                              __uint_as_float(v.cpk[k]));
     }
 }
 
@@ -1250,9 +1274,9 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             // entries interact), and a pair that fails the criterion -- or the
             // particle itself (r = 0) -- contributes exact zeros through dW = 0.
             const float4 pj = v.pf[j];
-            const float2 mk = v.pk[j];
             const float4 fa = v.fa[j], fb = v.fb[j], fc = v.fc[j];
             const float4 vhj = v.vh[j], vlj = v.vl[j];
+            const float2 mk = make_float2(vhj.w, vlj.w);  // (mass, packed cell)
             float dx, dy, dz;
             sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -1275,11 +1299,10 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     };
     if (!I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap) {
         const int cnt = v.nbr_cnt[k];
-        const int32_t* lst = v.nbr + (int64_t)k * v.cap;
-        for (int t = 0; t < cnt; t++) body(lst[t]);
+        walk_list(v.nbr, v.ls, k, cnt, body);
         const int xc = v.xcnt[k];
-        const int32_t* xl = v.xnbr + (int64_t)k * kExtraCap;
-        for (int t = 0; t < xc; t++) body(xl[t]);
+        const int32_t* xl = v.xnbr + k;
+        for (int t = 0; t < xc; t++, xl += v.ls) body(*xl);
     } else {
         traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
                  [&](int32_t j, float, float, float) { body(j); });
