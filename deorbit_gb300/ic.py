@@ -38,6 +38,13 @@ def tillotson(rho0, A, B, a, b, alpha, beta, u0, uiv, ucv, G=0.0, Y=0.0, wm=0.0,
     return m
 
 
+def ideal_gas(gamma):
+    """Ideal-gas material dict (eos.hpp:29): P = (gamma - 1) rho u."""
+    m = {k: 0.0 for k in MAT_FIELDS}
+    m.update(type=0, yield_model=0, gamma=gamma)
+    return m
+
+
 def iron(strength=True):
     """Reference iron set (eos.hpp:42-43); strength=False drops G and Y (hydro only)."""
     return tillotson(7800, 1.28e11, 1.05e11, 0.5, 1.5, 5, 5, 9.5e6, 2.4e6, 8.67e6,
@@ -206,6 +213,35 @@ def periodic_bar(nx=24, ny=6, dx=0.01, seed=7):
     return Scenario("periodic_bar", p, vel, mass, np.zeros(p.shape[0]), np.zeros(p.shape[0], np.int32), fixed,
                     np.array([x0, 0.0, 0.0]), np.array([x1, Lyz, Lyz]), np.array([0, 1, 1], np.int32),
                     dict(eta=1.3, h_init=1.3 * dx), mats, dx)
+
+
+def sod_tube(a_left=0.005, nx_left=100, ny_left=16, gamma=1.4):
+    """3D Sod shock tube (the reference's first validation gate, sod.cpp:8-50):
+    ideal gas, a thin slab periodic in y and z, density 1 / 0.125 and pressure
+    1 / 0.1 across x = 0 from lattices of spacing a and 2a (equal masses),
+    particles within 2 h_init of either end frozen; artificial viscosity
+    alpha 1, beta 2 and conductivity alpha_u 1."""
+    aL, aR = a_left, 2.0 * a_left
+    nxR, nyR = nx_left // 2, ny_left // 2
+    h_init = 1.3 * aL
+    xfix = 2.0 * h_init
+    rhoL, PL, PR = 1.0, 1.0, 0.1
+    rhoR = 0.125
+    m = rhoL * aL ** 3
+    left = lattice(nx_left, ny_left, ny_left, aL, (-0.5, 0.0, 0.0))
+    right = lattice(nxR, nyR, nyR, aR, (0.0, 0.0, 0.0))
+    pos = np.concatenate([left, right])
+    nL = left.shape[0]
+    u = np.r_[np.full(nL, PL / ((gamma - 1.0) * rhoL)), np.full(right.shape[0], PR / ((gamma - 1.0) * rhoR))]
+    fixed = ((pos[:, 0] < -0.5 + xfix) & (np.arange(pos.shape[0]) < nL)) | \
+            ((pos[:, 0] > 0.5 - xfix) & (np.arange(pos.shape[0]) >= nL))
+    mats = [ideal_gas(gamma)]
+    Lyz = ny_left * aL
+    return Scenario("sod_tube", pos, np.zeros_like(pos), np.full(pos.shape[0], m), u,
+                    np.zeros(pos.shape[0], np.int32), fixed.astype(np.uint8),
+                    np.array([-0.5, 0.0, 0.0]), np.array([0.5, Lyz, Lyz]), np.array([0, 1, 1], np.int32),
+                    dict(eta=1.3, h_init=h_init, alpha=1.0, beta=2.0, eps=0.01, alpha_u=1.0, cfl=0.2),
+                    mats, aL)
 
 
 def _graded_layers(dx0, growth, L):
