@@ -220,9 +220,13 @@ static __global__ void __launch_bounds__(512) k_diagnostics(View<R> v, int b, in
     }
 }
 
+// After a sort: offsets change, and positions may have (bins are stale).
 static __global__ void k_impact_reset_omax(ImpactD* imps, int nimp) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nimp) imps[b].omax_bits = 0u;
+    if (b < nimp) {
+        imps[b].omax_bits = 0u;
+        imps[b].bins_ok = 0;
+    }
 }
 
 static __global__ void k_set_mask_dt(ImpactD* imps, int nimp, const int32_t* mask, const double* dt,
@@ -271,7 +275,6 @@ public:
         DSPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
         DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
-        DSPH_CUDA(cudaMalloc(&ne_count_, sizeof(int32_t)));
         DSPH_CUDA(cudaMalloc(&ntask_, sizeof(int32_t)));
         DSPH_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
         DSPH_CUDA(cudaMallocHost(&flags_h_, sizeof(int32_t) * 4));
@@ -286,7 +289,6 @@ public:
         for (void* p : allocs_) cudaFree(p);
         cudaFree(mats_d_);
         cudaFree(flags_d_);
-        cudaFree(ne_count_);
         cudaFree(ntask_);
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
@@ -1349,7 +1351,6 @@ public:
         dfree(fa_); fa_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(fb_); fb_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(fc_); fc_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
-        dfree(ne_cells_); ne_cells_ = dalloc<int32_t>(nc);
         dfree(tasks_); tasks_ = dalloc<int32_t>(nc);
         dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
         dfree(refbin_); refbin_ = dalloc<unsigned long long>(nc);
@@ -1549,8 +1550,7 @@ public:
         cur_ = alt;
         N_ = n_new;
         launch_small(k_impact_reset_omax, nimp);
-        DSPH_CUDA(cudaMemsetAsync(ne_count_, 0, sizeof(int32_t), st_));
-        launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_, (const uint32_t*)skeys_, ne_cells_, ne_count_);
+        launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_);
         launch_small(k_impact_ranges, nimp, (const int32_t*)cell_cnt_);
         cls(keep_cls);
         grid_valid_ = true;
@@ -1628,14 +1628,14 @@ public:
         launch_small(k_impact_begin_round, nimp, 2);
         for (int round = 0; round < 4; round++) {
             cls(KC_GRID);
-            if (round > 0) launch_small(k_impact_begin_round, nimp, 0);
-            hmax_pass(0);
+            if (round > 0) launch_small(k_impact_begin_round, nimp, 0);  // max h carried over
+            else hmax_pass(0);
             launch_small(k_ref_grid, nimp);
             launch_n(k_ref_bins<R>, N_);
             cls(KC_DENSITY);
-            if (iters > 0) launch_n_raw(k_density<R>, N_, view(), iters);
+            if (iters > 0) launch_n_raw(k_density<R>, N_, view(), iters);  // also reduces the new max h
+            else hmax_pass(1);
             cls(KC_GRID);
-            hmax_pass(1);
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 1, 0, sizeof(int32_t), st_));
             launch_small(k_round_check, nimp, flags_d_);
             if (host_sync) {
@@ -1644,14 +1644,16 @@ public:
                 if (!flags_h_[1]) break;
             }
         }
-        final_grid_build();
+        final_grid_build(true);
     }
 
-    void final_grid_build() {
+    // Reference grid and bins for the force pass; after_rounds: the max h is the
+    // one the last density pass reduced.
+    void final_grid_build(bool after_rounds = false) {
         const int nimp = (int)imp_.size();
         cls(KC_GRID);
-        launch_small(k_impact_begin_round, nimp, 1);
-        hmax_pass(0);
+        launch_small(k_impact_begin_round, nimp, after_rounds ? 3 : 1);
+        if (!after_rounds) hmax_pass(0);
         launch_small(k_ref_grid, nimp);
         launch_n(k_ref_bins<R>, N_);
     }
@@ -1712,8 +1714,6 @@ public:
     float4* vl_ = nullptr;
     float2* pk_ = nullptr;
     float4 *fa_ = nullptr, *fb_ = nullptr, *fc_ = nullptr;
-    int32_t* ne_cells_ = nullptr;
-    int32_t* ne_count_ = nullptr;
     int32_t* tasks_ = nullptr;
     int32_t* ntask_ = nullptr;
     unsigned int* cell_hmax_ = nullptr;

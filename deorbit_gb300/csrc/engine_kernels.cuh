@@ -48,7 +48,8 @@ struct ImpactD {
     int64_t cell_base, ncells;
     // reference grid of the last build (sph.hpp:147-157)
     int32_t nc[3], rounds;
-    double cw[3];
+    double cw[3], icw[3];                          // cell widths and their reciprocals
+    int32_t bins_ok, pad2;                         // refbin matches this grid and the positions
     double h_max, hmax0;
     float hmax_f, margin;
     double inv_poly_eta;                           // 1 / W-polynomial at q = 1/eta
@@ -162,9 +163,16 @@ __device__ __forceinline__ int sat_int(double q) {
     return (int)q;
 }
 
-// Reference-grid bin of one coordinate (sph.hpp:142-146), exact FP64.
+// Reference-grid bin of one coordinate (sph.hpp:142-146), exact FP64: the
+// truncation of the IEEE quotient (c - lo) / cw.  The quotient is formed with
+// the reciprocal (one multiply instead of a division, which is slow in FP64);
+// it is within 2 ulp of the IEEE quotient, so the truncations agree unless an
+// integer lies within a few ulp of it -- then the division decides.
 __device__ __forceinline__ int ref_bin(const ImpactD& I, int a, double c) {
-    int i = sat_int(__ddiv_rn(__dsub_rn(c, I.dlo[a]), I.cw[a]));
+    const double d = __dsub_rn(c, I.dlo[a]);
+    double q = __dmul_rn(d, I.icw[a]);
+    if (fabs(q - rint(q)) <= fabs(q) * 0x1p-49 + 0x1p-1000) q = __ddiv_rn(d, I.cw[a]);
+    int i = sat_int(q);
     if (i < 0) i = 0;
     if (i >= I.nc[a]) i = I.nc[a] - 1;
     return i;
@@ -455,12 +463,10 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
 // After the gather: inverse permutation, traversal-cell coordinates and FP32
 // offsets from the cell origin, largest |offset| per impact.
 template <class R>
-static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid, const uint32_t* skey,
-                                   int32_t* ne_cells, int32_t* ne_count) {
+static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid) {
     int64_t k = gtid();
     if (k >= v.n) return;
     pos_of_gid[v.gid[k]] = (int32_t)k;
-    if (k == 0 || skey[k] != skey[k - 1]) ne_cells[atomicAdd(ne_count, 1)] = (int32_t)skey[k];
     ImpactD& I = v.imps[v.imp[k]];
     double fx, fy, fz;
     int cx = fine_cell(I, 0, v.x[k], fx);
@@ -495,15 +501,24 @@ static __global__ void k_impact_reset_slack(ImpactD* imps, int nimp) {
     if (b < nimp && imps[b].mask) imps[b].slack_flag = 0;
 }
 
+// set_active: 2 first round of a step, 0 a later round, 1 a grid build outside
+// the rounds, 3 the grid build after the rounds.  The max h at a round's start
+// (and at the build after the rounds) is the max the previous round's density
+// pass reduced (h does not change in between); otherwise it is reduced anew.
 static __global__ void k_impact_begin_round(ImpactD* imps, int nimp, int set_active) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nimp) return;
     ImpactD& I = imps[b];
     if (set_active) {
         I.active = I.mask;
-        if (set_active == 2 && I.mask) I.rounds = 0;
+        if (set_active == 2 && I.mask) {
+            I.rounds = 0;
+            I.bins_ok = 0;
+        }
     }
-    if (I.mask && I.active) I.hmax_bits = 0x3bc79ca10c924223ull;  // bits of 1e-30 (> 0)
+    if (I.mask && I.active)
+        I.hmax_bits = (set_active == 0 || set_active == 3) ? I.hm_bits
+                                                           : 0x3bc79ca10c924223ull;  // bits of 1e-30 (> 0)
 }
 
 template <class R>
@@ -527,6 +542,7 @@ static __global__ void k_ref_grid(ImpactD* imps, int nimp) {
     I.hmax0 = hm;
     I.hmax_f = (float)hm;
     double rc = 2.0 * hm;
+    bool same = I.bins_ok != 0;
     for (int a = 0; a < 3; a++) {
         double ext = I.dhi[a] - I.dlo[a];
         if (ext <= 0) ext = rc;
@@ -534,9 +550,13 @@ static __global__ void k_ref_grid(ImpactD* imps, int nimp) {
         int m = q >= 2097151.0 ? 2097151 : (int)q;
         if (m < 1) m = 1;
         if (I.per[a] && m < 3) m = 1;
+        const double cw = __ddiv_rn(ext, (double)m);
+        same = same && m == I.nc[a] && cw == I.cw[a];
         I.nc[a] = m;
-        I.cw[a] = __ddiv_rn(ext, (double)m);
+        I.cw[a] = cw;
+        I.icw[a] = __ddiv_rn(1.0, cw);
     }
+    I.bins_ok = same ? 1 : 0;  // same grid, positions unchanged since the bins were made
     float cwm = 3.0e38f;
     for (int a = 0; a < 3; a++)
         if (I.nc[a] > 1) cwm = fminf(cwm, (float)I.cw[a]);
@@ -549,7 +569,7 @@ static __global__ void k_ref_bins(View<R> v) {
     int64_t k = gtid();
     if (k >= v.n) return;
     const ImpactD& I = v.imps[v.imp[k]];
-    if (!(I.mask && I.active)) return;
+    if (!(I.mask && I.active) || I.bins_ok) return;
     unsigned long long b0 = (unsigned long long)ref_bin(I, 0, v.x[k]);
     unsigned long long b1 = (unsigned long long)ref_bin(I, 1, v.y[k]);
     unsigned long long b2 = (unsigned long long)ref_bin(I, 2, v.z[k]);
@@ -562,6 +582,7 @@ static __global__ void k_round_check(ImpactD* imps, int nimp, int32_t* flags) {
     if (b >= nimp) return;
     ImpactD& I = imps[b];
     if (!(I.mask && I.active)) return;
+    I.bins_ok = 1;  // this round's bins exist
     I.rounds++;
     double hm = bitsd(I.hm_bits);
     if (hm < 1e-30) hm = 1e-30;
@@ -1121,6 +1142,7 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
     v.rho[k] = rho;
     v.hh[k] = hi;
     v.pf[k].w = (float)hi;
+    impact_atomic_max(&I.hm_bits, (double)hi);  // the round's new max h
     if (!((float)hi <= v.hlist[k] * (1.0f + I.slack) * 0.99999f)) {
         atomicOr(&I.slack_flag, 1);
         atomicOr(&v.flags[2], 1);
