@@ -1201,7 +1201,7 @@ public:
                 I.nf[a] = nf;
                 I.w[a] = ext / nf;
             } else {
-                double pad = 0.1 * ext + 2 * w0;
+                double pad = 0.02 * ext + 2 * w0;  // room just past the domain before clamping
                 double span = ext + 2 * pad;
                 int nf = (int)std::ceil(span / w0);
                 double w = w0;
@@ -1345,6 +1345,8 @@ public:
         }
         for (int c = 0; c < kNDer; c++) { dfree(der_[c]); der_[c] = dalloc<R>(nc); }
         dfree(pf_); pf_ = dalloc<float4>(nc);
+        dfree(pf_tmp_); pf_tmp_ = dalloc<float4>(nc);
+        dfree(cpk_tmp_); cpk_tmp_ = dalloc<uint32_t>(nc);
         dfree(vh_); vh_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(vl_); vl_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(pk_); pk_ = dalloc<float2>(sizeof(R) == 4 ? nc : 1);
@@ -1522,7 +1524,8 @@ public:
         DSPH_CUDA(cudaMemsetAsync(cell_cnt_, 0, sizeof(int32_t) * (C_ + 1), st_));
         const int keep_cls = cur_cls_;
         cls(KC_SORT);
-        launch_n_raw(k_fine_keys<R>, N_, view(), keys_by_gid_, cell_cnt_);
+        launch_small(k_impact_reset_omax, nimp);
+        launch_n_raw(k_fine_keys<R>, N_, view(), keys_by_gid_, cell_cnt_, pf_tmp_, cpk_tmp_);
         prof_begin();
         launches_ += radix_sort_pairs(keys_by_gid_, nullptr, skeys_, sgid_, tkeys_, tgid_, G_,
                                       key_bits(), scratch_, st_);
@@ -1545,11 +1548,12 @@ public:
             g.b_in[1] = fixed_[cur_]; g.b_out[1] = fixed_[alt];
             g.imp_in = impc_[cur_]; g.imp_out = impc_[alt];
             g.gid_in = gid_[cur_]; g.gid_out = gid_[alt];
+            g.pf_in = pf_tmp_; g.pf_out = pf_;
+            g.cpk_in = cpk_tmp_; g.cpk_out = cpk_;
             launch_n_raw(k_gather<R>, n_new, n_new, (const int32_t*)src_, g);
         }
         cur_ = alt;
         N_ = n_new;
-        launch_small(k_impact_reset_omax, nimp);
         launch_n_raw(k_post_sort<R>, N_, view(), pos_of_gid_);
         launch_small(k_impact_ranges, nimp, (const int32_t*)cell_cnt_);
         cls(keep_cls);
@@ -1710,6 +1714,8 @@ public:
     int32_t* gid_[2] = {};
     R* der_[kNDer] = {};
     float4* pf_ = nullptr;
+    float4* pf_tmp_ = nullptr;     // offsets / cells in the pre-sort order
+    uint32_t* cpk_tmp_ = nullptr;
     float4* vh_ = nullptr;
     float4* vl_ = nullptr;
     float2* pk_ = nullptr;

@@ -408,20 +408,27 @@ __device__ __forceinline__ int fine_cell(const ImpactD& I, int a, double c, doub
 }
 
 // Traversal-cell key of every resident particle, scattered into gid order,
-// plus per-cell counts.
+// per-cell counts, and (in the current order, for the gather to carry) the
+// FP32 offset from the cell origin with h, the packed cell coordinates and the
+// per-impact largest |offset|.
 template <class R>
-static __global__ void k_fine_keys(View<R> v, uint32_t* keys_by_gid, int32_t* cell_count) {
+static __global__ void k_fine_keys(View<R> v, uint32_t* keys_by_gid, int32_t* cell_count, float4* pf_out,
+                                   uint32_t* cpk_out) {
     int64_t k = gtid();
     if (k >= v.n) return;
-    const ImpactD& I = v.imps[v.imp[k]];
+    ImpactD& I = v.imps[v.imp[k]];
     if (!I.alive) return;  // leaves the arrays at this sort (key stays invalid)
-    double f;
-    int cx = fine_cell(I, 0, v.x[k], f);
-    int cy = fine_cell(I, 1, v.y[k], f);
-    int cz = fine_cell(I, 2, v.z[k], f);
-    int64_t key = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2] + cz;
+    double fx, fy, fz;
+    const int cx = fine_cell(I, 0, v.x[k], fx);
+    const int cy = fine_cell(I, 1, v.y[k], fy);
+    const int cz = fine_cell(I, 2, v.z[k], fz);
+    const int64_t key = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2] + cz;
     keys_by_gid[v.gid[k]] = (uint32_t)key;
     atomicAdd(&cell_count[key], 1);
+    const float ox = (float)(fx * I.w[0]), oy = (float)(fy * I.w[1]), oz = (float)(fz * I.w[2]);
+    pf_out[k] = make_float4(ox, oy, oz, (float)v.hh[k]);
+    cpk_out[k] = (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22);
+    impact_atomic_max_u32(&I.omax_bits, __float_as_uint(fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz))));
 }
 
 static __global__ void k_make_src(int64_t n, const int32_t* sorted_gid, const int32_t* pos_of_gid,
@@ -444,6 +451,10 @@ struct GatherCols {
     uint16_t* imp_out;
     const int32_t* gid_in;
     int32_t* gid_out;
+    const float4* pf_in;     // offsets + h and packed cells made by k_fine_keys
+    float4* pf_out;
+    const uint32_t* cpk_in;
+    uint32_t* cpk_out;
 };
 
 template <class R>
@@ -458,6 +469,8 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
     g.b_out[1][k] = g.b_in[1][s];
     g.imp_out[k] = g.imp_in[s];
     g.gid_out[k] = g.gid_in[s];
+    g.pf_out[k] = g.pf_in[s];
+    g.cpk_out[k] = g.cpk_in[s];
 }
 
 // After the gather: inverse permutation, traversal-cell coordinates and FP32
@@ -467,17 +480,7 @@ static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid) {
     int64_t k = gtid();
     if (k >= v.n) return;
     pos_of_gid[v.gid[k]] = (int32_t)k;
-    ImpactD& I = v.imps[v.imp[k]];
-    double fx, fy, fz;
-    int cx = fine_cell(I, 0, v.x[k], fx);
-    int cy = fine_cell(I, 1, v.y[k], fy);
-    int cz = fine_cell(I, 2, v.z[k], fz);
-    float ox = (float)(fx * I.w[0]), oy = (float)(fy * I.w[1]), oz = (float)(fz * I.w[2]);
-    v.pf[k] = make_float4(ox, oy, oz, (float)v.hh[k]);
-    v.cpk[k] = (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22);
     if (sizeof(R) == 4) v.pk[k] = make_float2((float)v.mass[k], __uint_as_float(v.cpk[k]));
-    float om = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
-    impact_atomic_max_u32(&I.omax_bits, __float_as_uint(om));
 }
 
 // Per-impact sorted ranges from the cell pointer.
