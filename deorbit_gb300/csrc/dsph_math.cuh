@@ -29,6 +29,12 @@ template <class R> __device__ __forceinline__ R rmin(R a, R b) { return (b < a) 
 
 __device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
+
+// Divisions inside pair loops: the hardware approximation (__fdividef, 2 ulp)
+// in FP32 -- far inside the mixed form's error budget -- and the IEEE division
+// in FP64, whose results stay bit-comparable with the oracle's.
+__device__ __forceinline__ float pair_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double pair_div(double a, double b) { return a / b; }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return expf(x); }
 __device__ __forceinline__ double rcbrt(double x) { return cbrt(x); }

@@ -1126,7 +1126,8 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
                 sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 // the kernel vanishes at q >= 2; only the stencil restriction needs a test
-                float w = mk.x * kernel_W_bf<float>(sqrtf(r2), (float)ihi);
+                const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;  // hardware 1/sqrt (2 ulp)
+                float w = mk.x * kernel_W_bf<float>(r, (float)ihi);
                 if (need_member && !ref_member(bi, v.refbin[j], I)) w = 0.0f;
                 sum.add((R)w);
             }
@@ -1238,9 +1239,9 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
         const R dvr = vx * rx + vy * ry + vz * rz;
         R Pij = R(0);
         if (dvr < R(0)) {
-            const R mu = hbar * dvr / (r * r + eps * hbar * hbar);
+            const R mu = pair_div(hbar * dvr, r * r + eps * hbar * hbar);
             const R cbar = R(0.5) * (csi + csj);
-            Pij = (-alpha * cbar * mu + beta * mu * mu) / (R(0.5) * (rhoi + rhoj));
+            Pij = pair_div(-alpha * cbar * mu + beta * mu * mu, R(0.5) * (rhoi + rhoj));
         }
         const R term = Pi_over + pfj + Pij;
         du.add(R(0.5) * mj * term * (vx * gx + vy * gy + vz * gz));
@@ -1262,8 +1263,8 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
         az.add(stz * mj - gz * mm);
         if (alpha_u > R(0)) {
             const R rbar = R(0.5) * (rhoi + rhoj);
-            const R vsig = rsqrt_(rabs(Pi - v.P[j]) / rbar);
-            du.add(alpha_u * mj * vsig * (ui - (R)v.u[j]) * dW / rbar);
+            const R vsig = rsqrt_(pair_div(rabs(Pi - v.P[j]), rbar));
+            du.add(pair_div(alpha_u * mj * vsig * (ui - (R)v.u[j]) * dW, rbar));
         }
     };
     const float hs_pad = 2.0f * m;
@@ -1308,11 +1309,12 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             const float hs = (float)hi + pj.w;
             bool ok = r2 < hs * hs && r2 != 0.0f;
             if (need_member) ok = ok && ref_member(bi, v.refbin[j], I);
-            const R r = ok ? (R)sqrtf(r2) : R(1);
+            const float irs = ok ? rsqrtf(r2) : 1.0f;  // hardware 1/sqrt (2 ulp)
+            const R r = ok ? (R)(r2 * irs) : R(1);
             const R hbar = R(0.5) * (hi + (R)pj.w);
-            const R ihb = R(1) / hbar;
+            const R ihb = pair_div(R(1), hbar);
             const R dW = ok ? kernel_dW_bf<R>(r, ihb) : R(0);
-            const R wg = dW / r;
+            const R wg = dW * (R)irs;
             const R gx = (R)dx * wg, gy = (R)dy * wg, gz = (R)dz * wg;
             // hi parts nearly cancel exactly; lo parts restore the FP64 difference
             const R vx = (R)((vhi.x - vhj.x) + (vli.x - vlj.x));
