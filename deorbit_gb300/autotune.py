@@ -75,7 +75,8 @@ def key(precision, cls, device=0) -> str:
 
 
 def measure(sc, precision, cfg, device=0, steps=3, warmup=2) -> float:
-    """ms per KDK step of `sc` under configuration cfg (dict of engine options)."""
+    """ms per KDK step of `sc` (one scenario, or a list run as one batch)
+    under configuration cfg (dict of engine options)."""
     from . import ic, sph
 
     ctx = sph.Context(precision, device)
@@ -83,7 +84,9 @@ def measure(sc, precision, cfg, device=0, steps=3, warmup=2) -> float:
         ctx.set_tuning(cfg.get("block", 0), cfg.get("cell_factor", 0.0))
         ctx.set_option("slack", cfg.get("slack", 0.08))
         ctx.set_option("list_mode", cfg.get("list_mode", 1))
-        ic.to_context(ctx, sc)
+        mids = {}
+        for one in (sc if isinstance(sc, (list, tuple)) else [sc]):
+            ic.to_context(ctx, one, material_ids=mids)
         ctx.init()
         for _ in range(warmup):
             ctx.run(1)
@@ -96,8 +99,13 @@ def measure(sc, precision, cfg, device=0, steps=3, warmup=2) -> float:
 
 
 def tune(sc, precision, device=0, steps=3, warmup=2, candidates=None, force=False, verbose=False):
-    """Search the candidates on `sc`, cache and return (best_cfg, table)."""
-    cls = workload_class(sc)
+    """Search the candidates on `sc` (a scenario, or a list of scenarios run
+    as one batch and classed by their mean size), cache and return
+    (best_cfg, table)."""
+    if isinstance(sc, (list, tuple)):
+        cls = workload_class(sc[0], sum(x.n for x in sc) // len(sc))
+    else:
+        cls = workload_class(sc)
     k = key(precision, cls, device)
     cache = _load()
     if not force and k in cache:
@@ -119,7 +127,8 @@ def tune(sc, precision, device=0, steps=3, warmup=2, candidates=None, force=Fals
             print(f"  {cfg} -> {ms:.3f} ms/step ({time.perf_counter() - t0:.1f} s)", flush=True)
     best = min(table, key=lambda r: r["ms_per_step"])
     best = {k2: best[k2] for k2 in ("list_mode", "slack", "cell_factor", "block")}
-    cache[k] = {"best": best, "table": table, "n": sc.n, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
+    n = sum(x.n for x in sc) if isinstance(sc, (list, tuple)) else sc.n
+    cache[k] = {"best": best, "table": table, "n": n, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     _save(cache)
     return best, table
 
@@ -139,3 +148,31 @@ def apply(ctx, sc, precision, device=0, per_impact_n=None, default=None):
         ctx.set_option("slack", cfg.get("slack", 0.08))
         ctx.set_option("list_mode", cfg.get("list_mode", 1))
     return cfg
+
+
+def ship(device=0, verbose=True):
+    """Re-measure the table shipped for this GPU model (tuned_gb300.json on a
+    GB300): the 1,048,576-particle grazing impact in both forms, the batched
+    class (32 impacts of the 256-impact sweep run as one batch) and the
+    16,777,216-particle graded run (cell factor only).  Returns the entries."""
+    from . import ic
+
+    out = {}
+    runs = [(ic.grazing(), 1, None), (ic.grazing(), 0, None),
+            (ic.batch_impacts(256)[:32], 1, None),
+            (ic.large_graded(), 1, [dict(list_mode=0, slack=0.03, cell_factor=f, block=128)
+                                    for f in CELL_FACTORS])]
+    for sc, prec, cands in runs:
+        best, table = tune(sc, prec, device, candidates=cands, force=True, verbose=verbose)
+        cls = workload_class(sc[0], sum(x.n for x in sc) // len(sc)) if isinstance(sc, list) else workload_class(sc)
+        out[key(prec, cls, device)] = dict(_load()[key(prec, cls, device)],
+                                           source="autotune.ship on GB300")
+        if verbose:
+            print(key(prec, cls, device), "->", best, flush=True)
+    with open(SHIPPED if "GB300" in gpu_name(device) else CACHE + ".ship.json", "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    return out
+
+
+if __name__ == "__main__":
+    ship()

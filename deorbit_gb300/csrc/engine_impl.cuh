@@ -1171,6 +1171,7 @@ public:
         else if (q < 2.0) { double t = 2.0 - q; poly = 0.25 * t * t * t; }
         else poly = 0.0;
         I.inv_poly_eta = poly > 0 ? 1.0 / poly : 0.0;
+        I.inv_poly_eta_f = (float)I.inv_poly_eta;
         for (int a = 0; a < 3; a++) {
             I.dlo[a] = h.dlo[a]; I.dhi[a] = h.dhi[a]; I.per[a] = h.per[a];
         }
@@ -1748,7 +1749,7 @@ public:
     int64_t* flaw_ptr_d_ = nullptr;
     R* flaw_eps_d_ = nullptr;
     int block_ = 128;
-    double cell_factor_ = 0.75;
+    double cell_factor_ = 1.0;
     int list_mode_ = 0;   // 0: thread per particle, 1: warp per column run
     bool use_graphs_ = true;
     uint64_t layout_epoch_ = 1;

@@ -53,6 +53,7 @@ struct ImpactD {
     double h_max, hmax0;
     float hmax_f, margin;
     double inv_poly_eta;                           // 1 / W-polynomial at q = 1/eta
+    float inv_poly_eta_f, pad3;                    // the same in FP32 (no conversion in pair loops)
     float hcap;                                    // upper bound of h (2 max h0)
     float cwmin;                                   // smallest reference cell width (nc > 1)
     float slack;                                   // superset-list radius slack
@@ -1210,6 +1211,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     const bool strength = G > R(0);
     const R alpha = (R)I.alpha, beta = (R)I.beta, eps = (R)I.eps, eps_as = (R)I.eps_as;
     const R alpha_u = (R)I.alpha_u;
+    const R inv_poly = sizeof(R) == 4 ? (R)I.inv_poly_eta_f : (R)I.inv_poly_eta;
     const R hi = v.hh[k], rhoi = v.rho[k], csi = v.csig[k], Pi_over = v.pfr2[k];
     const R dsri = v.dsr2[k], di = v.dscale[k], Rai = v.Rart[k];
     const double vxi = v.vx[k], vyi = v.vy[k], vzi = v.vz[k];
@@ -1249,7 +1251,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
         if (eps_as > R(0)) {
             const R q = r * ihb;
             const R t = rmax(R(2) - q, R(0)), a = rmax(R(1) - q, R(0));
-            const R fr = (R(0.25) * t * t * t - a * a * a) * (R)I.inv_poly_eta;
+            const R fr = (R(0.25) * t * t * t - a * a * a) * inv_poly;
             R fn = fr * fr;
             fn *= fn;
             mterm += (Rai + Raj) * fn;
