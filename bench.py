@@ -61,6 +61,13 @@ ALG_BYTES = {
     "damage": (4 + 4 + 4 + 8 + 4 + 4, 0),
     "finish": (8 * 4 + 6 * 4 + 6 * 4, 0),
 }
+# FP32 flops executed per list entry (per iteration for k_density), from the
+# ncu instruction counters of the mixed kernels (2 x FFMA + FADD + FMUL over
+# the entries processed; captures in profiles/): the numerator of the FP32
+# issue fraction beside the HBM one.
+FLOPS_PER_ENTRY = {"force": 169, "density": 34}
+# nominal FP32 peak: 152 SMs x 128 lanes x 2 flops x 2.07 GHz (no measured figure exists)
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # whole step, per particle-step (carried state read + written, derived fields,
 # lists excluded): FP64 strength+damage 429 B, mixed 241 B
 STEP_BYTES = {8: 429, 4: 241}
@@ -470,11 +477,18 @@ def main():
             if len(f) >= 4 and not line.startswith("#") and f[0] == KERNEL_OF_CLASS[dom] + "_mixed":
                 # bytes per particle measured on a smaller case, scaled to this launch
                 traffic = (float(f[2]) + float(f[3])) * sc.n / float(f[1])
+    fp32 = None
+    if dom in FLOPS_PER_ENTRY:
+        iters = 2 if dom == "density" else 1
+        fl = FLOPS_PER_ENTRY[dom] * list_entries * iters
+        tf = fl / (avg_ms / 1000.0) / 1e12
+        fp32 = {"flops_per_launch": fl, "achieved_tflops": tf, "peak_tflops": FP32_PEAK_TFLOPS,
+                "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)", "frac": tf / FP32_PEAK_TFLOPS}
     roof = {"kernel": KERNEL_OF_CLASS[dom] + "<float>", "bound": "hbm", "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
             "peak_kind": f"{hbm_kind} copy bandwidth", "alg_bytes_per_launch": alg * sc.n,
             "alg_bytes_per_particle": alg, "list_entries_per_particle": list_entries / sc.n,
-            "avg_launch_ms": avg_ms, "launches": nl}
+            "avg_launch_ms": avg_ms, "launches": nl, "fp32_issue": fp32}
     step_bytes = STEP_BYTES[4] * sc.n
     step_roof = {"alg_bytes_per_particle_step": STEP_BYTES[4],
                  "achieved_gbs": step_bytes / (ms / args.steps / 1000.0) / 1e9}

@@ -1,5 +1,6 @@
 // capi.cu -- the C ABI of include/deorbit_sph.h over the engine, host-side
 // flaw seeding and the IC / snapshot / checkpoint file formats.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -527,6 +528,99 @@ std::vector<double> field(EngineBase& e, int b, const char* nm) {
 }
 
 }  // namespace
+
+namespace {
+
+// The reference builder's coordinate range (boundary_daemon.py:111-115):
+// start, start + step, ... by repeated addition while short of stop.
+std::vector<double> accumulated_range(double start, double stop, double step) {
+    std::vector<double> out;
+    double x = start;
+    while (step > 0 ? x < stop : x > stop) {
+        out.push_back(x);
+        x += step;
+        if (out.size() > (size_t)1 << 26) throw dsph::SphError(SPH_ERR_CAPACITY, "grazing IC lattice too large");
+    }
+    return out;
+}
+
+// Layout of build_grazing_ic (boundary_daemon.py:119-158), operation for
+// operation (Python float ** is the C pow; this file is built without FP
+// contraction), so the generated particles equal the reference's file.
+std::shared_ptr<dsph::GrazingLayout> grazing_layout(const sph_grazing_spec& s) {
+    if (!(s.D > 0) || s.cppr < 1 || !(s.v >= 0)) throw dsph::SphError(SPH_ERR_ARG, "grazing IC: need D > 0, cppr >= 1, v >= 0");
+    auto L = std::make_shared<dsph::GrazingLayout>();
+    const double a = s.D / 2.0;
+    const double dx = a / (double)s.cppr;
+    const double m_imp = s.rho_imp * std::pow(dx, 3.0);
+    const double th = s.theta_deg * (M_PI / 180.0);
+    const double vx = s.v * std::cos(th), vz = -s.v * std::sin(th);
+    const double Lx = std::max(20e3, 30.0 * s.D), Ly = std::max(4e3, 6.0 * s.D), Lz = std::max(6e3, 8.0 * s.D);
+    const double wall = 6.0 * dx;
+    const double mt = s.rho_target * std::pow(dx, 3.0);
+    L->xs = accumulated_range(-0.4 * Lx + dx / 2, 0.6 * Lx, dx);
+    L->ys = accumulated_range(-Ly / 2 + dx / 2, Ly / 2, dx);
+    L->zs = accumulated_range(-dx / 2, -Lz, -dx);
+    if (L->xs.empty() || L->ys.empty() || L->zs.empty()) throw dsph::SphError(SPH_ERR_ARG, "grazing IC: empty lattice");
+    L->wall = wall;
+    L->m_target = mt;
+    const double z0 = std::isnan(s.start_h) ? (a + 3.0 * dx) : s.start_h;
+    const double x0 = std::isnan(s.x_impact_frac) ? -0.35 * Lx : (s.x_impact_frac * Lx - z0 / std::tan(th));
+    const int na = (int)std::ceil(a / dx) + 1;
+    for (int i = -na; i <= na; i++)
+        for (int j = -na; j <= na; j++)
+            for (int k = -na; k <= na; k++)
+                if (std::pow(i * dx, 2.0) + std::pow(j * dx, 2.0) + std::pow(k * dx, 2.0) <= a * a) {
+                    L->px.push_back(i * dx + x0);
+                    L->py.push_back(j * dx);
+                    L->pz.push_back(k * dx + z0);
+                }
+    L->vx = vx;
+    L->vz = vz;
+    L->m_imp = m_imp;
+    L->tgt_mat = s.tgt_mat;
+    L->imp_mat = s.imp_mat;
+    L->dx = dx;
+    L->dlo[0] = L->xs.front() - dx;
+    L->dhi[0] = L->xs.back() + dx;
+    L->dlo[1] = L->ys.front() - dx;
+    L->dhi[1] = L->ys.back() + dx;
+    L->dlo[2] = L->zs.back() - dx;
+    L->dhi[2] = z0 + a + 0.5 * Lz;
+    if (L->n() > ((int64_t)1 << 31) - 1) throw dsph::SphError(SPH_ERR_CAPACITY, "grazing IC: too many particles");
+    return L;
+}
+
+}  // namespace
+
+void sph_grazing_spec_default(sph_grazing_spec* s) {
+    if (!s) return;
+    std::memset(s, 0, sizeof(*s));
+    s->theta_deg = 10.0;
+    s->v = 10000.0;
+    s->D = 1000.0;        // boundary_daemon.py:36-40
+    s->rho_imp = 7800.0;
+    s->rho_target = 2700.0;
+    s->x_impact_frac = NAN;
+    s->start_h = NAN;
+    s->cppr = 8;
+    s->tgt_mat = 0;
+    s->imp_mat = 1;
+}
+
+int sph_impact_create_grazing(sph_ctx* ctx, const sph_params* p, const sph_grazing_spec* s, int32_t* impact,
+                              double* dx_out, int64_t* n_out) {
+    return guard([&] {
+        need(p, "params");
+        need(s, "spec");
+        need(impact, "impact");
+        CTX_SET();
+        auto L = grazing_layout(*s);
+        *impact = E(ctx).impact_create_generated(*p, L);
+        if (dx_out) *dx_out = L->dx;
+        if (n_out) *n_out = L->n();
+    });
+}
 
 int sph_load_ic(sph_ctx* ctx, const char* path, const sph_params* p, int32_t* impact) {
     return guard([&] {

@@ -5,6 +5,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../../include/deorbit_sph.h"
 
@@ -15,6 +16,22 @@ struct SphError : std::runtime_error {
     SphError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// Layout of the campaign's grazing IC (boundary_daemon.py:119-158): the
+// target lattice is the product of three coordinate ranges (the reference's
+// accumulated ranges, computed on the host), generated on the device at
+// commit; the impactor sphere's particles are host-built in the reference's
+// order.  Built by grazing_layout() (capi.cu).
+struct GrazingLayout {
+    std::vector<double> xs, ys, zs;
+    double wall = 0, m_target = 0;
+    int32_t tgt_mat = 0, imp_mat = 1;
+    std::vector<double> px, py, pz;   // impactor particles
+    double vx = 0, vz = 0, m_imp = 0;
+    double dlo[3] = {0, 0, 0}, dhi[3] = {0, 0, 0}, dx = 0;
+    int64_t n_slab() const { return (int64_t)xs.size() * (int64_t)ys.size() * (int64_t)zs.size(); }
+    int64_t n() const { return n_slab() + (int64_t)px.size(); }
+};
+
 class EngineBase {
 public:
     virtual ~EngineBase() = default;
@@ -22,6 +39,8 @@ public:
     virtual int add_material(const sph_material& m) = 0;
     virtual int impact_create(const sph_params& p, const double dlo[3], const double dhi[3],
                               const int32_t per[3]) = 0;
+    // impact whose particles are generated at commit (grazing IC)
+    virtual int impact_create_generated(const sph_params& p, std::shared_ptr<const GrazingLayout> L) = 0;
     virtual void impact_set_domain(int b, const double dlo[3], const double dhi[3],
                                    const int32_t per[3]) = 0;
     virtual void impact_set_params(int b, const sph_params& p) = 0;

@@ -238,6 +238,48 @@ static __global__ void k_set_mask_dt(ImpactD* imps, int nimp, const int32_t* mas
     if (t_end) imps[b].t_end = t_end[b];
 }
 
+// Fills for generated impacts.
+template <class T>
+static __global__ void k_fill(T* p, int64_t n, T v) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+static __global__ void k_gid_iota(int32_t* gid, int32_t* pos_of_gid, int64_t n, int64_t gid_base, int64_t at) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    gid[at + i] = (int32_t)(gid_base + i);
+    pos_of_gid[gid_base + i] = (int32_t)(at + i);
+}
+
+// Target lattice of the grazing IC (boundary_daemon.py:136-143) at rows
+// [at, at + nx ny nz): particle l = (ix ny + iy) nz + iz sits at
+// (xs[ix], ys[iy], zs[iz]), at rest, frozen within `wall` of the x / y ends or
+// of the bottom layer -- the reference's loop order and comparisons.
+template <class R>
+static __global__ void k_gen_slab(int64_t at, int nx, int ny, int nz, const double* xs, const double* ys,
+                                  const double* zs, double wall, R mass_t, double* x, double* y, double* z,
+                                  double* vx, double* vy, double* vz, double* u, R* mass, uint8_t* fixed) {
+    const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= (int64_t)nx * ny * nz) return;
+    const int iz = (int)(l % nz);
+    const int64_t r = l / nz;
+    const int iy = (int)(r % ny), ix = (int)(r / ny);
+    const double X = xs[ix], Y = ys[iy], Z = zs[iz];
+    const bool fx = fabs(X - xs[0]) < wall || fabs(X - xs[nx - 1]) < wall;
+    const bool fxy = fx || fabs(Y - ys[0]) < wall || fabs(Y - ys[ny - 1]) < wall;
+    const bool frozen = fxy || Z < zs[nz - 1] + wall;
+    const int64_t k = at + l;
+    x[k] = X;
+    y[k] = Y;
+    z[k] = Z;
+    vx[k] = 0.0;
+    vy[k] = 0.0;
+    vz[k] = 0.0;
+    u[k] = 0.0;
+    mass[k] = mass_t;
+    fixed[k] = frozen ? 1 : 0;
+}
+
 // ----------------------------------------------------------------- engine
 template <class R>
 class Engine final : public EngineBase {
@@ -268,6 +310,7 @@ public:
         double t = 0, dt_last = 0;
         int64_t steps = 0;
         int64_t step_limit = 0;
+        std::shared_ptr<const GrazingLayout> gen;  // particles generated at commit
     };
 
     explicit Engine(int device) : dev_(device) {
@@ -338,6 +381,19 @@ public:
         return imp_[b];
     }
 
+    int impact_create_generated(const sph_params& p, std::shared_ptr<const GrazingLayout> L) override {
+        for (int m : {L->tgt_mat, L->imp_mat})
+            if (m < 0 || m >= (int)mats_h_.size()) throw SphError(SPH_ERR_ARG, "material id out of range");
+        const int32_t per[3] = {0, 0, 0};
+        const int b = impact_create(p, L->dlo, L->dhi, per);
+        ImpactH& h = imp_[b];
+        h.gen = L;
+        h.n = L->n();
+        h.mat_host.assign((size_t)h.n, L->imp_mat);
+        std::fill(h.mat_host.begin(), h.mat_host.begin() + L->n_slab(), L->tgt_mat);
+        return b;
+    }
+
     void impact_set_domain(int b, const double dlo[3], const double dhi[3], const int32_t per[3]) override {
         ImpactH& h = imp(b);
         if (h.committed) throw SphError(SPH_ERR_STATE, "domain is fixed once particles are on the device");
@@ -361,6 +417,7 @@ public:
                               const uint8_t* fixed) override {
         ImpactH& h = imp(b);
         if (h.committed) throw SphError(SPH_ERR_STATE, "particles can only be added before init");
+        if (h.gen) throw SphError(SPH_ERR_STATE, "the impact holds a generated IC");
         if (n < 0 || (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !mass || !u)))
             throw SphError(SPH_ERR_ARG, "null particle array");
         for (int64_t i = 0; i < n; i++) {
@@ -1406,6 +1463,7 @@ public:
             h.sx.clear(); h.sy.clear(); h.sz.clear(); h.svx.clear(); h.svy.clear(); h.svz.clear();
             h.smass.clear(); h.su.clear(); h.seps.clear(); h.sh0.clear(); h.smat.clear(); h.sfixed.clear();
             h.sx.shrink_to_fit(); h.sy.shrink_to_fit(); h.sz.shrink_to_fit();
+            h.gen.reset();
         }
         assign_cell_bases();
         push_table();
@@ -1418,7 +1476,66 @@ public:
         return false;
     }
 
+    template <class T>
+    void dfill(T* p, int64_t n, T v) {
+        if (n > 0) k_fill<T><<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(p, n, v);
+    }
+
+    // Generated impact: the target lattice by k_gen_slab, the impactor from its
+    // host-built coordinates, everything else filled on the device.
+    void upload_generated(size_t b, ImpactH& h) {
+        const GrazingLayout& L = *h.gen;
+        const int64_t n = h.n, at = N_, ns = L.n_slab(), ni = (int64_t)L.px.size();
+        const int c = cur_;
+        double* coord = dalloc_tmp<double>(L.xs.size() + L.ys.size() + L.zs.size());
+        std::vector<double> all(L.xs);
+        all.insert(all.end(), L.ys.begin(), L.ys.end());
+        all.insert(all.end(), L.zs.begin(), L.zs.end());
+        DSPH_CUDA(cudaMemcpyAsync(coord, all.data(), sizeof(double) * all.size(), cudaMemcpyHostToDevice, st_));
+        const int nx = (int)L.xs.size(), ny = (int)L.ys.size(), nz = (int)L.zs.size();
+        if (ns > 0)
+            k_gen_slab<R><<<(unsigned)((ns + 255) / 256), 256, 0, st_>>>(
+                at, nx, ny, nz, coord, coord + nx, coord + nx + ny, L.wall, (R)L.m_target, dcol_[c][0],
+                dcol_[c][1], dcol_[c][2], dcol_[c][4], dcol_[c][5], dcol_[c][6], dcol_[c][3],
+                rcol_[c][RC_MASS], fixed_[c]);
+        const int64_t ai = at + ns;
+        if (ni > 0) {
+            DSPH_CUDA(cudaMemcpyAsync(dcol_[c][0] + ai, L.px.data(), sizeof(double) * ni, cudaMemcpyHostToDevice, st_));
+            DSPH_CUDA(cudaMemcpyAsync(dcol_[c][1] + ai, L.py.data(), sizeof(double) * ni, cudaMemcpyHostToDevice, st_));
+            DSPH_CUDA(cudaMemcpyAsync(dcol_[c][2] + ai, L.pz.data(), sizeof(double) * ni, cudaMemcpyHostToDevice, st_));
+            dfill(dcol_[c][3] + ai, ni, 0.0);
+            dfill(dcol_[c][4] + ai, ni, L.vx);
+            dfill(dcol_[c][5] + ai, ni, 0.0);
+            dfill(dcol_[c][6] + ai, ni, L.vz);
+            dfill(rcol_[c][RC_MASS] + ai, ni, (R)L.m_imp);
+            dfill(fixed_[c] + ai, ni, (uint8_t)0);
+        }
+        dfill(mat_[c] + at, ns, (uint8_t)L.tgt_mat);
+        dfill(mat_[c] + ai, ni, (uint8_t)L.imp_mat);
+        const std::vector<R> eps(h.seps.begin(), h.seps.end()), h0(h.sh0.begin(), h.sh0.end());
+        if (eps.empty()) dfill(rcol_[c][RC_EPSACT] + at, n, (R)1e30);
+        else DSPH_CUDA(cudaMemcpyAsync(rcol_[c][RC_EPSACT] + at, eps.data(), sizeof(R) * n, cudaMemcpyHostToDevice, st_));
+        if (h0.empty()) dfill(rcol_[c][RC_H0] + at, n, (R)h.prm.h_init);
+        else DSPH_CUDA(cudaMemcpyAsync(rcol_[c][RC_H0] + at, h0.data(), sizeof(R) * n, cudaMemcpyHostToDevice, st_));
+        dfill(rcol_[c][RC_HH] + at, n, (R)h.prm.h_init);
+        for (int col : {RC_AX, RC_AY, RC_AZ, RC_DUDT, RC_D}) dfill(rcol_[c][col] + at, n, R(0));
+        for (int q = 0; q < 6; q++) {
+            dfill(rcol_[c][RC_S0 + q] + at, n, R(0));
+            dfill(rcol_[c][RC_DS0 + q] + at, n, R(0));
+        }
+        dfill(impc_[c] + at, n, (uint16_t)b);
+        k_gid_iota<<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(gid_[c], pos_of_gid_, n, h.gid_base, at);
+        DSPH_CUDA(cudaGetLastError());
+        DSPH_CUDA(cudaStreamSynchronize(st_));  // the host vectors above must outlive the copies
+        free_tmp();
+        N_ += n;
+    }
+
     void upload_impact(size_t b, ImpactH& h) {
+        if (h.gen) {
+            upload_generated(b, h);
+            return;
+        }
         int64_t n = h.n, at = N_;
         if (n == 0) return;
         auto up = [&](auto* dst, const auto& src) {

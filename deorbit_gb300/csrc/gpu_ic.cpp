@@ -5,6 +5,14 @@
 //
 //   gpu_ic <ic.bin> <dx> <t_end> [walltime] [--frac] [--snap DT]
 //          [--precision fp64|mixed] [--device N] [--checkpoint DT] [--restart chk.bin] [--profile]
+//          [--grazing THETA,V[,CPPR[,D]]]
+//
+// --grazing generates the campaign's grazing IC in place (the IC that
+// boundary_daemon.build_grazing_ic writes, boundary_daemon.py:119-158: basalt
+// half-space, iron sphere of diameter D at THETA deg and V m/s, CPPR lattice
+// cells per impactor radius; defaults 8 and 1000) instead of reading ic.bin,
+// and dx is the generated lattice spacing (the ic.bin and dx arguments are
+// then placeholders, e.g. "- 0").
 //
 // IC (run_ic.cpp:4-6): f8 header [xlo xhi ylo yhi zlo zhi n], then n x 10 f8
 // [x y z vx vy vz mass u mat fixed]; mat 0 basalt, 1 iron, 2 basalt (the
@@ -49,7 +57,7 @@ int fail(const char* what) {
 
 void usage() {
     std::printf("usage: gpu_ic ic.bin dx t_end [walltime] [--frac] [--snap DT] [--precision fp64|mixed] "
-                "[--device N] [--checkpoint DT] [--restart chk.bin] [--profile]\n");
+                "[--device N] [--checkpoint DT] [--restart chk.bin] [--profile] [--grazing THETA,V[,CPPR[,D]]]\n");
 }
 
 }  // namespace
@@ -59,6 +67,7 @@ int main(int argc, char** argv) {
     double gz = 0.0, damp = 1.0, snap_dt = 0.05, chk_dt = 0.0;
     int precision = SPH_MIXED, device = 0;
     const char* restart = nullptr;
+    const char* grazing = nullptr;
     std::vector<char*> av;
     for (int i = 0; i < argc; i++) {
         std::string s = argv[i];
@@ -69,6 +78,7 @@ int main(int argc, char** argv) {
         else if (s == "--snap" && i + 1 < argc) snap_dt = std::atof(argv[++i]);
         else if (s == "--checkpoint" && i + 1 < argc) chk_dt = std::atof(argv[++i]);
         else if (s == "--restart" && i + 1 < argc) restart = argv[++i];
+        else if (s == "--grazing" && i + 1 < argc) grazing = argv[++i];
         else if (s == "--device" && i + 1 < argc) device = std::atoi(argv[++i]);
         else if (s == "--precision" && i + 1 < argc) {
             std::string p = argv[++i];
@@ -86,7 +96,24 @@ int main(int argc, char** argv) {
         return 1;
     }
     const char* icf = av[1];
-    const double dx = std::atof(av[2]);
+    double dx = std::atof(av[2]);
+    sph_grazing_spec gs;
+    sph_grazing_spec_default(&gs);
+    if (grazing) {
+        double f[4] = {0, 0, 8, 1000.0};
+        int nf = std::sscanf(grazing, "%lf,%lf,%lf,%lf", &f[0], &f[1], &f[2], &f[3]);
+        if (nf < 2 || f[2] < 1) {
+            usage();
+            return 1;
+        }
+        gs.theta_deg = f[0];
+        gs.v = f[1];
+        gs.cppr = (int32_t)f[2];
+        gs.D = f[3];
+        gs.tgt_mat = 0;  // basalt
+        gs.imp_mat = 1;  // iron
+        dx = gs.D / 2.0 / gs.cppr;
+    }
     const double t_end = std::atof(av[3]);
     const double walltime = av.size() > 4 ? std::atof(av[4]) : 1e30;
     if (!(dx > 0) || !(snap_dt > 0)) {
@@ -120,6 +147,9 @@ int main(int argc, char** argv) {
     if (restart) {
         double dx_ck = 0.0;  // flaws, damage and stress come from the checkpoint
         CK(sph_load_checkpoint(ctx, restart, &p, &b, &dx_ck));
+    } else if (grazing) {
+        CK(sph_impact_create_grazing(ctx, &p, &gs, &b, &dx, nullptr));
+        if (frac) CK(sph_impact_seed_damage(ctx, b, dx, 12345));
     } else {
         CK(sph_load_ic(ctx, icf, &p, &b));
         if (frac) CK(sph_impact_seed_damage(ctx, b, dx, 12345));
@@ -132,7 +162,8 @@ int main(int argc, char** argv) {
     CK(sph_read_mat(ctx, b, mat.data()));
     int64_t n_iron = 0;
     for (int64_t i = 0; i < n; i++) n_iron += mat[i] == 1;
-    std::printf("loaded %s: n=%lld (%lld iron)  dx=%.0f  frac=%d  g=%.2f\n", restart ? restart : icf,
+    std::printf("loaded %s: n=%lld (%lld iron)  dx=%.0f  frac=%d  g=%.2f\n",
+                restart ? restart : (grazing ? "grazing IC (generated)" : icf),
                 (long long)n, (long long)n_iron, dx, frac ? 1 : 0, gz);
     if (profile) CK(sph_set_profiling(ctx, 1));
     CK(sph_init(ctx));

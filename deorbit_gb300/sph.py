@@ -59,6 +59,12 @@ class Conservation(C.Structure):
                 ("energy", C.c_double), ("momentum", C.c_double * 3)]
 
 
+class GrazingSpec(C.Structure):
+    _fields_ = [("theta_deg", C.c_double), ("v", C.c_double), ("D", C.c_double), ("rho_imp", C.c_double),
+                ("rho_target", C.c_double), ("x_impact_frac", C.c_double), ("start_h", C.c_double),
+                ("cppr", C.c_int32), ("tgt_mat", C.c_int32), ("imp_mat", C.c_int32), ("reserved", C.c_int32)]
+
+
 class Diagnostics(C.Structure):
     _fields_ = [("count", C.c_int64), ("melted", C.c_int64), ("mean_pos", C.c_double * 3),
                 ("mean_vel", C.c_double * 3), ("mean_speed", C.c_double), ("dispersion", C.c_double),
@@ -109,6 +115,8 @@ _SIGS = {
     "sph_read_fixed": (C.c_int, [_P, C.c_int32, _U8]),
     "sph_write_fixed": (C.c_int, [_P, C.c_int32, _U8]),
     "sph_conservation_get": (C.c_int, [_P, C.c_int32, C.POINTER(Conservation)]),
+    "sph_grazing_spec_default": (None, [C.c_void_p]),
+    "sph_impact_create_grazing": (C.c_int, [_P, C.POINTER(Params), C.c_void_p, _I32, _D, _I64]),
     "sph_impact_diagnostics": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                          C.POINTER(Diagnostics)]),
     "sph_eos_eval": (C.c_int, [_P, C.c_int32, C.c_int64, _D, _D, _D, _D]),
@@ -389,6 +397,21 @@ class Context:
         c = Conservation()
         check(lib().sph_conservation_get(self.h, b, C.byref(c)))
         return c
+
+    def create_grazing(self, prm: Params, theta_deg, v, cppr=8, D=1000.0, tgt_mat=0, imp_mat=1,
+                       x_impact_frac=None, start_h=None, rho_imp=7800.0, rho_target=2700.0):
+        """The campaign's grazing IC (boundary_daemon.build_grazing_ic) generated in
+        place: returns (impact, dx, n)."""
+        s = GrazingSpec()
+        lib().sph_grazing_spec_default(C.byref(s))
+        s.theta_deg, s.v, s.D, s.cppr = theta_deg, v, D, cppr
+        s.tgt_mat, s.imp_mat, s.rho_imp, s.rho_target = tgt_mat, imp_mat, rho_imp, rho_target
+        s.x_impact_frac = float("nan") if x_impact_frac is None else x_impact_frac
+        s.start_h = float("nan") if start_h is None else start_h
+        b, dx, n = C.c_int32(), C.c_double(), C.c_int64()
+        check(lib().sph_impact_create_grazing(self.h, C.byref(prm), C.byref(s), C.byref(b), C.byref(dx),
+                                              C.byref(n)))
+        return b.value, dx.value, n.value
 
     def diagnostics(self, b, mat_lo, mat_hi, u_melt=1.0e6) -> Diagnostics:
         """Projectile centroid, bulk velocity, speed, dispersion and melt count

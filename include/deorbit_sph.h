@@ -263,6 +263,28 @@ int sph_cell_sort_static(const uint32_t* keys, int64_t n, int64_t ncells, int32_
  * fixed] (run_ic.cpp:4-6).  Creates an impact with the given parameters and
  * the IC's domain; *impact receives its id. */
 int sph_load_ic(sph_ctx* ctx, const char* path, const sph_params* p, int32_t* impact);
+/* The campaign's grazing-impact IC generated in place (no reference C
+ * counterpart: restates boundary_daemon.py:119-158, build_grazing_ic, the Python
+ * builder of the IC files gpu_ic reads): a target half-space lattice of spacing
+ * dx = D / (2 cppr) with frozen walls, and an impactor lattice sphere of diameter
+ * D moving at theta below horizontal.  Same particles, order and domain as the
+ * reference builder's file; the target lattice (all but a few thousand
+ * particles) is generated on the device. */
+typedef struct sph_grazing_spec {
+    double theta_deg, v, D;
+    double rho_imp;         /* impactor density (reference: 7800) */
+    double rho_target;      /* target lattice density (reference: 2700) */
+    double x_impact_frac;   /* NaN: the campaign geometry (boundary_daemon.py:150) */
+    double start_h;         /* NaN: released at a + 3 dx */
+    int32_t cppr;           /* lattice cells per impactor radius */
+    int32_t tgt_mat, imp_mat;  /* material ids of this context */
+    int32_t reserved;
+} sph_grazing_spec;
+void sph_grazing_spec_default(sph_grazing_spec* s);
+/* New impact holding the generated IC; *dx_out and *n_out (may be NULL) get the
+ * lattice spacing and the particle count. */
+int sph_impact_create_grazing(sph_ctx* ctx, const sph_params* p, const sph_grazing_spec* s,
+                              int32_t* impact, double* dx_out, int64_t* n_out);
 /* Snapshot: int64 n, then n x f8 [x y z vx vy vz u rho h mat] (run_ic.cpp:15-30). */
 int sph_write_snapshot(sph_ctx* ctx, int32_t impact, const char* path);
 /* Lossless checkpoint, write-then-rename: f8 header [xlo xhi ylo yhi zlo zhi n t dx]

@@ -97,3 +97,18 @@ def test_mixed_run_and_restart(cuda_lib, tmp_path):
     assert r2.returncode == 0, r2.stdout + r2.stderr
     m = re.search(r"DONE: (\d+) steps to t=([0-9.]+)", r2.stdout)
     assert m and abs(float(m.group(2)) - 0.04) < 1e-9
+
+
+@pytest.mark.gpu
+def test_generated_grazing_ic_run(cuda_lib, tmp_path):
+    """--grazing generates the campaign IC in place (no IC file) and runs it."""
+    exe = cli()
+    r = subprocess.run([exe, "-", "0", "1.0", "--grazing", "5,15000,1,4000", "--snap", "0.4"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "loaded grazing IC (generated): n=11527 (7 iron)" in r.stdout, r.stdout
+    assert re.findall(r"melt=(\d+)%", r.stdout)
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("gpu_snap_"))
+    assert snaps
+    s = read_snapshot(tmp_path / snaps[-1])
+    assert s.shape == (11527, 10) and set(np.unique(s[:, 9])) == {0.0, 1.0}
