@@ -15,11 +15,15 @@
 
 namespace dsph {
 
+// A failed runtime call becomes an exception; the thread's last-error state is
+// cleared so that a later, unrelated check does not report it again.
 #define DSPH_CUDA(x)                                                                    \
     do {                                                                                \
         cudaError_t e_ = (x);                                                           \
-        if (e_ != cudaSuccess)                                                          \
+        if (e_ != cudaSuccess) {                                                        \
+            cudaGetLastError();                                                         \
             throw SphError(SPH_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+        }                                                                               \
     } while (0)
 
 // ----------------------------------------------------------------- aux kernels
@@ -1061,12 +1065,24 @@ private:
         }
     }
 
+    // A launch the runtime rejects (configuration, resources) is reported at
+    // once with the kernel's name, not at the next synchronisation.
+    void launched(const void* fn) {
+        const cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) return;
+        const char* name = nullptr;
+        if (cudaFuncGetName(&name, fn) != cudaSuccess || !name) name = "?";
+        cudaGetLastError();
+        throw SphError(SPH_ERR_CUDA, std::string("launch of ") + name + ": " + cudaGetErrorString(e));
+    }
+
     template <class Kern, class... Args>
     void launch_n_raw(Kern k, int64_t n, Args... args) {
         if (n <= 0) return;
         int bs = 256;
         prof_begin();
         k<<<(unsigned)((n + bs - 1) / bs), bs, 0, st_>>>(args...);
+        launched((const void*)k);
         prof_end();
         launches_++;
     }
@@ -1076,6 +1092,7 @@ private:
         if (bs <= 0) bs = 256;
         prof_begin();
         k<<<(unsigned)((n + bs - 1) / bs), bs, 0, st_>>>(view());
+        launched((const void*)k);
         prof_end();
         launches_++;
     }
@@ -1084,6 +1101,7 @@ private:
         if (nimp <= 0) return;
         prof_begin();
         k<<<(nimp + 127) / 128, 128, 0, st_>>>(tab_d_, nimp, args...);
+        launched((const void*)k);
         prof_end();
         launches_++;
     }
@@ -1637,6 +1655,11 @@ public:
     // Cell sort of all resident particles and gather of the carried state.
     void sort_reorder(bool count_changes) {
         if (N_ == 0 && !count_changes) return;
+        if (G_ == 0) {  // no particle was ever added: nothing to order
+            N_ = 0;
+            grid_valid_ = true;
+            return;
+        }
         const int nimp = (int)imp_.size();
         DSPH_CUDA(cudaMemsetAsync(keys_by_gid_, 0xff, sizeof(uint32_t) * std::max<int64_t>(G_, 1), st_));
         DSPH_CUDA(cudaMemsetAsync(cell_cnt_, 0, sizeof(int32_t) * (C_ + 1), st_));
@@ -1699,11 +1722,13 @@ public:
                 const int grid = std::max(1, std::min<int>(nsm_ * 8, (int)((N_ / 16 + 255) / 256) + 1));
                 prof_begin();
                 k_list_warp<R><<<grid, 256, 0, st_>>>(view(), (const int32_t*)tasks_, (const int32_t*)ntask_);
+                launched((const void*)k_list_warp<R>);
                 prof_end();
                 launches_++;
             } else if (list_mode_ == 2) {
                 prof_begin();
                 k_list_wpp<R><<<(unsigned)((N_ + 7) / 8), 256, 0, st_>>>(view());
+                launched((const void*)k_list_wpp<R>);
                 prof_end();
                 launches_++;
             } else {
@@ -1740,6 +1765,7 @@ public:
         if (n <= 0) return;
         prof_begin();
         k_hmax<R><<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(view(), which);
+        launched((const void*)k_hmax<R>);
         prof_end();
         launches_++;
     }
