@@ -212,16 +212,14 @@ def e2e_rate(sph, ctx, b, n, steps, warmup):
     except Exception:
         pinned = False
         bufs = {k: np.empty(n) for k in names}
-    for k in names:
-        bufs[k][:] = ctx.read(b, k)
+    outs = [bufs[k] for k in names]
+    ctx.read_many(b, names, outs)
 
     def one():
-        for k in names:
-            ctx.write(b, k, bufs[k])
+        ctx.write_many(b, bufs)          # the step's inputs, pinned host -> device
         dt = ctx.timestep(b)
         ctx.step(dt)
-        for k in names:
-            bufs[k][:] = ctx.read(b, k)
+        ctx.read_many(b, names, outs)    # the step's state, device -> pinned host
 
     for _ in range(warmup):
         one()

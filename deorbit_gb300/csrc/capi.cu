@@ -423,6 +423,27 @@ int sph_write_field(sph_ctx* ctx, int32_t impact, const char* name, const double
     });
 }
 
+int sph_read_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* const* names, double* const* outs) {
+    return guard([&] {
+        if (nfields < 0) throw SphError(SPH_ERR_ARG, "nfields < 0");
+        if (nfields > 0) { need(names, "names"); need(outs, "outs"); }
+        for (int f = 0; f < nfields; f++) { need(names[f], "names[f]"); need(outs[f], "outs[f]"); }
+        CTX_SET();
+        E(ctx).read_fields(impact, nfields, names, outs);
+    });
+}
+
+int sph_write_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* const* names,
+                     const double* const* ins) {
+    return guard([&] {
+        if (nfields < 0) throw SphError(SPH_ERR_ARG, "nfields < 0");
+        if (nfields > 0) { need(names, "names"); need(ins, "ins"); }
+        for (int f = 0; f < nfields; f++) { need(names[f], "names[f]"); need(ins[f], "ins[f]"); }
+        CTX_SET();
+        E(ctx).write_fields(impact, nfields, names, ins);
+    });
+}
+
 int sph_read_mat(sph_ctx* ctx, int32_t impact, int32_t* out) {
     return guard([&] {
         need(out, "out");

@@ -68,6 +68,8 @@ public:
     virtual int64_t impact_n(int b) = 0;
     virtual void read_field(int b, const char* name, double* out) = 0;
     virtual void write_field(int b, const char* name, const double* in) = 0;
+    virtual void read_fields(int b, int nf, const char* const* names, double* const* outs) = 0;
+    virtual void write_fields(int b, int nf, const char* const* names, const double* const* ins) = 0;
     virtual void read_mat(int b, int32_t* out) = 0;
     virtual void read_fixed(int b, uint8_t* out) = 0;
     virtual void write_fixed(int b, const uint8_t* in) = 0;

@@ -791,6 +791,44 @@ public:
         DSPH_CUDA(cudaStreamSynchronize(st_));
     }
 
+    // Several fields in one pass: every gather and copy is queued on the
+    // stream (through one staging slice per field) and the stream is
+    // synchronised once, so pinned caller buffers stream at link speed.
+    void read_fields(int b, int nf, const char* const* names, double* const* outs) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (h.n == 0 || nf <= 0) return;
+        ensure_stage((int64_t)nf * h.n);
+        for (int f = 0; f < nf; f++) {
+            double* slice = stage_d_ + (int64_t)f * h.n;
+            bool ok = with_column(names[f], [&](auto* col) {
+                launch_n_raw(k_read_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, slice);
+            });
+            if (!ok) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
+            DSPH_CUDA(cudaMemcpyAsync(outs[f], slice, sizeof(double) * h.n, cudaMemcpyDeviceToHost, st_));
+        }
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void write_fields(int b, int nf, const char* const* names, const double* const* ins) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (h.n == 0 || nf <= 0) return;
+        ensure_stage((int64_t)nf * h.n);
+        for (int f = 0; f < nf; f++) {
+            double* slice = stage_d_ + (int64_t)f * h.n;
+            DSPH_CUDA(cudaMemcpyAsync(slice, ins[f], sizeof(double) * h.n, cudaMemcpyHostToDevice, st_));
+            bool ok = with_column(names[f], [&](auto* col) {
+                launch_n_raw(k_write_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n,
+                             (const double*)slice);
+            });
+            if (!ok) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
+            std::string nm(names[f]);
+            if (nm == "x" || nm == "y" || nm == "z" || nm == "hh") grid_valid_ = false;
+        }
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
     void read_mat(int b, int32_t* out) override {
         ImpactH& h = imp(b);
         for (int64_t i = 0; i < h.n; i++) out[i] = h.mat_host[i];

@@ -111,6 +111,8 @@ _SIGS = {
     "sph_synchronize": (C.c_int, [_P]),
     "sph_read_field": (C.c_int, [_P, C.c_int32, C.c_char_p, _D]),
     "sph_write_field": (C.c_int, [_P, C.c_int32, C.c_char_p, _D]),
+    "sph_read_fields": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(_D)]),
+    "sph_write_fields": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(_D)]),
     "sph_read_mat": (C.c_int, [_P, C.c_int32, _I32]),
     "sph_read_fixed": (C.c_int, [_P, C.c_int32, _U8]),
     "sph_write_fixed": (C.c_int, [_P, C.c_int32, _U8]),
@@ -173,6 +175,12 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(_I32)
+
+
+def _out64(a, n):
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous and a.size == n):
+        raise ValueError(f"output buffer must be a contiguous float64 array of {n}")
+    return a
 
 
 def _f64(a, n=None):
@@ -370,14 +378,34 @@ class Context:
     def synchronize(self):
         check(lib().sph_synchronize(self.h))
 
-    def read(self, b, name) -> np.ndarray:
-        out = np.zeros(self.n(b))
+    def read(self, b, name, out=None) -> np.ndarray:
+        """One field in original particle order (into `out`, a contiguous
+        float64 array of n, when given: page-locked buffers copy fastest)."""
+        out = np.zeros(self.n(b)) if out is None else _out64(out, self.n(b))
         check(lib().sph_read_field(self.h, b, name.encode(), _dp(out)))
         return out
 
     def write(self, b, name, values):
         v = _f64(values, self.n(b))
         check(lib().sph_write_field(self.h, b, name.encode(), _dp(v)))
+
+    def read_many(self, b, names, outs=None):
+        """Several fields with one synchronisation: {name: array}."""
+        n = self.n(b)
+        outs = [np.zeros(n) for _ in names] if outs is None else [_out64(o, n) for o in outs]
+        cn = (C.c_char_p * len(names))(*[k.encode() for k in names])
+        ptrs = (_D * len(names))(*[_dp(o) for o in outs])
+        check(lib().sph_read_fields(self.h, b, len(names), cn, ptrs))
+        return dict(zip(names, outs))
+
+    def write_many(self, b, fields):
+        """Several fields ({name: values}) with one synchronisation."""
+        n = self.n(b)
+        names = list(fields)
+        vals = [_f64(fields[k], n) for k in names]
+        cn = (C.c_char_p * len(names))(*[k.encode() for k in names])
+        ptrs = (_D * len(names))(*[_dp(v) for v in vals])
+        check(lib().sph_write_fields(self.h, b, len(names), cn, ptrs))
 
     def mat(self, b) -> np.ndarray:
         out = np.zeros(self.n(b), np.int32)

@@ -190,6 +190,13 @@ int sph_synchronize(sph_ctx* ctx);
  * (replaces reading / writing System's public vectors, sph.hpp:73-81). */
 int sph_read_field(sph_ctx* ctx, int32_t impact, const char* name, double* out);
 int sph_write_field(sph_ctx* ctx, int32_t impact, const char* name, const double* in);
+/* Several fields in one call with one synchronisation (page-locked caller
+ * buffers transfer at link speed): out[f] / in[f] hold n doubles of field
+ * names[f], original order. */
+int sph_read_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* const* names,
+                    double* const* outs);
+int sph_write_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* const* names,
+                     const double* const* ins);
 int sph_read_mat(sph_ctx* ctx, int32_t impact, int32_t* out);
 int sph_read_fixed(sph_ctx* ctx, int32_t impact, uint8_t* out);
 int sph_write_fixed(sph_ctx* ctx, int32_t impact, const uint8_t* in);

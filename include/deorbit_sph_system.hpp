@@ -222,20 +222,31 @@ struct System {
         if (sync) pull();
     }
 
-    // Copy every field from the device into the mirror.
+    // Copy every field from the device into the mirror (one batched call).
     void pull() {
         need();
-        std::vector<double> x(n), y(n), z(n);
-        rd3("x", "y", "z", pos, x, y, z);
-        rd3("vx", "vy", "vz", vel, x, y, z);
-        rd3("ax", "ay", "az", acc, x, y, z);
-        const char* sn[6] = {"Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"};
-        const char* dn[6] = {"dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz"};
-        rdsym(sn, S, x);
-        rdsym(dn, dSdt, x);
-        rd("mass", mass); rd("rho", rho); rd("u", u); rd("dudt", dudt); rd("P", P); rd("cs", cs);
-        rd("csig", csig); rd("hh", hh); rd("eps_work", eps_work); rd("D", D); rd("eps_act", eps_act);
-        rd("sigmax", sigmax); rd("Pf", Pf); rd("Rart", Rart); rd("dscale", dscale);
+        static const char* names[] = {"x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az",
+                                      "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
+                                      "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz",
+                                      "mass", "rho", "u", "dudt", "P", "cs", "csig", "hh", "eps_work",
+                                      "D", "eps_act", "sigmax", "Pf", "Rart", "dscale"};
+        const int nf = (int)(sizeof(names) / sizeof(names[0]));
+        std::vector<std::vector<double>> buf(nf, std::vector<double>((size_t)n));
+        std::vector<double*> outs(nf);
+        for (int f = 0; f < nf; f++) outs[f] = buf[f].data();
+        if (n) check(sph_read_fields(ctx_, b_, nf, names, outs.data()));
+        for (int i = 0; i < n; i++) {
+            pos[i] = Vec3(buf[0][i], buf[1][i], buf[2][i]);
+            vel[i] = Vec3(buf[3][i], buf[4][i], buf[5][i]);
+            acc[i] = Vec3(buf[6][i], buf[7][i], buf[8][i]);
+            for (int c = 0; c < 6; c++) {
+                comp(S[i], c) = buf[9 + c][i];
+                comp(dSdt[i], c) = buf[15 + c][i];
+            }
+        }
+        std::vector<double>* scal[] = {&mass, &rho, &u, &dudt, &P, &cs, &csig, &hh, &eps_work,
+                                       &D, &eps_act, &sigmax, &Pf, &Rart, &dscale};
+        for (int q = 0; q < 15; q++) *scal[q] = buf[21 + q];
         std::vector<uint8_t> f(n);
         if (n) check(sph_read_fixed(ctx_, b_, f.data()));
         for (int i = 0; i < n; i++) fixed[i] = (char)f[i];
@@ -247,18 +258,29 @@ struct System {
 
     // Copy the carried fields of the mirror to the device (the state a step
     // reads: positions, velocities, old derivatives, u, h, mass, stress,
-    // damage, flaws, fixed flags).
+    // damage, flaws, fixed flags), in one batched call.
     void push() {
         need();
-        std::vector<double> tmp(n);
-        wr3("x", "y", "z", pos, tmp);
-        wr3("vx", "vy", "vz", vel, tmp);
-        wr3("ax", "ay", "az", acc, tmp);
-        const char* sn[6] = {"Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"};
-        const char* dn[6] = {"dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz"};
-        wrsym(sn, S, tmp);
-        wrsym(dn, dSdt, tmp);
-        wr("mass", mass); wr("u", u); wr("dudt", dudt); wr("hh", hh); wr("D", D); wr("eps_act", eps_act);
+        static const char* names[] = {"x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az",
+                                      "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
+                                      "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz",
+                                      "mass", "u", "dudt", "hh", "D", "eps_act"};
+        const int nf = (int)(sizeof(names) / sizeof(names[0]));
+        std::vector<std::vector<double>> buf(nf, std::vector<double>((size_t)n));
+        for (int i = 0; i < n; i++) {
+            buf[0][i] = pos[i].x; buf[1][i] = pos[i].y; buf[2][i] = pos[i].z;
+            buf[3][i] = vel[i].x; buf[4][i] = vel[i].y; buf[5][i] = vel[i].z;
+            buf[6][i] = acc[i].x; buf[7][i] = acc[i].y; buf[8][i] = acc[i].z;
+            for (int c = 0; c < 6; c++) {
+                buf[9 + c][i] = comp(S[i], c);
+                buf[15 + c][i] = comp(dSdt[i], c);
+            }
+        }
+        const std::vector<double>* scal[] = {&mass, &u, &dudt, &hh, &D, &eps_act};
+        for (int q = 0; q < 6; q++) buf[21 + q] = *scal[q];
+        std::vector<const double*> ins(nf);
+        for (int f = 0; f < nf; f++) ins[f] = buf[f].data();
+        if (n) check(sph_write_fields(ctx_, b_, nf, names, ins.data()));
         std::vector<uint8_t> f(n);
         for (int i = 0; i < n; i++) f[i] = fixed[i] ? 1 : 0;
         if (n) check(sph_write_fixed(ctx_, b_, f.data()));
@@ -304,39 +326,8 @@ private:
                                            vz.data(), mass.data(), u.data(), mat.data(), f.data()));
     }
 
-    void rd(const char* name, std::vector<double>& out) {
-        if (n) check(sph_read_field(ctx_, b_, name, out.data()));
-    }
-    void wr(const char* name, const std::vector<double>& in) {
-        if (n) check(sph_write_field(ctx_, b_, name, in.data()));
-    }
-    void rd3(const char* a, const char* b, const char* c, std::vector<Vec3>& out, std::vector<double>& x,
-             std::vector<double>& y, std::vector<double>& z) {
-        rd(a, x); rd(b, y); rd(c, z);
-        for (int i = 0; i < n; i++) out[i] = Vec3(x[i], y[i], z[i]);
-    }
-    void wr3(const char* a, const char* b, const char* c, const std::vector<Vec3>& in, std::vector<double>& tmp) {
-        for (int i = 0; i < n; i++) tmp[i] = in[i].x;
-        wr(a, tmp);
-        for (int i = 0; i < n; i++) tmp[i] = in[i].y;
-        wr(b, tmp);
-        for (int i = 0; i < n; i++) tmp[i] = in[i].z;
-        wr(c, tmp);
-    }
     static double& comp(Sym3& s, int c) {
         return c == 0 ? s.xx : c == 1 ? s.yy : c == 2 ? s.zz : c == 3 ? s.xy : c == 4 ? s.xz : s.yz;
-    }
-    void rdsym(const char* const* names, std::vector<Sym3>& out, std::vector<double>& tmp) {
-        for (int c = 0; c < 6; c++) {
-            rd(names[c], tmp);
-            for (int i = 0; i < n; i++) comp(out[i], c) = tmp[i];
-        }
-    }
-    void wrsym(const char* const* names, std::vector<Sym3>& in, std::vector<double>& tmp) {
-        for (int c = 0; c < 6; c++) {
-            for (int i = 0; i < n; i++) tmp[i] = comp(in[i], c);
-            wr(names[c], tmp);
-        }
     }
 };
 
