@@ -121,10 +121,26 @@ __device__ __forceinline__ R eig_max(R xx, R yy, R zz, R xy, R xz, R yz) {
     return q + R(2) * p * rcos(phi);
 }
 
+// Compression mu = rho / rho0 - 1 (eos.hpp:71) and the expansion
+// z = rho0 / rho - 1 (eos.hpp:83).  In FP32 the rounding of rho (and of the
+// quotient) is amplified 1/mu-fold in weakly compressed material, so the
+// mixed form forms rho - rho0 exactly (Sterbenz: rho within a factor two of
+// rho0) and adds rho_lo, the low part of the compensated density sum.  FP64
+// keeps the reference's operations.
+__device__ __forceinline__ void till_mu_z(double rho0, double rho, double /*rho_lo*/, double& mu, double& z) {
+    mu = rho / rho0 - 1.0;
+    z = rho0 / rho - 1.0;
+}
+__device__ __forceinline__ void till_mu_z(float rho0, float rho, float rho_lo, float& mu, float& z) {
+    const float d = (rho - rho0) + rho_lo;
+    mu = d / rho0;
+    z = -d / (rho + rho_lo);
+}
+
 // Tillotson condensed branch: value and analytic derivatives (eos.hpp:72-79).
 template <class R>
-__device__ __forceinline__ void till_cond(const MatT<R>& m, R rho, R u, R& P, R& dPdr, R& dPdu) {
-    R eta = rho / m.rho0, mu = eta - R(1);
+__device__ __forceinline__ void till_cond(const MatT<R>& m, R rho, R u, R mu, R& P, R& dPdr, R& dPdu) {
+    R eta = rho / m.rho0;
     R ue2 = m.u0 * eta * eta;
     R w = R(1) + u / ue2, iw = R(1) / w, aob = m.a + m.b * iw;
     P = aob * rho * u + m.A * mu + m.B * mu * mu;
@@ -135,12 +151,12 @@ __device__ __forceinline__ void till_cond(const MatT<R>& m, R rho, R u, R& P, R&
 
 // Tillotson expanded branch: value and analytic derivatives (eos.hpp:80-94).
 template <class R>
-__device__ __forceinline__ void till_expd(const MatT<R>& m, R rho, R u, R& P, R& dPdr, R& dPdu) {
-    R eta = rho / m.rho0, mu = eta - R(1);
+__device__ __forceinline__ void till_expd(const MatT<R>& m, R rho, R u, R mu, R z, R& P, R& dPdr, R& dPdu) {
+    R eta = rho / m.rho0;
     R ue2 = m.u0 * eta * eta;
     R w = R(1) + u / ue2, iw = R(1) / w;
     R irho = R(1) / rho;
-    R z = m.rho0 * irho - R(1), dzdr = -m.rho0 * irho * irho;
+    R dzdr = -m.rho0 * irho * irho;
     R E1 = rexp(-m.alpha * z * z), E2 = rexp(-m.beta * z);
     R Gt = m.b * rho * u * iw + m.A * mu * E2;
     P = m.a * rho * u + Gt * E1;
@@ -155,7 +171,7 @@ __device__ __forceinline__ void till_expd(const MatT<R>& m, R rho, R u, R& P, R&
 
 // Pressure (eos.hpp:52-68) and sound speed (eos.hpp:95-113) in one pass.
 template <class R>
-__device__ __forceinline__ void eos_P_cs(const MatT<R>& m, R rho, R u, R& P, R& cs) {
+__device__ __forceinline__ void eos_P_cs(const MatT<R>& m, R rho, R u, R& P, R& cs, R rho_lo = R(0)) {
     if (m.type == 0) {  // ideal gas
         P = (m.gamma - R(1)) * rho * u;
         cs = rsqrt_(rmax(m.gamma * P / rmax(rho, R(1e-30)), R(1e-12)));
@@ -166,17 +182,20 @@ __device__ __forceinline__ void eos_P_cs(const MatT<R>& m, R rho, R u, R& P, R& 
         cs = R(1e-3);
         return;
     }
-    R Pp, dPdr, dPdu;
-    if (rho >= m.rho0 || u <= m.uiv) {
-        till_cond(m, rho, u, Pp, dPdr, dPdu);
+    R Pp, dPdr, dPdu, mu, z;
+    till_mu_z(m.rho0, rho, rho_lo, mu, z);
+    // rho >= rho0 (eos.hpp:77); FP64 compares as the reference does
+    const bool compressed = sizeof(R) == 8 ? (rho >= m.rho0) : (mu >= R(0));
+    if (compressed || u <= m.uiv) {
+        till_cond(m, rho, u, mu, Pp, dPdr, dPdu);
         P = Pp;
     } else if (u >= m.ucv) {
-        till_expd(m, rho, u, Pp, dPdr, dPdu);
+        till_expd(m, rho, u, mu, z, Pp, dPdr, dPdu);
         P = Pp;
     } else {  // intermediate: energy-weighted blend of the two branches
         R Pc, dPcr, dPcu, Pe, dPer, dPeu;
-        till_cond(m, rho, u, Pc, dPcr, dPcu);
-        till_expd(m, rho, u, Pe, dPer, dPeu);
+        till_cond(m, rho, u, mu, Pc, dPcr, dPcu);
+        till_expd(m, rho, u, mu, z, Pe, dPer, dPeu);
         R inv = R(1) / (m.ucv - m.uiv);
         P = ((u - m.uiv) * Pe + (m.ucv - u) * Pc) * inv;
         Pp = P;

@@ -290,11 +290,11 @@ class Engine final : public EngineBase {
 public:
     static constexpr int kNR = 21;   // carried R columns
     static constexpr int kND = 7;    // carried FP64 columns: x y z u vx vy vz
-    static constexpr int kNDer = 19; // derived R columns
+    static constexpr int kNDer = 20; // derived R columns
     enum { RC_AX, RC_AY, RC_AZ, RC_DUDT, RC_MASS, RC_HH, RC_D, RC_EPSACT,
            RC_H0, RC_S0, RC_DS0 = RC_S0 + 6 };
     enum { DR_RHO, DR_P, DR_CS, DR_CSIG, DR_PF, DR_DSCALE, DR_RART, DR_SIGMAX, DR_EPSW, DR_PFR2,
-           DR_DSR2, DR_VOL, DR_DUDTN, DR_DSN0 };
+           DR_DSR2, DR_VOL, DR_DUDTN, DR_DSN0, DR_RHOLO = DR_DSN0 + 6 };
 
     struct ImpactH {
         sph_params prm{};
@@ -1207,6 +1207,7 @@ public:
         v.sigmax = der_[DR_SIGMAX]; v.epsw = der_[DR_EPSW]; v.pfr2 = der_[DR_PFR2];
         v.dsr2 = der_[DR_DSR2]; v.vol = der_[DR_VOL]; v.dudt_new = der_[DR_DUDTN];
         for (int c = 0; c < 6; c++) v.dS_new[c] = der_[DR_DSN0 + c];
+        v.rho_lo = der_[DR_RHOLO];
         v.pf = pf_; v.cpk = cpk_; v.refbin = refbin_;
         v.vh = vh_; v.vl = vl_;
         v.pk = pk_; v.fa = fa_; v.fb = fb_; v.fc = fc_;

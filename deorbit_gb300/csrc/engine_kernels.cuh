@@ -80,6 +80,7 @@ struct View {
     uint16_t* imp;
     int32_t* gid;
     R *rho, *P, *cs, *csig, *Pf, *dscale, *Rart, *sigmax, *epsw, *pfr2, *dsr2, *vol, *dudt_new;
+    R* rho_lo;          // mixed form: low part of the compensated density sum (0 in FP64)
     R* dS_new[6];
     float4* pf;
     float4 *vh, *vl;     // mixed form: FP64 velocity split into FP32 hi + lo
@@ -1067,6 +1068,8 @@ struct Kahan {
         s = t;
     }
     __device__ __forceinline__ R value() const { return s; }
+    // the part of the exact sum the rounded value misses (value() + low())
+    __device__ __forceinline__ R low() const { return -c; }
 };
 template <class R>
 struct Plain {
@@ -1074,6 +1077,7 @@ struct Plain {
     __device__ __forceinline__ void init() { s = R(0); }
     __device__ __forceinline__ void add(R x) { s += x; }
     __device__ __forceinline__ R value() const { return s; }
+    __device__ __forceinline__ R low() const { return R(0); }
 };
 template <class R>
 using AccT = typename std::conditional<sizeof(R) == 4, Kahan<R>, Plain<R>>::type;
@@ -1103,7 +1107,7 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
     const float m = sizeof(R) == 8 ? I.margin : 0.0f;
     const R mass_k = v.mass[k];
     const R h0 = I.use_h0 ? v.h0[k] : (R)I.h_init;
-    R rho = R(1e-30);
+    R rho = R(1e-30), rho_lo = R(0);
     for (int it = 0; it < iters; it++) {
         const R ihi = R(1) / hi;
         const bool need_member = 2.0f * (float)hi + 2.0f * m >= I.cwmin * 0.999f;
@@ -1142,9 +1146,11 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
                      [&](int32_t j, float, float, float) { body(j); });
         }
         rho = rmax(sum.value(), R(1e-30));
+        rho_lo = rho > R(1e-30) ? sum.low() : R(0);
         hi = rmin(R(2) * h0, rmax(R(0.5) * h0, (R)I.eta * rcbrt(mass_k / rho)));
     }
     v.rho[k] = rho;
+    v.rho_lo[k] = rho_lo;
     v.hh[k] = hi;
     v.pf[k].w = (float)hi;
     impact_atomic_max(&I.hm_bits, (double)hi);  // the round's new max h
@@ -1166,7 +1172,7 @@ static __global__ void k_eos(View<R> v) {
     const R rho = v.rho[k];
     const R u = (R)v.u[k];
     R P, cs;
-    eos_P_cs(m, rho, u, P, cs);
+    eos_P_cs(m, rho, u, P, cs, v.rho_lo[k]);
     v.P[k] = P;
     v.cs[k] = cs;
     v.csig[k] = rsqrt_(cs * cs + (R(4) / R(3)) * m.G / rmax(rho, R(1e-30)));
