@@ -1219,19 +1219,17 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     const R alpha_u = (R)I.alpha_u;
     const R inv_poly = sizeof(R) == 4 ? (R)I.inv_poly_eta_f : (R)I.inv_poly_eta;
     const R hi = v.hh[k], rhoi = v.rho[k], csi = v.csig[k], Pi_over = v.pfr2[k];
-    const R dsri = v.dsr2[k], di = v.dscale[k], Rai = v.Rart[k];
+    const R dsri = v.dsr2[k], Rai = v.Rart[k];
     const double vxi = v.vx[k], vyi = v.vy[k], vzi = v.vz[k];
     float4 vhi = make_float4(0, 0, 0, 0), vli = vhi;
     if (sizeof(R) == 4) { vhi = v.vh[k]; vli = v.vl[k]; }
     const R sxx = v.S[0][k], syy = v.S[1][k], szz = v.S[2][k];
     const R sxy = v.S[3][k], sxz = v.S[4][k], syz = v.S[5][k];
-    const R Pi = v.P[k], ui = (R)v.u[k];
     R L00 = 0, L01 = 0, L02 = 0, L10 = 0, L11 = 0, L12 = 0, L20 = 0, L21 = 0, L22 = 0;
     Acc ax, ay, az, du;
     ax.init(); ay.init(); az.init(); du.init();
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
-    const unsigned long long bi = v.refbin[k];
     const float m = sizeof(R) == 8 ? I.margin : 0.0f;
     const bool need_member = (float)hi + I.hmax_f + 2.0f * m >= I.cwmin * 0.999f;
     // one pair's contributions: strain-rate tensor, momentum, energy
@@ -1271,8 +1269,10 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
         az.add(stz * mj - gz * mm);
         if (alpha_u > R(0)) {
             const R rbar = R(0.5) * (rhoi + rhoj);
-            const R vsig = rsqrt_(pair_div(rabs(Pi - v.P[j]), rbar));
-            du.add(pair_div(alpha_u * mj * vsig * (ui - (R)v.u[j]) * dW, rbar));
+            // own P and u read here: the conductivity term is off in most runs,
+            // and keeping them live through the pair loop costs registers
+            const R vsig = rsqrt_(pair_div(rabs(v.P[k] - v.P[j]), rbar));
+            du.add(pair_div(alpha_u * mj * vsig * ((R)v.u[k] - (R)v.u[j]) * dW, rbar));
         }
     };
     const float hs_pad = 2.0f * m;
@@ -1289,7 +1289,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             double rr = sep_exact(v, I, k, j, dx, dy, dz);
             double hsum = __dadd_rn((double)hi, (double)hj);
             if (rr >= hsum || rr == 0.0) return;
-            if (need_member && !ref_member(bi, v.refbin[j], I)) return;
+            if (need_member && !ref_member(v.refbin[k], v.refbin[j], I)) return;
             const R rx = (R)dx, ry = (R)dy, rz = (R)dz, r = (R)rr;
             const R hbar = R(0.5) * (hi + hj);
             const R ihb = R(1) / hbar;
@@ -1316,7 +1316,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             const float r2 = dx * dx + dy * dy + dz * dz;
             const float hs = (float)hi + pj.w;
             bool ok = r2 < hs * hs && r2 != 0.0f;
-            if (need_member) ok = ok && ref_member(bi, v.refbin[j], I);
+            if (need_member) ok = ok && ref_member(v.refbin[k], v.refbin[j], I);  // own bins re-read: rarely needed
             const float irs = ok ? rsqrtf(r2) : 1.0f;  // hardware 1/sqrt (2 ulp)
             const R r = ok ? (R)(r2 * irs) : R(1);
             const R hbar = R(0.5) * (hi + (R)pj.w);
@@ -1371,7 +1371,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     v.ax[k] = ax.value();
     v.ay[k] = ay.value();
     v.az[k] = az.value();
-    v.dudt_new[k] = du.value() + epsw * di;
+    v.dudt_new[k] = du.value() + epsw * v.dscale[k];
 }
 
 // Crack growth (sph.hpp:336-348); multi-flaw extension by gid.
