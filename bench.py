@@ -37,9 +37,9 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s batched vs plain GPU at ≤1e-4 FP64 rel err; p50/p99 latency"
 UNIT = "particle-steps/s"
 
-# Algorithmic bytes per particle of one launch (compulsory reads of the
-# particle's own state and writes of its results; neighbour re-reads, lists
-# and sort scratch excluded).  See the design doc for the derivation.
+# Algorithmic bytes per particle of one launch: compulsory reads of the
+# particle's own state and writes of its results, plus the list entries the
+# kernel must write or read; neighbour re-reads and sort scratch excluded.
 # Kernel of each single-kernel class and its algorithmic bytes per particle
 # in the mixed form: (fixed bytes, list bytes per list entry).  The neighbour
 # list is written once per step by k_list_thread and read by every k_density
@@ -68,9 +68,25 @@ ALG_BYTES = {
 FLOPS_PER_ENTRY = {"force": 169, "density": 34}
 # nominal FP32 peak: 152 SMs x 128 lanes x 2 flops x 2.07 GHz (no measured figure exists)
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
-# whole step, per particle-step (carried state read + written, derived fields,
-# lists excluded): FP64 strength+damage 429 B, mixed 241 B
-STEP_BYTES = {8: 429, 4: 241}
+# Compulsory state traffic of one particle-step, strength + damage, from the
+# engine's layout: (bytes per field, access) with access "rw" for carried state
+# read and written once, "r" read-only, "w" written once.  Positions,
+# velocities and internal energy are FP64 in both forms; the rest is FP64 in
+# the plain form and FP32 in the mixed one.  Lists, neighbour re-reads and sort
+# scratch are excluded.
+def state_layout(real_bytes):
+    R = real_bytes
+    return {"pos": (24, "rw"), "vel": (24, "rw"), "u": (8, "rw"), "h": (R, "rw"), "acc": (3 * R, "rw"),
+            "dudt": (R, "rw"), "S": (6 * R, "rw"), "D": (R, "rw"), "dSdt": (6 * R, "rw"),
+            "mass": (R, "r"), "eps_act": (R, "r"), "mat": (1, "r"), "fixed": (1, "r"), "rho": (R, "w")}
+
+
+def step_bytes(real_bytes):
+    return sum(b * (2 if a == "rw" else 1) for b, a in state_layout(real_bytes).values())
+
+
+# frozen per form (a unit test recomputes them from state_layout)
+STEP_BYTES = {8: 426, 4: 270}
 
 
 def rank_info():
@@ -326,6 +342,47 @@ def large_section(sph, ic, device, steps, warmup, n_total=1 << 24):
             "replica_particles": rep.n}
 
 
+def halfspace_section(sph, ic, device, steps=200):
+    """The plain FP64 half-space impact (57,344 particles, 45 deg, 8 km/s,
+    hydro-only, CFL 0.3) for its full 200 steps: the FP64 GPU solver with the
+    host-driven timestep()/step() loop, and the CPU oracle (the reference's
+    algorithm, thread cap 16) on the same input, with the FP64 fields' rel-L2
+    between them at the end."""
+    sc = ic.impact_halfspace()
+    ctx = sph.Context(sph.FP64, device)
+    b = ic.to_context(ctx, sc)
+    ctx.init()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    dts = []
+    for _ in range(steps):
+        dt = ctx.timestep(b)
+        ctx.step(dt)
+        dts.append(dt)
+    ctx.synchronize()
+    t_gpu = time.perf_counter() - t0
+    names = ["x", "y", "z", "vx", "vy", "vz", "u", "rho", "P"]
+    gpu = ctx.read_many(b, names)
+    ctx.close()
+    threads = min(os.cpu_count() or 1, 16)
+    S = ic.to_oracle(sc, threads=threads)
+    S.init()
+    t0 = time.perf_counter()
+    for dt in dts:   # the GPU run's dt sequence (equal to the oracle's to 1e-9)
+        S.step(dt)
+    t_cpu = time.perf_counter() - t0
+    err = {}
+    for k in names:
+        r = S.field(k)
+        err[k] = float(np.linalg.norm(gpu[k] - r) / max(np.linalg.norm(r), 1e-300))
+    return {"workload": "half-space impact, 48x48x24 granite + iron sphere r = 8 dx, 45 deg, 8 km/s, "
+                        "hydro-only, CFL 0.3", "n_particles": sc.n, "steps": steps,
+            "gpu_fp64": {"value": sc.n * steps / t_gpu, "ms_per_step": 1000 * t_gpu / steps,
+                         "loop": "host-driven timestep()/step()"},
+            "cpu_oracle": {"value": sc.n * steps / t_cpu, "cores": threads, "nproc": os.cpu_count()},
+            "fp64_vs_oracle_rel_l2": err}
+
+
 def serving_section(device, rates=(2.0, 4.0, 8.0), count=24, steps=300):
     """Poisson request streams through the continuous-batching server."""
     from deorbit_gb300 import serve, sph
@@ -360,6 +417,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-halfspace", action="store_true")
     args = ap.parse_args()
     rank, world, local = rank_info()
 
@@ -392,7 +450,8 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": dict(wl, sample=sample.n),
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": S.threads(), "kind": "port",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": S.threads(), "nproc": os.cpu_count(),
+                                 "kind": "port",
                                  "sample": f"{sample.n} particles cropped from the {sc.n}-particle workload "
                                            f"around the impact point, {args.steps} KDK steps after init"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -454,6 +513,9 @@ def main():
     large = None
     if rank == 0 and not args.no_large:
         large = large_section(sph, ic, device, args.steps, args.warmup)
+    halfspace = None
+    if rank == 0 and world == 1 and not args.no_halfspace:
+        halfspace = halfspace_section(sph, ic, device)
 
     # ---- accuracy of the mixed form against FP64 (same dt sequence)
     err = mixed_error(sph, ic, sc, args.steps, device) if rank == 0 else None
@@ -497,7 +559,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         sample = ic.crop(sc, sample_n)
         v, el, thr = cpu_rate(ic, sample, 2, threads=min(os.cpu_count() or 1, 16))
-        cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+        cpu = {"value": v, "unit": UNIT, "cores": thr, "nproc": os.cpu_count(), "kind": "port",
                "sample": f"{sample.n} particles cropped from the {sc.n}-particle workload around the "
                          f"impact point, 2 KDK steps after init ({el:.1f} s)"}
 
@@ -514,7 +576,7 @@ def main():
                 "speedup_vs_plain_fp64": value / value64,
                 "mixed_vs_fp64_rel_l2": err,
                 "kernel_ms": {k: v[0] for k, v in kst.items()},
-                "batched": batched, "serving": serving, "large": large}
+                "batched": batched, "serving": serving, "large": large, "halfspace": halfspace}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -2,10 +2,10 @@
 (48 x 48 x 24 granite lattice + iron sphere of radius 8 dx, 45 deg, 8 km/s,
 CFL 0.3) for 200 steps against the oracle on the same seeded input.
 
-Tolerance: rel-L2 <= 1e-8 per field after 200 steps.  The two solvers sum the
-same terms in different orders; the differences start at ~1e-16 and grow with
-the impact's shock dynamics over the run -- the value measured is recorded in
-the assertion message.  The CFL dt of every step agrees to 1e-9."""
+Tolerance: rel-L2 <= 1e-12 per field after 200 steps.  The two solvers sum the
+same terms in different orders; the differences start at ~1e-16 and stay below
+1e-14 over this run (measured on GB300: 1e-16 positions, <= 7e-15 velocities,
+energy, density, pressure).  The CFL dt of every step agrees to 1e-9."""
 import os
 
 import numpy as np
@@ -17,7 +17,7 @@ from parity import field_errors, read_all
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-8
+TOL = 1e-12
 NAMES = ["x", "y", "z", "vx", "vy", "vz", "u", "rho", "P", "hh"]
 
 
