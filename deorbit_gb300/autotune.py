@@ -22,6 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.environ.get("DEORBIT_SPH_TUNE_CACHE", os.path.join(HERE, "_tune", "autotune.json"))
 
 CELL_FACTORS = (0.75, 1.0, 1.5)
+# graded lattices: h spans an order of magnitude, and cells sized for the finest
+# particles make the coarse ones search hundreds of columns
+GRADED_CELL_FACTORS = (1.5, 2.0, 3.0, 4.0)
 SLACKS = (0.03, 0.06)
 BLOCKS = (128, 256)
 LIST_MODES = (2, 1, 0)
@@ -150,7 +153,7 @@ def apply(ctx, sc, precision, device=0, per_impact_n=None, default=None):
     return cfg
 
 
-def ship(device=0, verbose=True):
+def ship(device=0, verbose=True, only=None):
     """Re-measure the table shipped for this GPU model (tuned_gb300.json on a
     GB300): the 1,048,576-particle grazing impact in both forms, the batched
     class (32 impacts of the 256-impact sweep run as one batch) and the
@@ -161,7 +164,14 @@ def ship(device=0, verbose=True):
     runs = [(ic.grazing(), 1, None), (ic.grazing(), 0, None),
             (ic.batch_impacts(256)[:32], 1, None),
             (ic.large_graded(), 1, [dict(list_mode=0, slack=0.03, cell_factor=f, block=128)
-                                    for f in CELL_FACTORS])]
+                                    for f in GRADED_CELL_FACTORS])]
+    if only is not None:  # re-measure some entries, keep the others
+        runs = [runs[i] for i in only]
+        try:
+            with open(SHIPPED) as f:
+                out = json.load(f)
+        except Exception:
+            out = {}
     for sc, prec, cands in runs:
         best, table = tune(sc, prec, device, candidates=cands, force=True, verbose=verbose)
         cls = workload_class(sc[0], sum(x.n for x in sc) // len(sc)) if isinstance(sc, list) else workload_class(sc)
@@ -175,4 +185,5 @@ def ship(device=0, verbose=True):
 
 
 if __name__ == "__main__":
-    ship()
+    import sys
+    ship(only=[int(a) for a in sys.argv[1:]] or None)
