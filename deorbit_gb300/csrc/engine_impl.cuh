@@ -320,6 +320,8 @@ public:
     explicit Engine(int device) : dev_(device) {
         DSPH_CUDA(cudaSetDevice(dev_));
         DSPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        DSPH_CUDA(cudaStreamCreateWithFlags(&copy_st_, cudaStreamNonBlocking));
+        DSPH_CUDA(cudaEventCreateWithFlags(&copy_ev_, cudaEventDisableTiming));
         DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
         DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
         DSPH_CUDA(cudaMalloc(&ntask_, sizeof(int32_t)));
@@ -340,9 +342,13 @@ public:
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
         for (auto& e : prof_pool_) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
-        for (int p = 0; p < 2; p++)
-            if (graph_exec_[p]) cudaGraphExecDestroy(graph_exec_[p]);
+        for (int g = 0; g < kGraphKinds; g++)
+            for (int p = 0; p < 2; p++)
+                if (graph_exec_[g][p]) cudaGraphExecDestroy(graph_exec_[g][p]);
         for (int i = 0; i < 16; i++) if (user_ev_[i]) cudaEventDestroy(user_ev_[i]);
+        cudaStreamSynchronize(copy_st_);
+        cudaEventDestroy(copy_ev_);
+        cudaStreamDestroy(copy_st_);
         cudaStreamDestroy(st_);
     }
 
@@ -597,7 +603,14 @@ public:
         for (size_t b = 0; b < imp_.size(); b++)
             if (imp_[b].used && imp_[b].alive && imp_[b].committed) mask[b] = 1;
         set_masks(mask, &dts, nullptr);
-        one_step(true);
+        if (use_graphs_ && !profiling_ && N_ > 0) {
+            const int p = cur_;
+            DSPH_CUDA(cudaGraphLaunch(ensure_graph(kGraphHostDt), st_));
+            launches_ += graph_launches_[kGraphHostDt][p];
+            cur_ = p ^ 1;  // the step's gather moved the carried state
+        } else {
+            one_step(true);
+        }
         grow_lists_after_overflow();
         pull_table();
         for (size_t b = 0; b < imp_.size(); b++)
@@ -677,18 +690,23 @@ public:
         set_masks(mask, nullptr, &te);
         const int nimp = (int)imp_.size();
         int s = 0;
-        if (use_graphs_ && !profiling_ && nsteps >= 2 && N_ > 0) {
+        if (use_graphs_ && !profiling_ && N_ > 0) {
             // two captured steps per launch (the gather alternates the carried
-            // buffers, so one graph covers both parities); an odd step first
+            // buffers, so a two-step graph returns to its own parity); an odd
+            // step first through the one-step graph of the current parity
             if (nsteps % 2) {
-                launch_small(k_run_control, nimp, 0);
-                one_step(false);
+                const int p = cur_;
+                DSPH_CUDA(cudaGraphLaunch(ensure_graph(kGraphOne), st_));
+                launches_ += graph_launches_[kGraphOne][p];
+                cur_ = p ^ 1;  // the step's gather moved the carried state
                 s = 1;
             }
-            cudaGraphExec_t ge = ensure_graph();
-            for (; s + 1 < nsteps; s += 2) {
-                DSPH_CUDA(cudaGraphLaunch(ge, st_));
-                launches_ += graph_launches_[cur_];
+            if (s + 1 < nsteps) {
+                cudaGraphExec_t ge = ensure_graph(kGraphTwo);
+                for (; s + 1 < nsteps; s += 2) {
+                    DSPH_CUDA(cudaGraphLaunch(ge, st_));
+                    launches_ += graph_launches_[kGraphTwo][cur_];
+                }
             }
             grow_lists_after_overflow();
         }
@@ -707,34 +725,40 @@ public:
         check_async();
     }
 
-    // Captures two device-controlled steps (no host round trips: all four
+    // Captures device-controlled steps (no host round trips: all four
     // adaptive-h rounds are issued and converged impacts skip them; list
     // overflow and slack are handled by the consumers' fallback) into one
-    // executable graph; re-captured whenever buffers, sizes or options change.
-    cudaGraphExec_t ensure_graph() {
+    // executable graph per kind and buffer parity: two run steps (device dt),
+    // one run step, or one step at the dt the host put in the impact table.
+    // Re-captured whenever buffers, sizes or options change.  Capture issues
+    // no work; the parity the graph starts from is restored afterwards.
+    cudaGraphExec_t ensure_graph(int kind) {
         const int p = cur_;
         const int64_t shape = N_ * 65536 + (int64_t)imp_.size();
-        if (graph_exec_[p] && graph_key_[p] == layout_epoch_ && graph_n_[p] == shape) return graph_exec_[p];
-        if (graph_exec_[p]) { cudaGraphExecDestroy(graph_exec_[p]); graph_exec_[p] = nullptr; }
+        cudaGraphExec_t& ge = graph_exec_[kind][p];
+        if (ge && graph_key_[kind][p] == layout_epoch_ && graph_n_[kind][p] == shape) return ge;
+        if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
         const int nimp = (int)imp_.size();
         const int64_t l0 = launches_;
         const uint64_t epoch0 = layout_epoch_;
+        const int64_t n0 = N_;
         DSPH_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < 2; k++) {
-            launch_small(k_run_control, nimp, 0);
+        for (int k = 0; k < (kind == kGraphTwo ? 2 : 1); k++) {
+            if (kind != kGraphHostDt) launch_small(k_run_control, nimp, 0);
             one_step(false);
         }
         cudaGraph_t g = nullptr;
         DSPH_CUDA(cudaStreamEndCapture(st_, &g));
-        DSPH_CUDA(cudaGraphInstantiate(&graph_exec_[p], g, 0));
+        DSPH_CUDA(cudaGraphInstantiate(&ge, g, 0));
         cudaGraphDestroy(g);
-        graph_launches_[p] = launches_ - l0;
+        graph_launches_[kind][p] = launches_ - l0;
         launches_ = l0;
-        if (cur_ != p || layout_epoch_ != epoch0)
+        cur_ = p;  // a one-step capture flips the parity without running anything
+        if (layout_epoch_ != epoch0 || N_ != n0)
             throw SphError(SPH_ERR_STATE, "graph capture changed the buffer layout");
-        graph_key_[p] = layout_epoch_;
-        graph_n_[p] = shape;
-        return graph_exec_[p];
+        graph_key_[kind][p] = layout_epoch_;
+        graph_n_[kind][p] = shape;
+        return ge;
     }
 
     void compute_density_h(int iters) override {
@@ -791,22 +815,28 @@ public:
         DSPH_CUDA(cudaStreamSynchronize(st_));
     }
 
-    // Several fields in one pass: every gather and copy is queued on the
-    // stream (through one staging slice per field) and the stream is
-    // synchronised once, so pinned caller buffers stream at link speed.
+    // Several fields in one pass, through one staging slice per field: the
+    // host copies run back to back on a copy stream while the compute stream
+    // gathers (reads) or scatters (writes) the neighbouring fields, each pair
+    // ordered by an event, and both streams are synchronised once -- pinned
+    // caller buffers stream at link speed.
     void read_fields(int b, int nf, const char* const* names, double* const* outs) override {
         ImpactH& h = imp(b);
         commit();
         if (h.n == 0 || nf <= 0) return;
+        for (int f = 0; f < nf; f++)
+            if (!with_column(names[f], [](auto*) {})) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
         ensure_stage((int64_t)nf * h.n);
         for (int f = 0; f < nf; f++) {
             double* slice = stage_d_ + (int64_t)f * h.n;
-            bool ok = with_column(names[f], [&](auto* col) {
+            with_column(names[f], [&](auto* col) {
                 launch_n_raw(k_read_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, slice);
             });
-            if (!ok) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
-            DSPH_CUDA(cudaMemcpyAsync(outs[f], slice, sizeof(double) * h.n, cudaMemcpyDeviceToHost, st_));
+            DSPH_CUDA(cudaEventRecord(copy_ev_, st_));
+            DSPH_CUDA(cudaStreamWaitEvent(copy_st_, copy_ev_, 0));
+            DSPH_CUDA(cudaMemcpyAsync(outs[f], slice, sizeof(double) * h.n, cudaMemcpyDeviceToHost, copy_st_));
         }
+        DSPH_CUDA(cudaStreamSynchronize(copy_st_));
         DSPH_CUDA(cudaStreamSynchronize(st_));
     }
 
@@ -814,18 +844,25 @@ public:
         ImpactH& h = imp(b);
         commit();
         if (h.n == 0 || nf <= 0) return;
+        for (int f = 0; f < nf; f++)
+            if (!with_column(names[f], [](auto*) {})) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
         ensure_stage((int64_t)nf * h.n);
+        // the staging slices may still feed earlier work on the compute stream
+        DSPH_CUDA(cudaEventRecord(copy_ev_, st_));
+        DSPH_CUDA(cudaStreamWaitEvent(copy_st_, copy_ev_, 0));
         for (int f = 0; f < nf; f++) {
             double* slice = stage_d_ + (int64_t)f * h.n;
-            DSPH_CUDA(cudaMemcpyAsync(slice, ins[f], sizeof(double) * h.n, cudaMemcpyHostToDevice, st_));
-            bool ok = with_column(names[f], [&](auto* col) {
+            DSPH_CUDA(cudaMemcpyAsync(slice, ins[f], sizeof(double) * h.n, cudaMemcpyHostToDevice, copy_st_));
+            DSPH_CUDA(cudaEventRecord(copy_ev_, copy_st_));
+            DSPH_CUDA(cudaStreamWaitEvent(st_, copy_ev_, 0));
+            with_column(names[f], [&](auto* col) {
                 launch_n_raw(k_write_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n,
                              (const double*)slice);
             });
-            if (!ok) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
             std::string nm(names[f]);
             if (nm == "x" || nm == "y" || nm == "z" || nm == "hh") grid_valid_ = false;
         }
+        DSPH_CUDA(cudaStreamSynchronize(copy_st_));
         DSPH_CUDA(cudaStreamSynchronize(st_));
     }
 
@@ -1879,6 +1916,8 @@ public:
     // ------------------------------------------------------------- members
     int dev_;
     cudaStream_t st_{};
+    cudaStream_t copy_st_{};   // host <-> device copies of the batched field I/O
+    cudaEvent_t copy_ev_{};
     std::vector<void*> allocs_, tmp_;
     std::vector<sph_material> mats_h_;
     MatT<R>* mats_d_ = nullptr;
@@ -1935,10 +1974,11 @@ public:
     int list_mode_ = 0;   // 0: thread per particle, 1: warp per column run
     bool use_graphs_ = true;
     uint64_t layout_epoch_ = 1;
-    cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
-    uint64_t graph_key_[2] = {0, 0};
-    int64_t graph_n_[2] = {-1, -1};
-    int64_t graph_launches_[2] = {0, 0};
+    enum { kGraphTwo = 0, kGraphOne = 1, kGraphHostDt = 2, kGraphKinds = 3 };
+    cudaGraphExec_t graph_exec_[kGraphKinds][2] = {};
+    uint64_t graph_key_[kGraphKinds][2] = {};
+    int64_t graph_n_[kGraphKinds][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+    int64_t graph_launches_[kGraphKinds][2] = {};
     int64_t launches_ = 0;
     bool profiling_ = false;
     cudaEvent_t ev_[6]{};
