@@ -1246,8 +1246,7 @@ public:
         for (int c = 0; c < 6; c++) v.dS_new[c] = der_[DR_DSN0 + c];
         v.rho_lo = der_[DR_RHOLO];
         v.pf = pf_; v.cpk = cpk_; v.refbin = refbin_;
-        v.vh = vh_; v.vl = vl_;
-        v.pk = pk_; v.fa = fa_; v.fb = fb_; v.fc = fc_;
+        v.pk = pk_; v.fr = fr_;
         v.cell_ptr = cell_cnt_;
         v.nbr = nbr_; v.nbr_cnt = nbr_cnt_; v.hlist = hlist_;
         v.xnbr = xnbr_; v.xcnt = xcnt_;
@@ -1499,12 +1498,8 @@ public:
         dfree(pf_); pf_ = dalloc<float4>(nc);
         dfree(pf_tmp_); pf_tmp_ = dalloc<float4>(nc);
         dfree(cpk_tmp_); cpk_tmp_ = dalloc<uint32_t>(nc);
-        dfree(vh_); vh_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
-        dfree(vl_); vl_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
         dfree(pk_); pk_ = dalloc<float2>(sizeof(R) == 4 ? nc : 1);
-        dfree(fa_); fa_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
-        dfree(fb_); fb_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
-        dfree(fc_); fc_ = dalloc<float4>(sizeof(R) == 4 ? nc : 1);
+        dfree(fr_); fr_ = dalloc<float4>(sizeof(R) == 4 ? 6 * nc : 2);  // 96-byte records, 32-byte aligned
         dfree(tasks_); tasks_ = dalloc<int32_t>(nc);
         dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
         dfree(refbin_); refbin_ = dalloc<unsigned long long>(nc);
@@ -1938,10 +1933,8 @@ public:
     float4* pf_ = nullptr;
     float4* pf_tmp_ = nullptr;     // offsets / cells in the pre-sort order
     uint32_t* cpk_tmp_ = nullptr;
-    float4* vh_ = nullptr;
-    float4* vl_ = nullptr;
     float2* pk_ = nullptr;
-    float4 *fa_ = nullptr, *fb_ = nullptr, *fc_ = nullptr;
+    float4* fr_ = nullptr;         // mixed-form force-source records, six float4 per particle
     int32_t* tasks_ = nullptr;
     int32_t* ntask_ = nullptr;
     unsigned int* cell_hmax_ = nullptr;

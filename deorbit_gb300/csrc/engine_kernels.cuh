@@ -83,10 +83,12 @@ struct View {
     R* rho_lo;          // mixed form: low part of the compensated density sum (0 in FP64)
     R* dS_new[6];
     float4* pf;
-    float4 *vh, *vl;     // mixed form: FP64 velocity split into FP32 hi + lo
     float2* pk;          // mixed form: (mass, packed cell) per particle, for density gathers
-    float4 *fa, *fb, *fc; // mixed form: packed force-source records (m/rho, rho, csig,
-                          // Pf/rho^2), (dscale/rho^2, Rart, S4, S5), (S0..S3)
+    float4* fr;          // mixed form: 96-byte force-source record of particle k at fr[6k..6k+5]:
+                         // [0] offsets + h, [1] FP32 hi part of the FP64 velocity + mass,
+                         // [2] lo part + packed cell, [3] (m/rho, rho, csig, Pf/rho^2),
+                         // [4] (dscale/rho^2, Rart, S4, S5), [5] (S0..S3); read as three
+                         // 32-byte loads
     uint32_t* cpk;
     unsigned long long* refbin;
     const int32_t* cell_ptr;
@@ -356,6 +358,15 @@ __device__ __forceinline__ void traverse_sphere(const View<R>& v, const ImpactD&
             }
         }
     }
+}
+
+// One 32-byte load (two float4 halves) of a 32-byte-aligned record that no
+// thread of the kernel writes: sm_100-class GPUs load 256 bits per thread in one
+// instruction, here through the read-only path.
+__device__ __forceinline__ void ld_f32x8_ro(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
 }
 
 // Own-list addressing: entry t of particle k lives at nbr[4k + nbr_slot(t, ls)],
@@ -1082,6 +1093,28 @@ struct Plain {
 template <class R>
 using AccT = typename std::conditional<sizeof(R) == 4, Kahan<R>, Plain<R>>::type;
 
+// Packed FP32 arithmetic: one sm_100-class instruction works on two lanes of a
+// float2, each rounded exactly as the scalar operation (x - y is formed as the
+// fused y * -1 + x, which rounds once, like the subtraction).
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+
+// Two compensated sums side by side (the Kahan steps above, lane by lane).
+struct Kahan2 {
+    float2 s, c;
+    __device__ __forceinline__ void init() { s = c = make_float2(0.0f, 0.0f); }
+    __device__ __forceinline__ void add(float2 x) {
+        const float2 y = sub2(x, c);
+        const float2 t = add2(s, y);
+        c = sub2(sub2(t, s), y);
+        s = t;
+    }
+};
+
 // Does particle k's superset list still cover it (count within capacity and h
 // within the slack, with an allowance for the FP32 distance)?
 template <class R>
@@ -1190,16 +1223,17 @@ static __global__ void k_eos(View<R> v) {
     v.dsr2[k] = irho2 * dsc;
     v.vol[k] = v.mass[k] / rho;
     if (sizeof(R) == 4) {
-        v.fa[k] = make_float4((float)v.vol[k], (float)rho, (float)v.csig[k], (float)v.pfr2[k]);
-        v.fb[k] = make_float4((float)v.dsr2[k], (float)v.Rart[k], (float)v.S[4][k], (float)v.S[5][k]);
-        v.fc[k] = make_float4((float)v.S[0][k], (float)v.S[1][k], (float)v.S[2][k], (float)v.S[3][k]);
+        float4* o = v.fr + 6 * k;
         const double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k];
         const float hx = (float)vx, hy = (float)vy, hz = (float)vz;
-        // .w lanes carry the mass and packed cell of the particle, so the force
-        // pass gathers six records per neighbour instead of seven
-        v.vh[k] = make_float4(hx, hy, hz, (float)v.mass[k]);
-        v.vl[k] = make_float4((float)(vx - (double)hx), (float)(vy - (double)hy), (float)(vz - (double)hz),
-                              __uint_as_float(v.cpk[k]));
+        o[0] = v.pf[k];
+        // .w lanes carry the mass and packed cell of the particle
+        o[1] = make_float4(hx, hy, hz, (float)v.mass[k]);
+        o[2] = make_float4((float)(vx - (double)hx), (float)(vy - (double)hy), (float)(vz - (double)hz),
+                           __uint_as_float(v.cpk[k]));
+        o[3] = make_float4((float)v.vol[k], (float)rho, (float)v.csig[k], (float)v.pfr2[k]);
+        o[4] = make_float4((float)v.dsr2[k], (float)v.Rart[k], (float)v.S[4][k], (float)v.S[5][k]);
+        o[5] = make_float4((float)v.S[0][k], (float)v.S[1][k], (float)v.S[2][k], (float)v.S[3][k]);
     }
 }
 
@@ -1222,12 +1256,18 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     const R dsri = v.dsr2[k], Rai = v.Rart[k];
     const double vxi = v.vx[k], vyi = v.vy[k], vzi = v.vz[k];
     float4 vhi = make_float4(0, 0, 0, 0), vli = vhi;
-    if (sizeof(R) == 4) { vhi = v.vh[k]; vli = v.vl[k]; }
+    if (sizeof(R) == 4) { vhi = v.fr[6 * k + 1]; vli = v.fr[6 * k + 2]; }
     const R sxx = v.S[0][k], syy = v.S[1][k], szz = v.S[2][k];
     const R sxy = v.S[3][k], sxz = v.S[4][k], syz = v.S[5][k];
     R L00 = 0, L01 = 0, L02 = 0, L10 = 0, L11 = 0, L12 = 0, L20 = 0, L21 = 0, L22 = 0;
     Acc ax, ay, az, du;
     ax.init(); ay.init(); az.init(); du.init();
+    // mixed form: the same sums in packed pairs -- (L00, L01), (L10, L11),
+    // (L20, L21), (L02, L12), and compensated (ax, ay), (az, du)
+    float2 Lp0 = f2(0.0f), Lp1 = f2(0.0f), Lp2 = f2(0.0f), Lpz = f2(0.0f);
+    float Lp22 = 0.0f;
+    Kahan2 kxy, kzu;
+    kxy.init(); kzu.init();
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
     const float m = sizeof(R) == 8 ? I.margin : 0.0f;
@@ -1277,7 +1317,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     };
     const float hs_pad = 2.0f * m;
     auto body = [&](int32_t j) {
-        if (sizeof(R) == 8) {
+        if constexpr (sizeof(R) == 8) {
             if (j == (int32_t)k) return;
             const float4 pjf = v.pf[j];
             float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
@@ -1307,29 +1347,73 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             // Branch-free: every record of the entry is loaded up front (most
             // entries interact), and a pair that fails the criterion -- or the
             // particle itself (r = 0) -- contributes exact zeros through dW = 0.
-            const float4 pj = v.pf[j];
-            const float4 fa = v.fa[j], fb = v.fb[j], fc = v.fc[j];
-            const float4 vhj = v.vh[j], vlj = v.vl[j];
-            const float2 mk = make_float2(vhj.w, vlj.w);  // (mass, packed cell)
+            float4 pj, vhj, vlj, fa, fb, fc;
+            const float4* rec = v.fr + 6 * (int64_t)j;
+            ld_f32x8_ro(rec, pj, vhj);
+            ld_f32x8_ro(rec + 2, vlj, fa);
+            ld_f32x8_ro(rec + 4, fb, fc);
+            const float mj = vhj.w;  // (mass, packed cell) ride in the .w lanes
             float dx, dy, dz;
-            sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
+            sep_f32(I, pi, ci, pj, __float_as_uint(vlj.w), dx, dy, dz);
             const float r2 = dx * dx + dy * dy + dz * dz;
-            const float hs = (float)hi + pj.w;
+            const float hif = (float)hi;
+            const float hs = hif + pj.w;
             bool ok = r2 < hs * hs && r2 != 0.0f;
             if (need_member) ok = ok && ref_member(v.refbin[k], v.refbin[j], I);  // own bins re-read: rarely needed
             const float irs = ok ? rsqrtf(r2) : 1.0f;  // hardware 1/sqrt (2 ulp)
-            const R r = ok ? (R)(r2 * irs) : R(1);
-            const R hbar = R(0.5) * (hi + (R)pj.w);
-            const R ihb = pair_div(R(1), hbar);
-            const R dW = ok ? kernel_dW_bf<R>(r, ihb) : R(0);
-            const R wg = dW * (R)irs;
-            const R gx = (R)dx * wg, gy = (R)dy * wg, gz = (R)dz * wg;
+            const float r = ok ? r2 * irs : 1.0f;
+            const float hbar = 0.5f * (hif + pj.w);
+            const float ihb = pair_div(1.0f, hbar);
+            const float dW = ok ? kernel_dW_bf<float>(r, ihb) : 0.0f;
+            const float wg = dW * irs;
+            const float2 gxy = mul2(f2(dx, dy), f2(wg));
+            const float gz = dz * wg;
             // hi parts nearly cancel exactly; lo parts restore the FP64 difference
-            const R vx = (R)((vhi.x - vhj.x) + (vli.x - vlj.x));
-            const R vy = (R)((vhi.y - vhj.y) + (vli.y - vlj.y));
-            const R vz = (R)((vhi.z - vhj.z) + (vli.z - vlj.z));
-            pair_math((R)dx, (R)dy, (R)dz, r, hbar, ihb, dW, gx, gy, gz, vx, vy, vz, (R)fa.x, (R)fa.y, (R)fa.z,
-                      (R)fa.w, (R)fb.x, (R)fb.y, (R)mk.x, (R)fc.x, (R)fc.y, (R)fc.z, (R)fc.w, (R)fb.z, (R)fb.w, j);
+            const float2 vxy = add2(sub2(f2(vhi.x, vhi.y), f2(vhj.x, vhj.y)), sub2(f2(vli.x, vli.y), f2(vlj.x, vlj.y)));
+            const float vz = (vhi.z - vhj.z) + (vli.z - vlj.z);
+            const float Vj = fa.x, rhoj = fa.y, csj = fa.z, pfj = fa.w, dsj = fb.x, Raj = fb.y;
+            if (strength) {  // Vj (v_j - v_i) (x) grad W
+                const float2 exy = mul2(vxy, f2(-Vj));
+                const float ez = -vz * Vj;
+                Lp0 = fma2(f2(exy.x), gxy, Lp0);
+                Lp1 = fma2(f2(exy.y), gxy, Lp1);
+                Lp2 = fma2(f2(ez), gxy, Lp2);
+                Lpz = fma2(exy, f2(gz), Lpz);
+                Lp22 = fmaf(ez, gz, Lp22);
+            }
+            const float dvr = vxy.x * dx + vxy.y * dy + vz * dz;
+            float Pij = 0.0f;
+            if (dvr < 0.0f) {
+                const float mu = pair_div(hbar * dvr, r * r + (float)eps * hbar * hbar);
+                const float cbar = 0.5f * ((float)csi + csj);
+                Pij = pair_div(-(float)alpha * cbar * mu + (float)beta * mu * mu, 0.5f * ((float)rhoi + rhoj));
+            }
+            const float term = (float)Pi_over + pfj + Pij;
+            float dut = 0.5f * mj * term * (vxy.x * gxy.x + vxy.y * gxy.y + vz * gz);
+            float mterm = term;
+            if (eps_as > R(0)) {
+                const float q = r * ihb;
+                const float t = fmaxf(2.0f - q, 0.0f), a = fmaxf(1.0f - q, 0.0f);
+                const float fr = (0.25f * t * t * t - a * a * a) * (float)inv_poly;
+                float fn = fr * fr;
+                fn *= fn;
+                mterm += ((float)Rai + Raj) * fn;
+            }
+            const float mm = mj * mterm;
+            // (S_i dscale_i / rho_i^2 + S_j dscale_j / rho_j^2) . grad W, x and y rows packed
+            const float2 own = fma2(f2((float)sxz, (float)syz), f2(gz),
+                                    fma2(f2((float)sxy, (float)syy), f2(gxy.y), mul2(f2((float)sxx, (float)sxy), f2(gxy.x))));
+            const float2 oth = fma2(f2(fb.z, fb.w), f2(gz), fma2(f2(fc.w, fc.y), f2(gxy.y), mul2(f2(fc.x, fc.w), f2(gxy.x))));
+            const float2 stxy = fma2(oth, f2(dsj), mul2(own, f2((float)dsri)));
+            const float stz = ((float)sxz * gxy.x + (float)syz * gxy.y + (float)szz * gz) * (float)dsri +
+                              (fb.z * gxy.x + fb.w * gxy.y + fc.z * gz) * dsj;
+            kxy.add(fma2(gxy, f2(-mm), mul2(stxy, f2(mj))));
+            if (alpha_u > R(0)) {
+                const float rbar = 0.5f * ((float)rhoi + rhoj);
+                const float vsig = rsqrt_(pair_div(fabsf((float)v.P[k] - (float)v.P[j]), rbar));
+                dut += pair_div((float)alpha_u * mj * vsig * ((float)v.u[k] - (float)v.u[j]) * dW, rbar);
+            }
+            kzu.add(f2(stz * mj - gz * mm, dut));
         }
     };
     if (!I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap) {
@@ -1341,6 +1425,11 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
     } else {
         traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
                  [&](int32_t j, float, float, float) { body(j); });
+    }
+    if constexpr (sizeof(R) == 4) {
+        L00 = Lp0.x; L01 = Lp0.y; L10 = Lp1.x; L11 = Lp1.y; L20 = Lp2.x; L21 = Lp2.y;
+        L02 = Lpz.x; L12 = Lpz.y; L22 = Lp22;
+        ax.s = kxy.s.x; ay.s = kxy.s.y; az.s = kzu.s.x; du.s = kzu.s.y;
     }
     R epsw = R(0);
     if (strength) {
