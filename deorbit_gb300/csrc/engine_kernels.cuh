@@ -377,14 +377,19 @@ __device__ __forceinline__ int64_t nbr_slot(int t, int64_t ls) {
 }
 
 // f(j) for entries 0..cnt-1 of particle k's own list, in list order.
+// The next index block is loaded one block ahead, so its (usually uncached)
+// read overlaps the current block's entries.
 template <class F>
 __device__ __forceinline__ void walk_list(const int32_t* nbr, int64_t ls, int64_t k, int cnt, F&& f) {
     const int4* p = reinterpret_cast<const int4*>(nbr) + k;
-    for (int t = 0; t < cnt; t += 4, p += ls) {
-        const int4 q = *p;
+    int4 q = cnt > 0 ? *p : make_int4(0, 0, 0, 0);
+    for (int t = 0; t < cnt; t += 4) {
+        p += ls;
+        const int4 qn = t + 4 < cnt ? *p : q;
         const int m = min(4, cnt - t);
 #pragma unroll 1
         for (int i = 0; i < m; i++) f(i == 0 ? q.x : i == 1 ? q.y : i == 2 ? q.z : q.w);
+        q = qn;
     }
 }
 
