@@ -25,6 +25,9 @@ CELL_FACTORS = (0.75, 1.0, 1.5)
 # graded lattices: h spans an order of magnitude, and cells sized for the finest
 # particles make the coarse ones search hundreds of columns
 GRADED_CELL_FACTORS = (1.5, 2.0, 3.0, 4.0)
+# (cell factor, z cell factor) pairs also tried there: flatter cells shorten the
+# column chords of the list build at the price of more cells to sort
+GRADED_FLAT_CELLS = ((3.0, 0.5), (4.0, 0.5), (3.0, 0.33))
 SLACKS = (0.03, 0.06)
 BLOCKS = (128, 256)
 LIST_MODES = (2, 1, 0)
@@ -85,6 +88,7 @@ def measure(sc, precision, cfg, device=0, steps=3, warmup=2) -> float:
     ctx = sph.Context(precision, device)
     try:
         ctx.set_tuning(cfg.get("block", 0), cfg.get("cell_factor", 0.0))
+        ctx.set_option("cell_factor_z", cfg.get("cell_factor_z", 1.0))
         ctx.set_option("slack", cfg.get("slack", 0.08))
         ctx.set_option("list_mode", cfg.get("list_mode", 1))
         mids = {}
@@ -129,7 +133,7 @@ def tune(sc, precision, device=0, steps=3, warmup=2, candidates=None, force=Fals
         if verbose:
             print(f"  {cfg} -> {ms:.3f} ms/step ({time.perf_counter() - t0:.1f} s)", flush=True)
     best = min(table, key=lambda r: r["ms_per_step"])
-    best = {k2: best[k2] for k2 in ("list_mode", "slack", "cell_factor", "block")}
+    best = {k2: best[k2] for k2 in ("list_mode", "slack", "cell_factor", "cell_factor_z", "block") if k2 in best}
     n = sum(x.n for x in sc) if isinstance(sc, (list, tuple)) else sc.n
     cache[k] = {"best": best, "table": table, "n": n, "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     _save(cache)
@@ -148,6 +152,7 @@ def apply(ctx, sc, precision, device=0, per_impact_n=None, default=None):
     cfg = lookup(sc, precision, device, per_impact_n) or default
     if cfg:
         ctx.set_tuning(int(cfg.get("block", 0)), float(cfg.get("cell_factor", 0.0)))
+        ctx.set_option("cell_factor_z", float(cfg.get("cell_factor_z", 1.0)))
         ctx.set_option("slack", cfg.get("slack", 0.08))
         ctx.set_option("list_mode", cfg.get("list_mode", 1))
     return cfg
@@ -157,14 +162,16 @@ def ship(device=0, verbose=True, only=None):
     """Re-measure the table shipped for this GPU model (tuned_gb300.json on a
     GB300): the 1,048,576-particle grazing impact in both forms, the batched
     class (32 impacts of the 256-impact sweep run as one batch) and the
-    16,777,216-particle graded run (cell factor only).  Returns the entries."""
+    16,777,216-particle graded run (cell factors only).  Returns the entries."""
     from . import ic
 
     out = {}
     runs = [(ic.grazing(), 1, None), (ic.grazing(), 0, None),
             (ic.batch_impacts(256)[:32], 1, None),
             (ic.large_graded(), 1, [dict(list_mode=0, slack=0.03, cell_factor=f, block=128)
-                                    for f in GRADED_CELL_FACTORS])]
+                                    for f in GRADED_CELL_FACTORS] +
+             [dict(list_mode=0, slack=0.03, cell_factor=f, cell_factor_z=fz, block=128)
+              for f, fz in GRADED_FLAT_CELLS])]
     if only is not None:  # re-measure some entries, keep the others
         runs = [runs[i] for i in only]
         try:

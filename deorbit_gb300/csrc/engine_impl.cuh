@@ -1056,6 +1056,11 @@ public:
             }
         } else if (k == "cell_factor") {
             set_tuning(0, value);
+        } else if (k == "cell_factor_z") {
+            if (!(value > 0.0 && value <= 4.0)) throw SphError(SPH_ERR_ARG, "cell_factor_z must be in (0, 4]");
+            for (auto& h : imp_)
+                if (h.committed) throw SphError(SPH_ERR_STATE, "cell factors must be set before particles are committed");
+            cell_factor_z_ = value;
         } else if (k == "block") {
             set_tuning((int)value, 0);
         } else {
@@ -1068,6 +1073,7 @@ public:
         if (k == "graphs") return use_graphs_ ? 1 : 0;
         if (k == "slack") return slack_;
         if (k == "cell_factor") return cell_factor_;
+        if (k == "cell_factor_z") return cell_factor_z_;
         if (k == "block") return block_;
         if (k == "list_capacity") return cap_nbr_;
         if (k == "list_entries") return (double)list_entries();
@@ -1328,10 +1334,11 @@ public:
     }
 
     // Fine traversal grid of an impact: cells of ~cell_factor * h_init over the
-    // domain (padded on open axes), exact period on periodic axes.
+    // domain (padded on open axes; z cells cell_factor_z times that height),
+    // exact period on periodic axes.
     void make_fine_grid(ImpactD& I, const ImpactH& h) {
-        double w0 = cell_factor_ * h.prm.h_init;
-        if (!(w0 > 0)) w0 = 1.0;
+        double w00 = cell_factor_ * h.prm.h_init;
+        if (!(w00 > 0)) w00 = 1.0;
         double bblo[3], bbhi[3];
         for (int a = 0; a < 3; a++) { bblo[a] = 1e300; bbhi[a] = -1e300; }
         const std::vector<double>* P[3] = {&h.sx, &h.sy, &h.sz};
@@ -1340,6 +1347,7 @@ public:
         const int lim[3] = {2047, 2047, 1023};
         int64_t cells = 1;
         for (int a = 0; a < 3; a++) {
+            const double w0 = a == 2 ? w00 * cell_factor_z_ : w00;
             double lo = h.dlo[a], ext = h.dhi[a] - h.dlo[a];
             if (!(ext > 0)) {  // no domain on this axis: cover the particles
                 lo = (bblo[a] <= bbhi[a] ? bblo[a] : 0.0) - 2 * w0;
@@ -1964,6 +1972,7 @@ public:
     R* flaw_eps_d_ = nullptr;
     int block_ = 128;
     double cell_factor_ = 1.0;
+    double cell_factor_z_ = 1.0;  // z cell height relative to the x / y width
     int list_mode_ = 0;   // 0: thread per particle, 1: warp per column run
     bool use_graphs_ = true;
     uint64_t layout_epoch_ = 1;

@@ -309,8 +309,10 @@ int sph_load_checkpoint(sph_ctx* ctx, const char* path, const sph_params* p, int
 int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor);
 /* Named engine options: "list_mode" (neighbour-list build: 0 thread per
  * particle, 1 warp per column run, 2 warp per particle), "cell_factor",
- * "block", "slack" (neighbour-list radius slack), "graphs" (1: sph_run uses
- * CUDA graphs); read-only "list_capacity" (entries per particle) and
+ * "cell_factor_z" (traversal cell height over width, (0, 4]; like
+ * "cell_factor", set before particles are committed), "block", "slack"
+ * (neighbour-list radius slack), "graphs" (1: sph_step and sph_run replay
+ * captured CUDA graphs); read-only "list_capacity" (entries per particle) and
  * "list_entries" (entries of the current lists, own plus reverse). */
 int sph_set_option(sph_ctx* ctx, const char* key, double value);
 int sph_get_option(sph_ctx* ctx, const char* key, double* value);

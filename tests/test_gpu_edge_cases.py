@@ -1,7 +1,8 @@
 """Edge cases of the step loop on the GPU: empty impacts, neighbour-list
 overflow (the consumers' traversal fallback and the capacity growth), a box
 periodic on all three axes, a particle that leaves the domain (clamped bins,
-sph.hpp:142-146), and removing an impact in the middle of a batch.  FP64 parity
+sph.hpp:142-146), flattened traversal cells, and removing an impact in the
+middle of a batch.  FP64 parity
 with the oracle where the oracle applies (rel-L2 <= 1e-9), bit-identity with an
 undisturbed run otherwise."""
 import os
@@ -18,9 +19,11 @@ pytestmark = pytest.mark.gpu
 NAMES = ["x", "y", "z", "vx", "vy", "vz", "u", "rho", "hh", "P"]
 
 
-def run_pair(sc, steps):
+def run_pair(sc, steps, **opts):
     from deorbit_gb300 import sph
     ctx = sph.Context(sph.FP64)
+    for k, val in opts.items():
+        ctx.set_option(k, val)
     b = ic.to_context(ctx, sc)
     orc = ic.to_oracle(sc, threads=min(os.cpu_count() or 1, 16))
     ctx.init()
@@ -98,6 +101,15 @@ def test_escaping_particle_matches_oracle(cuda_lib, oracle_lib):
     k = int(np.argmax(sc.pos[:, 2]))
     sc.vel[k] = (0.0, 0.0, 4.0e5)   # leaves through the top within a few steps
     errs, info, _ = run_pair(sc, 8)
+    assert max(errs.values()) < 1e-9, errs
+
+
+@pytest.mark.parametrize("cfz", [0.5, 0.25])
+def test_flat_z_cells_match_oracle(cuda_lib, oracle_lib, cfz):
+    """Traversal cells cell_factor_z times as high as wide: the same pairs,
+    found over shorter column chords."""
+    sc = ic.impact_halfspace(nx=12, ny=12, nz=6, r_cells=2.0)
+    errs, _, _ = run_pair(sc, 4, cell_factor_z=cfz)
     assert max(errs.values()) < 1e-9, errs
 
 
