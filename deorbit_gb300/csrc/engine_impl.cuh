@@ -638,6 +638,7 @@ public:
         density_rounds(2, host_sync);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[2], st_));
         if (host_sync) refresh_list_if_needed();
+        else refresh_list_device();
         cls(KC_EOS);
         launch_n(k_eos<R>, N_);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[3], st_));
@@ -1811,10 +1812,10 @@ public:
                 prof_end();
                 launches_++;
             } else {
-                launch_n(k_list_thread<R>, N_, block_);
+                launch_list_thread(0);
             }
             cls(KC_OTHER);
-            launch_n(k_sort_extra<R>, N_);
+            launch_n_raw(k_sort_extra<R>, N_, view(), 0);
             cls(keep);
             if (!host_check) return;
             DSPH_CUDA(cudaMemcpyAsync(flags_h_, flags_d_, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
@@ -1824,6 +1825,30 @@ public:
             alloc_lists();
         }
         throw SphError(SPH_ERR_CAPACITY, "neighbour list capacity could not be satisfied");
+    }
+
+    void launch_list_thread(int refresh) {
+        const int bs = block_ > 0 ? block_ : 256;
+        prof_begin();
+        k_list_thread<R><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
+        launched((const void*)k_list_thread<R>);
+        prof_end();
+        launches_++;
+    }
+
+    // Device-controlled counterpart of refresh_list_if_needed (captured
+    // steps): impacts whose h outgrew the slack in this step's density rounds
+    // rebuild their lists on the device, the others' kernels return at once,
+    // so the force pass keeps list walks instead of the traversal fallback.
+    void refresh_list_device() {
+        if (N_ <= 0 || list_mode_ != 0) return;  // other builders: the consumers' fallback
+        const int keep = cur_cls_;
+        cls(KC_LIST_FORCE);
+        launch_n(k_refresh_begin<R>, N_);
+        launch_list_thread(1);
+        launch_n_raw(k_sort_extra<R>, N_, view(), 1);
+        launch_small(k_impact_end_refresh, (int)imp_.size());
+        cls(keep);
     }
 
     // Rebuild the superset list when some h outgrew its slack (avoids the

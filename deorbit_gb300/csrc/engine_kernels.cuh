@@ -516,6 +516,22 @@ static __global__ void k_impact_ranges(ImpactD* imps, int nimp, const int32_t* c
     I.margin = 1.0e-5f * (om + wmax) + 8.0e-5f * I.hcap + 1.0e-30f;
 }
 
+// Start of an on-device list rebuild: empty the extra lists of the impacts
+// whose h outgrew the slack.
+template <class R>
+static __global__ void k_refresh_begin(View<R> v) {
+    int64_t k = gtid();
+    if (k >= v.n) return;
+    const ImpactD& I = v.imps[v.imp[k]];
+    if (I.mask && I.slack_flag) v.xcnt[k] = 0;
+}
+
+// End of an on-device list rebuild: the rebuilt lists cover the new h.
+static __global__ void k_impact_end_refresh(ImpactD* imps, int nimp) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nimp && imps[b].mask) imps[b].slack_flag = 0;
+}
+
 // Phase flags: 0 = clear reductions for masked impacts.
 static __global__ void k_impact_reset_slack(ImpactD* imps, int nimp) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -676,20 +692,24 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
 // packed cell word instead of a walk over the cell boundaries.  Every lane
 // visits the same candidates in the same order as traverse_sphere(), so the
 // lists equal those of a per-thread traversal entry for entry.
+//
+// refresh != 0: rebuild only the lists of impacts whose h outgrew the slack in
+// this step's density rounds (the others return at once).
 template <class R>
-static __global__ void k_list_thread(View<R> v) {
+static __global__ void k_list_thread(View<R> v, int refresh) {
     const unsigned full = 0xffffffffu;
     const int64_t k0 = gtid();
     const bool inb = k0 < v.n;
     const int64_t k = inb ? k0 : v.n - 1;
     const int ib = v.imp[k];
     const ImpactD& I = v.imps[ib];
+    const bool wanted = I.mask && (!refresh || I.slack_flag);
     const bool one_impact = __all_sync(full, ib == __shfl_sync(full, ib, 0));
     if (!one_impact || (I.per[0] | I.per[1] | I.per[2])) {
-        if (inb && I.mask) list_one(v, I, k);
+        if (inb && wanted) list_one(v, I, k);
         return;
     }
-    if (!I.mask) return;  // warp-uniform: one impact
+    if (!wanted) return;  // warp-uniform: one impact
     const bool act = inb;
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
@@ -1053,11 +1073,13 @@ static __global__ void __launch_bounds__(256) k_list_wpp(View<R> v) {
     }
 }
 
-// Sort each particle's extra list (filled by atomics) into ascending order.
+// Sort each particle's extra list (filled by atomics) into ascending order
+// (refresh != 0: only in impacts whose lists are being rebuilt).
 template <class R>
-static __global__ void k_sort_extra(View<R> v) {
+static __global__ void k_sort_extra(View<R> v, int refresh) {
     int64_t k = gtid();
     if (k >= v.n) return;
+    if (refresh && !v.imps[v.imp[k]].slack_flag) return;
     const int c = min(v.xcnt[k], kExtraCap);
     if (c < 2) return;
     int32_t* a = v.xnbr + k;  // entry t at a[t * ls]
