@@ -1253,7 +1253,7 @@ public:
         for (int c = 0; c < 6; c++) v.dS_new[c] = der_[DR_DSN0 + c];
         v.rho_lo = der_[DR_RHOLO];
         v.pf = pf_; v.cpk = cpk_; v.refbin = refbin_;
-        v.pk = pk_; v.fr = fr_;
+        v.pk = pk_; v.fr = fr_; v.lf = lf_;
         v.cell_ptr = cell_cnt_;
         v.nbr = nbr_; v.nbr_cnt = nbr_cnt_; v.hlist = hlist_;
         v.xnbr = xnbr_; v.xcnt = xcnt_;
@@ -1508,6 +1508,7 @@ public:
         dfree(pf_tmp_); pf_tmp_ = dalloc<float4>(nc);
         dfree(cpk_tmp_); cpk_tmp_ = dalloc<uint32_t>(nc);
         dfree(pk_); pk_ = dalloc<float2>(sizeof(R) == 4 ? nc : 1);
+        dfree(lf_); lf_ = dalloc<float4>(nc);
         dfree(fr_); fr_ = dalloc<float4>(sizeof(R) == 4 ? 6 * nc : 2);  // 96-byte records, 32-byte aligned
         dfree(tasks_); tasks_ = dalloc<int32_t>(nc);
         dfree(cpk_); cpk_ = dalloc<uint32_t>(nc);
@@ -1771,6 +1772,7 @@ public:
             g.gid_in = gid_[cur_]; g.gid_out = gid_[alt];
             g.pf_in = pf_tmp_; g.pf_out = pf_;
             g.cpk_in = cpk_tmp_; g.cpk_out = cpk_;
+            g.lf_out = lf_; g.imps = tab_d_;
             launch_n_raw(k_gather<R>, n_new, n_new, (const int32_t*)src_, g);
         }
         cur_ = alt;
@@ -1967,6 +1969,7 @@ public:
     float4* pf_tmp_ = nullptr;     // offsets / cells in the pre-sort order
     uint32_t* cpk_tmp_ = nullptr;
     float2* pk_ = nullptr;
+    float4* lf_ = nullptr;         // list-frame coordinates and h
     float4* fr_ = nullptr;         // mixed-form force-source records, six float4 per particle
     int32_t* tasks_ = nullptr;
     int32_t* ntask_ = nullptr;

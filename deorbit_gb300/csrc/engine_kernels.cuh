@@ -53,7 +53,8 @@ struct ImpactD {
     double h_max, hmax0;
     float hmax_f, margin;
     double inv_poly_eta;                           // 1 / W-polynomial at q = 1/eta
-    float inv_poly_eta_f, pad3;                    // the same in FP32 (no conversion in pair loops)
+    float inv_poly_eta_f;                          // the same in FP32 (no conversion in pair loops)
+    float lmargin;                                 // list-frame rounding bound on r (list radii)
     float hcap;                                    // upper bound of h (2 max h0)
     float cwmin;                                   // smallest reference cell width (nc > 1)
     float slack;                                   // superset-list radius slack
@@ -64,7 +65,7 @@ struct ImpactD {
     int64_t off, n;                                // sorted particle range
     int64_t gid_base;
     unsigned long long hmax_bits, hm_bits, dt_bits;
-    unsigned int omax_bits, pad1;
+    unsigned int omax_bits, pad1;                  // max |offset from the cell origin|
 };
 
 template <class R>
@@ -84,6 +85,8 @@ struct View {
     R* dS_new[6];
     float4* pf;
     float2* pk;          // mixed form: (mass, packed cell) per particle, for density gathers
+    float4* lf;          // list frame: FP32 coordinates relative to the traversal-grid origin,
+                         // and h; the list builders' pair distances (one load per candidate)
     float4* fr;          // mixed form: 96-byte force-source record of particle k at fr[6k..6k+5]:
                          // [0] offsets + h, [1] FP32 hi part of the FP64 velocity + mass,
                          // [2] lo part + packed cell, [3] (m/rho, rho, csig, Pf/rho^2),
@@ -473,6 +476,8 @@ struct GatherCols {
     float4* pf_out;
     const uint32_t* cpk_in;
     uint32_t* cpk_out;
+    float4* lf_out;          // list frame, formed from the cell and the offset
+    const ImpactD* imps;
 };
 
 template <class R>
@@ -485,10 +490,18 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
     for (int c = 0; c < g.nr; c++) static_cast<R*>(g.rout[c])[k] = static_cast<const R*>(g.rin[c])[s];
     g.b_out[0][k] = g.b_in[0][s];
     g.b_out[1][k] = g.b_in[1][s];
-    g.imp_out[k] = g.imp_in[s];
+    const uint16_t ib = g.imp_in[s];
+    g.imp_out[k] = ib;
     g.gid_out[k] = g.gid_in[s];
-    g.pf_out[k] = g.pf_in[s];
-    g.cpk_out[k] = g.cpk_in[s];
+    const float4 p = g.pf_in[s];
+    const uint32_t c = g.cpk_in[s];
+    g.pf_out[k] = p;
+    g.cpk_out[k] = c;
+    // one FP32 coordinate per particle (all its pairs use the same value):
+    // |lf - (x - glo)| <= 2 roundings of a value below nf w + max |offset|
+    const ImpactD& I = g.imps[ib];
+    g.lf_out[k] = make_float4((float)(c & 2047u) * I.wf[0] + p.x, (float)((c >> 11) & 2047u) * I.wf[1] + p.y,
+                              (float)(c >> 22) * I.wf[2] + p.z, p.w);
 }
 
 // After the gather: inverse permutation, traversal-cell coordinates and FP32
@@ -514,6 +527,11 @@ static __global__ void k_impact_ranges(ImpactD* imps, int nimp, const int32_t* c
     float om = __uint_as_float(I.omax_bits);
     float wmax = fmaxf(fmaxf(I.wf[0], I.wf[1]), I.wf[2]);
     I.margin = 1.0e-5f * (om + wmax) + 8.0e-5f * I.hcap + 1.0e-30f;
+    // list-frame r: each coordinate within two FP32 roundings of a value below
+    // c_max = max (nf w) + max |offset|, differences and r^2 rounded in FP32
+    // (<= 2^-23 r): the error of r stays below 1e-6 (c_max + 4 hcap)
+    const float cmax = fmaxf(fmaxf(I.wf[0] * I.nf[0], I.wf[1] * I.nf[1]), I.wf[2] * I.nf[2]) + om;
+    I.lmargin = 1.0e-6f * (cmax + 4.0f * I.hcap) + 1.0e-30f;
 }
 
 // Start of an on-device list rebuild: empty the extra lists of the impacts
@@ -630,13 +648,24 @@ static __global__ void k_round_check(ImpactD* imps, int nimp, int32_t* flags) {
     }
 }
 
+// Pair distance^2 of the list builders on non-periodic impacts, from the list
+// frame: IEEE differences are exactly antisymmetric, so both sides of a pair
+// get the same r^2 bit for bit and the own / reverse tests partition the pairs
+// exactly.  Periodic impacts use the cell-relative offsets (minimum image).
+__device__ __forceinline__ float list_r2(float4 a, float4 b) {
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+
 // One particle's list by its own traversal (periodic impacts, and warps that
 // straddle two impacts).
 template <class R>
 __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int64_t k) {
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
-    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const float4 li = v.lf[k];
+    const bool periodic = I.per[0] | I.per[1] | I.per[2];
+    const float m = (sizeof(R) == 8 ? I.margin : 0.0f) + I.lmargin;
     const float sl = 1.0f + I.slack;
     const float ri = 2.0f * pi.w * sl + m;
     const float ri2 = ri * ri;
@@ -644,20 +673,28 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
     const int cap = v.cap;
     int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
     traverse_sphere(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
-        const float4 pj = v.pf[j];
-        float dx = (pi.x - pj.x) + dxc;
-        float dy = (pi.y - pj.y) + dyc;
-        float dz = (pi.z - pj.z) + dzc;
-        if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
-        if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
-        if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
-        const float r2 = dx * dx + dy * dy + dz * dz;
+        float r2, hj;
+        if (!periodic) {
+            const float4 lj = v.lf[j];
+            r2 = list_r2(li, lj);
+            hj = lj.w;
+        } else {
+            const float4 pj = v.pf[j];
+            float dx = (pi.x - pj.x) + dxc;
+            float dy = (pi.y - pj.y) + dyc;
+            float dz = (pi.z - pj.z) + dzc;
+            if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
+            if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
+            if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
+            r2 = dx * dx + dy * dy + dz * dz;
+            hj = pj.w;
+        }
         if (r2 < ri2) {
             if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
             cnt++;
             // does j's own search miss k although the pair can interact?
-            const float rj = 2.0f * pj.w * sl + m;
-            const float rb = (pi.w + pj.w) * sl + m;
+            const float rj = 2.0f * hj * sl + m;
+            const float rb = (pi.w + hj) * sl + m;
             if (!(r2 < rj * rj) && r2 < rb * rb) {
                 const int slot = atomicAdd(&v.xcnt[j], 1);
                 if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
@@ -713,7 +750,8 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
     const bool act = inb;
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
-    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const float4 li = v.lf[k];
+    const float m = (sizeof(R) == 8 ? I.margin : 0.0f) + I.lmargin;
     const float sl = 1.0f + I.slack;
     const float ri = 2.0f * pi.w * sl + m;
     const float ri2 = ri * ri;
@@ -738,7 +776,6 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
         const float xa = (float)(ix - c[0]) * w0 - pi.x;
         float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
         if (ix == 0 || ix == nf0 - 1) bx = 0.0f;
-        const float dxc = (float)(c[0] - ix) * w0;
         const bool in_x = act && ix >= lo0 && ix <= hi0;
         for (int iy = ulo1; iy <= uhi1; iy++) {
             const float ya = (float)(iy - c[1]) * w1 - pi.y;
@@ -757,21 +794,16 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
                 len = v.cell_ptr[colbase + zh + 1] - s;
             }
             const int maxlen = __reduce_max_sync(full, len);
-            const float dyc = (float)(c[1] - iy) * w1;
             for (int t = 0; t < maxlen; t++) {
                 const bool ok = t < len;
                 const int32_t j = ok ? s + t : (int32_t)k;
-                const float4 pj = v.pf[j];
-                const float dzc = (float)(c[2] - (int)(v.cpk[j] >> 22)) * w2;
-                const float dx = (pi.x - pj.x) + dxc;
-                const float dy = (pi.y - pj.y) + dyc;
-                const float dz = (pi.z - pj.z) + dzc;
-                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float4 lj = v.lf[j];
+                const float r2 = list_r2(li, lj);
                 if (ok && r2 < ri2) {
                     if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
                     cnt++;
-                    const float rj = 2.0f * pj.w * sl + m;
-                    const float rb = (pi.w + pj.w) * sl + m;
+                    const float rj = 2.0f * lj.w * sl + m;
+                    const float rb = (pi.w + lj.w) * sl + m;
                     if (!(r2 < rj * rj) && r2 < rb * rb) {
                         const int slot = atomicAdd(&v.xcnt[j], 1);
                         if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
@@ -835,7 +867,8 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
         const int64_t k = t0 + (active ? lane : 0);
         const float4 pi = v.pf[k];
         const uint32_t ci = v.cpk[k];
-        const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+        const float4 li = v.lf[k];
+        const float m = (sizeof(R) == 8 ? I.margin : 0.0f) + I.lmargin;
         const float sl = 1.0f + I.slack;
         const float ri = 2.0f * pi.w * sl + m;
         const float ri2 = ri * ri;
@@ -880,7 +913,6 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
                 const float xa = (float)(ix - icx) * w0 - pi.x;
                 float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
                 if (ix == 0 || ix == I.nf[0] - 1) bx = 0.0f;
-                const float dxc = (float)(icx - ix) * w0;
                 for (int iy = loy; iy <= hiy; iy++) {
                     const float ya = (float)(iy - icy) * w1 - pi.y;
                     float by = ya > 0.0f ? ya : (ya + w1 < 0.0f ? -(ya + w1) : 0.0f);
@@ -900,25 +932,16 @@ static __global__ void __launch_bounds__(256) k_list_warp(View<R> v, const int32
                     int zl = (int)floorf(zlo / w2), zh = (int)floorf(zhi / w2);
                     zl = max(0, min(nf2 - 1, zl));
                     zh = max(0, min(nf2 - 1, zh));
-                    const float dyc = (float)(icy - iy) * w1;
                     const int64_t colbase = I.cell_base + ((int64_t)ix * I.nf[1] + iy) * nf2;
-                    int cz = zl;
                     const int32_t s = v.cell_ptr[colbase + zl];
                     const int32_t e = v.cell_ptr[colbase + zh + 1];
-                    int32_t next = v.cell_ptr[colbase + cz + 1];
                     for (int32_t j = s; j < e; j++) {
-                        while (j >= next) {
-                            cz++;
-                            next = v.cell_ptr[colbase + cz + 1];
-                        }
-                        const float4 pj = v.pf[j];
-                        const float dzc = (float)(icz - cz) * w2;
-                        const float dx = (pi.x - pj.x) + dxc, dy = (pi.y - pj.y) + dyc, dz = (pi.z - pj.z) + dzc;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float4 lj = v.lf[j];
+                        const float r2 = list_r2(li, lj);
                         if (active && r2 < ri2) {
                             if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
                             cnt++;
-                            const float rj = 2.0f * pj.w * sl + m, rb = (pi.w + pj.w) * sl + m;
+                            const float rj = 2.0f * lj.w * sl + m, rb = (pi.w + lj.w) * sl + m;
                             if (!(r2 < rj * rj) && r2 < rb * rb) {
                                 const int slot = atomicAdd(&v.xcnt[j], 1);
                                 if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
@@ -955,7 +978,8 @@ static __global__ void __launch_bounds__(256) k_list_wpp(View<R> v) {
     if (!I.mask) return;
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
-    const float m = sizeof(R) == 8 ? I.margin : 0.0f;
+    const float4 li = v.lf[k];
+    const float m = (sizeof(R) == 8 ? I.margin : 0.0f) + I.lmargin;
     const float sl = 1.0f + I.slack;
     const float ri = 2.0f * pi.w * sl + m;
     const float ri2 = ri * ri;
@@ -1039,18 +1063,26 @@ static __global__ void __launch_bounds__(256) k_list_wpp(View<R> v) {
             if (!__any_sync(0xffffffffu, have)) break;
             bool hit = false;
             if (have) {
-                const float4 pj = v.pf[j];
-                float dx = (pi.x - pj.x) + dxc;
-                float dy = (pi.y - pj.y) + dyc;
-                float dz = (pi.z - pj.z) + dzc;
-                if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
-                if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
-                if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
-                const float r2 = dx * dx + dy * dy + dz * dz;
+                float r2, hj;
+                if (sphere) {
+                    const float4 lj = v.lf[j];
+                    r2 = list_r2(li, lj);
+                    hj = lj.w;
+                } else {
+                    const float4 pj = v.pf[j];
+                    float dx = (pi.x - pj.x) + dxc;
+                    float dy = (pi.y - pj.y) + dyc;
+                    float dz = (pi.z - pj.z) + dzc;
+                    if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
+                    if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
+                    if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
+                    r2 = dx * dx + dy * dy + dz * dz;
+                    hj = pj.w;
+                }
                 hit = r2 < ri2;
                 if (hit) {
-                    const float rj = 2.0f * pj.w * sl + m;
-                    const float rb = (pi.w + pj.w) * sl + m;
+                    const float rj = 2.0f * hj * sl + m;
+                    const float rb = (pi.w + hj) * sl + m;
                     if (!(r2 < rj * rj) && r2 < rb * rb) {
                         const int slot = atomicAdd(&v.xcnt[j], 1);
                         if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
@@ -1213,6 +1245,7 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
     v.rho_lo[k] = rho_lo;
     v.hh[k] = hi;
     v.pf[k].w = (float)hi;
+    v.lf[k].w = (float)hi;
     impact_atomic_max(&I.hm_bits, (double)hi);  // the round's new max h
     if (!((float)hi <= v.hlist[k] * (1.0f + I.slack) * 0.99999f)) {
         atomicOr(&I.slack_flag, 1);
