@@ -175,11 +175,21 @@ __device__ __forceinline__ int sat_int(double q) {
 // the reciprocal (one multiply instead of a division, which is slow in FP64);
 // it is within 2 ulp of the IEEE quotient, so the truncations agree unless an
 // integer lies within a few ulp of it -- then the division decides.
+//
+// Cheaper still: the quotient in FP32 is within 4e-7 |q| of the exact one, so
+// when it lies farther than 1e-6 (|q| + 1) from every integer its truncation is
+// the exact bin; only the rest take the FP64 route.
 __device__ __forceinline__ int ref_bin(const ImpactD& I, int a, double c) {
     const double d = __dsub_rn(c, I.dlo[a]);
-    double q = __dmul_rn(d, I.icw[a]);
-    if (fabs(q - rint(q)) <= fabs(q) * 0x1p-49 + 0x1p-1000) q = __ddiv_rn(d, I.cw[a]);
-    int i = sat_int(q);
+    int i;
+    const float qf = (float)d * (float)I.icw[a];
+    if (fabsf(qf) < 1.0e6f && fabsf(qf - rintf(qf)) > 1.0e-6f * (fabsf(qf) + 1.0f)) {
+        i = (int)qf;
+    } else {
+        double q = __dmul_rn(d, I.icw[a]);
+        if (fabs(q - rint(q)) <= fabs(q) * 0x1p-49 + 0x1p-1000) q = __ddiv_rn(d, I.cw[a]);
+        i = sat_int(q);
+    }
     if (i < 0) i = 0;
     if (i >= I.nc[a]) i = I.nc[a] - 1;
     return i;
