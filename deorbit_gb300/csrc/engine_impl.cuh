@@ -1391,6 +1391,7 @@ public:
         }
         for (int a = 0; a < 3; a++) {
             I.iw[a] = 1.0 / I.w[a];
+            I.iwf[a] = (float)I.iw[a];
             I.wf[a] = (float)I.w[a];
             I.Lf[a] = (float)(h.dhi[a] - h.dlo[a]);
         }

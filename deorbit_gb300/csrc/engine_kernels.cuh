@@ -43,7 +43,7 @@ struct ImpactD {
     int32_t per[3], active;                        // active: density round still running
     // traversal grid (fixed while the impact is resident)
     double glo[3], w[3], iw[3];
-    float wf[3], Lf[3];
+    float wf[3], Lf[3], iwf[3];
     int32_t nf[3], alive;
     int64_t cell_base, ncells;
     // reference grid of the last build (sph.hpp:147-157)
@@ -428,13 +428,17 @@ static __global__ void k_kick_drift(View<R> v) {
     v.z[k] += vz * dt;
 }
 
-__device__ __forceinline__ int fine_cell(const ImpactD& I, int a, double c, double& frac) {
-    double q = (c - I.glo[a]) * I.iw[a];
-    double fl = floor(q);
-    int i = sat_int(fl);
+// Traversal cell along axis a and the FP32 offset from its origin.  The cell
+// may be chosen from the FP32 quotient (any cell works as long as the offset is
+// taken from that cell's origin); the offset itself is one FP64 fused
+// multiply-add, rounded once to FP32.
+__device__ __forceinline__ int fine_cell(const ImpactD& I, int a, double c, float& off) {
+    const double d = c - I.glo[a];
+    const float qf = (float)d * I.iwf[a];
+    int i = qf >= 2147483520.0f ? 2147483647 : (qf == qf ? (int)floorf(qf) : 0);
     if (i < 0) i = 0;
     if (i >= I.nf[a]) i = I.nf[a] - 1;
-    frac = q - (double)i;  // offset in cells from the (clamped) cell origin
+    off = (float)fma(-(double)i, I.w[a], d);
     return i;
 }
 
@@ -449,14 +453,13 @@ static __global__ void k_fine_keys(View<R> v, uint32_t* keys_by_gid, int32_t* ce
     if (k >= v.n) return;
     ImpactD& I = v.imps[v.imp[k]];
     if (!I.alive) return;  // leaves the arrays at this sort (key stays invalid)
-    double fx, fy, fz;
-    const int cx = fine_cell(I, 0, v.x[k], fx);
-    const int cy = fine_cell(I, 1, v.y[k], fy);
-    const int cz = fine_cell(I, 2, v.z[k], fz);
+    float ox, oy, oz;
+    const int cx = fine_cell(I, 0, v.x[k], ox);
+    const int cy = fine_cell(I, 1, v.y[k], oy);
+    const int cz = fine_cell(I, 2, v.z[k], oz);
     const int64_t key = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2] + cz;
     keys_by_gid[v.gid[k]] = (uint32_t)key;
     atomicAdd(&cell_count[key], 1);
-    const float ox = (float)(fx * I.w[0]), oy = (float)(fy * I.w[1]), oz = (float)(fz * I.w[2]);
     pf_out[k] = make_float4(ox, oy, oz, (float)v.hh[k]);
     cpk_out[k] = (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22);
     impact_atomic_max_u32(&I.omax_bits, __float_as_uint(fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz))));
