@@ -163,6 +163,41 @@ __device__ __forceinline__ void impact_atomic_max_u32(unsigned int* addr, unsign
     }
 }
 
+// Block-wide combine before a per-impact atomic on ordered bits: when every
+// thread of the block targets the same address, the block's extreme leaves as
+// one atomic (a kernel-wide reduction then issues one atomic per block, not per
+// warp); otherwise each thread with a value issues its own.  Every thread of
+// the block must call it.
+template <bool MAX>
+__device__ __forceinline__ void block_atomic_ext(unsigned long long* addr, unsigned long long b, bool has) {
+    __shared__ unsigned long long part[32];
+    __shared__ unsigned long long* first;
+    const unsigned long long none = MAX ? 0ull : ~0ull;
+    if (!has) b = none;
+    if (threadIdx.x == 0) first = addr;
+    __syncthreads();
+    const bool same = __syncthreads_and(addr == first);
+    if (!same) {
+        if (has) { if (MAX) atomicMax(addr, b); else atomicMin(addr, b); }
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+        b = MAX ? (x > b ? x : b) : (x < b ? x : b);
+    }
+    if (lane == 0) part[warp] = b;
+    __syncthreads();
+    if (warp == 0) {
+        b = lane < (int)((blockDim.x + 31) >> 5) ? part[lane] : none;
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+            b = MAX ? (x > b ? x : b) : (x < b ? x : b);
+        }
+        if (lane == 0 && b != none) { if (MAX) atomicMax(addr, b); else atomicMin(addr, b); }
+    }
+}
+
 __device__ __forceinline__ int sat_int(double q) {
     if (q != q) return 0;
     if (q >= 2147483647.0) return 2147483647;
@@ -591,11 +626,12 @@ static __global__ void k_impact_begin_round(ImpactD* imps, int nimp, int set_act
 
 template <class R>
 static __global__ void k_hmax(View<R> v, int which) {
-    int64_t k = gtid();
-    if (k >= v.n) return;
+    const int64_t k0 = gtid();
+    const bool inb = k0 < v.n;
+    const int64_t k = inb ? k0 : v.n - 1;
     ImpactD& I = v.imps[v.imp[k]];
-    if (!(I.mask && I.active)) return;
-    impact_atomic_max(which == 0 ? &I.hmax_bits : &I.hm_bits, (double)v.hh[k]);
+    const bool has = inb && I.mask && I.active;
+    block_atomic_ext<true>(which == 0 ? &I.hmax_bits : &I.hm_bits, dbits((double)v.hh[k]), has);
 }
 
 // Reference grid of an impact (sph.hpp:147-157): h_max -> nc, cw.
@@ -1634,14 +1670,26 @@ static __global__ void k_dt_begin(ImpactD* imps, int nimp) {
 }
 
 // CFL step (sph.hpp:350-355): per-impact min of cfl h / (csig (1 + alpha) + 1e-30).
+// The FP64 quotient is formed only where it can be the minimum: an FP32
+// estimate (within 3e-7 of it) is reduced over the warp first, and only lanes
+// within 1e-5 of the warp's smallest estimate -- which include the lane of the
+// exact minimum -- divide in FP64 (warps that straddle two impacts: all lanes).
 template <class R>
 static __global__ void k_dt(View<R> v) {
-    int64_t k = gtid();
-    if (k >= v.n) return;
-    ImpactD& I = v.imps[v.imp[k]];
-    if (!I.mask) return;
-    double d = I.cfl * (double)v.hh[k] / ((double)v.csig[k] * (1.0 + I.alpha) + 1e-30);
-    impact_atomic_min(&I.dt_bits, d);
+    const unsigned full = 0xffffffffu;
+    const int64_t k0 = gtid();
+    const bool inb = k0 < v.n;
+    const int64_t k = inb ? k0 : v.n - 1;
+    const int ib = v.imp[k];
+    ImpactD& I = v.imps[ib];
+    const bool live = inb && I.mask;
+    const float qf = live ? (float)v.hh[k] / ((float)v.csig[k] * (1.0f + (float)I.alpha) + 1e-30f) : INFINITY;
+    const bool uniform = __all_sync(full, ib == __shfl_sync(full, ib, 0));
+    const float qmin = __uint_as_float(__reduce_min_sync(full, __float_as_uint(qf)));  // qf >= 0
+    const bool cand = live && (!uniform || !(qf > qmin * (1.0f + 1.0e-5f)));
+    double d = 0.0;
+    if (cand) d = I.cfl * (double)v.hh[k] / ((double)v.csig[k] * (1.0 + I.alpha) + 1e-30);
+    block_atomic_ext<false>(&I.dt_bits, dbits(d), cand);
 }
 
 // Device-side step control for batched runs: dt = min(CFL dt, t_end - t);
