@@ -168,11 +168,11 @@ __device__ __forceinline__ void impact_atomic_max_u32(unsigned int* addr, unsign
 // one atomic (a kernel-wide reduction then issues one atomic per block, not per
 // warp); otherwise each thread with a value issues its own.  Every thread of
 // the block must call it.
-template <bool MAX>
-__device__ __forceinline__ void block_atomic_ext(unsigned long long* addr, unsigned long long b, bool has) {
-    __shared__ unsigned long long part[32];
-    __shared__ unsigned long long* first;
-    const unsigned long long none = MAX ? 0ull : ~0ull;
+template <bool MAX, class U>
+__device__ __forceinline__ void block_atomic_ext(U* addr, U b, bool has) {
+    __shared__ U part[32];
+    __shared__ U* first;
+    const U none = MAX ? U(0) : ~U(0);
     if (!has) b = none;
     if (threadIdx.x == 0) first = addr;
     __syncthreads();
@@ -183,7 +183,7 @@ __device__ __forceinline__ void block_atomic_ext(unsigned long long* addr, unsig
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+        const U x = __shfl_xor_sync(0xffffffffu, b, o);
         b = MAX ? (x > b ? x : b) : (x < b ? x : b);
     }
     if (lane == 0) part[warp] = b;
@@ -191,7 +191,7 @@ __device__ __forceinline__ void block_atomic_ext(unsigned long long* addr, unsig
     if (warp == 0) {
         b = lane < (int)((blockDim.x + 31) >> 5) ? part[lane] : none;
         for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+            const U x = __shfl_xor_sync(0xffffffffu, b, o);
             b = MAX ? (x > b ? x : b) : (x < b ? x : b);
         }
         if (lane == 0 && b != none) { if (MAX) atomicMax(addr, b); else atomicMin(addr, b); }
@@ -477,17 +477,12 @@ __device__ __forceinline__ int fine_cell(const ImpactD& I, int a, double c, floa
     return i;
 }
 
-// Traversal-cell key of every resident particle, scattered into gid order,
-// per-cell counts, and (in the current order, for the gather to carry) the
-// FP32 offset from the cell origin with h, the packed cell coordinates and the
-// per-impact largest |offset|.
+// One particle's key, counts, offsets and packed cell; returns the bits of its
+// largest |offset| (ordered as the non-negative floats).
 template <class R>
-static __global__ void k_fine_keys(View<R> v, uint32_t* keys_by_gid, int32_t* cell_count, float4* pf_out,
-                                   uint32_t* cpk_out) {
-    int64_t k = gtid();
-    if (k >= v.n) return;
-    ImpactD& I = v.imps[v.imp[k]];
-    if (!I.alive) return;  // leaves the arrays at this sort (key stays invalid)
+__device__ __forceinline__ unsigned int fine_keys_one(const View<R>& v, const ImpactD& I, int64_t k,
+                                                      uint32_t* keys_by_gid, int32_t* cell_count, float4* pf_out,
+                                                      uint32_t* cpk_out) {
     float ox, oy, oz;
     const int cx = fine_cell(I, 0, v.x[k], ox);
     const int cy = fine_cell(I, 1, v.y[k], oy);
@@ -497,7 +492,24 @@ static __global__ void k_fine_keys(View<R> v, uint32_t* keys_by_gid, int32_t* ce
     atomicAdd(&cell_count[key], 1);
     pf_out[k] = make_float4(ox, oy, oz, (float)v.hh[k]);
     cpk_out[k] = (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22);
-    impact_atomic_max_u32(&I.omax_bits, __float_as_uint(fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz))));
+    return __float_as_uint(fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz)));
+}
+
+// Traversal-cell key of every resident particle, scattered into gid order,
+// per-cell counts, and (in the current order, for the gather to carry) the
+// FP32 offset from the cell origin with h, the packed cell coordinates and the
+// per-impact largest |offset|.
+template <class R>
+static __global__ void k_fine_keys(View<R> v, uint32_t* keys_by_gid, int32_t* cell_count, float4* pf_out,
+                                   uint32_t* cpk_out) {
+    const int64_t k0 = gtid();
+    const bool inb = k0 < v.n;
+    const int64_t k = inb ? k0 : v.n - 1;
+    ImpactD& I = v.imps[v.imp[k]];
+    const bool live = inb && I.alive;  // a dead impact's particles leave at this sort (key stays invalid)
+    unsigned int om = 0u;
+    if (live) om = fine_keys_one(v, I, k, keys_by_gid, cell_count, pf_out, cpk_out);
+    block_atomic_ext<true>(&I.omax_bits, om, live);
 }
 
 static __global__ void k_make_src(int64_t n, const int32_t* sorted_gid, const int32_t* pos_of_gid,
