@@ -702,12 +702,15 @@ public:
                 cur_ = p ^ 1;  // the step's gather moved the carried state
                 s = 1;
             }
-            if (s + 1 < nsteps) {
-                cudaGraphExec_t ge = ensure_graph(kGraphTwo);
-                for (; s + 1 < nsteps; s += 2) {
-                    DSPH_CUDA(cudaGraphLaunch(ge, st_));
-                    launches_ += graph_launches_[kGraphTwo][cur_];
+            // every 16 steps the list-overflow flag is read back, so a grown
+            // neighbour count costs at most 16 steps of the consumers' fallback
+            for (int since = 0; s + 1 < nsteps; s += 2) {
+                if (++since > 8) {
+                    grow_lists_after_overflow();
+                    since = 1;
                 }
+                DSPH_CUDA(cudaGraphLaunch(ensure_graph(kGraphTwo), st_));
+                launches_ += graph_launches_[kGraphTwo][cur_];
             }
             grow_lists_after_overflow();
         }
