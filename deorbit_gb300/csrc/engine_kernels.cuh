@@ -564,8 +564,8 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
                               (float)(c >> 22) * I.wf[2] + p.z, p.w);
 }
 
-// After the gather: inverse permutation, traversal-cell coordinates and FP32
-// offsets from the cell origin, largest |offset| per impact.
+// After the gather: inverse permutation (gid -> sorted position) and, in the
+// mixed form, the (mass, packed cell) records of the density gathers.
 template <class R>
 static __global__ void k_post_sort(View<R> v, int32_t* pos_of_gid) {
     int64_t k = gtid();
@@ -774,9 +774,10 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
 //   extra list of j: k itself, when j's own search misses k (r >= 2 h_j (1 + s))
 //              but the pair can interact (r < (h_j + h_k)(1 + s)); such a k is
 //              always inside k's own sphere, so every force pair is found once.
-// The FP32 pair distance is computed bit-symmetrically from either side, so the
-// two tests partition the pairs exactly; the FP64 form adds its margin m to
-// both radii.  Extra lists are appended with atomics and sorted afterwards, so
+// The FP32 pair distance comes from the list frame (list_r2) and is the same
+// bit for bit from either side, so the two tests partition the pairs exactly;
+// every radius carries the frame's rounding bound, and the FP64 form adds its
+// margin m as well.  Extra lists are appended with atomics and sorted afterwards, so
 // list contents and order depend only on the state.  Consumers apply the exact
 // criteria, the reference-stencil restriction, and fall back to a traversal
 // for a particle whose h outgrew the slack or whose list overflowed.
@@ -786,10 +787,10 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
 // warp walks the union of its lanes' column boxes in a fixed order; each lane
 // takes the columns of its own box that meet its sphere, over the z-range of
 // its own chord, and the candidate loop runs to the longest chord of the warp
-// with the other lanes predicated off.  A candidate's z-cell comes from its
-// packed cell word instead of a walk over the cell boundaries.  Every lane
-// visits the same candidates in the same order as traverse_sphere(), so the
-// lists equal those of a per-thread traversal entry for entry.
+// with the other lanes predicated off; a candidate costs one 16-byte load of
+// its list-frame record.  Every lane visits the same candidates in the same
+// order as traverse_sphere(), so the lists equal those of a per-thread
+// traversal entry for entry.
 //
 // refresh != 0: rebuild only the lists of impacts whose h outgrew the slack in
 // this step's density rounds (the others return at once).
