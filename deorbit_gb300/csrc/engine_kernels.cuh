@@ -856,21 +856,26 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
                 len = v.cell_ptr[colbase + zh + 1] - s;
             }
             const int maxlen = __reduce_max_sync(full, len);
-            for (int t = 0; t < maxlen; t++) {
-                const bool ok = t < len;
-                const int32_t j = ok ? s + t : (int32_t)k;
-                const float4 lj = v.lf[j];
-                const float r2 = list_r2(li, lj);
-                if (ok && r2 < ri2) {
-                    if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
-                    cnt++;
-                    const float rj = 2.0f * lj.w * sl + m;
-                    const float rb = (pi.w + lj.w) * sl + m;
-                    if (!(r2 < rj * rj) && r2 < rb * rb) {
-                        const int slot = atomicAdd(&v.xcnt[j], 1);
-                        if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
-                    }
+            auto take = [&](int32_t j, float4 lj, float r2) {
+                if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
+                cnt++;
+                const float rj = 2.0f * lj.w * sl + m;
+                const float rb = (pi.w + lj.w) * sl + m;
+                if (!(r2 < rj * rj) && r2 < rb * rb) {
+                    const int slot = atomicAdd(&v.xcnt[j], 1);
+                    if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
                 }
+            };
+            // two candidates per trip: independent load / distance chains,
+            // appended in candidate order (four per trip was slower: the
+            // chords are short and the tail trips run mostly predicated off)
+            for (int t = 0; t < maxlen; t += 2) {
+                const bool ok0 = t < len, ok1 = t + 1 < len;
+                const int32_t j0 = ok0 ? s + t : (int32_t)k, j1 = ok1 ? s + t + 1 : (int32_t)k;
+                const float4 l0 = v.lf[j0], l1 = v.lf[j1];
+                const float r20 = list_r2(li, l0), r21 = list_r2(li, l1);
+                if (ok0 && r20 < ri2) take(j0, l0, r20);
+                if (ok1 && r21 < ri2) take(j1, l1, r21);
             }
         }
     }
