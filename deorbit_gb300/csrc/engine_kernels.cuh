@@ -441,6 +441,23 @@ __device__ __forceinline__ void walk_list(const int32_t* nbr, int64_t ls, int64_
     }
 }
 
+// walk_list with the entries handed over two at a time where a block allows
+// (f2(j0, j1) must apply them in that order; f1 takes a lone entry).
+template <class F1, class F2>
+__device__ __forceinline__ void walk_list_pairs(const int32_t* nbr, int64_t ls, int64_t k, int cnt, F1&& f1,
+                                                F2&& f2) {
+    const int4* p = reinterpret_cast<const int4*>(nbr) + k;
+    int4 q = cnt > 0 ? *p : make_int4(0, 0, 0, 0);
+    for (int t = 0; t < cnt; t += 4) {
+        p += ls;
+        const int4 qn = t + 4 < cnt ? *p : q;
+        const int m = min(4, cnt - t);
+        if (m >= 2) f2(q.x, q.y); else f1(q.x);
+        if (m == 4) f2(q.z, q.w); else if (m == 3) f1(q.z);
+        q = qn;
+    }
+}
+
 // ---------------------------------------------------------------- kernels
 
 // Kick (half step with the old acceleration) and drift (sph.hpp:360-361).
@@ -1273,8 +1290,19 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
         AccT<R> sum;
         sum.init();
         const float th2 = (2.0f * (float)hi + m) * (2.0f * (float)hi + m);
+        // mixed form: one entry's m_j W(r, h_i) from its offset record and (mass, cell)
+        auto w_mixed = [&](int32_t j, float4 pj, float2 mk) -> float {
+            float dx, dy, dz;
+            sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            // the kernel vanishes at q >= 2; only the stencil restriction needs a test
+            const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;  // hardware 1/sqrt (2 ulp)
+            float w = mk.x * kernel_W_bf<float>(r, (float)ihi);
+            if (need_member && !ref_member(bi, v.refbin[j], I)) w = 0.0f;
+            return w;
+        };
         auto body = [&](int32_t j) {
-            if (sizeof(R) == 8) {
+            if constexpr (sizeof(R) == 8) {
                 float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
                 sep_f32(I, pi, ci, v.pf[j], v.cpk[j], fx, fy, fz);
                 if (!(fx * fx + fy * fy + fz * fz < th2)) return;
@@ -1284,21 +1312,23 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(
                 if (need_member && !ref_member(bi, v.refbin[j], I)) return;
                 sum.add(v.mass[j] * kernel_W_ih<R>((R)rr, ihi));
             } else {
-                const float4 pj = v.pf[j];
-                const float2 mk = v.pk[j];
-                float dx, dy, dz;
-                sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                // the kernel vanishes at q >= 2; only the stencil restriction needs a test
-                const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;  // hardware 1/sqrt (2 ulp)
-                float w = mk.x * kernel_W_bf<float>(r, (float)ihi);
-                if (need_member && !ref_member(bi, v.refbin[j], I)) w = 0.0f;
-                sum.add((R)w);
+                sum.add((R)w_mixed(j, v.pf[j], v.pk[j]));
             }
         };
         if (list_covers(v, I, k, (float)hi)) {
             const int cnt = v.nbr_cnt[k];
-            walk_list(v.nbr, v.ls, k, cnt, body);
+            if constexpr (sizeof(R) == 4) {
+                // two entries per trip: both loads in flight, summed in list order
+                walk_list_pairs(v.nbr, v.ls, k, cnt, body, [&](int32_t j0, int32_t j1) {
+                    const float4 p0 = v.pf[j0], p1 = v.pf[j1];
+                    const float2 m0 = v.pk[j0], m1 = v.pk[j1];
+                    const float w0 = w_mixed(j0, p0, m0), w1 = w_mixed(j1, p1, m1);
+                    sum.add((R)w0);
+                    sum.add((R)w1);
+                });
+            } else {
+                walk_list(v.nbr, v.ls, k, cnt, body);
+            }
         } else {
             const float hf = (float)hi;
             traverse(v, I, pi, ci, 2.0f * hf * 1.0001f + 2.0f * I.margin + 1e-6f * hf,
