@@ -28,6 +28,9 @@ GRADED_CELL_FACTORS = (1.5, 2.0, 3.0, 4.0)
 # (cell factor, z cell factor) pairs also tried there: flatter cells shorten the
 # column chords of the list build at the price of more cells to sort
 GRADED_FLAT_CELLS = ((3.0, 0.5), (4.0, 0.5), (3.0, 0.33))
+# (cell factor, z cell factor) pairs also tried with the per-thread builder on
+# uniform lattices: slightly flatter cells shorten the chords of the list build
+FLAT_CELLS = ((1.0, 0.75), (0.85, 0.75), (1.0, 0.6))
 SLACKS = (0.03, 0.06)
 BLOCKS = (128, 256)
 LIST_MODES = (2, 1, 0)
@@ -121,6 +124,8 @@ def tune(sc, precision, device=0, steps=3, warmup=2, candidates=None, force=Fals
         candidates = [dict(list_mode=lm, slack=sl, cell_factor=f, block=b)
                       for lm, sl, f, b in itertools.product(LIST_MODES, SLACKS, CELL_FACTORS, BLOCKS)
                       if not (lm == 1 and b != 128)]
+        candidates += [dict(list_mode=0, slack=sl, cell_factor=f, cell_factor_z=fz, block=b)
+                       for sl, (f, fz), b in itertools.product(SLACKS, FLAT_CELLS, BLOCKS)]
     table = []
     for cfg in candidates:
         t0 = time.perf_counter()
