@@ -119,8 +119,8 @@ __device__ __forceinline__ double bitsd(unsigned long long b) {
     return __longlong_as_double((long long)b);
 }
 
-// Per-impact atomic max / min on the bit pattern of a non-negative double (bit
-// order equals value order there).  A full warp whose lanes all target the same
+// Per-impact atomic max on the bit pattern of a non-negative double (bit order
+// equals value order there).  A full warp whose lanes all target the same
 // impact combines in registers first and issues one atomic.
 __device__ __forceinline__ bool warp_same_target(const void* addr) {
     unsigned act = __activemask();
@@ -135,28 +135,6 @@ __device__ __forceinline__ void impact_atomic_max(unsigned long long* addr, doub
             unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
             b = x > b ? x : b;
         }
-        if ((threadIdx.x & 31) == 0) atomicMax(addr, b);
-    } else {
-        atomicMax(addr, b);
-    }
-}
-
-__device__ __forceinline__ void impact_atomic_min(unsigned long long* addr, double v) {
-    unsigned long long b = dbits(v);
-    if (warp_same_target(addr)) {
-        for (int o = 16; o > 0; o >>= 1) {
-            unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
-            b = x < b ? x : b;
-        }
-        if ((threadIdx.x & 31) == 0) atomicMin(addr, b);
-    } else {
-        atomicMin(addr, b);
-    }
-}
-
-__device__ __forceinline__ void impact_atomic_max_u32(unsigned int* addr, unsigned int b) {
-    if (warp_same_target(addr)) {
-        b = __reduce_max_sync(0xffffffffu, b);
         if ((threadIdx.x & 31) == 0) atomicMax(addr, b);
     } else {
         atomicMax(addr, b);
