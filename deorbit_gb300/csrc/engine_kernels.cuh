@@ -816,10 +816,15 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
     const float R2 = Rs * Rs;
     int c[3];
     unpack_cell(ci, c[0], c[1], c[2]);
-    const float w0 = I.wf[0], w1 = I.wf[1], w2 = I.wf[2];
+    const float w0 = I.wf[0], w1 = I.wf[1];
+    const float iw0 = I.iwf[0], iw1 = I.iwf[1], iw2 = I.iwf[2];
     const int nf0 = I.nf[0], nf1 = I.nf[1], nf2 = I.nf[2];
-    int lo0 = c[0] + (int)floorf((pi.x - Rs) / w0), hi0 = c[0] + (int)floorf((pi.x + Rs) / w0);
-    int lo1 = c[1] + (int)floorf((pi.y - Rs) / w1), hi1 = c[1] + (int)floorf((pi.y + Rs) / w1);
+    // cell ranges by reciprocal multiplies, widened by 1e-5 cell (far above
+    // their rounding): a range may gain a cell whose candidates all fail the
+    // distance test, never lose one
+    constexpr float kWiden = 1.0e-5f;
+    int lo0 = c[0] + (int)floorf((pi.x - Rs) * iw0 - kWiden), hi0 = c[0] + (int)floorf((pi.x + Rs) * iw0 + kWiden);
+    int lo1 = c[1] + (int)floorf((pi.y - Rs) * iw1 - kWiden), hi1 = c[1] + (int)floorf((pi.y + Rs) * iw1 + kWiden);
     lo0 = lo0 < 0 ? 0 : (lo0 > nf0 - 1 ? nf0 - 1 : lo0);
     hi0 = hi0 < 0 ? 0 : (hi0 > nf0 - 1 ? nf0 - 1 : hi0);
     lo1 = lo1 < 0 ? 0 : (lo1 > nf1 - 1 ? nf1 - 1 : lo1);
@@ -841,9 +846,10 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
             const float d2 = bx * bx + by * by;
             int32_t s = 0, len = 0;
             if (in_x && iy >= lo1 && iy <= hi1 && d2 < R2) {
-                const float hz = sqrtf(R2 - d2);
-                int zl = c[2] + (int)floorf((pi.z - hz) / w2);
-                int zh = c[2] + (int)floorf((pi.z + hz) / w2);
+                const float q = R2 - d2;
+                const float hz = q * rsqrtf(q) * (1.0f + 1.0e-6f);  // hardware 1/sqrt (2 ulp), widened
+                int zl = c[2] + (int)floorf((pi.z - hz) * iw2 - kWiden);
+                int zh = c[2] + (int)floorf((pi.z + hz) * iw2 + kWiden);
                 zl = zl < 0 ? 0 : (zl > nf2 - 1 ? nf2 - 1 : zl);
                 zh = zh < 0 ? 0 : (zh > nf2 - 1 ? nf2 - 1 : zh);
                 const int64_t colbase = I.cell_base + ((int64_t)ix * nf1 + iy) * nf2;
