@@ -50,9 +50,10 @@ class Request:
 
 class Server:
     def __init__(self, precision=sph.MIXED, device=0, hbm_budget_bytes=160e9, chunk=4,
-                 fields=RESULT_FIELDS, bytes_per_particle=None):
+                 fields=RESULT_FIELDS, bytes_per_particle=None, ctx=None):
         self.precision = precision
-        self.ctx = sph.Context(precision, device)
+        # ctx: an engine context to serve from (default: a new one on `device`)
+        self.ctx = ctx if ctx is not None else sph.Context(precision, device)
         self.budget = float(hbm_budget_bytes)
         self.bpp = bytes_per_particle or BYTES_PER_PARTICLE[precision]
         self.chunk = int(chunk)
