@@ -447,15 +447,17 @@ static __global__ void k_kick_drift(View<R> v) {
     if (!I.mask || v.fixed[k]) return;
     const double dt = I.dt;
     const double hd = 0.5 * dt;
-    double vx = v.vx[k] + (double)v.ax[k] * hd;
-    double vy = v.vy[k] + (double)v.ay[k] * hd;
-    double vz = v.vz[k] + (double)v.az[k] * hd;
+    // all loads before the stores (the columns may alias as far as the compiler knows)
+    const double x = v.x[k], y = v.y[k], z = v.z[k];
+    const double vx = v.vx[k] + (double)v.ax[k] * hd;
+    const double vy = v.vy[k] + (double)v.ay[k] * hd;
+    const double vz = v.vz[k] + (double)v.az[k] * hd;
     v.vx[k] = vx;
     v.vy[k] = vy;
     v.vz[k] = vz;
-    v.x[k] += vx * dt;
-    v.y[k] += vy * dt;
-    v.z[k] += vz * dt;
+    v.x[k] = x + vx * dt;
+    v.y[k] = y + vy * dt;
+    v.z[k] = z + vz * dt;
 }
 
 // Traversal cell along axis a and the FP32 offset from its origin.  The cell
@@ -540,16 +542,29 @@ static __global__ void k_gather(int64_t n, const int32_t* src, GatherCols g) {
     int64_t k = gtid();
     if (k >= n) return;
     int64_t s = src[k];
+    // every load first, then every store: the column pointers may alias as far
+    // as the compiler knows, so interleaved copies would wait for each load in turn
+    double dv[7];
+    R rv[24];
 #pragma unroll
-    for (int c = 0; c < 7; c++) g.dout[c][k] = g.din[c][s];
-    for (int c = 0; c < g.nr; c++) static_cast<R*>(g.rout[c])[k] = static_cast<const R*>(g.rin[c])[s];
-    g.b_out[0][k] = g.b_in[0][s];
-    g.b_out[1][k] = g.b_in[1][s];
+    for (int c = 0; c < 7; c++) dv[c] = g.din[c][s];
+#pragma unroll
+    for (int c = 0; c < 24; c++)
+        if (c < g.nr) rv[c] = static_cast<const R*>(g.rin[c])[s];
+    const uint8_t b0 = g.b_in[0][s], b1 = g.b_in[1][s];
     const uint16_t ib = g.imp_in[s];
-    g.imp_out[k] = ib;
-    g.gid_out[k] = g.gid_in[s];
+    const int32_t gid = g.gid_in[s];
     const float4 p = g.pf_in[s];
     const uint32_t c = g.cpk_in[s];
+#pragma unroll
+    for (int q = 0; q < 7; q++) g.dout[q][k] = dv[q];
+#pragma unroll
+    for (int q = 0; q < 24; q++)
+        if (q < g.nr) static_cast<R*>(g.rout[q])[k] = rv[q];
+    g.b_out[0][k] = b0;
+    g.b_out[1][k] = b1;
+    g.imp_out[k] = ib;
+    g.gid_out[k] = gid;
     g.pf_out[k] = p;
     g.cpk_out[k] = c;
     // one FP32 coordinate per particle (all its pairs use the same value):
@@ -1343,38 +1358,57 @@ static __global__ void k_eos(View<R> v) {
     const ImpactD& I = v.imps[v.imp[k]];
     if (!I.mask) return;
     const MatT<R> m = v.mats[v.mat[k]];
+    // all loads before the stores (the columns may alias as far as the compiler knows)
     const R rho = v.rho[k];
     const R u = (R)v.u[k];
+    const R rho_lo = v.rho_lo[k];
+    const R mass = v.mass[k];
+    R S[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) S[c] = v.S[c][k];
+    const R D = I.damage_on ? v.D[k] : R(0);
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    float4 pfk = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t cpk = 0;
+    if (sizeof(R) == 4) {
+        vx = v.vx[k]; vy = v.vy[k]; vz = v.vz[k];
+        pfk = v.pf[k];
+        cpk = v.cpk[k];
+    }
     R P, cs;
-    eos_P_cs(m, rho, u, P, cs, v.rho_lo[k]);
-    v.P[k] = P;
-    v.cs[k] = cs;
-    v.csig[k] = rsqrt_(cs * cs + (R(4) / R(3)) * m.G / rmax(rho, R(1e-30)));
+    eos_P_cs(m, rho, u, P, cs, rho_lo);
+    const R csig = rsqrt_(cs * cs + (R(4) / R(3)) * m.G / rmax(rho, R(1e-30)));
     R pf = P, dsc = R(1);
+    R sigmax = R(0);
     if (I.damage_on) {
-        v.sigmax[k] = -P + eig_max(v.S[0][k], v.S[1][k], v.S[2][k], v.S[3][k], v.S[4][k], v.S[5][k]);
-        dsc = R(1) - v.D[k];
+        sigmax = -P + eig_max(S[0], S[1], S[2], S[3], S[4], S[5]);
+        dsc = R(1) - D;
         if (P < R(0)) pf = dsc * P;
     }
+    const R irho2 = R(1) / (rho * rho);
+    const R Rart = (I.eps_as > 0 && pf < R(0)) ? (R)I.eps_as * (-pf) * irho2 : R(0);
+    const R pfr2 = pf * irho2, dsr2 = irho2 * dsc, vol = mass / rho;
+    v.P[k] = P;
+    v.cs[k] = cs;
+    v.csig[k] = csig;
+    if (I.damage_on) v.sigmax[k] = sigmax;
     v.Pf[k] = pf;
     v.dscale[k] = dsc;
-    const R irho2 = R(1) / (rho * rho);
-    v.Rart[k] = (I.eps_as > 0 && pf < R(0)) ? (R)I.eps_as * (-pf) * irho2 : R(0);
-    v.pfr2[k] = pf * irho2;
-    v.dsr2[k] = irho2 * dsc;
-    v.vol[k] = v.mass[k] / rho;
+    v.Rart[k] = Rart;
+    v.pfr2[k] = pfr2;
+    v.dsr2[k] = dsr2;
+    v.vol[k] = vol;
     if (sizeof(R) == 4) {
         float4* o = v.fr + 6 * k;
-        const double vx = v.vx[k], vy = v.vy[k], vz = v.vz[k];
         const float hx = (float)vx, hy = (float)vy, hz = (float)vz;
-        o[0] = v.pf[k];
+        o[0] = pfk;
         // .w lanes carry the mass and packed cell of the particle
-        o[1] = make_float4(hx, hy, hz, (float)v.mass[k]);
+        o[1] = make_float4(hx, hy, hz, (float)mass);
         o[2] = make_float4((float)(vx - (double)hx), (float)(vy - (double)hy), (float)(vz - (double)hz),
-                           __uint_as_float(v.cpk[k]));
-        o[3] = make_float4((float)v.vol[k], (float)rho, (float)v.csig[k], (float)v.pfr2[k]);
-        o[4] = make_float4((float)v.dsr2[k], (float)v.Rart[k], (float)v.S[4][k], (float)v.S[5][k]);
-        o[5] = make_float4((float)v.S[0][k], (float)v.S[1][k], (float)v.S[2][k], (float)v.S[3][k]);
+                           __uint_as_float(cpk));
+        o[3] = make_float4((float)vol, (float)rho, (float)csig, (float)pfr2);
+        o[4] = make_float4((float)dsr2, (float)Rart, (float)S[4], (float)S[5]);
+        o[5] = make_float4((float)S[0], (float)S[1], (float)S[2], (float)S[3]);
     }
 }
 
@@ -1652,17 +1686,22 @@ static __global__ void k_finish(View<R> v) {
     if (!v.fixed[k]) {
         const double dt = I.dt;
         const R hd = (R)(0.5 * dt);
-        v.vx[k] += (double)v.ax[k] * (0.5 * dt);
-        v.vy[k] += (double)v.ay[k] * (0.5 * dt);
-        v.vz[k] += (double)v.az[k] * (0.5 * dt);
+        // all loads before the stores (the columns may alias as far as the compiler knows)
+        const double vx = v.vx[k] + (double)v.ax[k] * (0.5 * dt);
+        const double vy = v.vy[k] + (double)v.ay[k] * (0.5 * dt);
+        const double vz = v.vz[k] + (double)v.az[k] * (0.5 * dt);
         double u = v.u[k] + (0.5 * dt) * ((double)v.dudt[k] + (double)dn);
-        if (u < 1e-12) u = 1e-12;
-        v.u[k] = u;
         R s[6];
 #pragma unroll
         for (int c = 0; c < 6; c++) s[c] = v.S[c][k] + hd * (v.dS[c][k] + dsn[c]);
+        const R Pk = v.P[k], Dk = v.D[k];
         const MatT<R>& m = v.mats[v.mat[k]];
-        const R Y = yield_stress(m, v.P[k], v.D[k]);
+        v.vx[k] = vx;
+        v.vy[k] = vy;
+        v.vz[k] = vz;
+        if (u < 1e-12) u = 1e-12;
+        v.u[k] = u;
+        const R Y = yield_stress(m, Pk, Dk);
         if (Y <= R(0)) {
 #pragma unroll
             for (int c = 0; c < 6; c++) s[c] = R(0);
