@@ -480,14 +480,16 @@ template <class R>
 __device__ __forceinline__ unsigned int fine_keys_one(const View<R>& v, const ImpactD& I, int64_t k,
                                                       uint32_t* keys_by_gid, int32_t* cell_count, float4* pf_out,
                                                       uint32_t* cpk_out) {
+    const float h = (float)v.hh[k];  // loaded before the stores below
+    const int32_t gid = v.gid[k];
     float ox, oy, oz;
     const int cx = fine_cell(I, 0, v.x[k], ox);
     const int cy = fine_cell(I, 1, v.y[k], oy);
     const int cz = fine_cell(I, 2, v.z[k], oz);
     const int64_t key = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2] + cz;
-    keys_by_gid[v.gid[k]] = (uint32_t)key;
+    keys_by_gid[gid] = (uint32_t)key;
     atomicAdd(&cell_count[key], 1);
-    pf_out[k] = make_float4(ox, oy, oz, (float)v.hh[k]);
+    pf_out[k] = make_float4(ox, oy, oz, h);
     cpk_out[k] = (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22);
     return __float_as_uint(fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz)));
 }
