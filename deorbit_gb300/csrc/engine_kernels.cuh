@@ -1272,7 +1272,7 @@ __device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, 
 // own h and the neighbours' positions and masses, so running the iterations
 // back to back per particle gives the same result as one launch per iteration.
 template <class R>
-static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_density(View<R> v, int iters) {
+static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_density(View<R> v, int iters) {
     int64_t k = gtid();
     if (k >= v.n) return;
     ImpactD& I = v.imps[v.imp[k]];
