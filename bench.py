@@ -250,7 +250,9 @@ def e2e_rate(sph, ctx, b, n, steps, warmup):
 
 
 def cpu_rate(ic, sc, steps, threads=0):
-    S = ic.to_oracle(sc, threads=threads)
+    from oracle import oracle as O
+
+    S = O.from_scenario(sc, threads=threads)
     S.init()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -365,7 +367,9 @@ def halfspace_section(sph, ic, device, steps=200):
     gpu = ctx.read_many(b, names)
     ctx.close()
     threads = min(os.cpu_count() or 1, 16)
-    S = ic.to_oracle(sc, threads=threads)
+    from oracle import oracle as O
+
+    S = O.from_scenario(sc, threads=threads)
     S.init()
     t0 = time.perf_counter()
     for dt in dts:   # the GPU run's dt sequence (equal to the oracle's to 1e-9)
@@ -435,9 +439,10 @@ def main():
         # tree is not on this machine); rank 0 only
         if rank != 0:
             return
-        from oracle import oracle  # noqa: F401
+        from oracle import oracle as O
+
         sample = ic.crop(sc, sample_n)
-        S = ic.to_oracle(sample, threads=min(os.cpu_count() or 1, 16))
+        S = O.from_scenario(sample, threads=min(os.cpu_count() or 1, 16))
         S.init()
         for _ in range(args.warmup):
             S.step(S.timestep())

@@ -214,6 +214,28 @@ int sph_seed_flaws_multi_host(int64_t n, const int32_t* mat, const sph_material*
     });
 }
 
+namespace {
+// Makes `dev` current for the enclosing scope and restores the thread's
+// previous current device when the scope ends.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+        cudaGetLastError();
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+}  // namespace
+
 int sph_create(sph_ctx** out, int precision, int device) {
     return guard([&] {
         need(out, "out");
@@ -225,6 +247,7 @@ int sph_create(sph_ctx** out, int precision, int device) {
             throw SphError(SPH_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
         }
         if (device < 0 || device >= ndev) throw SphError(SPH_ERR_ARG, "bad device ordinal");
+        DeviceGuard dg(device);
         auto c = std::make_unique<sph_ctx>();
         c->device = device;
         if (precision == SPH_FP64) c->eng = dsph::make_engine_fp64(device);
@@ -237,12 +260,15 @@ int sph_create(sph_ctx** out, int precision, int device) {
 int sph_destroy(sph_ctx* ctx) {
     return guard([&] {
         if (!ctx) return;
-        cudaSetDevice(ctx->device);
+        DeviceGuard dg(ctx->device);
         delete ctx;
     });
 }
 
-#define CTX_SET() cudaSetDevice(ctx ? ctx->device : 0)
+// Every call on a context runs with the context's device current and gives
+// the calling thread its previous current device back on return (also on
+// errors), so mixing contexts and caller-owned buffers on other devices is safe.
+#define CTX_SET() DeviceGuard dsph_device_guard_(ctx ? ctx->device : 0)
 
 int sph_add_material(sph_ctx* ctx, const sph_material* m, int32_t* id) {
     return guard([&] {
@@ -521,6 +547,16 @@ int sph_debug_neighbors(sph_ctx* ctx, int32_t impact, int32_t kind, int32_t* cou
         if (kind != SPH_NBR_DENSITY && kind != SPH_NBR_FORCE) throw SphError(SPH_ERR_ARG, "bad kind");
         CTX_SET();
         int64_t t = E(ctx).debug_neighbors(impact, kind, counts, ids, cap);
+        if (total) *total = t;
+    });
+}
+
+int sph_debug_flaws(sph_ctx* ctx, int32_t impact, int64_t* ptr, double* eps, int64_t cap,
+                    int64_t* total) {
+    return guard([&] {
+        need(ptr, "ptr");
+        CTX_SET();
+        int64_t t = E(ctx).debug_flaws(impact, ptr, eps, cap);
         if (total) *total = t;
     });
 }

@@ -40,13 +40,13 @@ namespace dsph {
 
 // Scratch layout shared by both entry points: keys_out, keys_tmp, vals_tmp
 // (n each), the radix / scan scratch, one flag word.
-size_t cell_sort_scratch_bytes(int64_t n, int64_t ncells) {
-    size_t a = 256;
-    auto up = [a](size_t x) { return (x + a - 1) / a * a; };
-    size_t b = 3 * up(sizeof(uint32_t) * (size_t)(n > 0 ? n : 1));
-    size_t s1 = radix_scratch_bytes(n > 0 ? n : 1), s2 = scan_scratch_bytes(ncells + 1);
-    b += up(s1 > s2 ? s1 : s2) + a;
-    return b;
+constexpr size_t round_up_256(size_t x) { return (x + 255) / 256 * 256; }
+constexpr size_t cell_sort_scratch_bytes(int64_t n, int64_t ncells) {
+    return 3 * round_up_256(sizeof(uint32_t) * (size_t)(n > 0 ? n : 1)) +
+           round_up_256(radix_scratch_bytes(n > 0 ? n : 1) > scan_scratch_bytes(ncells + 1)
+                            ? radix_scratch_bytes(n > 0 ? n : 1)
+                            : scan_scratch_bytes(ncells + 1)) +
+           256;
 }
 
 // Runs the sort with caller-provided scratch; returns SPH_* status.
@@ -127,6 +127,9 @@ namespace {
 constexpr int64_t kStaticMaxKeys = 1 << 18;    // 262,144 keys per call
 constexpr int64_t kStaticMaxCells = 1 << 24;   // 16,777,216 cells per call
 constexpr size_t kStaticScratchBytes = 3670016;
+// the largest accepted call must fit the array (the layout grows with both sizes)
+static_assert(dsph::cell_sort_scratch_bytes(kStaticMaxKeys, kStaticMaxCells) <= kStaticScratchBytes,
+              "static cell-sort scratch too small for its documented limits");
 
 __device__ __align__(256) unsigned char g_cell_sort_scratch[kStaticScratchBytes];
 
@@ -136,7 +139,9 @@ void* g_static_addr[256] = {};
 // Device address of the scratch array on the current device.  The host-side
 // name g_cell_sort_scratch is only a stand-in for the symbol, not a device
 // address, so the address is looked up once per device (with that device
-// current) and cached.
+// current) and cached.  The cache assumes one context per device for the life
+// of the process (the runtime's primary context): after cudaDeviceReset, or
+// under another driver-API context, the cached address is stale.
 int static_scratch(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -178,9 +183,18 @@ extern "C" int sph_cell_sort_static(const uint32_t* keys, int64_t n, int64_t nce
         dsph::set_error_message("sph_cell_sort_static: null pointer");
         return SPH_ERR_ARG;
     }
-    if (dsph::cell_sort_scratch_bytes(n, ncells) > kStaticScratchBytes) {
-        dsph::set_error_message("sph_cell_sort_static: scratch layout exceeds the static array");
-        return SPH_ERR_CAPACITY;
+    // every call waits for its result on the host, which a stream being
+    // captured into a graph cannot do: refuse before touching the stream
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess) {
+        cudaGetLastError();
+        dsph::set_error_message("sph_cell_sort_static: invalid stream");
+        return SPH_ERR_ARG;
+    }
+    if (cap != cudaStreamCaptureStatusNone) {
+        dsph::set_error_message("sph_cell_sort_static: the stream is being captured; the call "
+                                "synchronizes and cannot be captured");
+        return SPH_ERR_STATE;
     }
     void* scratch = nullptr;
     int rc = static_scratch(&scratch);

@@ -81,6 +81,7 @@ public:
                                  int64_t start_len, int32_t* ids) = 0;
     virtual int64_t debug_neighbors(int b, int kind, int32_t* counts, int32_t* ids,
                                     int64_t cap) = 0;
+    virtual int64_t debug_flaws(int b, int64_t* ptr, double* eps, int64_t cap) = 0;
     virtual void set_tuning(int block, double cell_factor) = 0;
     virtual void set_option(const char* key, double value) = 0;
     virtual double get_option(const char* key) = 0;

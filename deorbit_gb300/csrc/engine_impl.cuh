@@ -83,9 +83,11 @@ static __global__ void k_ref_keys(View<R> v, int b, const int32_t* pos_of_gid, i
     atomicAdd(&counts[c], 1);
 }
 
-// Exact neighbour sets (FP64 criteria) for the parity hook.
+// Exact neighbour sets (FP64 criteria) for the parity hook: with offs null
+// only the counts, else the set of sorted position idx at out[offs[idx]...].
 template <class R>
-static __global__ void k_debug_nbr(View<R> v, int b, int kind, int32_t* out, int32_t* cnt_out, int cap) {
+static __global__ void k_debug_nbr(View<R> v, int b, int kind, int32_t* out, int32_t* cnt_out,
+                                   const int64_t* offs) {
     int64_t idx = gtid();
     const ImpactD& I = v.imps[b];
     if (idx >= I.n) return;
@@ -109,11 +111,11 @@ static __global__ void k_debug_nbr(View<R> v, int b, int kind, int32_t* out, int
             take = !(j == (int32_t)k || r >= hsum || r == 0.0);
         }
         if (take) {
-            if (cnt < cap) out[idx * (int64_t)cap + cnt] = v.gid[j] - (int32_t)I.gid_base;
+            if (offs) out[offs[idx] + cnt] = v.gid[j] - (int32_t)I.gid_base;
             cnt++;
         }
     });
-    cnt_out[idx] = cnt;
+    if (!offs) cnt_out[idx] = cnt;
 }
 
 // Compensated FP64 conservation sums of one impact, fixed summation order.
@@ -993,36 +995,75 @@ public:
         pull_table();
         const ImpactD& I = tab_[b];
         int64_t n = I.n;
-        const int pcap = 512;
-        int32_t* out = dalloc_tmp<int32_t>(n * pcap + 1);
+        // pass 1: set sizes per sorted position
         int32_t* cnt = dalloc_tmp<int32_t>(n + 1);
-        if (n > 0) launch_n_raw(k_debug_nbr<R>, n, view(), b, kind, out, cnt, pcap);
-        std::vector<int32_t> hout((size_t)n * pcap), hcnt(n);
+        if (n > 0) launch_n_raw(k_debug_nbr<R>, n, view(), b, kind, (int32_t*)nullptr, cnt, (const int64_t*)nullptr);
+        std::vector<int32_t> hcnt(n), gidv(n);  // gidv: local id of each sorted position
         if (n > 0) {
-            DSPH_CUDA(cudaMemcpyAsync(hout.data(), out, sizeof(int32_t) * n * pcap, cudaMemcpyDeviceToHost, st_));
             DSPH_CUDA(cudaMemcpyAsync(hcnt.data(), cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st_));
+            DSPH_CUDA(cudaMemcpyAsync(gidv.data(), gid_[cur_] + I.off, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st_));
         }
-        // local id of each sorted position in this impact
-        std::vector<int32_t> gidv(n);
-        if (n > 0) DSPH_CUDA(cudaMemcpyAsync(gidv.data(), gid_[cur_] + I.off, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st_));
         DSPH_CUDA(cudaStreamSynchronize(st_));
-        free_tmp();
         std::vector<int64_t> where(h.n, -1);
         for (int64_t q = 0; q < n; q++) where[gidv[q] - h.gid_base] = q;
         int64_t total = 0;
         for (int64_t l = 0; l < h.n; l++) {
-            int64_t q = where[l];
-            int c = q >= 0 ? hcnt[q] : 0;
-            if (c > pcap) throw SphError(SPH_ERR_CAPACITY, "debug neighbour set larger than 512");
-            counts[l] = c;
-            if (ids && total + c <= cap) {
-                int32_t* dst = ids + total;
-                std::copy(hout.begin() + q * pcap, hout.begin() + q * pcap + c, dst);
-                std::sort(dst, dst + c);
-            }
-            total += c;
+            counts[l] = where[l] >= 0 ? hcnt[where[l]] : 0;
+            total += counts[l];
         }
-        if (total > cap && ids) throw SphError(SPH_ERR_CAPACITY, "neighbour id buffer too small");
+        if (!ids || total > cap) {
+            free_tmp();
+            if (ids) throw SphError(SPH_ERR_CAPACITY, "neighbour id buffer too small");
+            return total;
+        }
+        // pass 2: each set written at its place in the caller's (original) order
+        std::vector<int64_t> offs(std::max<int64_t>(n, 1));
+        {
+            int64_t o = 0;
+            for (int64_t l = 0; l < h.n; l++) {
+                if (where[l] >= 0) offs[where[l]] = o;
+                o += counts[l];
+            }
+        }
+        int64_t* offs_d = dalloc_tmp<int64_t>(std::max<int64_t>(n, 1));
+        int32_t* out = dalloc_tmp<int32_t>(total + 1);
+        if (n > 0) {
+            DSPH_CUDA(cudaMemcpyAsync(offs_d, offs.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st_));
+            launch_n_raw(k_debug_nbr<R>, n, view(), b, kind, out, cnt, (const int64_t*)offs_d);
+            if (total > 0) DSPH_CUDA(cudaMemcpyAsync(ids, out, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st_));
+        }
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        free_tmp();
+        int64_t o = 0;
+        for (int64_t l = 0; l < h.n; l++) {
+            std::sort(ids + o, ids + o + counts[l]);
+            o += counts[l];
+        }
+        return total;
+    }
+
+    // Multi-flaw CSR of one impact as the device holds it (original particle
+    // order; activation strains in the engine's precision, widened to double).
+    int64_t debug_flaws(int b, int64_t* ptr, double* eps, int64_t cap) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (!(h.multi && flaw_ptr_d_)) {
+            for (int64_t l = 0; l <= h.n; l++) ptr[l] = 0;
+            return 0;
+        }
+        std::vector<int64_t> dptr(h.n + 1);
+        DSPH_CUDA(cudaMemcpyAsync(dptr.data(), flaw_ptr_d_ + h.gid_base, sizeof(int64_t) * (h.n + 1),
+                                  cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        const int64_t base = dptr[0], total = dptr[h.n] - base;
+        for (int64_t l = 0; l <= h.n; l++) ptr[l] = dptr[l] - base;
+        if (eps && total > cap) throw SphError(SPH_ERR_CAPACITY, "flaw buffer too small");
+        if (eps && total > 0) {
+            std::vector<R> e(total);
+            DSPH_CUDA(cudaMemcpyAsync(e.data(), flaw_eps_d_ + base, sizeof(R) * total, cudaMemcpyDeviceToHost, st_));
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+            for (int64_t q = 0; q < total; q++) eps[q] = (double)e[q];
+        }
         return total;
     }
 

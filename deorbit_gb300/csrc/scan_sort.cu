@@ -153,15 +153,9 @@ __global__ void k_digit_scatter(const uint32_t* keys_in, const int32_t* vals_in,
     }
 }
 
-inline int64_t tiles_of(int64_t n) { return (n + kTile - 1) / kTile; }
+
 
 }  // namespace
-
-size_t scan_scratch_bytes(int64_t n) { return sizeof(int32_t) * (size_t)(tiles_of(n) + 1); }
-
-size_t radix_scratch_bytes(int64_t n) {
-    return sizeof(int32_t) * (size_t)(256 * tiles_of(n) + tiles_of(256 * tiles_of(n)) + 2);
-}
 
 int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch,
                        cudaStream_t st) {

@@ -12,9 +12,13 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kTile = kScanThreads * kScanItems;  // 2048
 
-// Scratch sizes (bytes) for the launchers below.
-size_t scan_scratch_bytes(int64_t n);
-size_t radix_scratch_bytes(int64_t n);
+// Scratch sizes (bytes) for the launchers below (constexpr, so fixed-size
+// scratch arrays can be checked against them at compile time).
+constexpr int64_t tiles_of(int64_t n) { return (n + kTile - 1) / kTile; }
+constexpr size_t scan_scratch_bytes(int64_t n) { return sizeof(int32_t) * (size_t)(tiles_of(n) + 1); }
+constexpr size_t radix_scratch_bytes(int64_t n) {
+    return sizeof(int32_t) * (size_t)(256 * tiles_of(n) + tiles_of(256 * tiles_of(n)) + 2);
+}
 
 // out[i] = sum_{k<i} in[i]; out may alias in.  n <= 2^31 - 1.
 // Returns the number of kernel launches issued.

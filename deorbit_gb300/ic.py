@@ -134,9 +134,10 @@ def impact_halfspace(nx=48, ny=48, nz=24, dx=10.0, r_cells=8.0, angle_deg=45.0, 
 
 
 def grazing(n_total=1 << 20, radius=500.0, dx=None, angle_deg=3.0, speed=8000.0, jitter=0.01,
-            aspect=(8.0, 4.0, 1.0), seed=20261203, flaws="multi", eps_as=0.3, cfl=0.2):
+            aspect=(8.0, 4.0, 1.0), seed=20261203, flaws="multi", eps_as=0.3, cfl=0.2, gap=1.0):
     """Strength + damage grazing impact: iron sphere (von Mises, 1 GPa) into a
-    granite slab (Collins yield, multi-flaw Weibull), exactly n_total particles."""
+    granite slab (Collins yield, multi-flaw Weibull), exactly n_total particles.
+    The sphere's lowest point starts `gap` lattice spacings above the surface."""
     rng = np.random.default_rng(seed)
     if dx is None:  # slab of aspect ax:ay:az (in sphere diameters) holding n_total
         vol = (n_total * 1.0) / 1.0
@@ -160,7 +161,7 @@ def grazing(n_total=1 << 20, radius=500.0, dx=None, angle_deg=3.0, speed=8000.0,
     slab = slab[keep]
     th = math.radians(angle_deg)
     x0 = 0.15 * nx * dx
-    cen = np.array([x0, 0.0, R + dx])
+    cen = np.array([x0, 0.0, R + gap * dx])
     imp = imp + cen
     slab = _jitter(slab, dx, jitter, rng)
     imp = _jitter(imp, dx, jitter, rng)
@@ -407,30 +408,6 @@ def to_context(ctx, sc: Scenario, prm_overrides=None, material_ids=None):
     if sc.h0 is not None:
         ctx.set_h0(b, sc.h0)
     return b
-
-
-def to_oracle(sc: Scenario, threads=0):
-    """The same scenario in the CPU oracle (test infrastructure)."""
-    from oracle import oracle as O
-
-    S = O.OracleSystem()
-    if threads:
-        S.set_threads(threads)
-    for d in sc.materials:
-        S.add_material(_material_struct(O.Material, d))
-    p = dict(sc.params)
-    S.set_params(**p)
-    S.set_domain(sc.lo, sc.hi, tuple(bool(x) for x in sc.periodic))
-    S.add_many(sc.pos, sc.vel, sc.mass, sc.u, sc.mat, sc.fixed)
-    if sc.flaws is not None:
-        kind, seed = sc.flaws
-        if kind == "multi":
-            S.seed_flaws_multi(sc.dx, seed)
-        else:
-            S.seed_damage(sc.dx, seed)
-    if sc.h0 is not None:
-        S.set_h0(sc.h0)
-    return S
 
 
 def write_ic(sc: Scenario, path):

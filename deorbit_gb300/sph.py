@@ -124,6 +124,7 @@ _SIGS = {
     "sph_eos_eval": (C.c_int, [_P, C.c_int32, C.c_int64, _D, _D, _D, _D]),
     "sph_debug_ref_cells": (C.c_int, [_P, C.c_int32, _I32, _D, _I32, C.c_int64, _I32]),
     "sph_debug_neighbors": (C.c_int, [_P, C.c_int32, C.c_int32, _I32, _I32, C.c_int64, _I64]),
+    "sph_debug_flaws": (C.c_int, [_P, C.c_int32, _I64, _D, C.c_int64, _I64]),
     "sph_load_ic": (C.c_int, [_P, C.c_char_p, C.POINTER(Params), _I32]),
     "sph_write_snapshot": (C.c_int, [_P, C.c_int32, C.c_char_p]),
     "sph_write_checkpoint": (C.c_int, [_P, C.c_int32, C.c_char_p, C.c_double]),
@@ -483,6 +484,17 @@ class Context:
         check(lib().sph_debug_neighbors(self.h, b, kind, _ip(counts), _ip(ids), ids.size,
                                         total.ctypes.data_as(_I64)))
         return counts, ids[: int(total[0])]
+
+    def flaws(self, b):
+        """Device multi-flaw CSR of impact b: (ptr[n+1], eps[total])."""
+        n = self.n(b)
+        ptr = np.zeros(n + 1, np.int64)
+        total = np.zeros(1, np.int64)
+        check(lib().sph_debug_flaws(self.h, b, ptr.ctypes.data_as(_I64), None, 0, total.ctypes.data_as(_I64)))
+        eps = np.zeros(max(int(total[0]), 1))
+        check(lib().sph_debug_flaws(self.h, b, ptr.ctypes.data_as(_I64), _dp(eps), eps.size,
+                                    total.ctypes.data_as(_I64)))
+        return ptr, eps[: int(total[0])]
 
     def load_ic(self, path, prm: Params) -> int:
         b = C.c_int32()

@@ -123,7 +123,9 @@ int sph_seed_flaws_multi_host(int64_t n, const int32_t* mat, const sph_material*
                               int64_t cap, int64_t* total, double* eps_act);
 
 /* ---- context -------------------------------------------------------------- */
-/* Replaces constructing a `System` (sph.hpp:72).  device: CUDA ordinal. */
+/* Replaces constructing a `System` (sph.hpp:72).  device: CUDA ordinal.  Every
+ * call on a context makes the context's device current while it runs and
+ * restores the calling thread's previous current device before returning. */
 int sph_create(sph_ctx** out, int precision, int device);
 int sph_destroy(sph_ctx* ctx);
 /* Replaces `materials.push_back(...)` (sph.hpp:82); materials are shared by all
@@ -238,6 +240,12 @@ int sph_debug_ref_cells(sph_ctx* ctx, int32_t impact, int32_t nc[3], double cw[3
  * SPH_ERR_CAPACITY when cap is too small. */
 int sph_debug_neighbors(sph_ctx* ctx, int32_t impact, int32_t kind, int32_t* counts,
                         int32_t* ids, int64_t cap, int64_t* total);
+/* Multi-flaw activation strains as the device holds them (extension; the
+ * counterpart of the seeded flaw arrays): ptr[n+1] CSR in original particle
+ * order, eps[cap] (NULL: sizes only; the engine's precision, widened to
+ * double), *total the flaw count.  All-zero ptr for single-flaw impacts. */
+int sph_debug_flaws(sph_ctx* ctx, int32_t impact, int64_t* ptr, double* eps, int64_t cap,
+                    int64_t* total);
 
 /* ---- primitives on caller-owned device memory ------------------------------
  * Stable radix cell sort (the cell-list build of sph.hpp:147-162 as a
@@ -259,9 +267,12 @@ int sph_cell_sort(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm
  * loading it reserves until the process exits.  Limits: n <= 262144 keys and
  * ncells <= 16777216 per call (SPH_ERR_CAPACITY beyond).  The first call on a
  * device looks up the array's device address (once per device, with that
- * device current); make that first call before any stream capture.  All calls
- * share the one array, so calls that overlap on the GPU (other streams or
- * threads) race; serialize them.  Returns when the result is complete. */
+ * device current, cached for the life of the process: the runtime's primary
+ * context is assumed, so the address is not valid after cudaDeviceReset).
+ * Every call waits for its result on the host, so it cannot be captured into a
+ * CUDA graph: on a stream under capture it returns SPH_ERR_STATE without
+ * touching the stream.  All calls share the one array, so calls that overlap
+ * on the GPU (other streams or threads) race; serialize them. */
 int sph_cell_sort_static(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm,
                          int32_t* cell_start, void* stream);
 

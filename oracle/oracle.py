@@ -48,10 +48,18 @@ class Params(C.Structure):
         ("as_n", C.c_int32), ("damage_on", C.c_int32), ("flaw_model", C.c_int32), ("pad_", C.c_int32)]
 
 
-def build(ref: bool = False) -> None:
-    """Compile liborc.so (and the reference shim when asked and available)."""
-    targets = ["all"] + (["ref"] if ref else [])
+def build(ref=False) -> None:
+    """Compile liborc.so; ref=True also the reference shim (the reference tree
+    must be present), ref="auto" the shim only where the tree is present."""
+    targets = ["all"] + (["ref-auto"] if ref == "auto" else ["ref"] if ref else [])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+def reference_dir() -> str:
+    """Root of the reference checkout used by the fixture generators
+    (DEORBIT_REFERENCE, default as in oracle/Makefile)."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "refdir"], check=True, capture_output=True, text=True)
+    return r.stdout.strip()
 
 
 _lib = None
@@ -413,3 +421,34 @@ class RefSystem(_Base):
     def set_fixed(self, fixed):
         f = np.ascontiguousarray(fixed, dtype=np.uint8)
         ref_lib().ref_set_fixed(self.h, f.ctypes.data_as(_U8))
+
+
+def material_from_dict(d) -> Material:
+    """orc_material from a material dict with the fields of Material."""
+    m = Material()
+    for name, _ in Material._fields_:
+        setattr(m, name, int(d[name]) if name in ("type", "yield_model") else float(d[name]))
+    return m
+
+
+def from_scenario(sc, threads=0, cls=None):
+    """The oracle system of a workload scenario (deorbit_gb300.ic.Scenario):
+    same materials, parameters, domain, particles, flaws and per-particle h0 as
+    the CUDA solver is given."""
+    S = (cls or OracleSystem)()
+    if threads:
+        S.set_threads(threads)
+    for d in sc.materials:
+        S.add_material(material_from_dict(d))
+    S.set_params(**dict(sc.params))
+    S.set_domain(sc.lo, sc.hi, tuple(bool(x) for x in sc.periodic))
+    S.add_many(sc.pos, sc.vel, sc.mass, sc.u, sc.mat, sc.fixed)
+    if sc.flaws is not None:
+        kind, seed = sc.flaws
+        if kind == "multi":
+            S.seed_flaws_multi(sc.dx, seed)
+        else:
+            S.seed_damage(sc.dx, seed)
+    if sc.h0 is not None:
+        S.set_h0(sc.h0)
+    return S

@@ -1,8 +1,8 @@
 """Generate the golden vectors under tests/golden/ from the REFERENCE solver.
 
 Runs the reference's own System (hydrocodes/sph/sph.hpp) and EOS
-(hydrocodes/common/eos.hpp), compiled unmodified from /root/reference by
-oracle/Makefile into oracle/_ref/libsphref.so, on seeded inputs and stores
+(hydrocodes/common/eos.hpp), compiled unmodified from the reference checkout
+(DEORBIT_REFERENCE) by oracle/Makefile into oracle/_ref/libsphref.so, on seeded inputs and stores
 inputs and outputs as compressed .npz.  Needs the reference tree; the fixtures
 it writes are committed so that the tests never need it.
 

@@ -1,7 +1,7 @@
 """Golden ICs of the campaign's grazing-impact builder, from the REFERENCE.
 
 Calls the reference's own `build_grazing_ic` (src/deorbit/impact/boundary_daemon.py,
-imported from /root/reference) on small configurations and stores, per case, the
+imported from the reference checkout, DEORBIT_REFERENCE) on small configurations and stores, per case, the
 arguments, the returned (dx, N), the 7-double header and the SHA-256 of the particle
 records (N x 10 float64, the file's body), plus every 97th record.  Needs the reference
 tree; the fixture it writes (grazing_ic.json) is committed so the tests never need it.
@@ -19,7 +19,6 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = "/root/reference/src"
 
 # (theta_deg, v, cppr, D, x_impact_frac, start_h): small lattices (the slab is at least
 # 20 x 4 x 6 km, so resolution comes from a coarse dx = D / (2 cppr))
@@ -31,7 +30,10 @@ CASES = [
 
 
 def main():
-    sys.path.insert(0, REF_SRC)
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), ""))
+    from oracle import oracle as O
+
+    sys.path.insert(0, os.path.join(O.reference_dir(), "src"))
     from deorbit.impact import boundary_daemon as bd  # the reference builder
 
     out = {"source": "boundary_daemon.build_grazing_ic (reference)", "sph": {k: bd.SPH[k] for k in

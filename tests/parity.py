@@ -4,6 +4,7 @@ from __future__ import annotations
 import numpy as np
 
 from deorbit_gb300 import ic
+from oracle import oracle as O
 
 STATE = ["x", "y", "z", "vx", "vy", "vz", "u", "rho", "hh", "P", "cs", "csig",
          "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz", "D"]
@@ -40,7 +41,7 @@ def pair(sc, precision):
 
     ctx = sph.Context(precision)
     b = ic.to_context(ctx, sc)
-    orc = ic.to_oracle(sc)
+    orc = O.from_scenario(sc)
     return ctx, b, orc
 
 

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from deorbit_gb300 import ic
+from oracle import oracle as O
 
 from parity import rel_l2
 
@@ -58,7 +59,7 @@ def test_frac_run_matches_oracle(cuda_lib, oracle_lib, tmp_path):
 
     # the oracle with the driver's stepping: CFL dt, last step clipped at
     # t_end, a snapshot at the first step reaching each snapshot time
-    orc = ic.to_oracle(sc)
+    orc = O.from_scenario(sc)
     orc.init()
     t, next_snap, want, steps = 0.0, snap, [], 0
     names = ["x", "y", "z", "vx", "vy", "vz", "u", "rho", "hh"]

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from deorbit_gb300 import ic
+from oracle import oracle as O
 
 from facade import compile_driver
 from parity import rel_l2
@@ -32,7 +33,7 @@ def test_facade_driver_matches_oracle(cuda_lib, oracle_lib, tmp_path, mixed):
     n = int(raw[:1].view(np.int64)[0])
     rec = raw[1:].reshape(n, len(FIELDS))
     gpu = {k: rec[:, i] for i, k in enumerate(FIELDS)}
-    orc = ic.to_oracle(ic.sheared_cube(L=L))
+    orc = O.from_scenario(ic.sheared_cube(L=L))
     orc.init()
     for _ in range(steps):
         orc.step(orc.timestep())

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from deorbit_gb300 import ic
+from oracle import oracle as O
 
 from parity import field_errors, read_all
 
@@ -25,7 +26,7 @@ def run_pair(sc, steps, **opts):
     for k, val in opts.items():
         ctx.set_option(k, val)
     b = ic.to_context(ctx, sc)
-    orc = ic.to_oracle(sc, threads=min(os.cpu_count() or 1, 16))
+    orc = O.from_scenario(sc, threads=min(os.cpu_count() or 1, 16))
     ctx.init()
     orc.init()
     for _ in range(steps):

@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 from deorbit_gb300 import ic
+from oracle import oracle as O
 
 from parity import field_errors, read_all
 
@@ -152,7 +153,7 @@ def test_sod_fp64_matches_oracle(cuda_lib, oracle_lib):
     sc = ic.sod_tube()
     ctx = sph.Context(sph.FP64)
     b = ic.to_context(ctx, sc)
-    orc = ic.to_oracle(sc, threads=min(os.cpu_count() or 1, 16))
+    orc = O.from_scenario(sc, threads=min(os.cpu_count() or 1, 16))
     ctx.init()
     orc.init()
     for _ in range(40):

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from deorbit_gb300 import ic
+from oracle import oracle as O
 
 from parity import field_errors, read_all
 
@@ -27,7 +28,7 @@ def test_halfspace_200_steps_fp64(cuda_lib, oracle_lib):
     assert sc.n > 57000
     ctx = sph.Context(sph.FP64)
     b = ic.to_context(ctx, sc)
-    orc = ic.to_oracle(sc, threads=min(os.cpu_count() or 1, 16))
+    orc = O.from_scenario(sc, threads=min(os.cpu_count() or 1, 16))
     ctx.init()
     orc.init()
     c0 = ctx.conservation(b)
