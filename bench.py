@@ -15,9 +15,13 @@ e2e     the same metric through the C ABI with host buffers: every step
         writes the carried state from pinned host memory, steps, and reads it
         back (a drop-in caller that keeps System's vectors on the host).
 plain_fp64  the FP64 plain form on the same workload (the 4x comparison).
+accuracy_vs_oracle  both GPU forms against the FP64 CPU oracle on a bounded
+        sample of the workload (per-field rel-L2, pass / fail at 1e-4).
 cpu_baseline  the FP64 CPU oracle on host cores (reference thread cap of 16)
-        over a cropped sample of the same workload.
---impl reference  times that CPU oracle as the reference arm.
+        over the same workload (2 steps), with the precision-matched ratio
+        (plain FP64 GPU over CPU) beside the mixed one.
+--impl reference  times that CPU oracle as the reference arm on the same
+        workload (--cpu-sample N: a cropped sample instead).
 """
 from __future__ import annotations
 
@@ -66,8 +70,16 @@ ALG_BYTES = {
 # the entries processed; captures in profiles/): the numerator of the FP32
 # issue fraction beside the HBM one.
 FLOPS_PER_ENTRY = {"force": 169, "density": 34}
-# nominal FP32 peak: 152 SMs x 128 lanes x 2 flops x 2.07 GHz (no measured figure exists)
-FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+# FP32 lanes per SM of compute capability 10.x (sm_100 / sm_103): the FP32
+# issue peak is SMs x lanes x 2 flops (FMA) x the maximum SM clock, both read
+# from the device at run time
+FP32_LANES_PER_SM = 128
+
+
+def fp32_peak_tflops(device, sm_max_mhz):
+    import torch
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    return sms * FP32_LANES_PER_SM * 2 * sm_max_mhz * 1e6 / 1e12, sms
 # Compulsory state traffic of one particle-step, strength + damage, from the
 # engine's layout: (bytes per field, access) with access "rw" for carried state
 # read and written once, "r" read-only, "w" written once.  Positions,
@@ -214,6 +226,58 @@ def mixed_error(sph, ic, sc, steps, device):
         out[grp] = float(np.linalg.norm(a - r) / nr) if nr > 0 else float(np.linalg.norm(a - r))
     c64.close()
     c32.close()
+    return out
+
+
+ACC_FIELDS = (("pos", ["x", "y", "z"]), ("vel", ["vx", "vy", "vz"]), ("u", ["u"]), ("rho", ["rho"]),
+              ("P", ["P"]), ("S", ["Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"]), ("D", ["D"]))
+
+
+def _group_errors(get_a, get_r, mask=None):
+    out = {}
+    for grp, names in ACC_FIELDS:
+        a = np.concatenate([get_a(k) if mask is None else get_a(k)[mask] for k in names])
+        r = np.concatenate([get_r(k) if mask is None else get_r(k)[mask] for k in names])
+        nr = np.linalg.norm(r)
+        out[grp] = float(np.linalg.norm(a - r) / nr) if nr > 0 else float(np.linalg.norm(a - r))
+    return out
+
+
+def accuracy_vs_oracle(sph, ic, sc, steps, device, tol=1e-4):
+    """Both GPU forms against the FP64 CPU oracle on the same input (a bounded
+    sample of the workload) after `steps` steps on the oracle's dt sequence:
+    rel-L2 per field group, pass / fail against `tol`, and the particles whose
+    damage differs by a flaw activation taken one step apart ("flips"), with the
+    damage-switched fields over the particles without a flip."""
+    from oracle import oracle as O
+
+    S = O.from_scenario(sc, threads=min(os.cpu_count() or 1, 16))
+    S.init()
+    dts = []
+    for _ in range(steps):
+        dts.append(S.timestep())
+        S.step(dts[-1])
+    names = [k for _, ks in ACC_FIELDS for k in ks]
+    ref = {k: S.field(k) for k in names}
+    S.close()
+    out = {"sample": f"{sc.n} particles cropped around the impact point, {steps} steps on the oracle's dt "
+                     f"sequence", "tol": tol}
+    for prec, name in ((sph.FP64, "fp64"), (sph.MIXED, "mixed")):
+        ctx = sph.Context(prec, device)
+        b = ic.to_context(ctx, sc)
+        ctx.init()
+        for dt in dts:
+            ctx.step(dt)
+        got = {k: ctx.read(b, k) for k in names}
+        ctx.close()
+        errs = _group_errors(got.__getitem__, ref.__getitem__)
+        flip = np.abs(got["D"] - ref["D"]) > 1e-6
+        rec = {"rel_l2": errs, "pass": sorted(k for k, v in errs.items() if v <= tol),
+               "fail": sorted(k for k, v in errs.items() if not v <= tol), "damage_flips": int(flip.sum())}
+        if flip.any():
+            e2 = _group_errors(got.__getitem__, ref.__getitem__, mask=~flip)
+            rec["rel_l2_without_flips"] = {"S": e2["S"], "D": e2["D"]}
+        out[name] = rec
     return out
 
 
@@ -414,7 +478,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="grazing", choices=["grazing", "halfspace"])
     ap.add_argument("--n", type=int, default=1 << 20)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="particles of the CPU legs (0: the whole workload)")
+    ap.add_argument("--acc-sample", type=int, default=1 << 17,
+                    help="particles of the accuracy-vs-oracle sample")
+    ap.add_argument("--acc-steps", type=int, default=10)
+    ap.add_argument("--no-acc", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
@@ -428,7 +497,7 @@ def main():
     from deorbit_gb300 import ic
 
     sc = workload(args.workload, args.n)
-    sample_n = min(args.cpu_sample, sc.n)
+    sample_n = min(args.cpu_sample, sc.n) if args.cpu_sample > 0 else sc.n
     wl = {"workload": f"{args.workload} impact, strength+damage" if args.workload == "grazing"
           else "halfspace impact, hydro only", "n_particles": sc.n, "dx_m": sc.dx,
           "materials": "granite (Collins, multi-flaw) + iron (von Mises)" if args.workload == "grazing"
@@ -442,8 +511,10 @@ def main():
         from oracle import oracle as O
 
         sample = ic.crop(sc, sample_n)
+        t_init = time.perf_counter()
         S = O.from_scenario(sample, threads=min(os.cpu_count() or 1, 16))
         S.init()
+        t_init = time.perf_counter() - t_init
         for _ in range(args.warmup):
             S.step(S.timestep())
         t0 = time.perf_counter()
@@ -451,14 +522,16 @@ def main():
             S.step(S.timestep())
         el = time.perf_counter() - t0
         v = sample.n * args.steps / el
+        what = (f"the whole {sc.n}-particle workload" if sample.n == sc.n else
+                f"{sample.n} particles cropped from the {sc.n}-particle workload around the impact point")
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": dict(wl, sample=sample.n),
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": S.threads(), "nproc": os.cpu_count(),
                                  "kind": "port",
-                                 "sample": f"{sample.n} particles cropped from the {sc.n}-particle workload "
-                                           f"around the impact point, {args.steps} KDK steps after init"},
+                                 "sample": f"{what}, {args.steps} KDK steps after init and {args.warmup} "
+                                           f"warm-up steps (init {t_init:.1f} s)"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -522,8 +595,12 @@ def main():
     if rank == 0 and world == 1 and not args.no_halfspace:
         halfspace = halfspace_section(sph, ic, device)
 
-    # ---- accuracy of the mixed form against FP64 (same dt sequence)
+    # ---- accuracy of the mixed form against FP64 (same dt sequence), and of
+    # both forms against the oracle on a bounded sample
     err = mixed_error(sph, ic, sc, args.steps, device) if rank == 0 else None
+    acc = None
+    if rank == 0 and not args.no_acc:
+        acc = accuracy_vs_oracle(sph, ic, ic.crop(sc, min(args.acc_sample, sc.n)), args.acc_steps, device)
 
     # ---- roofline of the dominant mixed-form kernel (largest total time of
     # the classes that hold one kernel; per-launch time from CUDA events)
@@ -543,12 +620,16 @@ def main():
                 # bytes per particle measured on a smaller case, scaled to this launch
                 traffic = (float(f[2]) + float(f[3])) * sc.n / float(f[1])
     fp32 = None
+    clocks = clk.summary()
     if dom in FLOPS_PER_ENTRY:
         iters = 2 if dom == "density" else 1
         fl = FLOPS_PER_ENTRY[dom] * list_entries * iters
         tf = fl / (avg_ms / 1000.0) / 1e12
-        fp32 = {"flops_per_launch": fl, "achieved_tflops": tf, "peak_tflops": FP32_PEAK_TFLOPS,
-                "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)", "frac": tf / FP32_PEAK_TFLOPS}
+        mhz = clocks.get("sm_max_mhz") or 2070.0
+        peak32, sms = fp32_peak_tflops(device, mhz)
+        fp32 = {"flops_per_launch": fl, "achieved_tflops": tf, "peak_tflops": peak32,
+                "peak_kind": f"{sms} SMs x {FP32_LANES_PER_SM} lanes x 2 x {mhz:.0f} MHz (device properties and "
+                             f"the sampled maximum SM clock)", "frac": tf / peak32}
     roof = {"kernel": KERNEL_OF_CLASS[dom] + "<float>", "bound": "hbm", "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
             "peak_kind": f"{hbm_kind} copy bandwidth", "alg_bytes_per_launch": alg * sc.n,
@@ -564,9 +645,11 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         sample = ic.crop(sc, sample_n)
         v, el, thr = cpu_rate(ic, sample, 2, threads=min(os.cpu_count() or 1, 16))
+        what = (f"the whole {sc.n}-particle workload" if sample.n == sc.n else
+                f"{sample.n} particles cropped from the {sc.n}-particle workload around the impact point")
         cpu = {"value": v, "unit": UNIT, "cores": thr, "nproc": os.cpu_count(), "kind": "port",
-               "sample": f"{sample.n} particles cropped from the {sc.n}-particle workload around the "
-                         f"impact point, 2 KDK steps after init ({el:.1f} s)"}
+               "sample": f"{what}, 2 KDK steps after init ({el:.1f} s)",
+               "plain_fp64_gpu_over_cpu": value64 / v, "mixed_gpu_over_cpu": value / v}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -575,11 +658,12 @@ def main():
                 "config": dict(wl, form="mixed (FP32 pairs/EOS/stress, FP64 positions/energies)",
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
                 "roofline": roof, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches, "clocks": clk.summary(),
+                "gpu_launches": launches, "clocks": clocks,
                 "plain_fp64": {"value": value64, "ms_per_step": ms64 / args.steps,
                                "kernel_ms": {k: v[0] for k, v in kst64.items()}},
                 "speedup_vs_plain_fp64": value / value64,
                 "mixed_vs_fp64_rel_l2": err,
+                "accuracy_vs_oracle": acc,
                 "kernel_ms": {k: v[0] for k, v in kst.items()},
                 "batched": batched, "serving": serving, "large": large, "halfspace": halfspace}
         print(json.dumps(line), flush=True)

@@ -14,9 +14,17 @@ Tolerances:
   FP64      rel-L2 <= 1e-9 per field after 20 steps, stress and damage included,
             with the CFL dt agreeing to 1e-9 every step; the device's multi-flaw
             CSR equal to the oracle's bit for bit
-  mixed     rel-L2 <= 1e-4 per field after 20 steps (the mixed-form target), on
-            the oracle's dt sequence; the device's flaw thresholds equal to the
-            oracle's rounded to FP32
+  mixed     on the oracle's dt sequence, after 20 steps: rel-L2 <= 1e-4 per field
+            (the mixed-form target) for every field damage does not switch; the
+            device's flaw thresholds equal to the oracle's rounded to FP32.
+            Damage is an integer step function of sigma_max / E (the number of
+            flaws whose threshold it exceeds, with D capped at n_act / n_f), so a
+            particle whose sigma_max sits within FP32 rounding of a threshold
+            activates a flaw one step earlier or later than in FP64 and its D
+            differs by ~1 / n_f for good (a "flip").  One flip among 30,000
+            particles is ~3e-4 of D's rel-L2.  The test therefore asserts D and S
+            (which D scales) at 1e-4 over the particles without a flip, and that
+            flips stay below 1 in 1,000 particles.
 """
 import numpy as np
 import pytest
@@ -107,8 +115,15 @@ def test_mixed_matches_oracle(sph_mod, which):
     print(which, "mixed", {k: f"{v:.1e}" for k, v in errs.items()}, "D differs at", flips)
     assert np.array_equal(flaws[0], oflaws[0])
     assert np.array_equal(flaws[1], oflaws[1].astype(np.float32).astype(np.float64))
-    bad = {k: v for k, v in errs.items() if not v <= MIXED_TOL}
+    switched = ("D", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz")
+    bad = {k: v for k, v in errs.items() if k not in switched and not v <= MIXED_TOL}
     assert not bad, bad
+    keep = np.abs(gpu["D"] - orc["D"]) <= 1e-6
+    errs_kept = {k: rel_l2(gpu[k][keep], orc[k][keep]) for k in switched}
+    print(which, "mixed, particles without a flip", {k: f"{v:.1e}" for k, v in errs_kept.items()})
+    bad = {k: v for k, v in errs_kept.items() if not v <= MIXED_TOL}
+    assert not bad, bad
+    assert flips <= sc.n // 1000, flips
 
 
 def test_scenarios_exercise_the_extensions():
