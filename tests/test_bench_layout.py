@@ -16,4 +16,4 @@ def test_roofline_tables_are_consistent():
     for fixed, per_entry in bench.ALG_BYTES.values():
         assert fixed > 0 and per_entry >= 0
     assert set(bench.FLOPS_PER_ENTRY) <= set(bench.ALG_BYTES)
-    assert 70 < bench.FP32_PEAK_TFLOPS < 90
+    assert bench.FP32_LANES_PER_SM == 128  # FP32 lanes per SM of compute capability 10.x
