@@ -451,7 +451,7 @@ def halfspace_section(sph, ic, device, steps=200):
             "fp64_vs_oracle_rel_l2": err}
 
 
-def serving_section(device, rates=(2.0, 4.0, 8.0), count=24, steps=300):
+def serving_section(device, rates=(4.0, 8.0, 16.0), count=200, steps=300):
     """Poisson request streams through the continuous-batching server."""
     from deorbit_gb300 import serve, sph
     out = {"workload": f"{count} requests per rate, N log-uniform 10k-500k, half strength + damage, "
@@ -459,6 +459,8 @@ def serving_section(device, rates=(2.0, 4.0, 8.0), count=24, steps=300):
     for rate in rates:
         reqs = serve.poisson_requests(count, rate, steps=steps)
         srv = serve.Server(sph.MIXED, device, hbm_budget_bytes=160e9, chunk=4)
+        from deorbit_gb300 import autotune
+        autotune.apply(srv.ctx, reqs[0][1], sph.MIXED, device)
         base = srv.now()
         for t, sc, st in reqs:
             srv.submit(sc, st, arrival=base + t)

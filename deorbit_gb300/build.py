@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdeorbit_sph.so")
 
-SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu"]
+SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off: host code (flaw seeding, file formats) gives the same
 # results on x86 and on Arm, where g++ would otherwise fuse a*b+c.
@@ -53,7 +53,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or not _newer(o, [s] + hdrs):
             jobs.append([nv] + NVCC_FLAGS + ARCH + ["-c", s, "-o", o])

@@ -14,10 +14,6 @@
 using dsph::EngineBase;
 using dsph::SphError;
 
-struct sph_ctx {
-    std::unique_ptr<EngineBase> eng;
-    int device = 0;
-};
 
 namespace {
 

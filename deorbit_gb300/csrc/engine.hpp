@@ -52,6 +52,16 @@ public:
     virtual void impact_seed_damage(int b, double dx, uint32_t seed) = 0;
     virtual int64_t impact_seed_flaws_multi(int b, double dx, uint32_t seed) = 0;
     virtual void impact_set_h0(int b, const double* h0) = 0;
+    // Flaws seeded on the host beforehand, set before the impact is committed:
+    // eps_act per particle and, when ptr is non-null, the multi-flaw CSR
+    // (ptr[n+1], eps[nflaws]) with flaw_model MULTI.
+    virtual void impact_set_flaws(int b, const double* eps_act, const int64_t* ptr, const double* eps,
+                                  int64_t nflaws) = 0;
+    virtual std::vector<sph_material> materials() = 0;
+    // Bytes of the engine's device allocations now, and as predicted after
+    // committing n more particles (capacity growth at the current list capacity).
+    virtual int64_t device_bytes() = 0;
+    virtual int64_t device_bytes_after_adding(int64_t n) = 0;
     virtual void impact_set_time(int b, double t) = 0;
     virtual void impact_set_step_limit(int b, int64_t steps) = 0;
     virtual void impact_remove(int b) = 0;
@@ -93,6 +103,16 @@ public:
     virtual void event_record(int slot) = 0;
     virtual double event_elapsed(int a, int b) = 0;
 };
+
+}  // namespace dsph
+
+// The opaque context of the C ABI.
+struct sph_ctx {
+    std::unique_ptr<dsph::EngineBase> eng;
+    int device = 0;
+};
+
+namespace dsph {
 
 std::unique_ptr<EngineBase> make_engine_fp64(int device);
 std::unique_ptr<EngineBase> make_engine_mixed(int device);

@@ -326,6 +326,8 @@ public:
         DSPH_CUDA(cudaEventCreateWithFlags(&copy_ev_, cudaEventDisableTiming));
         DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
         DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
+        DSPH_CUDA(cudaMalloc(&wait_err_d_, sizeof(int32_t)));
+        DSPH_CUDA(cudaMemsetAsync(wait_err_d_, 0, sizeof(int32_t), st_));
         DSPH_CUDA(cudaMalloc(&ntask_, sizeof(int32_t)));
         DSPH_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
         DSPH_CUDA(cudaMallocHost(&flags_h_, sizeof(int32_t) * 4));
@@ -340,6 +342,7 @@ public:
         for (void* p : allocs_) cudaFree(p);
         cudaFree(mats_d_);
         cudaFree(flags_d_);
+        cudaFree(wait_err_d_);
         cudaFree(ntask_);
         cudaFreeHost(flags_h_);
         for (int i = 0; i < 6; i++) cudaEventDestroy(ev_[i]);
@@ -496,6 +499,55 @@ public:
         }
     }
 
+    void impact_set_flaws(int b, const double* eps_act, const int64_t* ptr, const double* eps,
+                          int64_t nflaws) override {
+        ImpactH& h = imp(b);
+        if (h.committed) throw SphError(SPH_ERR_STATE, "flaws are set before the impact is initialised");
+        if (eps_act) h.seps.assign(eps_act, eps_act + h.n);
+        if (ptr) {
+            if (ptr[0] != 0 || ptr[h.n] != nflaws) throw SphError(SPH_ERR_ARG, "flaw CSR does not match its count");
+            h.flaw_ptr.assign(ptr, ptr + h.n + 1);
+            h.flaw_eps.assign(eps, eps + nflaws);
+            h.multi = true;
+            h.prm.flaw_model = SPH_FLAWS_MULTI;
+        }
+    }
+
+    std::vector<sph_material> materials() override { return mats_h_; }
+
+    // Device bytes per particle of capacity: both carried buffers, derived
+    // columns, geometry and force records, reverse lists and the own list at
+    // the current list capacity (the allocations of ensure_particle_capacity
+    // and alloc_lists), plus the per-id sort arrays.
+    int64_t bytes_per_particle() const {
+        const int64_t R4 = sizeof(R) == 4;
+        int64_t b = 2 * (kND * 8 + kNR * (int64_t)sizeof(R) + 1 + 1 + 2 + 4) + kNDer * (int64_t)sizeof(R);
+        b += 16 + 16 + 4 + 8 * R4 + 16 + 96 * R4 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 4 * kExtraCap;
+        b += 16 * (((int64_t)cap_nbr_ + 3) / 4);
+        b += 4 + 12 + 8;  // pos_of_gid, three key arrays, two id arrays
+        return b;
+    }
+    int64_t device_bytes() override { return dev_bytes_; }
+    int64_t device_bytes_after_adding(int64_t n) override {
+        int64_t staged = 0, staged_flaws = 0;
+        for (auto& h : imp_)
+            if (h.used && h.alive && !h.committed) {
+                staged += h.n;
+                staged_flaws += (int64_t)h.flaw_eps.size();
+            }
+        const int64_t need = N_ + staged + n;
+        int64_t extra = 0;
+        if (need > cap_) {
+            const int64_t nc = std::max<int64_t>(need, (int64_t)(cap_ * 1.5) + 1024);
+            extra += (nc - cap_) * bytes_per_particle();
+        }
+        // multi-flaw thresholds (~ln n per particle) and their per-id pointers
+        const double lnn = std::log((double)std::max<int64_t>(n, 2));
+        extra += (int64_t)((double)n * (lnn + 1.0)) * (int64_t)sizeof(R) + 8 * (n + staged) +
+                 staged_flaws * (int64_t)sizeof(R);
+        return dev_bytes_ + extra;
+    }
+
     void impact_set_step_limit(int b, int64_t steps) override {
         ImpactH& h = imp(b);
         h.step_limit = steps;
@@ -645,7 +697,7 @@ public:
         launch_n(k_eos<R>, N_);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[3], st_));
         cls(KC_FORCE);
-        launch_n(k_force<R>, N_, 128);
+        launch_force();
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[4], st_));
         cls(KC_DAMAGE);
         launch_n(k_damage<R>, N_);
@@ -790,7 +842,20 @@ public:
         check_async();
     }
 
-    void synchronize() override { DSPH_CUDA(cudaStreamSynchronize(st_)); }
+    void synchronize() override {
+        DSPH_CUDA(cudaStreamSynchronize(st_));
+        check_waits();
+    }
+    // A kernel whose bounded wait on its bulk copies ran out leaves its outputs
+    // unwritten and sets the error word; the next synchronisation reports it.
+    void check_waits() {
+        int32_t e = 0;
+        DSPH_CUDA(cudaMemcpy(&e, wait_err_d_, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        if (e) {
+            DSPH_CUDA(cudaMemset(wait_err_d_, 0, sizeof(int32_t)));
+            throw SphError(SPH_ERR_TIMEOUT, "a kernel's bounded wait for its staged copies ran out");
+        }
+    }
 
     // ------------------------------------------------------------- fields
     void read_field(int b, const char* name, double* out) override {
@@ -1108,6 +1173,16 @@ public:
             cell_factor_z_ = value;
         } else if (k == "block") {
             set_tuning((int)value, 0);
+        } else if (k == "force_staging") {
+            const int fsv = (int)value;
+            if (!(value == fsv && (fsv == 0 || fsv == 22 || fsv == 23 || fsv == 42)))
+                throw SphError(SPH_ERR_ARG, "force_staging is 0 (off) or 10 x entries + stages: 22, 23, 42");
+            if constexpr (sizeof(R) == 4) {
+                if (fsv == 22) allow_force_smem<2, 2>();
+                if (fsv == 23) allow_force_smem<2, 3>();
+                if (fsv == 42) allow_force_smem<4, 2>();
+            }
+            force_staging_ = fsv;
         } else {
             throw SphError(SPH_ERR_ARG, "unknown option " + k);
         }
@@ -1115,6 +1190,7 @@ public:
     double get_option(const char* key) override {
         std::string k(key);
         if (k == "list_mode") return list_mode_;
+        if (k == "force_staging") return force_staging_;
         if (k == "graphs") return use_graphs_ ? 1 : 0;
         if (k == "slack") return slack_;
         if (k == "cell_factor") return cell_factor_;
@@ -1122,6 +1198,8 @@ public:
         if (k == "block") return block_;
         if (k == "list_capacity") return cap_nbr_;
         if (k == "list_entries") return (double)list_entries();
+        if (k == "device_bytes") return (double)dev_bytes_;
+        if (k == "bytes_per_particle") return (double)bytes_per_particle();
         throw SphError(SPH_ERR_ARG, "unknown option " + k);
     }
     int64_t launches() override { return launches_; }
@@ -1163,13 +1241,20 @@ private:
             throw SphError(SPH_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         }
         allocs_.push_back(p);
+        alloc_bytes_.push_back((int64_t)(sizeof(T) * std::max<size_t>(n, 1)));
+        dev_bytes_ += alloc_bytes_.back();
         layout_epoch_++;
         return static_cast<T*>(p);
     }
     void dfree(void* p) {
         if (!p) return;
         auto it = std::find(allocs_.begin(), allocs_.end(), p);
-        if (it != allocs_.end()) allocs_.erase(it);
+        if (it != allocs_.end()) {
+            const size_t i = (size_t)(it - allocs_.begin());
+            dev_bytes_ -= alloc_bytes_[i];
+            alloc_bytes_.erase(alloc_bytes_.begin() + (std::ptrdiff_t)i);
+            allocs_.erase(it);
+        }
         cudaFree(p);
     }
     template <class T>
@@ -1222,6 +1307,42 @@ private:
         prof_end();
         launches_++;
     }
+    // The force pass; in the mixed form optionally with its neighbour records
+    // staged in shared memory by bulk copies (option "force_staging").
+    template <int SE, int SS>
+    void launch_force_staged(unsigned grid) {
+        using FS = ForceStaging<SE, SS>;
+        static_assert(FS::kSmemBytes <= 227 * 1024, "force staging exceeds the shared memory of a block");
+        k_force<R, SE, SS><<<grid, FS::kBlock, FS::kSmemBytes, st_>>>(view(), wait_err_d_);
+        launched((const void*)k_force<R, SE, SS>);
+    }
+    void launch_force() {
+        if (N_ <= 0) return;
+        prof_begin();
+        const unsigned grid = (unsigned)((N_ + 127) / 128);
+        bool done = false;
+        if constexpr (sizeof(R) == 4) {
+            done = true;
+            switch (force_staging_) {
+                case 22: launch_force_staged<2, 2>(grid); break;
+                case 23: launch_force_staged<2, 3>(grid); break;
+                case 42: launch_force_staged<4, 2>(grid); break;
+                default: done = false;
+            }
+        }
+        if (!done) {
+            k_force<R, 0, 0><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
+            launched((const void*)k_force<R, 0, 0>);
+        }
+        prof_end();
+        launches_++;
+    }
+    template <int SE, int SS>
+    void allow_force_smem() {
+        DSPH_CUDA(cudaFuncSetAttribute(k_force<R, SE, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       ForceStaging<SE, SS>::kSmemBytes));
+    }
+
     template <class Kern, class... Args>
     void launch_small(Kern k, int nimp, Args... args) {
         if (nimp <= 0) return;
@@ -1962,7 +2083,7 @@ public:
         cls(KC_EOS);
         launch_n(k_eos<R>, N_);
         cls(KC_FORCE);
-        launch_n(k_force<R>, N_, 128);
+        launch_force();
     }
 
     void dt_reduce() {
@@ -2034,6 +2155,10 @@ public:
     double slack_ = 0.03;
     int cap_nbr_ = 160;
     int32_t* flags_d_ = nullptr;
+    int32_t* wait_err_d_ = nullptr;   // set by a kernel whose bounded wait ran out
+    std::vector<int64_t> alloc_bytes_;  // sizes of allocs_, in the same order
+    int64_t dev_bytes_ = 0;
+    int force_staging_ = 0;
     int32_t* flags_h_ = nullptr;
     void* scratch_ = nullptr;
     size_t scratch_bytes_ = 0;

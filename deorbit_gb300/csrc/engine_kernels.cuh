@@ -395,6 +395,52 @@ __device__ __forceinline__ void ld_f32x8_ro(const float4* p, float4& a, float4& 
         : "l"(p));
 }
 
+// ---- bulk-copy staging (cp.async.bulk through the TMA engine, mbarrier completion)
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// makes initialised barriers visible to the bulk-copy (async) proxy
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+// this thread's arrival on the barrier's current phase, announcing `bytes` of
+// bulk copies that will complete on it
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the barrier phase of the given parity, at most `limit` polls
+// (each poll may suspend the thread for a bounded, hardware-chosen time);
+// false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit) {
+    for (int i = 0; i < limit; i++)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+// global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte
+// aligned), completing as transaction bytes on the barrier
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 // Own-list addressing: entry t of particle k lives at nbr[4k + nbr_slot(t, ls)],
 // i.e. 4-entry blocks stored block-major, so one int4 load brings a lane four
 // entries and a warp's block loads are contiguous.
@@ -1417,13 +1463,55 @@ static __global__ void k_eos(View<R> v) {
 // Velocity gradient -> Jaumann dS/dt and deviatoric power (sph.hpp:212-258)
 // fused with the momentum / energy pair loop (sph.hpp:277-317).  Writes acc,
 // the new dudt and dSdt, eps_work.
-template <class R>
-static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(View<R> v) {
+// Shared-memory staging of the neighbour records of the mixed force pass: every
+// lane owns a ring of SS stages of SE entries; a stage is filled by one
+// 96-byte bulk copy (cp.async.bulk, the TMA engine) per entry straight from the
+// record array, completing on the warp's mbarrier of that stage, while the lane
+// evaluates the pairs of the other stages from shared memory.  A lane's slot is
+// SE x 96 bytes plus 16 of padding, so the 32 lanes' 16-byte reads of the same
+// field fall in distinct bank groups.
+template <int SE, int SS>
+struct ForceStaging {
+    static constexpr int kLaneBytes = SE * 96 + 16;
+    static constexpr int kStageBytes = 32 * kLaneBytes;
+    static constexpr int kWarpBytes = 16 * SS + SS * kStageBytes;
+    static constexpr int kBlock = 128;
+    static constexpr int kSmemBytes = (kBlock / 32) * kWarpBytes;
+};
+constexpr long long kWaitNs = 500000000ll;   // a bounded wait gives up after 0.5 s
+constexpr int kWaitPolls = 1 << 26;          // ... or after this many polls
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// mbar_wait bounded in time as well as in polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    if (mbar_test(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (int i = 0; i < kWaitPolls; i += 64) {
+        if (mbar_wait(bar, parity, 64)) return true;
+        if ((long long)(global_ns() - t0) > kWaitNs) return false;
+    }
+    return false;
+}
+
+template <class R, int SE = 0, int SS = 0>
+static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(View<R> v, int32_t* wait_err) {
     using Acc = AccT<R>;
+    constexpr bool kStaged = SS > 0 && sizeof(R) == 4;
     int64_t k = gtid();
-    if (k >= v.n) return;
+    bool live = k < v.n;
+    if constexpr (!kStaged) {
+        if (!live) return;
+    }
+    if (!live) k = v.n - 1;  // staged: every lane of the warp takes part in the barrier phases
     const ImpactD& I = v.imps[v.imp[k]];
-    if (!I.mask) return;
+    if constexpr (!kStaged) {
+        if (!I.mask) return;
+    }
+    live = live && I.mask;
     const R G = v.mats[v.mat[k]].G;
     const bool strength = G > R(0);
     const R alpha = (R)I.alpha, beta = (R)I.beta, eps = (R)I.eps, eps_as = (R)I.eps_as;
@@ -1492,6 +1580,73 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             du.add(pair_div(alpha_u * mj * vsig * ((R)v.u[k] - (R)v.u[j]) * dW, rbar));
         }
     };
+    // mixed form: one list entry's contributions from its six record float4s
+    // (global memory or a shared-memory stage); exact zeros for a failing pair
+    auto rec_body = [&](int32_t j, const float4 pj, const float4 vhj, const float4 vlj, const float4 fa,
+                        const float4 fb, const float4 fc) {
+        const float mj = vhj.w;  // (mass, packed cell) ride in the .w lanes
+        float dx, dy, dz;
+        sep_f32(I, pi, ci, pj, __float_as_uint(vlj.w), dx, dy, dz);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float hif = (float)hi;
+        const float hs = hif + pj.w;
+        bool ok = r2 < hs * hs && r2 != 0.0f;
+        if (need_member) ok = ok && ref_member(v.refbin[k], v.refbin[j], I);  // own bins re-read: rarely needed
+        const float irs = ok ? rsqrtf(r2) : 1.0f;  // hardware 1/sqrt (2 ulp)
+        const float r = ok ? r2 * irs : 1.0f;
+        const float hbar = 0.5f * (hif + pj.w);
+        const float ihb = pair_div(1.0f, hbar);
+        const float dW = ok ? kernel_dW_bf<float>(r, ihb) : 0.0f;
+        const float wg = dW * irs;
+        const float2 gxy = mul2(f2(dx, dy), f2(wg));
+        const float gz = dz * wg;
+        // hi parts nearly cancel exactly; lo parts restore the FP64 difference
+        const float2 vxy = add2(sub2(f2(vhi.x, vhi.y), f2(vhj.x, vhj.y)), sub2(f2(vli.x, vli.y), f2(vlj.x, vlj.y)));
+        const float vz = (vhi.z - vhj.z) + (vli.z - vlj.z);
+        const float Vj = fa.x, rhoj = fa.y, csj = fa.z, pfj = fa.w, dsj = fb.x, Raj = fb.y;
+        if (strength) {  // Vj (v_j - v_i) (x) grad W
+            const float2 exy = mul2(vxy, f2(-Vj));
+            const float ez = -vz * Vj;
+            Lp0 = fma2(f2(exy.x), gxy, Lp0);
+            Lp1 = fma2(f2(exy.y), gxy, Lp1);
+            Lp2 = fma2(f2(ez), gxy, Lp2);
+            Lpz = fma2(exy, f2(gz), Lpz);
+            Lp22 = fmaf(ez, gz, Lp22);
+        }
+        const float dvr = vxy.x * dx + vxy.y * dy + vz * dz;
+        float Pij = 0.0f;
+        if (dvr < 0.0f) {
+            const float mu = pair_div(hbar * dvr, r * r + (float)eps * hbar * hbar);
+            const float cbar = 0.5f * ((float)csi + csj);
+            Pij = pair_div(-(float)alpha * cbar * mu + (float)beta * mu * mu, 0.5f * ((float)rhoi + rhoj));
+        }
+        const float term = (float)Pi_over + pfj + Pij;
+        float dut = 0.5f * mj * term * (vxy.x * gxy.x + vxy.y * gxy.y + vz * gz);
+        float mterm = term;
+        if (eps_as > R(0)) {
+            const float q = r * ihb;
+            const float t = fmaxf(2.0f - q, 0.0f), a = fmaxf(1.0f - q, 0.0f);
+            const float fr = (0.25f * t * t * t - a * a * a) * (float)inv_poly;
+            float fn = fr * fr;
+            fn *= fn;
+            mterm += ((float)Rai + Raj) * fn;
+        }
+        const float mm = mj * mterm;
+        // (S_i dscale_i / rho_i^2 + S_j dscale_j / rho_j^2) . grad W, x and y rows packed
+        const float2 own = fma2(f2((float)sxz, (float)syz), f2(gz),
+                                fma2(f2((float)sxy, (float)syy), f2(gxy.y), mul2(f2((float)sxx, (float)sxy), f2(gxy.x))));
+        const float2 oth = fma2(f2(fb.z, fb.w), f2(gz), fma2(f2(fc.w, fc.y), f2(gxy.y), mul2(f2(fc.x, fc.w), f2(gxy.x))));
+        const float2 stxy = fma2(oth, f2(dsj), mul2(own, f2((float)dsri)));
+        const float stz = ((float)sxz * gxy.x + (float)syz * gxy.y + (float)szz * gz) * (float)dsri +
+                          (fb.z * gxy.x + fb.w * gxy.y + fc.z * gz) * dsj;
+        kxy.add(fma2(gxy, f2(-mm), mul2(stxy, f2(mj))));
+        if (alpha_u > R(0)) {
+            const float rbar = 0.5f * ((float)rhoi + rhoj);
+            const float vsig = rsqrt_(pair_div(fabsf((float)v.P[k] - (float)v.P[j]), rbar));
+            dut += pair_div((float)alpha_u * mj * vsig * ((float)v.u[k] - (float)v.u[j]) * dW, rbar);
+        }
+        kzu.add(f2(stz * mj - gz * mm, dut));
+    };
     const float hs_pad = 2.0f * m;
     auto body = [&](int32_t j) {
         if constexpr (sizeof(R) == 8) {
@@ -1529,71 +1684,86 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             ld_f32x8_ro(rec, pj, vhj);
             ld_f32x8_ro(rec + 2, vlj, fa);
             ld_f32x8_ro(rec + 4, fb, fc);
-            const float mj = vhj.w;  // (mass, packed cell) ride in the .w lanes
-            float dx, dy, dz;
-            sep_f32(I, pi, ci, pj, __float_as_uint(vlj.w), dx, dy, dz);
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const float hif = (float)hi;
-            const float hs = hif + pj.w;
-            bool ok = r2 < hs * hs && r2 != 0.0f;
-            if (need_member) ok = ok && ref_member(v.refbin[k], v.refbin[j], I);  // own bins re-read: rarely needed
-            const float irs = ok ? rsqrtf(r2) : 1.0f;  // hardware 1/sqrt (2 ulp)
-            const float r = ok ? r2 * irs : 1.0f;
-            const float hbar = 0.5f * (hif + pj.w);
-            const float ihb = pair_div(1.0f, hbar);
-            const float dW = ok ? kernel_dW_bf<float>(r, ihb) : 0.0f;
-            const float wg = dW * irs;
-            const float2 gxy = mul2(f2(dx, dy), f2(wg));
-            const float gz = dz * wg;
-            // hi parts nearly cancel exactly; lo parts restore the FP64 difference
-            const float2 vxy = add2(sub2(f2(vhi.x, vhi.y), f2(vhj.x, vhj.y)), sub2(f2(vli.x, vli.y), f2(vlj.x, vlj.y)));
-            const float vz = (vhi.z - vhj.z) + (vli.z - vlj.z);
-            const float Vj = fa.x, rhoj = fa.y, csj = fa.z, pfj = fa.w, dsj = fb.x, Raj = fb.y;
-            if (strength) {  // Vj (v_j - v_i) (x) grad W
-                const float2 exy = mul2(vxy, f2(-Vj));
-                const float ez = -vz * Vj;
-                Lp0 = fma2(f2(exy.x), gxy, Lp0);
-                Lp1 = fma2(f2(exy.y), gxy, Lp1);
-                Lp2 = fma2(f2(ez), gxy, Lp2);
-                Lpz = fma2(exy, f2(gz), Lpz);
-                Lp22 = fmaf(ez, gz, Lp22);
-            }
-            const float dvr = vxy.x * dx + vxy.y * dy + vz * dz;
-            float Pij = 0.0f;
-            if (dvr < 0.0f) {
-                const float mu = pair_div(hbar * dvr, r * r + (float)eps * hbar * hbar);
-                const float cbar = 0.5f * ((float)csi + csj);
-                Pij = pair_div(-(float)alpha * cbar * mu + (float)beta * mu * mu, 0.5f * ((float)rhoi + rhoj));
-            }
-            const float term = (float)Pi_over + pfj + Pij;
-            float dut = 0.5f * mj * term * (vxy.x * gxy.x + vxy.y * gxy.y + vz * gz);
-            float mterm = term;
-            if (eps_as > R(0)) {
-                const float q = r * ihb;
-                const float t = fmaxf(2.0f - q, 0.0f), a = fmaxf(1.0f - q, 0.0f);
-                const float fr = (0.25f * t * t * t - a * a * a) * (float)inv_poly;
-                float fn = fr * fr;
-                fn *= fn;
-                mterm += ((float)Rai + Raj) * fn;
-            }
-            const float mm = mj * mterm;
-            // (S_i dscale_i / rho_i^2 + S_j dscale_j / rho_j^2) . grad W, x and y rows packed
-            const float2 own = fma2(f2((float)sxz, (float)syz), f2(gz),
-                                    fma2(f2((float)sxy, (float)syy), f2(gxy.y), mul2(f2((float)sxx, (float)sxy), f2(gxy.x))));
-            const float2 oth = fma2(f2(fb.z, fb.w), f2(gz), fma2(f2(fc.w, fc.y), f2(gxy.y), mul2(f2(fc.x, fc.w), f2(gxy.x))));
-            const float2 stxy = fma2(oth, f2(dsj), mul2(own, f2((float)dsri)));
-            const float stz = ((float)sxz * gxy.x + (float)syz * gxy.y + (float)szz * gz) * (float)dsri +
-                              (fb.z * gxy.x + fb.w * gxy.y + fc.z * gz) * dsj;
-            kxy.add(fma2(gxy, f2(-mm), mul2(stxy, f2(mj))));
-            if (alpha_u > R(0)) {
-                const float rbar = 0.5f * ((float)rhoi + rhoj);
-                const float vsig = rsqrt_(pair_div(fabsf((float)v.P[k] - (float)v.P[j]), rbar));
-                dut += pair_div((float)alpha_u * mj * vsig * ((float)v.u[k] - (float)v.u[j]) * dW, rbar);
-            }
-            kzu.add(f2(stz * mj - gz * mm, dut));
+            rec_body(j, pj, vhj, vlj, fa, fb, fc);
         }
     };
-    if (!I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap) {
+    if constexpr (kStaged) {
+        using FS = ForceStaging<SE, SS>;
+        extern __shared__ __align__(128) unsigned char force_smem[];
+        const unsigned full = 0xffffffffu;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        unsigned char* wb = force_smem + warp * FS::kWarpBytes;
+        uint64_t* bars = reinterpret_cast<uint64_t*>(wb);  // stage s's barrier at bars[2 s]
+        unsigned char* mine = wb + 16 * SS + lane * FS::kLaneBytes;  // stage s at + s * kStageBytes
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < SS; q++) mbar_init(&bars[2 * q], 32);
+            mbar_init_fence();
+        }
+        __syncwarp();
+        const bool use_list = live && !I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap;
+        const int cnt = use_list ? v.nbr_cnt[k] : 0;
+        const int cmax = __reduce_max_sync(full, cnt);
+        int32_t jb[SS][SE];
+        uint32_t parity = 0;  // bit q: parity of stage q's pending phase
+        // fill stage q with entries t0 .. t0 + SE - 1 of this lane's list (0 bytes past its end)
+        auto issue = [&](const int q, const int t0) {
+            const int32_t* blk = v.nbr + 4 * k + nbr_slot(t0, v.ls);
+            if constexpr (SE == 4) {
+                const int4 b4 = t0 < cnt ? *reinterpret_cast<const int4*>(blk) : make_int4(0, 0, 0, 0);
+                jb[q][0] = b4.x; jb[q][SE > 1 ? 1 : 0] = b4.y; jb[q][SE > 2 ? 2 : 0] = b4.z; jb[q][SE - 1] = b4.w;
+            } else {
+                const int2 b2 = t0 < cnt ? *reinterpret_cast<const int2*>(blk) : make_int2(0, 0);
+                jb[q][0] = b2.x; jb[q][SE - 1] = b2.y;
+            }
+            const int nv = max(0, min(SE, cnt - t0));
+            mbar_arrive_tx(&bars[2 * q], 96u * (uint32_t)nv);
+#pragma unroll
+            for (int e = 0; e < SE; e++)
+                if (e < nv)
+                    bulk_g2s(mine + q * FS::kStageBytes + e * 96, v.fr + 6 * (int64_t)jb[q][e], 96u, &bars[2 * q]);
+        };
+#pragma unroll
+        for (int q = 0; q < SS; q++) issue(q, q * SE);
+        bool failed = false;
+        for (int base = 0; base < cmax && !failed; base += SS * SE) {
+#pragma unroll
+            for (int q = 0; q < SS; q++) {
+                const int t0 = base + q * SE;
+                const bool ok = mbar_wait_bounded(&bars[2 * q], (parity >> q) & 1u);
+                if (__any_sync(full, !ok)) {
+                    failed = true;
+                    break;
+                }
+                parity ^= 1u << q;
+                const float4* rb = reinterpret_cast<const float4*>(mine + q * FS::kStageBytes);
+#pragma unroll
+                for (int e = 0; e < SE; e++)
+                    if (t0 + e < cnt)
+                        rec_body(jb[q][e], rb[6 * e], rb[6 * e + 1], rb[6 * e + 2], rb[6 * e + 3], rb[6 * e + 4],
+                                 rb[6 * e + 5]);
+                issue(q, t0 + SS * SE);
+            }
+        }
+        if (failed) {
+            // a stage's copies did not land in time: report it, let every copy
+            // still in flight into this warp's slots complete (bounded), leave
+            // this warp's outputs unwritten
+            if (lane == 0) atomicOr(wait_err, 1);
+#pragma unroll
+            for (int q = 0; q < SS; q++) mbar_wait_bounded(&bars[2 * q], (parity >> q) & 1u);
+            return;
+        }
+        if (!live) return;
+        if (use_list) {
+            const int xc = v.xcnt[k];
+            const int32_t* xl = v.xnbr + k;
+            for (int t = 0; t < xc; t++, xl += v.ls) body(*xl);
+        } else {
+            traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
+                     [&](int32_t j, float, float, float) { body(j); });
+        }
+    } else if (!I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap) {
         const int cnt = v.nbr_cnt[k];
         walk_list(v.nbr, v.ls, k, cnt, body);
         const int xc = v.xcnt[k];

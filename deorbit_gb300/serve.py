@@ -1,33 +1,33 @@
-"""Continuous-batching server for impact runs on one GPU.
+"""Continuous-batching server for impact runs on one GPU (Python front end
+of the library's native server, sph_serve_* in the C ABI).
 
 Requests (a Scenario and a step count) arrive over time.  The server keeps one
-engine context; a request is admitted as soon as its particles fit the HBM
-budget next to the resident ones, initialised in place while the others keep
-their state, then advanced together with every other resident impact -- one
-kernel launch per phase covers all of them, each with its own CFL dt and step
-limit.  A finished request's fields are read back and its slot and memory
-released, which admits the next one.  Results of a request do not depend on
-what else is resident (all per-particle work is confined to the particle's own
-impact and reductions are order-independent), so a request gives the same
-result alone and in the mix.
+engine context; a request is admitted as soon as it has arrived and its
+particles fit the device-memory budget next to the resident ones -- judged from
+the engine's own allocations and its per-particle footprint at the current
+neighbour-list capacity, which grows when an impact compresses -- initialised in
+place while the others keep their state, then advanced together with every
+other resident impact: one kernel launch per phase covers all of them, each with
+its own CFL dt and step limit.  A finished request's fields are read back and its
+slot and memory released, which admits the next one.  Flaw seeding of queued
+requests (the multi-flaw law draws ~N ln N thresholds) runs on the server's
+worker thread while the GPU advances the residents.  Results of a request do
+not depend on what else is resident (all per-particle work is confined to the
+particle's own impact and reductions are order-independent), so a request gives
+the same result alone and in the mix.
 
 Latency is measured from arrival (submit time) to the moment its results are
 in host memory.
 """
 from __future__ import annotations
 
-import collections
+import ctypes as C
 import dataclasses
 import time
 
 import numpy as np
 
 from . import ic, sph
-
-# Device bytes per resident particle of the mixed form at the default list
-# capacity (carried state double-buffered, derived fields, geometry, lists,
-# sort buffers); the FP64 form needs about 1.6x.
-BYTES_PER_PARTICLE = {sph.MIXED: 1500, sph.FP64: 2400}
 
 RESULT_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "u", "rho", "P", "D")
 
@@ -42,116 +42,140 @@ class Request:
     finished: float | None = None
     impact: int | None = None
     result: dict | None = None
+    failed: bool = False
 
     @property
     def latency(self):
         return None if self.finished is None else self.finished - self.arrival
 
 
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
 class Server:
     def __init__(self, precision=sph.MIXED, device=0, hbm_budget_bytes=160e9, chunk=4,
-                 fields=RESULT_FIELDS, bytes_per_particle=None, ctx=None):
+                 fields=RESULT_FIELDS, ctx=None):
         self.precision = precision
         # ctx: an engine context to serve from (default: a new one on `device`)
         self.ctx = ctx if ctx is not None else sph.Context(precision, device)
-        self.budget = float(hbm_budget_bytes)
-        self.bpp = bytes_per_particle or BYTES_PER_PARTICLE[precision]
-        self.chunk = int(chunk)
-        self.fields = fields
-        self.pending = collections.deque()
-        self.active = {}
+        self.fields = tuple(fields)
+        self.h = C.c_void_p()
+        sph.check(sph.lib().sph_serve_create(self.ctx.h, float(hbm_budget_bytes), int(chunk),
+                                             ",".join(self.fields).encode(), C.byref(self.h)))
+        self.requests = {}
         self.done = []
         self.mat_ids = {}
-        self.t0 = time.perf_counter()
-        self.particle_steps = 0
-        self.busy_time = 0.0
 
     # ------------------------------------------------------------ clock
     def now(self):
-        return time.perf_counter() - self.t0
+        t = C.c_double()
+        sph.check(sph.lib().sph_serve_now(self.h, C.byref(t)))
+        return t.value
 
     # ------------------------------------------------------------ requests
     def submit(self, scenario: ic.Scenario, steps: int, arrival: float | None = None) -> Request:
-        r = Request(len(self.pending) + len(self.active) + len(self.done), scenario, int(steps),
-                    self.now() if arrival is None else float(arrival))
-        self.pending.append(r)
+        sc = scenario
+        ids = []
+        for d in sc.materials:  # materials are added to the context once and shared
+            key = tuple(sorted(d.items()))
+            if key not in self.mat_ids:
+                self.mat_ids[key] = self.ctx.add_material(ic._material_struct(sph.Material, d))
+            ids.append(self.mat_ids[key])
+        mat = np.ascontiguousarray(np.asarray(ids if ids else [0], np.int32)[sc.mat])
+        prm = sph.params(**sc.params)
+        keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in (
+            ("x", sc.pos[:, 0]), ("y", sc.pos[:, 1]), ("z", sc.pos[:, 2]), ("vx", sc.vel[:, 0]),
+            ("vy", sc.vel[:, 1]), ("vz", sc.vel[:, 2]), ("mass", sc.mass), ("u", sc.u))}
+        fixed = np.ascontiguousarray(sc.fixed, dtype=np.uint8)
+        q = sph.Request()
+        q.params = C.pointer(prm)
+        for a in range(3):
+            q.lo[a], q.hi[a], q.periodic[a] = float(sc.lo[a]), float(sc.hi[a]), int(sc.periodic[a])
+        q.n = sc.n
+        for k, v in keep.items():
+            setattr(q, k, _dp(v))
+        q.mat = mat.ctypes.data_as(C.POINTER(C.c_int32))
+        q.fixed = fixed.ctypes.data_as(C.POINTER(C.c_uint8))
+        h0 = None
+        if sc.h0 is not None:
+            h0 = np.ascontiguousarray(sc.h0, dtype=np.float64)
+            q.h0 = _dp(h0)
+        kind, seed = sc.flaws if sc.flaws is not None else (None, 0)
+        q.flaws = sph.SERVE_FLAWS[kind]
+        q.flaw_dx, q.flaw_seed = float(sc.dx), int(seed) & 0xffffffff
+        q.steps = int(steps)
+        q.arrival = -1.0 if arrival is None else float(arrival)
+        rid = C.c_int64()
+        sph.check(sph.lib().sph_serve_submit(self.h, C.byref(q), C.byref(rid)))  # copies the arrays
+        rec = sph.ServeRecord()
+        sph.check(sph.lib().sph_serve_request_info(self.h, rid.value, C.byref(rec)))
+        r = Request(rid.value, sc, int(steps), rec.arrival)
+        self.requests[r.rid] = r
         return r
 
-    def resident_particles(self):
-        return sum(r.scenario.n for r in self.active.values())
+    def _collect(self, rid):
+        r = self.requests[rid]
+        rec = sph.ServeRecord()
+        sph.check(sph.lib().sph_serve_request_info(self.h, rid, C.byref(rec)))
+        r.admitted, r.finished, r.impact = rec.admitted, rec.finished, rec.impact
+        if rec.state == sph.SERVE_DONE:
+            r.result = {}
+            for k in self.fields:
+                out = np.empty(r.scenario.n)
+                sph.check(sph.lib().sph_serve_result(self.h, rid, k.encode(), _dp(out)))
+                r.result[k] = out
+        else:
+            r.failed = True
+        sph.check(sph.lib().sph_serve_release(self.h, rid))
+        self.done.append(r)
 
-    def _admit(self, now):
-        admitted = []
-        while self.pending and self.pending[0].arrival <= now:
-            r = self.pending[0]
-            need = (self.resident_particles() + r.scenario.n) * self.bpp
-            if self.active and need > self.budget:
-                break  # wait for memory to free up (FIFO admission)
-            self.pending.popleft()
-            b = ic.to_context(self.ctx, r.scenario, material_ids=self.mat_ids)
-            self.ctx.set_step_limit(b, r.steps)
-            r.impact = b
-            r.admitted = now
-            self.active[b] = r
-            admitted.append(r)
-        if admitted:
-            self.ctx.init()  # initialises only the newly admitted impacts
-        return admitted
-
-    def _retire(self):
-        finished = []
-        for b, r in list(self.active.items()):
-            if self.ctx.info(b).steps >= r.steps:
-                r.result = {k: self.ctx.read(b, k) for k in self.fields}
-                r.finished = self.now()
-                self.ctx.remove(b)
-                del self.active[b]
-                self.done.append(r)
-                finished.append(r)
-        return finished
-
-    def step(self):
-        """Admit what has arrived, advance all residents by one chunk, retire."""
-        self._admit(self.now())
-        if not self.active:
-            return 0
-        steps = min(self.chunk, min(r.steps - self.ctx.info(b).steps for b, r in self.active.items()))
-        steps = max(steps, 1)
-        n = self.resident_particles()
-        t = time.perf_counter()
-        self.ctx.run(steps)
-        self.ctx.synchronize()
-        self.busy_time += time.perf_counter() - t
-        self.particle_steps += n * steps
-        self._retire()
-        return steps
+    def step(self, max_wait_s=0.01):
+        """One serving round: admit what has arrived, advance the residents by
+        one chunk, retire; returns the requests finished in this round."""
+        cap = 256
+        ids = (C.c_int64 * cap)()
+        nd = C.c_int32()
+        sph.check(sph.lib().sph_serve_poll(self.h, float(max_wait_s), ids, cap, C.byref(nd)))
+        fin = [ids[i] for i in range(min(nd.value, cap))]
+        for rid in fin:
+            self._collect(rid)
+        return [self.requests[rid] for rid in fin]
 
     def serve(self, timeout=None):
         """Run until every submitted request is done (requests with future
         arrival times are admitted when the clock reaches them)."""
-        while self.pending or self.active:
-            if timeout is not None and self.now() > timeout:
+        t0 = time.perf_counter()
+        while len(self.done) < len(self.requests):
+            if timeout is not None and time.perf_counter() - t0 > timeout:
                 raise TimeoutError("serving did not drain in time")
-            if not self.active and self.pending and self.pending[0].arrival > self.now():
-                time.sleep(min(0.01, self.pending[0].arrival - self.now()))
-                continue
             self.step()
+            for rid, r in self.requests.items():  # requests the server could not prepare
+                if r.finished is None and not r.failed:
+                    rec = sph.ServeRecord()
+                    sph.check(sph.lib().sph_serve_request_info(self.h, rid, C.byref(rec)))
+                    if rec.state == sph.SERVE_FAILED:
+                        self._collect(rid)
         return self.done
 
     def report(self):
-        lat = np.array([r.latency for r in self.done if r.latency is not None])
-        wall = max((r.finished for r in self.done), default=0.0) - min((r.arrival for r in self.done), default=0.0)
+        st = sph.ServeSummary()
+        sph.check(sph.lib().sph_serve_stats(self.h, C.byref(st)))
         return {
-            "requests": len(self.done),
-            "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
-            "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
-            "mean_latency_s": float(lat.mean()) if lat.size else None,
-            "throughput_particle_steps_per_s": self.particle_steps / wall if wall > 0 else None,
-            "gpu_busy_particle_steps_per_s": self.particle_steps / self.busy_time if self.busy_time else None,
-            "particle_steps": self.particle_steps,
+            "requests": int(st.done),
+            "p50_latency_s": st.p50_latency_s if st.done else None,
+            "p99_latency_s": st.p99_latency_s if st.done else None,
+            "mean_latency_s": st.mean_latency_s if st.done else None,
+            "throughput_particle_steps_per_s": st.throughput or None,
+            "gpu_busy_particle_steps_per_s": st.busy_throughput or None,
+            "particle_steps": st.particle_steps,
+            "peak_device_bytes": st.peak_device_bytes,
         }
 
     def close(self):
+        if self.h:
+            sph.check(sph.lib().sph_serve_destroy(self.h))
+            self.h = C.c_void_p()
         self.ctx.close()
 
 

@@ -71,6 +71,30 @@ class Diagnostics(C.Structure):
                 ("u_max", C.c_double)]
 
 
+class Request(C.Structure):
+    """sph_request: one impact run submitted to a server."""
+    _fields_ = [("params", C.POINTER(Params)), ("lo", C.c_double * 3), ("hi", C.c_double * 3),
+                ("periodic", C.c_int32 * 3), ("flaws", C.c_int32), ("n", C.c_int64)] + [
+        (k, C.POINTER(C.c_double)) for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "u")] + [
+        ("mat", C.POINTER(C.c_int32)), ("fixed", C.POINTER(C.c_uint8)), ("h0", C.POINTER(C.c_double)),
+        ("flaw_dx", C.c_double), ("flaw_seed", C.c_uint32), ("reserved", C.c_int32), ("steps", C.c_int64),
+        ("arrival", C.c_double)]
+
+
+class ServeRecord(C.Structure):
+    _fields_ = [("n", C.c_int64), ("steps", C.c_int64), ("state", C.c_int32), ("impact", C.c_int32),
+                ("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double)]
+
+
+class ServeSummary(C.Structure):
+    _fields_ = [("done", C.c_int64), ("queued", C.c_int64), ("resident", C.c_int64)] + [
+        (k, C.c_double) for k in ("p50_latency_s", "p99_latency_s", "mean_latency_s", "particle_steps",
+                                  "throughput", "busy_throughput", "busy_s", "peak_device_bytes")]
+
+
+SERVE_FLAWS = {None: 0, "single": 1, "multi": 2}
+SERVE_QUEUED, SERVE_RESIDENT, SERVE_DONE, SERVE_FAILED = 0, 1, 2, 3
+
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
 _I64 = C.POINTER(C.c_int64)
@@ -141,6 +165,15 @@ _SIGS = {
     "sph_kernel_stats_reset": (C.c_int, [_P]),
     "sph_event_record": (C.c_int, [_P, C.c_int32]),
     "sph_event_elapsed": (C.c_int, [_P, C.c_int32, C.c_int32, _D]),
+    "sph_serve_create": (C.c_int, [_P, C.c_double, C.c_int32, C.c_char_p, C.POINTER(_P)]),
+    "sph_serve_destroy": (C.c_int, [_P]),
+    "sph_serve_now": (C.c_int, [_P, _D]),
+    "sph_serve_submit": (C.c_int, [_P, C.POINTER(Request), _I64]),
+    "sph_serve_poll": (C.c_int, [_P, C.c_double, _I64, C.c_int32, _I32]),
+    "sph_serve_request_info": (C.c_int, [_P, C.c_int64, C.POINTER(ServeRecord)]),
+    "sph_serve_result": (C.c_int, [_P, C.c_int64, C.c_char_p, _D]),
+    "sph_serve_release": (C.c_int, [_P, C.c_int64]),
+    "sph_serve_stats": (C.c_int, [_P, C.POINTER(ServeSummary)]),
 }
 
 KERNEL_CLASSES = ["kick", "sort", "grid", "list_density", "density", "eos", "list_force", "force",

@@ -276,6 +276,76 @@ int sph_cell_sort(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm
 int sph_cell_sort_static(const uint32_t* keys, int64_t n, int64_t ncells, int32_t* perm,
                          int32_t* cell_start, void* stream);
 
+/* ---- serving: continuous batching of impact runs ---------------------------
+ * Replaces the campaign's one-process-per-impact loop (boundary_daemon.py:
+ * 215-255 runs gpu_ic once per impact) with one resident server.  A server
+ * keeps one context busy with a stream of requests (one impact each): a
+ * request is admitted once it has arrived and its particles fit the device-
+ * memory budget beside the resident impacts (the engine's own allocations and
+ * its per-particle footprint at the current neighbour-list capacity),
+ * initialised in place while the others keep their state, advanced with them
+ * in chunks of device-controlled steps (own CFL dt and step limit each) and
+ * retired when it has taken its steps: its fields are copied to host memory and
+ * its slot and memory released.  Flaw seeding of queued requests runs on a
+ * worker thread of the server while the GPU works.  sph_serve_poll and every
+ * other call that touches the context belong to one thread (the serving
+ * thread); sph_serve_submit may be called from any thread.  A request's
+ * results do not depend on what else is resident. */
+typedef struct sph_server sph_server;
+enum sph_serve_flaws { SPH_SERVE_FLAWS_NONE = 0, SPH_SERVE_FLAWS_SINGLE = 1, SPH_SERVE_FLAWS_MULTI = 2 };
+enum sph_serve_state { SPH_SERVE_QUEUED = 0, SPH_SERVE_RESIDENT = 1, SPH_SERVE_DONE = 2, SPH_SERVE_FAILED = 3 };
+typedef struct sph_request {
+    const sph_params* params;   /* as sph_impact_create */
+    double lo[3], hi[3];        /* domain */
+    int32_t periodic[3];
+    int32_t flaws;              /* sph_serve_flaws: seeding as sph_impact_seed_damage /
+                                   sph_impact_seed_flaws_multi with flaw_dx, flaw_seed */
+    int64_t n;                  /* particles, arrays as sph_impact_add_particles */
+    const double *x, *y, *z, *vx, *vy, *vz, *mass, *u;
+    const int32_t* mat;         /* material ids of the server's context (NULL: 0) */
+    const uint8_t* fixed;       /* NULL: none fixed */
+    const double* h0;           /* NULL: h_init everywhere (sph_impact_set_h0) */
+    double flaw_dx;
+    uint32_t flaw_seed;
+    int32_t reserved;
+    int64_t steps;              /* KDK steps to take */
+    double arrival;             /* seconds on the server clock; < 0: now */
+} sph_request;
+typedef struct sph_serve_record {
+    int64_t n, steps;
+    int32_t state;              /* sph_serve_state */
+    int32_t impact;             /* impact id while resident */
+    double arrival, admitted, finished;   /* server clock, seconds (-1: not yet) */
+} sph_serve_record;
+typedef struct sph_serve_summary {
+    int64_t done, queued, resident;
+    double p50_latency_s, p99_latency_s, mean_latency_s;   /* arrival -> results in host memory */
+    double particle_steps;
+    double throughput;          /* particle-steps / (last finish - first arrival) */
+    double busy_throughput;     /* particle-steps / time spent advancing */
+    double busy_s;
+    double peak_device_bytes;   /* largest engine allocation seen after an admission */
+} sph_serve_summary;
+/* fields: comma-separated field names kept for each finished request (NULL:
+ * x,y,z,vx,vy,vz,u,rho,P,D); the server clock starts here. */
+int sph_serve_create(sph_ctx* ctx, double hbm_budget_bytes, int32_t chunk, const char* fields,
+                     sph_server** out);
+/* Stops the worker and removes the impacts still resident (the context stays). */
+int sph_serve_destroy(sph_server* srv);
+int sph_serve_now(sph_server* srv, double* t);
+/* Queues a copy of the request; *id receives its id. */
+int sph_serve_submit(sph_server* srv, const sph_request* req, int64_t* id);
+/* One serving round: admit, advance the residents by up to `chunk` steps,
+ * retire the finished ones (their ids in done_ids[cap], the count in *ndone).
+ * With nothing resident it waits up to max_wait_s for the next arrival. */
+int sph_serve_poll(sph_server* srv, double max_wait_s, int64_t* done_ids, int32_t cap, int32_t* ndone);
+int sph_serve_request_info(sph_server* srv, int64_t id, sph_serve_record* out);
+/* A finished request's field (n doubles, original particle order). */
+int sph_serve_result(sph_server* srv, int64_t id, const char* field, double* out);
+/* Frees a finished request's results. */
+int sph_serve_release(sph_server* srv, int64_t id);
+int sph_serve_stats(sph_server* srv, sph_serve_summary* out);
+
 /* ---- files (formats of run_ic.cpp / gpu_ic.cpp) ----------------------------
  * IC: f8 header [xlo xhi ylo yhi zlo zhi n], then n x [x y z vx vy vz mass u mat
  * fixed] (run_ic.cpp:4-6).  Creates an impact with the given parameters and

@@ -1,112 +1,74 @@
-"""Host logic of the continuous-batching server (deorbit_gb300/serve.py) on the
-CPU: FIFO admission under the HBM budget, arrival times, step limits, retirement
-and the latency report -- against a stand-in engine context that counts steps
-(the GPU path itself is covered by tests/test_gpu_serving.py)."""
-import types
+"""Host logic of the native continuous-batching server (sph_serve_* in
+libdeorbit_sph.so, deorbit_gb300/csrc/serve.cpp) on the CPU: FIFO admission
+under the device-memory budget, an oversized request served alone, arrival
+times, chunks that never overshoot a step limit, retirement with results kept
+in host memory, release, the latency report, and flaw seeding on the server's
+worker thread -- driven by tests/serve_harness.cpp against a stand-in engine
+that counts steps (the GPU path itself is covered by tests/test_gpu_serving.py)."""
+import os
+import subprocess
 
 import numpy as np
 import pytest
 
-from deorbit_gb300 import ic, serve
+from deorbit_gb300 import serve
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIBDIR = os.path.join(ROOT, "deorbit_gb300", "_lib")
 
 
-class CountingContext:
-    """Counts steps per impact the way the engine's step limits do."""
+@pytest.fixture(scope="module")
+def harness(cuda_lib, tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("serve") / "serve_harness")
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "deorbit_gb300", "csrc"), "-I", cuda_inc,
+           os.path.join(ROOT, "tests", "serve_harness.cpp"), "-o", exe, "-L", LIBDIR, "-ldeorbit_sph",
+           f"-Wl,-rpath,{LIBDIR}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
 
-    def __init__(self):
-        self.impacts = {}
-        self.next_id = 0
-        self.inits = 0
-        self.runs = []
-
-    def add(self, n):
-        b = self.next_id
-        self.next_id += 1
-        self.impacts[b] = {"n": n, "steps": 0, "limit": 0}
-        return b
-
-    def set_step_limit(self, b, steps):
-        self.impacts[b]["limit"] = steps
-
-    def init(self):
-        self.inits += 1
-
-    def run(self, steps):
-        self.runs.append((steps, sorted(self.impacts)))
-        for d in self.impacts.values():
-            d["steps"] = min(d["limit"], d["steps"] + steps)
-
-    def synchronize(self):
-        pass
-
-    def info(self, b):
-        return types.SimpleNamespace(steps=self.impacts[b]["steps"])
-
-    def read(self, b, name):
-        return np.zeros(self.impacts[b]["n"])
-
-    def remove(self, b):
-        del self.impacts[b]
-
-    def close(self):
-        pass
+    def run(case):
+        p = subprocess.run([exe, case], capture_output=True, text=True, timeout=60)
+        assert p.returncode == 0, p.stdout + p.stderr
+        return {line.split()[0]: line.split()[1:] for line in p.stdout.splitlines() if line.strip()}
+    return run
 
 
-@pytest.fixture
-def server(monkeypatch):
-    ctx = CountingContext()
-    monkeypatch.setattr(ic, "to_context", lambda c, sc, material_ids=None: c.add(sc.n))
-    srv = serve.Server(ctx=ctx, hbm_budget_bytes=2500 * 100, bytes_per_particle=100, chunk=4)
-    return srv, ctx
+def test_fifo_admission_within_budget(harness):
+    o = harness("fifo")
+    # two of three 1000-particle requests fit the 2500-particle budget
+    assert o["after_first_poll"][:3] == ["1", "1", "0"] and o["resident"] == ["2"]
+    assert o["order"] == ["0", "1", "2"] and o["third_admitted_after"] == ["1"]
 
 
-def scenario(n):
-    return types.SimpleNamespace(n=n)
+def test_oversized_request_runs_alone(harness):
+    o = harness("oversized")
+    assert o["after_first_poll"] == ["2", "0"]   # larger than the budget: admitted alone, the next waits
+    assert o["small_after_big"] == ["1"]
 
 
-def test_fifo_admission_within_budget(server):
-    srv, ctx = server
-    a = srv.submit(scenario(1000), 6, arrival=0.0)
-    b = srv.submit(scenario(1000), 6, arrival=0.0)
-    c = srv.submit(scenario(1000), 6, arrival=0.0)   # 3000 particles > the 2500 budget
-    srv.step()
-    assert a.admitted is not None and b.admitted is not None and c.admitted is None
-    assert set(ctx.impacts) == {a.impact, b.impact}
-    srv.serve(timeout=10.0)
-    assert c.admitted is not None and c.admitted >= max(a.finished, b.finished)
-    assert [r.rid for r in srv.done] == [0, 1, 2]
+def test_step_limits_and_chunks(harness):
+    o = harness("chunks")
+    # chunks never overshoot the nearest limit: 4, 1 (first done), 4 (second done)
+    assert o["runs"] == ["4", "1", "4"]
+    assert o["particle_steps"] == [str(100 * 4 * 2 + 100 * 1 * 2 + 100 * 4)]
+    assert o["done"] == ["2"] and o["residents_left"] == ["0"]   # every impact released
+    assert o["result_fields"] == ["0", "1"]   # kept fields read back in host memory
+    assert o["unkept_field_rc"] == ["-1"] and o["released_rc"] == ["-1"]
 
 
-def test_oversized_request_runs_alone(server):
-    srv, ctx = server
-    big = srv.submit(scenario(10_000), 3, arrival=0.0)   # larger than the whole budget
-    small = srv.submit(scenario(10), 3, arrival=0.0)
-    srv.step()
-    assert big.admitted is not None and small.admitted is None
-    srv.serve(timeout=10.0)
-    assert small.admitted >= big.finished
+def test_future_arrivals_wait_for_the_clock(harness):
+    o = harness("future")
+    assert o["not_yet"] == ["0"] and o["runs"] == ["0"]
+    assert o["admitted_after_arrival"] == ["1"] and o["done"] == ["1"] and o["p50_nonneg"] == ["1"]
+    assert o["particle_steps"] == ["200"]
 
 
-def test_step_limits_and_chunks(server):
-    srv, ctx = server
-    r1 = srv.submit(scenario(100), 5, arrival=0.0)
-    r2 = srv.submit(scenario(100), 9, arrival=0.0)
-    srv.serve(timeout=10.0)
-    # chunks never overshoot the nearest limit: 4, 1 (r1 done), 4 (r2 done)
-    assert [s for s, _ in ctx.runs] == [4, 1, 4]
-    assert srv.particle_steps == 100 * 4 * 2 + 100 * 1 * 2 + 100 * 4
-    assert r1.result is not None and set(r1.result) == set(serve.RESULT_FIELDS)
-    assert not ctx.impacts  # every impact released
-
-
-def test_future_arrivals_wait_for_the_clock(server):
-    srv, ctx = server
-    late = srv.submit(scenario(100), 2, arrival=srv.now() + 0.05)
-    assert srv.step() == 0 and late.admitted is None
-    srv.serve(timeout=10.0)
-    assert late.admitted >= late.arrival
-    rep = srv.report()
-    assert rep["requests"] == 1 and rep["p50_latency_s"] >= 0.0 and rep["particle_steps"] == 200
+def test_flaws_seeded_before_admission(harness):
+    o = harness("seeding")
+    # multi-flaw: ceil(N ln N) thresholds for 500 particles; single: eps_act only
+    assert o["flaws"] == [str(int(np.ceil(500 * np.log(500)))), "0"]
 
 
 def test_poisson_stream_shape():
