@@ -177,13 +177,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def time_form(sph, ic, sc, precision, steps, warmup, device):
+def time_form(sph, ic, sc, precision, steps, warmup, device, options=None):
     """Init (untimed), W warm-up steps, then exactly K timed steps in the
     production mode (captured CUDA graphs, no per-kernel events); then K more
-    steps with per-kernel CUDA events for the kernel breakdown (not timed)."""
+    steps with per-kernel CUDA events for the kernel breakdown (not timed).
+    options: engine options set after the tuned ones."""
     from deorbit_gb300 import autotune
     ctx = sph.Context(precision, device)
     autotune.apply(ctx, sc, precision, device)
+    for k, v in (options or {}).items():
+        ctx.set_option(k, v)
     b = ic.to_context(ctx, sc)
     ctx.init()
     ctx.run(max(warmup, 3))  # also captures the step graphs
@@ -486,6 +489,8 @@ def main():
                     help="particles of the accuracy-vs-oracle sample")
     ap.add_argument("--acc-steps", type=int, default=10)
     ap.add_argument("--no-acc", action="store_true")
+    ap.add_argument("--force-staging", type=int, default=None,
+                    help="mixed form: force-pass record staging (engine option force_staging)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
@@ -563,7 +568,8 @@ def main():
     # ---- mixed form (headline)
     barrier()
     with ClockSampler(device) as clk:
-        ctx, b, ms, kst, launches = time_form(sph, ic, sc, sph.MIXED, args.steps, args.warmup, device)
+        opts = {} if args.force_staging is None else {"force_staging": args.force_staging}
+        ctx, b, ms, kst, launches = time_form(sph, ic, sc, sph.MIXED, args.steps, args.warmup, device, opts)
     list_entries = ctx.get_option("list_entries")
     barrier()
     ms = max_over_ranks(ms)

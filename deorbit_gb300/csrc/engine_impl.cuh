@@ -1175,12 +1175,15 @@ public:
             set_tuning((int)value, 0);
         } else if (k == "force_staging") {
             const int fsv = (int)value;
-            if (!(value == fsv && (fsv == 0 || fsv == 22 || fsv == 23 || fsv == 42)))
-                throw SphError(SPH_ERR_ARG, "force_staging is 0 (off) or 10 x entries + stages: 22, 23, 42");
+            if (!(value == fsv && (fsv == 0 || fsv == 22 || fsv == 23 || fsv == 42 || fsv == 122 || fsv == 142)))
+                throw SphError(SPH_ERR_ARG, "force_staging is 0 (off), 10 x entries + stages with bulk copies "
+                                            "(22, 23, 42) or 100 + that with 16-byte async copies (122, 142)");
             if constexpr (sizeof(R) == 4) {
-                if (fsv == 22) allow_force_smem<2, 2>();
-                if (fsv == 23) allow_force_smem<2, 3>();
-                if (fsv == 42) allow_force_smem<4, 2>();
+                if (fsv == 22) allow_force_smem<2, 2, false>();
+                if (fsv == 23) allow_force_smem<2, 3, false>();
+                if (fsv == 42) allow_force_smem<4, 2, false>();
+                if (fsv == 122) allow_force_smem<2, 2, true>();
+                if (fsv == 142) allow_force_smem<4, 2, true>();
             }
             force_staging_ = fsv;
         } else {
@@ -1309,12 +1312,12 @@ private:
     }
     // The force pass; in the mixed form optionally with its neighbour records
     // staged in shared memory by bulk copies (option "force_staging").
-    template <int SE, int SS>
+    template <int SE, int SS, bool ASYNC>
     void launch_force_staged(unsigned grid) {
         using FS = ForceStaging<SE, SS>;
         static_assert(FS::kSmemBytes <= 227 * 1024, "force staging exceeds the shared memory of a block");
-        k_force<R, SE, SS><<<grid, FS::kBlock, FS::kSmemBytes, st_>>>(view(), wait_err_d_);
-        launched((const void*)k_force<R, SE, SS>);
+        k_force<R, SE, SS, ASYNC><<<grid, FS::kBlock, FS::kSmemBytes, st_>>>(view(), wait_err_d_);
+        launched((const void*)k_force<R, SE, SS, ASYNC>);
     }
     void launch_force() {
         if (N_ <= 0) return;
@@ -1324,22 +1327,24 @@ private:
         if constexpr (sizeof(R) == 4) {
             done = true;
             switch (force_staging_) {
-                case 22: launch_force_staged<2, 2>(grid); break;
-                case 23: launch_force_staged<2, 3>(grid); break;
-                case 42: launch_force_staged<4, 2>(grid); break;
+                case 22: launch_force_staged<2, 2, false>(grid); break;
+                case 23: launch_force_staged<2, 3, false>(grid); break;
+                case 42: launch_force_staged<4, 2, false>(grid); break;
+                case 122: launch_force_staged<2, 2, true>(grid); break;
+                case 142: launch_force_staged<4, 2, true>(grid); break;
                 default: done = false;
             }
         }
         if (!done) {
-            k_force<R, 0, 0><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
-            launched((const void*)k_force<R, 0, 0>);
+            k_force<R, 0, 0, false><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
+            launched((const void*)k_force<R, 0, 0, false>);
         }
         prof_end();
         launches_++;
     }
-    template <int SE, int SS>
+    template <int SE, int SS, bool ASYNC>
     void allow_force_smem() {
-        DSPH_CUDA(cudaFuncSetAttribute(k_force<R, SE, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        DSPH_CUDA(cudaFuncSetAttribute(k_force<R, SE, SS, ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ForceStaging<SE, SS>::kSmemBytes));
     }
 

@@ -441,6 +441,16 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
+// global -> shared 16-byte asynchronous copy through L1 (cp.async.ca), and the
+// arrival on a barrier once every cp.async this thread issued before it has
+// landed (the barrier's expected count includes this arrival)
+__device__ __forceinline__ void async16_g2s(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void async_arrive(uint64_t* bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Own-list addressing: entry t of particle k lives at nbr[4k + nbr_slot(t, ls)],
 // i.e. 4-entry blocks stored block-major, so one int4 load brings a lane four
 // entries and a warp's block loads are contiguous.
@@ -1497,7 +1507,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
-template <class R, int SE = 0, int SS = 0>
+// ASYNC selects the copy engine of the staging: false = one bulk copy per
+// entry (cp.async.bulk, TMA), true = six 16-byte cp.async per entry (the load
+// path through L1, completion tracked by cp.async.mbarrier.arrive).
+template <class R, int SE = 0, int SS = 0, bool ASYNC = false>
 static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(View<R> v, int32_t* wait_err) {
     using Acc = AccT<R>;
     constexpr bool kStaged = SS > 0 && sizeof(R) == 4;
@@ -1717,11 +1730,24 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
                 jb[q][0] = b2.x; jb[q][SE - 1] = b2.y;
             }
             const int nv = max(0, min(SE, cnt - t0));
-            mbar_arrive_tx(&bars[2 * q], 96u * (uint32_t)nv);
+            if constexpr (ASYNC) {
 #pragma unroll
-            for (int e = 0; e < SE; e++)
-                if (e < nv)
-                    bulk_g2s(mine + q * FS::kStageBytes + e * 96, v.fr + 6 * (int64_t)jb[q][e], 96u, &bars[2 * q]);
+                for (int e = 0; e < SE; e++)
+                    if (e < nv) {
+                        const float4* src = v.fr + 6 * (int64_t)jb[q][e];
+                        float4* dst = reinterpret_cast<float4*>(mine + q * FS::kStageBytes + e * 96);
+#pragma unroll
+                        for (int c = 0; c < 6; c++) async16_g2s(dst + c, src + c);
+                    }
+                async_arrive(&bars[2 * q]);
+            } else {
+                mbar_arrive_tx(&bars[2 * q], 96u * (uint32_t)nv);
+#pragma unroll
+                for (int e = 0; e < SE; e++)
+                    if (e < nv)
+                        bulk_g2s(mine + q * FS::kStageBytes + e * 96, v.fr + 6 * (int64_t)jb[q][e], 96u,
+                                 &bars[2 * q]);
+            }
         };
 #pragma unroll
         for (int q = 0; q < SS; q++) issue(q, q * SE);

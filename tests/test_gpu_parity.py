@@ -283,7 +283,7 @@ def test_diagnostics_match_host_reduction(sph_mod):
     ctx.close()
 
 
-@pytest.mark.parametrize("staging", [22, 23, 42])
+@pytest.mark.parametrize("staging", [22, 23, 42, 122, 142])
 def test_staged_force_pass_is_bit_identical(sph_mod, staging):
     """The force pass with its neighbour records staged in shared memory by
     bulk copies (entries x stages per lane) evaluates the same pairs in the same
