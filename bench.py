@@ -374,6 +374,19 @@ def batched_section(sph, ic, device, steps, warmup, count=256):
         ms = ctx.event_elapsed(0, 1)
         out[name] = {"value": n_tot * steps / (ms / 1000.0), "ms_per_step": ms / steps,
                      "gpu_launches": ctx.launches() - l0}
+        # the kernels' own device time per step (CUDA events around every launch,
+        # K further steps): what the graph-replayed step spends beyond it is the
+        # most one persistent launch of the whole step could remove
+        ctx.set_profiling(True)
+        ctx.kernel_stats_reset()
+        ctx.run(steps)
+        ctx.synchronize()
+        kst = ctx.kernel_stats()
+        ctx.set_profiling(False)
+        ksum = sum(v[0] for v in kst.values()) / steps
+        out[name]["kernel_sum_ms_per_step"] = ksum
+        out[name]["launches_per_step"] = out[name]["gpu_launches"] / steps
+        out[name]["beyond_kernels_ms_per_step"] = ms / steps - ksum
         ctx.close()
     sample = scs[:: max(1, count // 8)][:8]
     out["plain_fp64_single"] = {"value": plain_single_rate(sph, ic, sample, steps, device),
@@ -408,6 +421,7 @@ def large_section(sph, ic, device, steps, warmup, n_total=1 << 24):
             "n_particles": sc.n, "value": sc.n * steps / (ms / 1000.0), "ms_per_step": ms / steps,
             "ic_build_s": t_ic,
             "replica_mixed_vs_fp64_rel_l2": mixed_error(sph, ic, rep, steps, device),
+            "replica_vs_oracle": accuracy_vs_oracle(sph, ic, rep, steps, device),
             "replica_particles": rep.n}
 
 
