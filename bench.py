@@ -505,6 +505,9 @@ def main():
     ap.add_argument("--no-acc", action="store_true")
     ap.add_argument("--force-staging", type=int, default=None,
                     help="mixed form: force-pass record staging (engine option force_staging)")
+    ap.add_argument("--host-direct", type=int, default=None,
+                    help="mixed form: 0 sends host field buffers through device staging copies "
+                         "(engine option host_direct; default: kernels reach them directly)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
@@ -583,6 +586,8 @@ def main():
     barrier()
     with ClockSampler(device) as clk:
         opts = {} if args.force_staging is None else {"force_staging": args.force_staging}
+        if args.host_direct is not None:
+            opts["host_direct"] = args.host_direct
         ctx, b, ms, kst, launches = time_form(sph, ic, sc, sph.MIXED, args.steps, args.warmup, device, opts)
     list_entries = ctx.get_option("list_entries")
     barrier()
@@ -595,7 +600,9 @@ def main():
         r, el, nbytes, pinned = e2e_rate(sph, ctx, b, sc.n, args.steps, min(args.warmup, 2))
         el = max_over_ranks(el)
         e2e = {"value": world * sc.n * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes + 8, "pinned_host": pinned}
+               "d2h_bytes_per_step": nbytes + 8, "pinned_host": pinned,
+               "host_path": "direct (kernels over the CPU-GPU link)" if ctx.get_option("host_direct")
+               else "device staging copies"}
     ctx.close()
 
     # ---- plain FP64 form

@@ -330,6 +330,14 @@ public:
         DSPH_CUDA(cudaMemsetAsync(wait_err_d_, 0, sizeof(int32_t), st_));
         DSPH_CUDA(cudaMalloc(&ntask_, sizeof(int32_t)));
         DSPH_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
+        {
+            int pa = 0;
+            if (cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, dev_) != cudaSuccess) {
+                cudaGetLastError();
+                pa = 0;
+            }
+            pageable_access_ = pa != 0;
+        }
         DSPH_CUDA(cudaMallocHost(&flags_h_, sizeof(int32_t) * 4));
         DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t) * 4, st_));
         for (int i = 0; i < 6; i++) DSPH_CUDA(cudaEventCreate(&ev_[i]));
@@ -891,14 +899,48 @@ public:
     // gathers (reads) or scatters (writes) the neighbouring fields, each pair
     // ordered by an event, and both streams are synchronised once -- pinned
     // caller buffers stream at link speed.
+    // Address through which kernels reach a caller's host buffer directly over
+    // the coherent CPU-GPU link (page-locked memory, or any host memory where
+    // the device reads pageable memory through the host page tables), or null:
+    // then the buffer goes through a device staging copy.
+    void* host_direct(const void* p) {
+        if (!host_direct_ || !p) return nullptr;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if ((a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged) && a.devicePointer)
+            return a.devicePointer;
+        if (a.type == cudaMemoryTypeUnregistered && pageable_access_) return const_cast<void*>(p);
+        return nullptr;
+    }
+
     void read_fields(int b, int nf, const char* const* names, double* const* outs) override {
         ImpactH& h = imp(b);
         commit();
         if (h.n == 0 || nf <= 0) return;
         for (int f = 0; f < nf; f++)
             if (!with_column(names[f], [](auto*) {})) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
-        ensure_stage((int64_t)nf * h.n);
+        // fields whose buffers the device reaches directly: one kernel each,
+        // writing the caller's memory in original order
+        std::vector<int> staged;
         for (int f = 0; f < nf; f++) {
+            double* dst = static_cast<double*>(host_direct(outs[f]));
+            if (!dst) {
+                staged.push_back(f);
+                continue;
+            }
+            with_column(names[f], [&](auto* col) {
+                launch_n_raw(k_read_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, dst);
+            });
+        }
+        if (staged.empty()) {
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+            return;
+        }
+        ensure_stage((int64_t)nf * h.n);
+        for (int f : staged) {
             double* slice = stage_d_ + (int64_t)f * h.n;
             with_column(names[f], [&](auto* col) {
                 launch_n_raw(k_read_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, slice);
@@ -917,11 +959,28 @@ public:
         if (h.n == 0 || nf <= 0) return;
         for (int f = 0; f < nf; f++)
             if (!with_column(names[f], [](auto*) {})) throw SphError(SPH_ERR_ARG, std::string("unknown field ") + names[f]);
+        std::vector<int> staged;
+        for (int f = 0; f < nf; f++) {
+            const double* src = static_cast<const double*>(host_direct(ins[f]));
+            if (!src) {
+                staged.push_back(f);
+                continue;
+            }
+            with_column(names[f], [&](auto* col) {
+                launch_n_raw(k_write_col<std::remove_pointer_t<decltype(col)>>, h.n, col, pos_of_gid_, h.gid_base, h.n, src);
+            });
+            std::string nm(names[f]);
+            if (nm == "x" || nm == "y" || nm == "z" || nm == "hh") grid_valid_ = false;
+        }
+        if (staged.empty()) {
+            DSPH_CUDA(cudaStreamSynchronize(st_));  // the caller may reuse its buffers on return
+            return;
+        }
         ensure_stage((int64_t)nf * h.n);
         // the staging slices may still feed earlier work on the compute stream
         DSPH_CUDA(cudaEventRecord(copy_ev_, st_));
         DSPH_CUDA(cudaStreamWaitEvent(copy_st_, copy_ev_, 0));
-        for (int f = 0; f < nf; f++) {
+        for (int f : staged) {
             double* slice = stage_d_ + (int64_t)f * h.n;
             DSPH_CUDA(cudaMemcpyAsync(slice, ins[f], sizeof(double) * h.n, cudaMemcpyHostToDevice, copy_st_));
             DSPH_CUDA(cudaEventRecord(copy_ev_, copy_st_));
@@ -1173,6 +1232,8 @@ public:
             cell_factor_z_ = value;
         } else if (k == "block") {
             set_tuning((int)value, 0);
+        } else if (k == "host_direct") {
+            host_direct_ = value != 0;
         } else if (k == "force_staging") {
             const int fsv = (int)value;
             if (!(value == fsv && (fsv == 0 || fsv == 22 || fsv == 23 || fsv == 42 || fsv == 122 || fsv == 142)))
@@ -1194,6 +1255,8 @@ public:
         std::string k(key);
         if (k == "list_mode") return list_mode_;
         if (k == "force_staging") return force_staging_;
+        if (k == "host_direct") return host_direct_ ? 1 : 0;
+        if (k == "pageable_access") return pageable_access_ ? 1 : 0;
         if (k == "graphs") return use_graphs_ ? 1 : 0;
         if (k == "slack") return slack_;
         if (k == "cell_factor") return cell_factor_;
@@ -2164,6 +2227,8 @@ public:
     std::vector<int64_t> alloc_bytes_;  // sizes of allocs_, in the same order
     int64_t dev_bytes_ = 0;
     int force_staging_ = 0;
+    bool host_direct_ = true;      // field I/O reaches device-accessible host buffers directly
+    bool pageable_access_ = false; // the device reads pageable host memory (host page tables)
     int32_t* flags_h_ = nullptr;
     void* scratch_ = nullptr;
     size_t scratch_bytes_ = 0;
