@@ -506,8 +506,8 @@ def main():
     ap.add_argument("--force-staging", type=int, default=None,
                     help="mixed form: force-pass record staging (engine option force_staging)")
     ap.add_argument("--host-direct", type=int, default=None,
-                    help="mixed form: 0 sends host field buffers through device staging copies "
-                         "(engine option host_direct; default: kernels reach them directly)")
+                    help="mixed form: 1 lets kernels reach host field buffers directly over the "
+                         "CPU-GPU link (engine option host_direct; default: device staging copies)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")

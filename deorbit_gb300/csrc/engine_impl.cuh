@@ -2227,7 +2227,8 @@ public:
     std::vector<int64_t> alloc_bytes_;  // sizes of allocs_, in the same order
     int64_t dev_bytes_ = 0;
     int force_staging_ = 0;
-    bool host_direct_ = true;      // field I/O reaches device-accessible host buffers directly
+    bool host_direct_ = false;     // field I/O reaches device-accessible host buffers directly
+                                   // (option; measured no faster than the staging copies on GB300)
     bool pageable_access_ = false; // the device reads pageable host memory (host page tables)
     int32_t* flags_h_ = nullptr;
     void* scratch_ = nullptr;

@@ -315,7 +315,7 @@ def test_field_io_direct_and_staged_paths_agree(sph_mod):
     import torch
     sc = small_impact()
     names = ["x", "y", "z", "vx", "vy", "vz", "u", "hh", "D", "Sxy"]
-    rng = np.random.default_rng(8)
+    noise = {k: 1e-6 * np.random.default_rng(8 + i).standard_normal(sc.n) for i, k in enumerate(names)}
     out = {}
     for direct in (1, 0):
         ctx = sph_mod.Context(1)
@@ -324,7 +324,7 @@ def test_field_io_direct_and_staged_paths_agree(sph_mod):
         ctx.init()
         ctx.run(2)
         base = ctx.read_many(b, names)
-        new = {k: base[k] * (1.0 + 1e-6 * rng.standard_normal(sc.n)) for k in names}
+        new = {k: base[k] * (1.0 + noise[k]) for k in names}
         pinned = {k: torch.from_numpy(new[k].copy()).pin_memory().numpy() for k in names[:5]}
         ins = {**pinned, **{k: new[k].copy() for k in names[5:]}}   # both kinds of buffer in one call
         ctx.write_many(b, ins)
