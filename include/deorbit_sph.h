@@ -393,8 +393,16 @@ int sph_set_tuning(sph_ctx* ctx, int32_t block_threads, double cell_factor);
  * "cell_factor_z" (traversal cell height over width, (0, 4]; like
  * "cell_factor", set before particles are committed), "block", "slack"
  * (neighbour-list radius slack), "graphs" (1: sph_step and sph_run replay
- * captured CUDA graphs); read-only "list_capacity" (entries per particle) and
- * "list_entries" (entries of the current lists, own plus reverse). */
+ * captured CUDA graphs), "force_staging" (mixed form: neighbour records of
+ * the force pass staged in shared memory; 0 off, 22 / 23 / 42 bulk copies of
+ * 2 or 4 entries x 2 or 3 stages, 122 / 142 16-byte async copies),
+ * "host_direct" (1: field reads and writes reach device-accessible host
+ * buffers directly over the CPU-GPU link; 0: device staging copies);
+ * read-only "list_capacity" (entries per particle), "list_entries" (entries
+ * of the current lists, own plus reverse), "device_bytes" (the context's
+ * device allocations), "bytes_per_particle" (device bytes per particle of
+ * capacity at the current list capacity) and "pageable_access" (1 where the
+ * device reads pageable host memory). */
 int sph_set_option(sph_ctx* ctx, const char* key, double value);
 int sph_get_option(sph_ctx* ctx, const char* key, double* value);
 /* Number of kernel launches issued by this context since creation. */
