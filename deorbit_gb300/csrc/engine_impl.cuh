@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -99,7 +100,7 @@ static __global__ void k_debug_nbr(View<R> v, int b, int kind, int32_t* out, int
     const float Rs = (kind == 0 ? 2.0f * pi.w : pi.w + I.hmax_f) + 2.0f * m;
     const double hi = (double)v.hh[k];
     int cnt = 0;
-    traverse(v, I, pi, ci, Rs, [&](int32_t j, float, float, float) {
+    traverse<R, true>(v, I, pi, ci, Rs, [&](int32_t j, float, float, float) {
         if (!ref_member(bi, v.refbin[j], I)) return;
         double dx, dy, dz;
         double r = sep_exact(v, I, k, j, dx, dy, dz);
@@ -1232,6 +1233,10 @@ public:
             cell_factor_z_ = value;
         } else if (k == "block") {
             set_tuning((int)value, 0);
+        } else if (k == "levels") {
+            for (auto& h : imp_)
+                if (h.committed) throw SphError(SPH_ERR_STATE, "levels are set before particles are committed");
+            levels_ = value != 0;
         } else if (k == "host_direct") {
             host_direct_ = value != 0;
         } else if (k == "force_staging") {
@@ -1256,6 +1261,8 @@ public:
         if (k == "list_mode") return list_mode_;
         if (k == "force_staging") return force_staging_;
         if (k == "host_direct") return host_direct_ ? 1 : 0;
+        if (k == "levels") return levels_ ? 1 : 0;
+        if (k == "levels_active") return levels_active_ ? 1 : 0;
         if (k == "pageable_access") return pageable_access_ ? 1 : 0;
         if (k == "graphs") return use_graphs_ ? 1 : 0;
         if (k == "slack") return slack_;
@@ -1387,7 +1394,7 @@ private:
         prof_begin();
         const unsigned grid = (unsigned)((N_ + 127) / 128);
         bool done = false;
-        if constexpr (sizeof(R) == 4) {
+        if (sizeof(R) == 4 && !levels_active_) {
             done = true;
             switch (force_staging_) {
                 case 22: launch_force_staged<2, 2, false>(grid); break;
@@ -1398,7 +1405,10 @@ private:
                 default: done = false;
             }
         }
-        if (!done) {
+        if (levels_active_) {  // graded impacts resident: the level-aware pass (never staged)
+            k_force<R, 0, 0, false, true><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
+            launched((const void*)k_force<R, 0, 0, false, true>);
+        } else if (!done) {
             k_force<R, 0, 0, false><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
             launched((const void*)k_force<R, 0, 0, false>);
         }
@@ -1629,15 +1639,86 @@ public:
             I.Lf[a] = (float)(h.dhi[a] - h.dlo[a]);
         }
         I.ncells = cells;
+        I.nlev = 1;
+        I.lev_h0[0] = 0.0f;
+        I.lev_base[0] = 0;
+        for (int a = 0; a < 3; a++) {
+            I.lev_lo[0][a] = 0;
+            I.lev_nf[0][a] = I.nf[a];
+        }
+        make_levels(I, h, budget);
+    }
+
+    // Levels of a graded impact: power-of-two bands of the reference smoothing
+    // length h0 above its smallest value, each with cells 2^L base cells wide
+    // over the box of its particles (padded by a tenth of the domain per side,
+    // at least two level cells), when the h0 range spans more than a factor 2.
+    void make_levels(ImpactD& I, const ImpactH& h, int64_t budget) {
+        if (!levels_ || !h.use_h0 || h.per[0] || h.per[1] || h.per[2] || h.sh0.empty()) return;
+        float h0min = 3.4e38f, h0max = 0.0f;
+        for (double v0 : h.sh0) {
+            h0min = std::min(h0min, (float)v0);
+            h0max = std::max(h0max, (float)v0);
+        }
+        if (!(h0min > 0.0f) || !(h0max >= 2.0f * h0min)) return;
+        int nlev = 1;
+        while (nlev < kMaxLevels && h0max >= h0min * (float)(1 << nlev)) nlev++;
+        float th[kMaxLevels];
+        th[0] = 0.0f;
+        for (int L = 1; L < nlev; L++) th[L] = h0min * (float)(1 << L);
+        int lo[kMaxLevels][3], hi[kMaxLevels][3];
+        for (int L = 0; L < nlev; L++)
+            for (int a = 0; a < 3; a++) { lo[L][a] = INT_MAX; hi[L][a] = INT_MIN; }
+        const std::vector<double>* P[3] = {&h.sx, &h.sy, &h.sz};
+        for (int64_t i = 0; i < h.n; i++) {
+            const float v0 = (float)h.sh0[i];
+            int L = 0;
+            while (L + 1 < nlev && v0 >= th[L + 1]) L++;
+            for (int a = 0; a < 3; a++) {
+                const double q = ((*P[a])[i] - I.glo[a]) * I.iw[a];
+                int ib = q < 0 ? 0 : (q >= I.nf[a] ? I.nf[a] - 1 : (int)std::floor(q));
+                lo[L][a] = std::min(lo[L][a], ib >> L);
+                hi[L][a] = std::max(hi[L][a], ib >> L);
+            }
+        }
+        int64_t total = 0, lbase[kMaxLevels];
+        int llo[kMaxLevels][3], lnf[kMaxLevels][3];
+        for (int L = 0; L < nlev; L++) {
+            int64_t cells = 1;
+            for (int a = 0; a < 3; a++) {
+                const int top = (I.nf[a] - 1) >> L;
+                if (lo[L][a] > hi[L][a]) { lo[L][a] = 0; hi[L][a] = 0; }  // an empty level: one cell
+                const int pad = std::max(2, (int)std::ceil(0.1 * (double)I.nf[a] / (double)(1 << L)));
+                llo[L][a] = std::max(0, lo[L][a] - pad);
+                const int e = std::min(top, hi[L][a] + pad);
+                lnf[L][a] = e - llo[L][a] + 1;
+                cells *= lnf[L][a];
+            }
+            lbase[L] = total;
+            total += cells;
+        }
+        if (total > budget) return;  // keep one grid
+        I.nlev = nlev;
+        for (int L = 0; L < nlev; L++) {
+            I.lev_h0[L] = th[L];
+            I.lev_base[L] = lbase[L];
+            for (int a = 0; a < 3; a++) {
+                I.lev_lo[L][a] = llo[L][a];
+                I.lev_nf[L][a] = lnf[L][a];
+            }
+        }
+        I.ncells = total;
     }
 
     void assign_cell_bases() {
         int64_t base = 0;
+        levels_active_ = false;
         for (size_t b = 0; b < imp_.size(); b++) {
             ImpactD& I = tab_[b];
             if (imp_[b].used && imp_[b].alive && imp_[b].committed) {
                 I.cell_base = base;
                 base += I.ncells;
+                levels_active_ = levels_active_ || I.nlev > 1;
             } else {
                 I.cell_base = 0;
                 I.alive = 0;
@@ -2032,7 +2113,7 @@ public:
             DSPH_CUDA(cudaMemsetAsync(flags_d_, 0, sizeof(int32_t), st_));
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 2, 0, sizeof(int32_t), st_));
             DSPH_CUDA(cudaMemsetAsync(xcnt_, 0, sizeof(int32_t) * N_, st_));
-            if (list_mode_ == 1) {
+            if (list_mode_ == 1 && !levels_active_) {  // graded impacts: the per-thread builder
                 DSPH_CUDA(cudaMemsetAsync(ntask_, 0, sizeof(int32_t), st_));
                 launch_n_raw(k_column_tasks<R>, N_, view(), tasks_, ntask_);
                 const int grid = std::max(1, std::min<int>(nsm_ * 8, (int)((N_ / 16 + 255) / 256) + 1));
@@ -2041,7 +2122,7 @@ public:
                 launched((const void*)k_list_warp<R>);
                 prof_end();
                 launches_++;
-            } else if (list_mode_ == 2) {
+            } else if (list_mode_ == 2 && !levels_active_) {
                 prof_begin();
                 k_list_wpp<R><<<(unsigned)((N_ + 7) / 8), 256, 0, st_>>>(view());
                 launched((const void*)k_list_wpp<R>);
@@ -2066,8 +2147,13 @@ public:
     void launch_list_thread(int refresh) {
         const int bs = block_ > 0 ? block_ : 256;
         prof_begin();
-        k_list_thread<R><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
-        launched((const void*)k_list_thread<R>);
+        if (levels_active_) {
+            k_list_thread<R, true><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
+            launched((const void*)k_list_thread<R, true>);
+        } else {
+            k_list_thread<R><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
+            launched((const void*)k_list_thread<R>);
+        }
         prof_end();
         launches_++;
     }
@@ -2121,7 +2207,10 @@ public:
             launch_small(k_ref_grid, nimp);
             launch_n(k_ref_bins<R>, N_);
             cls(KC_DENSITY);
-            if (iters > 0) launch_n_raw(k_density<R>, N_, view(), iters);  // also reduces the new max h
+            if (iters > 0) {  // also reduces the new max h
+                if (levels_active_) launch_n_raw(k_density<R, true>, N_, view(), iters);
+                else launch_n_raw(k_density<R>, N_, view(), iters);
+            }
             else hmax_pass(1);
             cls(KC_GRID);
             DSPH_CUDA(cudaMemsetAsync(flags_d_ + 1, 0, sizeof(int32_t), st_));
@@ -2227,6 +2316,8 @@ public:
     std::vector<int64_t> alloc_bytes_;  // sizes of allocs_, in the same order
     int64_t dev_bytes_ = 0;
     int force_staging_ = 0;
+    bool levels_ = false;          // traversal-grid levels for impacts with a wide h0 range
+    bool levels_active_ = false;   // some resident impact has levels
     bool host_direct_ = false;     // field I/O reaches device-accessible host buffers directly
                                    // (option; measured no faster than the staging copies on GB300)
     bool pageable_access_ = false; // the device reads pageable host memory (host page tables)

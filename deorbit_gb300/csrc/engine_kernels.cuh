@@ -34,6 +34,7 @@ constexpr int kListDensity = 0;
 constexpr int kListForce = 1;
 constexpr int kListSuperset = 2;
 constexpr int kExtraCap = 32;   // reverse-pair entries per particle
+constexpr int kMaxLevels = 4;   // traversal-grid levels of an impact (graded lattices)
 
 // Per-impact parameters and per-step scalars, resident on the device.
 struct ImpactD {
@@ -66,6 +67,17 @@ struct ImpactD {
     int64_t gid_base;
     unsigned long long hmax_bits, hm_bits, dt_bits;
     unsigned int omax_bits, pad1;                  // max |offset from the cell origin|
+    // Traversal-grid levels (graded lattices; nlev = 1 otherwise): level L holds
+    // the particles with lev_h0[L] <= h0 < lev_h0[L + 1]; its cells are 2^L base
+    // cells wide on every axis and cover the box lev_lo .. lev_lo + lev_nf - 1
+    // (in level cells); its cell ids start at cell_base + lev_base[L].  Particles
+    // keep base-grid coordinates of their cell's origin, so pair separations
+    // are formed exactly as on one grid.
+    int32_t nlev, lev_esc;                         // lev_esc bit L: level L had clamped particles
+    unsigned int lev_esc_next, pad3;               // gathered by the key pass for the next traversals
+    float lev_h0[kMaxLevels];
+    int32_t lev_lo[kMaxLevels][3], lev_nf[kMaxLevels][3];
+    int64_t lev_base[kMaxLevels];
 };
 
 template <class R>
@@ -263,12 +275,96 @@ __device__ __forceinline__ double sep_exact(const View<R>& v, const ImpactD& I, 
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
 }
 
+// traverse_sphere() on the levels of a graded impact (non-periodic): for every
+// level, the cell columns of its box that meet the sphere of radius Rs and, per
+// column, the level cells of the sphere's chord.  Ranges are formed in base
+// cells relative to the particle's own cell (as on one grid) and shifted to the
+// level, widened by 1e-5 base cells: a range may gain a cell, never lose one.
+// A level none of whose particles was clamped into its box is skipped when the
+// sphere's range misses the box; box border columns are never pruned, so
+// clamped particles are met as on one grid.  f(j, dxc, dyc, dzc) as in
+// traverse(), with the cell-origin differences in base cells.
+template <class R, class F>
+__device__ __forceinline__ void traverse_levels(const View<R>& v, const ImpactD& I, float4 pi, uint32_t ci,
+                                             float Rs, F&& f) {
+    constexpr float kWiden = 1.0e-5f;
+    int c[3];
+    unpack_cell(ci, c[0], c[1], c[2]);
+    const float o[3] = {pi.x, pi.y, pi.z};
+    int blo[3], bhi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        blo[a] = c[a] + (int)floorf((o[a] - Rs) * I.iwf[a] - kWiden);
+        bhi[a] = c[a] + (int)floorf((o[a] + Rs) * I.iwf[a] + kWiden);
+    }
+    const float R2 = Rs * Rs;
+    const float w0 = I.wf[0], w1 = I.wf[1], w2 = I.wf[2];
+    for (int L = 0; L < I.nlev; L++) {
+        const int lo0 = I.lev_lo[L][0], lo1 = I.lev_lo[L][1], lo2 = I.lev_lo[L][2];
+        const int e0 = lo0 + I.lev_nf[L][0] - 1, e1 = lo1 + I.lev_nf[L][1] - 1, e2 = lo2 + I.lev_nf[L][2] - 1;
+        int l0 = blo[0] >> L, h0 = bhi[0] >> L, l1 = blo[1] >> L, h1 = bhi[1] >> L;
+        const int l2 = blo[2] >> L, h2 = bhi[2] >> L;
+        if (!((I.lev_esc >> L) & 1) &&
+            (h0 < lo0 || l0 > e0 || h1 < lo1 || l1 > e1 || h2 < lo2 || l2 > e2))
+            continue;  // no particle of this level can be within Rs
+        l0 = l0 < lo0 ? lo0 : (l0 > e0 ? e0 : l0);
+        h0 = h0 < lo0 ? lo0 : (h0 > e0 ? e0 : h0);
+        l1 = l1 < lo1 ? lo1 : (l1 > e1 ? e1 : l1);
+        h1 = h1 < lo1 ? lo1 : (h1 > e1 ? e1 : h1);
+        const float wl0 = w0 * (float)(1 << L), wl1 = w1 * (float)(1 << L);
+        const int n1 = I.lev_nf[L][1], n2 = I.lev_nf[L][2];
+        const int64_t lbase = I.cell_base + I.lev_base[L] - lo2;
+        for (int ix = l0; ix <= h0; ix++) {
+            const float xa = (float)((ix << L) - c[0]) * w0 - o[0];  // column x-interval [xa, xa + wl0) rel. to i
+            float bx = xa > 0.0f ? xa : (xa + wl0 < 0.0f ? -(xa + wl0) : 0.0f);
+            if (ix == lo0 || ix == e0) bx = 0.0f;
+            const float dxc = (float)(c[0] - (ix << L)) * w0;
+            for (int iy = l1; iy <= h1; iy++) {
+                const float ya = (float)((iy << L) - c[1]) * w1 - o[1];
+                float by = ya > 0.0f ? ya : (ya + wl1 < 0.0f ? -(ya + wl1) : 0.0f);
+                if (iy == lo1 || iy == e1) by = 0.0f;
+                const float d2 = bx * bx + by * by;
+                if (d2 >= R2) continue;
+                const float hz = sqrtf(R2 - d2);
+                int zl = (c[2] + (int)floorf((o[2] - hz) * I.iwf[2] - kWiden)) >> L;
+                int zh = (c[2] + (int)floorf((o[2] + hz) * I.iwf[2] + kWiden)) >> L;
+                zl = zl < lo2 ? lo2 : (zl > e2 ? e2 : zl);
+                zh = zh < lo2 ? lo2 : (zh > e2 ? e2 : zh);
+                const float dyc = (float)(c[1] - (iy << L)) * w1;
+                const int64_t colbase = lbase + ((int64_t)(ix - lo0) * n1 + (iy - lo1)) * n2;
+                int cz = zl;
+                const int32_t s0 = v.cell_ptr[colbase + zl];
+                const int32_t e = v.cell_ptr[colbase + zh + 1];
+                int32_t next = v.cell_ptr[colbase + cz + 1];
+                float dzc = (float)(c[2] - (cz << L)) * w2;
+                for (int32_t j = s0; j < e; j++) {
+                    while (j >= next) {
+                        cz++;
+                        next = v.cell_ptr[colbase + cz + 1];
+                        dzc = (float)(c[2] - (cz << L)) * w2;
+                    }
+                    f(j, dxc, dyc, dzc);
+                }
+            }
+        }
+    }
+}
+
 // Visit every traversal cell column that intersects the sphere of radius Rs
 // around particle k (sorted index), cell by cell; calls f(j, dxc, dyc, dzc)
 // where d?c are the FP32 cell-origin differences (i's cell minus j's cell).
-template <class R, class F>
+// LV: the kernel also serves impacts with traversal-grid levels (instantiated
+// only where a resident impact has them, so that the one-grid kernels keep
+// their register allocation).
+template <class R, bool LV = false, class F>
 __device__ __forceinline__ void traverse(const View<R>& v, const ImpactD& I, float4 pi,
                                          uint32_t ci, float Rs, F&& f) {
+    if constexpr (LV) {
+        if (I.nlev > 1) {  // graded impacts (never periodic)
+            traverse_levels(v, I, pi, ci, Rs, f);
+            return;
+        }
+    }
     int c[3];
     unpack_cell(ci, c[0], c[1], c[2]);
     const float o[3] = {pi.x, pi.y, pi.z};
@@ -328,12 +424,18 @@ __device__ __forceinline__ void traverse(const View<R>& v, const ImpactD& I, flo
 // sphere and, per column, only the z-cells within the sphere's chord there
 // (non-periodic impacts; periodic ones use the full box).  Border columns are
 // never pruned by x / y because clamped particles may lie outside their cell.
-template <class R, class F>
+template <class R, bool LV = false, class F>
 __device__ __forceinline__ void traverse_sphere(const View<R>& v, const ImpactD& I, float4 pi,
                                                 uint32_t ci, float Rs, F&& f) {
     if (I.per[0] | I.per[1] | I.per[2]) {
         traverse(v, I, pi, ci, Rs, f);
         return;
+    }
+    if constexpr (LV) {
+        if (I.nlev > 1) {
+            traverse_levels(v, I, pi, ci, Rs, f);
+            return;
+        }
     }
     int c[3];
     unpack_cell(ci, c[0], c[1], c[2]);
@@ -539,10 +641,45 @@ __device__ __forceinline__ unsigned int fine_keys_one(const View<R>& v, const Im
     const float h = (float)v.hh[k];  // loaded before the stores below
     const int32_t gid = v.gid[k];
     float ox, oy, oz;
-    const int cx = fine_cell(I, 0, v.x[k], ox);
-    const int cy = fine_cell(I, 1, v.y[k], oy);
-    const int cz = fine_cell(I, 2, v.z[k], oz);
-    const int64_t key = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2] + cz;
+    int cx, cy, cz;
+    int64_t key;
+    if (I.nlev <= 1) {
+        cx = fine_cell(I, 0, v.x[k], ox);
+        cy = fine_cell(I, 1, v.y[k], oy);
+        cz = fine_cell(I, 2, v.z[k], oz);
+        key = I.cell_base + ((int64_t)cx * I.nf[1] + cy) * I.nf[2] + cz;
+    } else {
+        // the particle's level from its reference smoothing length, its cell in
+        // that level's box (clamped, noted), and the cell's origin in base cells
+        const float h0 = (float)v.h0[k];
+        int L = 0;
+        while (L + 1 < I.nlev && h0 >= I.lev_h0[L + 1]) L++;
+        const double pc[3] = {v.x[k], v.y[k], v.z[k]};
+        int cb[3];
+        float off[3];
+        bool clamped = false;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double d = pc[a] - I.glo[a];
+            const float qf = (float)d * I.iwf[a];
+            int ib = qf >= 2147483520.0f ? 2147483647 : (qf == qf ? (int)floorf(qf) : 0);
+            if (ib < 0) { ib = 0; clamped = true; }
+            if (ib >= I.nf[a]) { ib = I.nf[a] - 1; clamped = true; }
+            int il = ib >> L;
+            const int lo = I.lev_lo[L][a], hi = lo + I.lev_nf[L][a] - 1;
+            if (il < lo) { il = lo; clamped = true; }
+            if (il > hi) { il = hi; clamped = true; }
+            cb[a] = il << L;
+            off[a] = (float)fma(-(double)cb[a], I.w[a], d);
+        }
+        if (clamped) atomicOr(const_cast<unsigned int*>(&I.lev_esc_next), 1u << L);
+        cx = cb[0]; cy = cb[1]; cz = cb[2];
+        ox = off[0]; oy = off[1]; oz = off[2];
+        key = I.cell_base + I.lev_base[L] +
+              ((int64_t)((cx >> L) - I.lev_lo[L][0]) * I.lev_nf[L][1] + ((cy >> L) - I.lev_lo[L][1])) *
+                  I.lev_nf[L][2] +
+              ((cz >> L) - I.lev_lo[L][2]);
+    }
     keys_by_gid[gid] = (uint32_t)key;
     atomicAdd(&cell_count[key], 1);
     pf_out[k] = make_float4(ox, oy, oz, h);
@@ -651,6 +788,8 @@ static __global__ void k_impact_ranges(ImpactD* imps, int nimp, const int32_t* c
     int64_t s = cell_ptr[I.cell_base], e = cell_ptr[I.cell_base + I.ncells];
     I.off = s;
     I.n = e - s;
+    I.lev_esc = (int32_t)I.lev_esc_next;  // the key pass of this sort
+    I.lev_esc_next = 0u;
     // FP32 filter margin: bounds the rounding of offsets and cell-origin terms
     float om = __uint_as_float(I.omax_bits);
     float wmax = fmaxf(fmaxf(I.wf[0], I.wf[1]), I.wf[2]);
@@ -788,7 +927,7 @@ __device__ __forceinline__ float list_r2(float4 a, float4 b) {
 
 // One particle's list by its own traversal (periodic impacts, and warps that
 // straddle two impacts).
-template <class R>
+template <class R, bool LV = false>
 __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int64_t k) {
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
@@ -801,7 +940,7 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
     int cnt = 0;
     const int cap = v.cap;
     int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
-    traverse_sphere(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
+    traverse_sphere<R, LV>(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
         float r2, hj;
         if (!periodic) {
             const float4 lj = v.lf[j];
@@ -835,6 +974,74 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
     if (cnt > cap) atomicMax(&v.flags[0], cnt);
 }
 
+// The warp-union walk of the list build on the levels of a graded impact
+// (all 32 lanes in one impact, non-periodic): level by level, the warp walks
+// the union of its lanes' level-cell column boxes; each lane takes the columns
+// of its own box that meet its sphere, over the level cells of its own chord,
+// and run(s, len) tests the lane's candidates s .. s + len - 1 (len = 0 where
+// the lane takes nothing; run reduces over the warp).  Every lane meets the
+// columns and cells of traverse_levels() in its order, so the lists equal
+// those of the per-thread build entry for entry.
+template <class R, class Run>
+__device__ __forceinline__ void warp_walk_levels(const View<R>& v, const ImpactD& I, bool act, float4 pi,
+                                                 uint32_t ci, float Rs, Run&& run) {
+    const unsigned full = 0xffffffffu;
+    constexpr float kWiden = 1.0e-5f;
+    int c[3];
+    unpack_cell(ci, c[0], c[1], c[2]);
+    const float o[3] = {pi.x, pi.y, pi.z};
+    int blo[3], bhi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        blo[a] = c[a] + (int)floorf((o[a] - Rs) * I.iwf[a] - kWiden);
+        bhi[a] = c[a] + (int)floorf((o[a] + Rs) * I.iwf[a] + kWiden);
+    }
+    const float R2 = Rs * Rs;
+    const float w0 = I.wf[0], w1 = I.wf[1];
+    const int nlev = I.nlev;
+    for (int L = 0; L < nlev; L++) {
+        const int lo0 = I.lev_lo[L][0], lo1 = I.lev_lo[L][1], lo2 = I.lev_lo[L][2];
+        const int e0 = lo0 + I.lev_nf[L][0] - 1, e1 = lo1 + I.lev_nf[L][1] - 1, e2 = lo2 + I.lev_nf[L][2] - 1;
+        int l0 = blo[0] >> L, h0 = bhi[0] >> L, l1 = blo[1] >> L, h1 = bhi[1] >> L;
+        const int l2 = blo[2] >> L, h2 = bhi[2] >> L;
+        const bool lane = act && (((I.lev_esc >> L) & 1) ||
+                                  !(h0 < lo0 || l0 > e0 || h1 < lo1 || l1 > e1 || h2 < lo2 || l2 > e2));
+        l0 = l0 < lo0 ? lo0 : (l0 > e0 ? e0 : l0);
+        h0 = h0 < lo0 ? lo0 : (h0 > e0 ? e0 : h0);
+        l1 = l1 < lo1 ? lo1 : (l1 > e1 ? e1 : l1);
+        h1 = h1 < lo1 ? lo1 : (h1 > e1 ? e1 : h1);
+        const int ul0 = __reduce_min_sync(full, lane ? l0 : INT_MAX), uh0 = __reduce_max_sync(full, lane ? h0 : INT_MIN);
+        const int ul1 = __reduce_min_sync(full, lane ? l1 : INT_MAX), uh1 = __reduce_max_sync(full, lane ? h1 : INT_MIN);
+        const float wl0 = w0 * (float)(1 << L), wl1 = w1 * (float)(1 << L);
+        const int n1 = I.lev_nf[L][1], n2 = I.lev_nf[L][2];
+        const int64_t lbase = I.cell_base + I.lev_base[L] - lo2;
+        for (int ix = ul0; ix <= uh0; ix++) {  // empty when no lane meets this level
+            const float xa = (float)((ix << L) - c[0]) * w0 - o[0];
+            float bx = xa > 0.0f ? xa : (xa + wl0 < 0.0f ? -(xa + wl0) : 0.0f);
+            if (ix == lo0 || ix == e0) bx = 0.0f;
+            const bool in_x = lane && ix >= l0 && ix <= h0;
+            for (int iy = ul1; iy <= uh1; iy++) {
+                const float ya = (float)((iy << L) - c[1]) * w1 - o[1];
+                float by = ya > 0.0f ? ya : (ya + wl1 < 0.0f ? -(ya + wl1) : 0.0f);
+                if (iy == lo1 || iy == e1) by = 0.0f;
+                const float d2 = bx * bx + by * by;
+                int32_t s = 0, len = 0;
+                if (in_x && iy >= l1 && iy <= h1 && d2 < R2) {
+                    const float hz = sqrtf(R2 - d2);
+                    int zl = (c[2] + (int)floorf((o[2] - hz) * I.iwf[2] - kWiden)) >> L;
+                    int zh = (c[2] + (int)floorf((o[2] + hz) * I.iwf[2] + kWiden)) >> L;
+                    zl = zl < lo2 ? lo2 : (zl > e2 ? e2 : zl);
+                    zh = zh < lo2 ? lo2 : (zh > e2 ? e2 : zh);
+                    const int64_t colbase = lbase + ((int64_t)(ix - lo0) * n1 + (iy - lo1)) * n2;
+                    s = v.cell_ptr[colbase + zl];
+                    len = v.cell_ptr[colbase + zh + 1] - s;
+                }
+                run(s, len);
+            }
+        }
+    }
+}
+
 // Neighbour-list build, one thread per particle k.  Each particle searches only
 // its own sphere of radius 2 h_k (1 + slack) and records
 //   own list   every j with r < 2 h_k (1 + s)  -- a superset of the density set
@@ -862,7 +1069,7 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
 //
 // refresh != 0: rebuild only the lists of impacts whose h outgrew the slack in
 // this step's density rounds (the others return at once).
-template <class R>
+template <class R, bool LV = false>
 static __global__ void k_list_thread(View<R> v, int refresh) {
     const unsigned full = 0xffffffffu;
     const int64_t k0 = gtid();
@@ -873,7 +1080,7 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
     const bool wanted = I.mask && (!refresh || I.slack_flag);
     const bool one_impact = __all_sync(full, ib == __shfl_sync(full, ib, 0));
     if (!one_impact || (I.per[0] | I.per[1] | I.per[2])) {
-        if (inb && wanted) list_one(v, I, k);
+        if (inb && wanted) list_one<R, LV>(v, I, k);
         return;
     }
     if (!wanted) return;  // warp-uniform: one impact
@@ -887,6 +1094,44 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
     const float ri2 = ri * ri;
     const float Rs = ri + m;
     const float R2 = Rs * Rs;
+    int cnt = 0;
+    const int cap = v.cap;
+    int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
+    auto take = [&](int32_t j, float4 lj, float r2) {
+        if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
+        cnt++;
+        const float rj = 2.0f * lj.w * sl + m;
+        const float rb = (pi.w + lj.w) * sl + m;
+        if (!(r2 < rj * rj) && r2 < rb * rb) {
+            const int slot = atomicAdd(&v.xcnt[j], 1);
+            if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
+        }
+    };
+    // two candidates per trip: independent load / distance chains, appended
+    // in candidate order (four per trip was slower: the chords are short and
+    // the tail trips run mostly predicated off)
+    auto run = [&](int32_t s, int32_t len) {
+        const int maxlen = __reduce_max_sync(full, len);
+        for (int t = 0; t < maxlen; t += 2) {
+            const bool ok0 = t < len, ok1 = t + 1 < len;
+            const int32_t j0 = ok0 ? s + t : (int32_t)k, j1 = ok1 ? s + t + 1 : (int32_t)k;
+            const float4 l0 = v.lf[j0], l1 = v.lf[j1];
+            const float r20 = list_r2(li, l0), r21 = list_r2(li, l1);
+            if (ok0 && r20 < ri2) take(j0, l0, r20);
+            if (ok1 && r21 < ri2) take(j1, l1, r21);
+        }
+    };
+    if constexpr (LV) {
+        if (I.nlev > 1) {  // warp-uniform: graded impact with traversal-grid levels
+            warp_walk_levels(v, I, act, pi, ci, Rs, run);
+            if (act) {
+                v.nbr_cnt[k] = cnt;
+                v.hlist[k] = pi.w;
+                if (cnt > cap) atomicMax(&v.flags[0], cnt);
+            }
+            return;
+        }
+    }
     int c[3];
     unpack_cell(ci, c[0], c[1], c[2]);
     const float w0 = I.wf[0], w1 = I.wf[1];
@@ -904,9 +1149,6 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
     hi1 = hi1 < 0 ? 0 : (hi1 > nf1 - 1 ? nf1 - 1 : hi1);
     const int ulo0 = __reduce_min_sync(full, act ? lo0 : INT_MAX), uhi0 = __reduce_max_sync(full, act ? hi0 : INT_MIN);
     const int ulo1 = __reduce_min_sync(full, act ? lo1 : INT_MAX), uhi1 = __reduce_max_sync(full, act ? hi1 : INT_MIN);
-    int cnt = 0;
-    const int cap = v.cap;
-    int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
     for (int ix = ulo0; ix <= uhi0; ix++) {
         const float xa = (float)(ix - c[0]) * w0 - pi.x;
         float bx = xa > 0.0f ? xa : (xa + w0 < 0.0f ? -(xa + w0) : 0.0f);
@@ -929,28 +1171,7 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
                 s = v.cell_ptr[colbase + zl];
                 len = v.cell_ptr[colbase + zh + 1] - s;
             }
-            const int maxlen = __reduce_max_sync(full, len);
-            auto take = [&](int32_t j, float4 lj, float r2) {
-                if (cnt < cap) out[nbr_slot(cnt, v.ls)] = j;
-                cnt++;
-                const float rj = 2.0f * lj.w * sl + m;
-                const float rb = (pi.w + lj.w) * sl + m;
-                if (!(r2 < rj * rj) && r2 < rb * rb) {
-                    const int slot = atomicAdd(&v.xcnt[j], 1);
-                    if (slot < kExtraCap) v.xnbr[(int64_t)slot * v.ls + j] = (int32_t)k;
-                }
-            };
-            // two candidates per trip: independent load / distance chains,
-            // appended in candidate order (four per trip was slower: the
-            // chords are short and the tail trips run mostly predicated off)
-            for (int t = 0; t < maxlen; t += 2) {
-                const bool ok0 = t < len, ok1 = t + 1 < len;
-                const int32_t j0 = ok0 ? s + t : (int32_t)k, j1 = ok1 ? s + t + 1 : (int32_t)k;
-                const float4 l0 = v.lf[j0], l1 = v.lf[j1];
-                const float r20 = list_r2(li, l0), r21 = list_r2(li, l1);
-                if (ok0 && r20 < ri2) take(j0, l0, r20);
-                if (ok1 && r21 < ri2) take(j1, l1, r21);
-            }
+            run(s, len);
         }
     }
     if (act) {
@@ -1327,7 +1548,7 @@ __device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, 
 // compensated sum in the mixed form.  An iteration reads only the particle's
 // own h and the neighbours' positions and masses, so running the iterations
 // back to back per particle gives the same result as one launch per iteration.
-template <class R>
+template <class R, bool LV = false>
 static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_density(View<R> v, int iters) {
     int64_t k = gtid();
     if (k >= v.n) return;
@@ -1388,7 +1609,7 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_density(
             }
         } else {
             const float hf = (float)hi;
-            traverse(v, I, pi, ci, 2.0f * hf * 1.0001f + 2.0f * I.margin + 1e-6f * hf,
+            traverse<R, LV>(v, I, pi, ci, 2.0f * hf * 1.0001f + 2.0f * I.margin + 1e-6f * hf,
                      [&](int32_t j, float, float, float) { body(j); });
         }
         rho = rmax(sum.value(), R(1e-30));
@@ -1510,7 +1731,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // ASYNC selects the copy engine of the staging: false = one bulk copy per
 // entry (cp.async.bulk, TMA), true = six 16-byte cp.async per entry (the load
 // path through L1, completion tracked by cp.async.mbarrier.arrive).
-template <class R, int SE = 0, int SS = 0, bool ASYNC = false>
+template <class R, int SE = 0, int SS = 0, bool ASYNC = false, bool LV = false>
 static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(View<R> v, int32_t* wait_err) {
     using Acc = AccT<R>;
     constexpr bool kStaged = SS > 0 && sizeof(R) == 4;
@@ -1786,7 +2007,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             const int32_t* xl = v.xnbr + k;
             for (int t = 0; t < xc; t++, xl += v.ls) body(*xl);
         } else {
-            traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
+            traverse<R, LV>(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
                      [&](int32_t j, float, float, float) { body(j); });
         }
     } else if (!I.slack_flag && v.nbr_cnt[k] <= v.cap && v.xcnt[k] <= kExtraCap) {
@@ -1796,7 +2017,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
         const int32_t* xl = v.xnbr + k;
         for (int t = 0; t < xc; t++, xl += v.ls) body(*xl);
     } else {
-        traverse(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
+        traverse<R, LV>(v, I, pi, ci, pi.w + I.hmax_f + 2.0f * I.margin + 1e-6f * pi.w,
                  [&](int32_t j, float, float, float) { body(j); });
     }
     if constexpr (sizeof(R) == 4) {
