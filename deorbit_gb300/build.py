@@ -17,7 +17,11 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdeorbit_sph.so")
 
-SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu", "serve.cpp"]
+SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu", "serve.cpp",
+           "euler.cu"]
+# Per-source flags: the grid solver evaluates every expression in the
+# reference's operation order, without fused multiply-adds.
+SOURCE_FLAGS = {"euler.cu": ["--fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off: host code (flaw seeding, file formats) gives the same
 # results on x86 and on Arm, where g++ would otherwise fuse a*b+c.
@@ -41,7 +45,7 @@ def _newer(target: str, deps) -> bool:
 
 def _headers():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp"))] + [
-        os.path.join(ROOT, "include", "deorbit_sph.h")]
+        os.path.join(ROOT, "include", "deorbit_sph.h"), os.path.join(ROOT, "include", "deorbit_euler.h")]
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
@@ -56,7 +60,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or not _newer(o, [s] + hdrs):
-            jobs.append([nv] + NVCC_FLAGS + ARCH + ["-c", s, "-o", o])
+            jobs.append([nv] + NVCC_FLAGS + SOURCE_FLAGS.get(src, []) + ARCH + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,219 @@
+"""Workloads of the Eulerian grid hydrocode.
+
+Each `Case` holds a grid shape, cell width, material, solver settings and the
+initial fields, plus the CFL number and end time of its run.  The 1-D / 2-D /
+3-D gate problems restate the initial conditions of the reference driver's
+modes (hydrocodes/euler/hydro_cpu.cpp:449-905, cited per case); `impact3d`
+is this repository's 3-D Cartesian half-space impact used as the grid
+solver's throughput workload (seeded, synthetic, no dataset).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import ic
+
+GAM = 1.4
+
+
+@dataclass
+class Case:
+    name: str
+    shape: tuple
+    dx: float
+    material: dict
+    params: dict = field(default_factory=dict)
+    fields: dict = field(default_factory=dict)
+    cfl: float = 0.4
+    t_end: float = 0.0
+
+    @property
+    def n(self):
+        return self.shape[0] * self.shape[1] * self.shape[2]
+
+
+def aluminum():
+    """Material::aluminum (eos.hpp:48-49)."""
+    return ic.tillotson(2700, 7.52e10, 6.5e10, 0.5, 1.63, 5, 5, 5.0e6, 3.0e6, 1.39e7)
+
+
+def _centres(n, dx):
+    return (np.arange(n, dtype=np.float64) + 0.5) * dx
+
+
+def _zeros(n):
+    return np.zeros(n, dtype=np.float64)
+
+
+def sod(N=200):
+    """hydro_cpu.cpp:449-454: Sod tube, ideal gas 1.4, t_end 0.2, CFL 0.4."""
+    dx = 1.0 / N
+    x = _centres(N, dx)
+    r = np.where(x < 0.5, 1.0, 0.125)
+    p = np.where(x < 0.5, 1.0, 0.1)
+    return Case("sod", (N, 1, 1), dx, ic.ideal_gas(GAM), {}, {"r": r, "E": p / (GAM - 1)}, 0.4, 0.2)
+
+
+def tracer(N=200):
+    """hydro_cpu.cpp:455-465: a tracer blob advected by a uniform flow."""
+    dx = 1.0 / N
+    x = _centres(N, dx)
+    rho0, p0, v0 = 1.0, 1.0, 2.0
+    f = {"r": np.full(N, rho0), "mu": np.full(N, rho0 * v0),
+         "E": np.full(N, p0 / (GAM - 1) + 0.5 * rho0 * v0 * v0),
+         "rc": rho0 * np.where((x > 0.3) & (x < 0.5), 1.0, 0.0)}
+    return Case("tracer", (N, 1, 1), dx, ic.ideal_gas(GAM), {}, f, 0.4, 0.15)
+
+
+def sedov(N=64):
+    """hydro_cpu.cpp:466-477: 3-D point blast, E0 = 1 in the central cell."""
+    L, E0, rho0 = 2.0, 1.0, 1.0
+    dx = L / N
+    n = N * N * N
+    E = np.full(n, 1e-4 / (GAM - 1))
+    ic_ = N // 2
+    E[(ic_ * N + ic_) * N + ic_] += E0 / (dx * dx * dx)
+    return Case("sedov", (N, N, N), dx, ic.ideal_gas(GAM), {}, {"r": np.full(n, rho0), "E": E}, 0.3, 0.5)
+
+
+def sedov_axi(Nr=64, Nz=128):
+    """hydro_cpu.cpp:478-489: on-axis point blast in cylindrical (r, z)."""
+    dx = 2.0 / 64
+    E0, rho0 = 1.0, 1.0
+    n = Nr * Nz
+    E = np.full(n, 1e-4 / (GAM - 1))
+    kc = Nz // 2
+    E[kc] += E0 / (math.pi * dx * dx * dx)
+    return Case("sedov_axi", (Nr, 1, Nz), dx, ic.ideal_gas(GAM), {"axisym": 1},
+                {"r": np.full(n, rho0), "E": E}, 0.3, 0.5)
+
+
+def _pulse(N, L, A):
+    rho0 = 2700.0
+    dx = L / N
+    x = _centres(N, dx)
+    x0, wid = 0.3 * L, 8e3
+    vy = A * np.exp(-((x - x0) / wid) * ((x - x0) / wid))
+    return dx, {"r": np.full(N, rho0), "mv": rho0 * vy, "E": 0.5 * rho0 * vy * vy}
+
+
+def shear(N=800):
+    """hydro_cpu.cpp:682-694: small elastic shear pulse in basalt."""
+    m = ic.basalt()
+    dx, f = _pulse(N, 400e3, 1.0)
+    cs = math.sqrt(m["G"] / 2700.0)
+    return Case("shear", (N, 1, 1), dx, m, {}, f, 0.3, 20e3 / cs)
+
+
+def yield_pulse(N=400):
+    """hydro_cpu.cpp:695-703: shear pulse driven past the von Mises surface."""
+    m = ic.basalt()
+    dx, f = _pulse(N, 400e3, 2000.0)
+    cs = math.sqrt(m["G"] / 2700.0)
+    return Case("yield", (N, 1, 1), dx, m, {}, f, 0.3, 15e3 / cs)
+
+
+def vacuum(N=400):
+    """hydro_cpu.cpp:704-715: expansion into vacuum with the vacuum-aware flux."""
+    dx = 1.0 / N
+    x = _centres(N, dx)
+    left = x < 0.5
+    r = np.where(left, 1.0, 1e-6)
+    E = np.where(left, 1.0 / (GAM - 1), 1e-6 / (GAM - 1))
+    return Case("vacuum", (N, 1, 1), dx, ic.ideal_gas(GAM), {"rho_vac": 1e-3}, {"r": r, "E": E}, 0.4, 0.10)
+
+
+def bshock(N=400):
+    """hydro_cpu.cpp:716-720: basalt shock tube (Tillotson)."""
+    L = 400e3
+    dx = L / N
+    x = _centres(N, dx)
+    rr = np.where(x < 0.5 * L, 3000.0, 2700.0)
+    ee = np.where(x < 0.5 * L, 1e6, 0.0)
+    return Case("bshock", (N, 1, 1), dx, ic.basalt(), {}, {"r": rr, "E": rr * ee}, 0.4, 4.0)
+
+
+def freefall(N=50):
+    """hydro_cpu.cpp:721-727: uniform gas under gravity."""
+    return Case("freefall", (1, 1, N), 10.0, ic.ideal_gas(GAM), {"gz": 9.8},
+                {"r": np.ones(N), "E": np.full(N, 1e5 / (GAM - 1))}, 0.4, 10.0)
+
+
+def atmos(N=200):
+    """hydro_cpu.cpp:728-735: isothermal atmosphere under gravity."""
+    gz, P0, rho0 = 9.8, 1e5, 1.0
+    H = P0 / (rho0 * gz)
+    L = 4 * H
+    dx = L / N
+    z = _centres(N, dx)
+    cs = math.sqrt(GAM * P0 / rho0)
+    f = {"r": rho0 * np.exp(-z / H), "E": (P0 * np.exp(-z / H)) / (GAM - 1)}
+    return Case("atmos", (1, 1, N), dx, ic.ideal_gas(GAM), {"gz": gz}, f, 0.4, 0.05 * L / cs)
+
+
+def tensile(N=100):
+    """hydro_cpu.cpp:736-743: a stretched basalt bar (tensile damage)."""
+    L, rho0, rate = 10e3, 2700.0, 1e-2
+    dx = L / N
+    x = _centres(N, dx)
+    vx = rate * (x - 0.5 * L)
+    return Case("tensile", (N, 1, 1), dx, ic.basalt(), {},
+                {"r": np.full(N, rho0), "mu": rho0 * vx, "E": 0.5 * rho0 * vx * vx}, 0.3, 0.1)
+
+
+def alimpact(N=400):
+    """hydro_cpu.cpp:744-752: symmetric Al-on-Al planar impact."""
+    L, rho0, up = 2.0, 2700.0, 5000.0
+    dx = L / N
+    x = _centres(N, dx)
+    vx = np.where(x < 0.5 * L, up, -up)
+    return Case("alimpact", (N, 1, 1), dx, aluminum(), {},
+                {"r": np.full(N, rho0), "mu": rho0 * vx, "E": 0.5 * rho0 * vx * vx}, 0.3, 3e-5)
+
+
+def surface(N=64):
+    """hydro_cpu.cpp:901-905: a basalt half-space with a near-void above."""
+    L = 200e3
+    dx = L / N
+    z = _centres(N, dx)
+    return Case("surface", (1, 1, N), dx, ic.basalt(), {},
+                {"r": np.where(z < 0.5 * L, 2700.0, 0.27), "E": np.zeros(N)}, 0.4, 2.0)
+
+
+def impact3d(N=64, a_cells=None, speed=8000.0, angle_deg=30.0, af=False, t_end=None):
+    """3-D Cartesian impact: a basalt sphere (radius a_cells cells, default N/16)
+    at speed (m/s) and angle_deg from vertical into a basalt half-space filling
+    the lower half of an N^3 grid of 50 m cells, near-void (0.27 kg/m^3) above.
+    Strength with the pressure-dependent ROCK yield, tensile damage, gravity
+    3.71 m/s^2, near-void cells out of CFL and strength (rho < 100), and
+    optionally shock-activated acoustic fluidization."""
+    dx = 50.0
+    a = float(a_cells if a_cells is not None else max(2.0, N / 16))
+    n = N * N * N
+    c = _centres(N, dx)
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    rho0 = 2700.0
+    zs = 0.5 * N * dx
+    r = np.where(Z < zs, rho0, 0.27)
+    th = math.radians(angle_deg)
+    cx, cy, cz = 0.5 * N * dx - 2.0 * a * dx * math.sin(th), 0.5 * N * dx, zs + (a + 1.0) * dx
+    sphere = (X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2 < (a * dx) ** 2
+    r = np.where(sphere, rho0, r)
+    vx = np.where(sphere, speed * math.sin(th), 0.0)
+    vz = np.where(sphere, -speed * math.cos(th), 0.0)
+    f = {"r": r.reshape(-1), "mu": (r * vx).reshape(-1), "mw": (r * vz).reshape(-1),
+         "E": (0.5 * r * (vx * vx + vz * vz)).reshape(-1), "rc": np.where(sphere, r, 0.0).reshape(-1)}
+    prm = {"rock": 1, "gz": 3.71, "rho_cfl": 100.0}
+    if af:
+        prm.update(tdec=2.0, eta_af=1e7, c_act=0.1)
+    if t_end is None:
+        t_end = 4.0 * a * dx / speed
+    return Case(f"impact3d_{N}", (N, N, N), dx, ic.basalt(), prm, f, 0.3, t_end)
+
+
+GATES = {"sod": sod, "tracer": tracer, "sedov": sedov, "sedov_axi": sedov_axi, "shear": shear,
+         "yield": yield_pulse, "vacuum": vacuum, "bshock": bshock, "freefall": freefall, "atmos": atmos,
+         "tensile": tensile, "alimpact": alimpact, "surface": surface}

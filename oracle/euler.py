@@ -1,0 +1,203 @@
+"""ctypes front end for the CPU oracle of the Eulerian grid hydrocode
+(TEST INFRASTRUCTURE ONLY).
+
+Two back ends with one interface:
+  * OracleGrid -- oracle/liborc.so (eorc_*), the C restatement of the
+    reference's CPU Euler solver (hydrocodes/euler/hydro_cpu.cpp);
+  * RefGrid    -- oracle/_ref/libeulerref.so (eref_*), the reference's own
+    hydro_cpu.cpp compiled unmodified (only where the reference tree is
+    present).
+
+Only tests/ and bench.py's CPU legs import this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import oracle as O
+
+REF_SO = os.path.join(O.HERE, "_ref", "libeulerref.so")
+
+FIELDS = "r mu mv mw E Sxx Syy Szz Sxy Sxz Syz D af rc vib Pmax".split()
+RHS = "r mu mv mw E Sxx Syy Szz Sxy Sxz Syz D rc vib".split()
+
+
+class Params(C.Structure):
+    """Layout of eorc_params: the file-scope settings of hydro_cpu.cpp:15-36."""
+
+    _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
+                                          "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad_"}
+
+
+_D = C.POINTER(C.c_double)
+
+
+def _declare(lib, p):
+    sig = {
+        f"{p}params_default": (None, [C.POINTER(Params)]),
+        f"{p}create": (C.c_void_p, [C.c_int, C.c_int, C.c_int, C.c_double]),
+        f"{p}destroy": (None, [C.c_void_p]),
+        f"{p}set_material": (None, [C.c_void_p, C.POINTER(O.Material)]),
+        f"{p}set_params": (None, [C.c_void_p, C.POINTER(Params)]),
+        f"{p}field": (_D, [C.c_void_p, C.c_char_p]),
+        f"{p}rhs": (_D, [C.c_void_p, C.c_char_p]),
+        f"{p}lop": (None, [C.c_void_p]),
+        f"{p}vonmises": (None, [C.c_void_p, C.c_int]),
+        f"{p}grow_damage": (None, [C.c_void_p, C.c_double]),
+        f"{p}update_af": (None, [C.c_void_p, C.c_double]),
+        f"{p}maxspeed": (C.c_double, [C.c_void_p]),
+        f"{p}step_rk2": (None, [C.c_void_p, C.c_double]),
+        f"{p}run": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _D]),
+        f"{p}pcell": (C.c_double, [C.c_void_p, C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+_ref = None
+_declared = False
+
+
+def _orc():
+    global _declared
+    lib = O.lib()
+    if not _declared:
+        _declare(lib, "eorc_")
+        _declared = True
+    return lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def _eref():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("reference Euler shim not built (make -C oracle ref)")
+        _ref = C.CDLL(REF_SO)
+        _declare(_ref, "eref_")
+    return _ref
+
+
+def default_params(ref=False) -> Params:
+    p = Params()
+    (_eref().eref_params_default if ref else _orc().eorc_params_default)(C.byref(p))
+    return p
+
+
+class _Grid:
+    _prefix = ""
+
+    def __init__(self, nx, ny, nz, dx, material=None, params=None):
+        self._lib = self._load()
+        self.shape = (int(nx), int(ny), int(nz))
+        self.n = int(nx) * int(ny) * int(nz)
+        self.dx = float(dx)
+        self.h = self._f("create")(int(nx), int(ny), int(nz), float(dx))
+        if material is not None:
+            self.set_material(material)
+        self.params = default_params(ref=self._prefix == "eref_")
+        if params:
+            self.set_params(params)
+
+    def _f(self, name):
+        return getattr(self._lib, self._prefix + name)
+
+    def set_material(self, m: O.Material):
+        self.material = m
+        self._f("set_material")(self.h, C.byref(m))
+
+    def set_params(self, values: dict):
+        for k, v in values.items():
+            setattr(self.params, k, v)
+        self._f("set_params")(self.h, C.byref(self.params))
+
+    def _view(self, getter, name):
+        p = self._f(getter)(self.h, name.encode())
+        if not p:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(self.n,))
+
+    def field(self, name):
+        return self._view("field", name).copy()
+
+    def set_field(self, name, values):
+        self._view("field", name)[:] = np.asarray(values, dtype=np.float64).reshape(-1)
+
+    def rhs(self, name):
+        return self._view("rhs", name).copy()
+
+    def fields(self, names=FIELDS):
+        return {k: self.field(k) for k in names}
+
+    def lop(self):
+        self._f("lop")(self.h)
+
+    def vonmises(self, reg=True):
+        self._f("vonmises")(self.h, int(reg))
+
+    def grow_damage(self, dt):
+        self._f("grow_damage")(self.h, float(dt))
+
+    def update_af(self, dt):
+        self._f("update_af")(self.h, float(dt))
+
+    def maxspeed(self) -> float:
+        return self._f("maxspeed")(self.h)
+
+    def step(self, dt):
+        self._f("step_rk2")(self.h, float(dt))
+
+    def run(self, cfl, t_end, max_steps=-1):
+        t = np.zeros(1)
+        s = self._f("run")(self.h, float(cfl), float(t_end), int(max_steps), t.ctypes.data_as(_D))
+        return int(s), float(t[0])
+
+    def pcell(self, c) -> float:
+        return self._f("pcell")(self.h, int(c))
+
+    def close(self):
+        if self.h:
+            self._f("destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OracleGrid(_Grid):
+    _prefix = "eorc_"
+
+    @staticmethod
+    def _load():
+        return _orc()
+
+
+class RefGrid(_Grid):
+    _prefix = "eref_"
+
+    @staticmethod
+    def _load():
+        return _eref()
+
+
+def from_case(case, cls=OracleGrid):
+    """A grid loaded with a workload case (deorbit_gb300.grid_ic.Case)."""
+    g = cls(*case.shape, case.dx, material=O.material_from_dict(case.material), params=case.params)
+    for k, v in case.fields.items():
+        g.set_field(k, v)
+    return g

@@ -1,0 +1,543 @@
+/* euler_oracle.c -- CPU oracle of the Eulerian grid hydrocode (TEST ONLY).
+ * See euler_oracle.h.  Line references are to hydrocodes/euler/hydro_cpu.cpp
+ * of the reference; the operation order of every expression is the
+ * reference's (bit-exact pinning against the reference compiled here). */
+#include "euler_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NF 16 /* per-cell fields of the grid */
+#define ND 14 /* fields of the right-hand side */
+static const char* FIELD_NAMES[NF] = {"r",   "mu",  "mv", "mw", "E",  "Sxx", "Syy", "Szz",
+                                      "Sxy", "Sxz", "Syz", "D", "af", "rc",  "vib", "Pmax"};
+static const char* RHS_NAMES[ND] = {"r", "mu", "mv", "mw", "E", "Sxx", "Syy", "Szz",
+                                    "Sxy", "Sxz", "Syz", "D", "rc", "vib"};
+enum { F_R, F_MU, F_MV, F_MW, F_E, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ, F_D, F_AF, F_RC, F_VIB, F_PMAX };
+enum { D_R, D_MU, D_MV, D_MW, D_E, D_SXX, D_SYY, D_SZZ, D_SXY, D_SXZ, D_SYZ, D_D, D_RC, D_VIB };
+
+struct eorc_grid {
+    int nx, ny, nz, n;
+    double dx;
+    double* f[NF];
+    double* d[ND];
+    orc_material mat;
+    eorc_params p;
+};
+
+static inline double dmax2(double a, double b) { return a < b ? b : a; } /* std::max */
+static inline double dmin2(double a, double b) { return b < a ? b : a; } /* std::min */
+static inline int imax2(int a, int b) { return a < b ? b : a; }
+static inline int imin2(int a, int b) { return b < a ? b : a; }
+
+void eorc_params_default(eorc_params* p) { /* hydro_cpu.cpp:17-36, 222 */
+    memset(p, 0, sizeof *p);
+    p->p_coh = 1.0e6;
+    p->damp = 1.0;
+    p->y_i0 = 1.0e7;
+    p->mu_i = 1.2;
+    p->mu_d = 0.6;
+    p->y_m = 2.5e9;
+    p->c_reg = 0.1;
+    p->af_sat = 1.0;
+}
+
+eorc_grid* eorc_create(int nx, int ny, int nz, double dx) {
+    eorc_grid* g = (eorc_grid*)calloc(1, sizeof *g);
+    g->nx = nx; g->ny = ny; g->nz = nz; g->n = nx * ny * nz; g->dx = dx;
+    for (int q = 0; q < NF; q++) g->f[q] = (double*)calloc((size_t)(g->n > 0 ? g->n : 1), sizeof(double));
+    for (int q = 0; q < ND; q++) g->d[q] = (double*)calloc((size_t)(g->n > 0 ? g->n : 1), sizeof(double));
+    g->mat = orc_mat_ideal(1.4);
+    eorc_params_default(&g->p);
+    return g;
+}
+
+void eorc_destroy(eorc_grid* g) {
+    if (!g) return;
+    for (int q = 0; q < NF; q++) free(g->f[q]);
+    for (int q = 0; q < ND; q++) free(g->d[q]);
+    free(g);
+}
+
+void eorc_set_material(eorc_grid* g, const orc_material* m) { g->mat = *m; }
+void eorc_set_params(eorc_grid* g, const eorc_params* p) { g->p = *p; }
+
+double* eorc_field(eorc_grid* g, const char* name) {
+    for (int q = 0; q < NF; q++)
+        if (!strcmp(name, FIELD_NAMES[q])) return g->f[q];
+    return NULL;
+}
+
+double* eorc_rhs(eorc_grid* g, const char* name) {
+    for (int q = 0; q < ND; q++)
+        if (!strcmp(name, RHS_NAMES[q])) return g->d[q];
+    return NULL;
+}
+
+static inline int idx(const eorc_grid* g, int i, int j, int k) { return (i * g->ny + j) * g->nz + k; }
+
+/* hydro_cpu.cpp:38 */
+static inline void eos_pc(const orc_material* m, double rho, double e, double* p, double* cs) {
+    *p = orc_pressure(m, rho, e);
+    if (*p < 0) *p = 0;
+    *cs = orc_sound_speed(m, rho, e);
+}
+
+/* hydro_cpu.cpp:94 */
+static inline double eint(const eorc_grid* g, int c) {
+    const double* r = g->f[F_R];
+    double ke = 0.5 * (g->f[F_MU][c] * g->f[F_MU][c] + g->f[F_MV][c] * g->f[F_MV][c] +
+                       g->f[F_MW][c] * g->f[F_MW][c]) / r[c];
+    return (g->f[F_E][c] - ke) / r[c];
+}
+
+double eorc_pcell(const eorc_grid* g, int c) { /* hydro_cpu.cpp:95 */
+    double p, cs;
+    eos_pc(&g->mat, g->f[F_R][c], eint(g, c), &p, &cs);
+    return p;
+}
+
+typedef struct { double r, mn, mt1, mt2, E; } F5;
+
+/* Exact rarefaction into vacuum sampled at the face, hydro_cpu.cpp:43-53. */
+static F5 vac_flux(const orc_material* m, double rM, double vnM, double t1M, double t2M, double eM, int side) {
+    double pM, cM;
+    eos_pc(m, rM, eM, &pM, &cM);
+    double g = rM * cM * cM / dmax2(pM, 1e-30);
+    if (g < 1.01) g = 1.01;
+    if (g > 1e5) g = 1e5;
+    double s = (double)side, vn = s * vnM;
+    if (vn - cM >= 0) {
+        double E = rM * eM + 0.5 * rM * (vnM * vnM + t1M * t1M + t2M * t2M);
+        F5 o = {rM * vnM, rM * vnM * vnM + pM, rM * vnM * t1M, rM * vnM * t2M, (E + pM) * vnM};
+        return o;
+    }
+    if (vn + 2 * cM / (g - 1) <= 0) {
+        F5 z = {0, 0, 0, 0, 0};
+        return z;
+    }
+    double u0 = 2.0 / (g + 1) * (cM + 0.5 * (g - 1) * vn), c0 = u0;
+    double r0 = rM * pow(c0 / cM, 2.0 / (g - 1)), p0 = pM * pow(r0 / rM, g), e0 = p0 / ((g - 1) * r0), un0 = s * u0;
+    double E0 = r0 * e0 + 0.5 * r0 * (un0 * un0 + t1M * t1M + t2M * t2M);
+    F5 o = {r0 * un0, r0 * un0 * un0 + p0, r0 * un0 * t1M, r0 * un0 * t2M, (E0 + p0) * un0};
+    return o;
+}
+
+static inline F5 flux_of(double r, double vn, double t1, double t2, double p, double E) {
+    F5 o = {r * vn, r * vn * vn + p, r * vn * t1, r * vn * t2, (E + p) * vn};
+    return o;
+}
+
+static inline F5 hllc_star(double r, double vn, double t1, double t2, double p, double E, double S, double Ss, F5 Fk) {
+    double f = r * (S - vn) / (S - Ss);
+    F5 Us = {f, f * Ss, f * t1, f * t2, f * (E / r + (Ss - vn) * (Ss + p / (r * (S - vn))))};
+    F5 U = {r, r * vn, r * t1, r * t2, E};
+    F5 o = {Fk.r + S * (Us.r - U.r), Fk.mn + S * (Us.mn - U.mn), Fk.mt1 + S * (Us.mt1 - U.mt1),
+            Fk.mt2 + S * (Us.mt2 - U.mt2), Fk.E + S * (Us.E - U.E)};
+    return o;
+}
+
+/* HLLC face flux, hydro_cpu.cpp:54-74. */
+static F5 hllc(const eorc_grid* gr, double rL, double vnL, double t1L, double t2L, double eL, double rR, double vnR,
+               double t1R, double t2R, double eR) {
+    const orc_material* m = &gr->mat;
+    const double rho_vac = gr->p.rho_vac;
+    if (rho_vac > 0) {
+        int vL = rL < rho_vac, vR = rR < rho_vac;
+        if (vL && vR) {
+            F5 z = {0, 0, 0, 0, 0};
+            return z;
+        }
+        if (vR) return vac_flux(m, rL, vnL, t1L, t2L, eL, +1);
+        if (vL) return vac_flux(m, rR, vnR, t1R, t2R, eR, -1);
+    }
+    double pL, cL, pR, cR;
+    eos_pc(m, rL, eL, &pL, &cL);
+    eos_pc(m, rR, eR, &pR, &cR);
+    double SL = dmin2(vnL - cL, vnR - cR), SR = dmax2(vnL + cL, vnR + cR);
+    double Ss = (pR - pL + rL * vnL * (SL - vnL) - rR * vnR * (SR - vnR)) / (rL * (SL - vnL) - rR * (SR - vnR));
+    double EL = rL * eL + 0.5 * rL * (vnL * vnL + t1L * t1L + t2L * t2L),
+           ER = rR * eR + 0.5 * rR * (vnR * vnR + t1R * t1R + t2R * t2R);
+    if (SL >= 0) return flux_of(rL, vnL, t1L, t2L, pL, EL);
+    if (SR <= 0) return flux_of(rR, vnR, t1R, t2R, pR, ER);
+    if (Ss >= 0) return hllc_star(rL, vnL, t1L, t2L, pL, EL, SL, Ss, flux_of(rL, vnL, t1L, t2L, pL, EL));
+    return hllc_star(rR, vnR, t1R, t2R, pR, ER, SR, Ss, flux_of(rR, vnR, t1R, t2R, pR, ER));
+}
+
+static inline double mm(double a, double b) { /* hydro_cpu.cpp:89 */
+    return (a * b <= 0) ? 0.0 : (fabs(a) < fabs(b) ? a : b);
+}
+
+static inline void prim(const eorc_grid* g, int c, double* W) { /* hydro_cpu.cpp:101 */
+    W[0] = g->f[F_R][c];
+    W[1] = g->f[F_MU][c] / W[0];
+    W[2] = g->f[F_MV][c] / W[0];
+    W[3] = g->f[F_MW][c] / W[0];
+    W[4] = eint(g, c);
+}
+
+static inline int sweep_cell(const eorc_grid* g, int dir, int p, int a, int b) {
+    return dir == 0 ? idx(g, p, a, b) : (dir == 1 ? idx(g, a, p, b) : idx(g, a, b, p));
+}
+
+/* One direction of the unsplit MUSCL + HLLC update, hydro_cpu.cpp:103-134
+ * (the plain, not well-balanced, form). */
+static void sweep(const eorc_grid* g, int dir, double* Fr, double* Fmn, double* Ft1, double* Ft2, double* FE,
+                  double* Frc) {
+    double** d = ((eorc_grid*)g)->d;
+    const double* r = g->f[F_R];
+    const double* rc = g->f[F_RC];
+    const double invdx = 1.0 / g->dx;
+    const int nL = dir == 0 ? g->nx : (dir == 1 ? g->ny : g->nz), nA = dir == 0 ? g->ny : g->nx,
+              nB = dir == 2 ? g->ny : g->nz;
+    const int in = dir == 0 ? 1 : (dir == 1 ? 2 : 3), it1 = dir == 0 ? 2 : 1, it2 = dir == 2 ? 2 : 3;
+    const int axi = g->p.axisym && dir == 0;
+    for (int a = 0; a < nA; a++)
+        for (int b = 0; b < nB; b++) {
+            for (int f = 0; f <= nL; f++) {
+                int iL = imax2(0, f - 1), iR = imin2(nL - 1, f), iLL = imax2(0, f - 2), iRR = imin2(nL - 1, f + 1);
+                double A[5], B[5], AA[5], BB[5], L[5], R[5];
+                prim(g, sweep_cell(g, dir, iL, a, b), A);
+                prim(g, sweep_cell(g, dir, iR, a, b), B);
+                prim(g, sweep_cell(g, dir, iLL, a, b), AA);
+                prim(g, sweep_cell(g, dir, iRR, a, b), BB);
+                for (int q = 0; q < 5; q++) {
+                    L[q] = A[q] + 0.5 * mm(A[q] - AA[q], B[q] - A[q]);
+                    R[q] = B[q] - 0.5 * mm(B[q] - A[q], BB[q] - B[q]);
+                }
+                if (L[0] < 1e-9) L[0] = A[0];
+                if (R[0] < 1e-9) R[0] = B[0];
+                if (L[4] < 0) L[4] = A[4];
+                if (R[4] < 0) R[4] = B[4];
+                F5 fl = hllc(g, L[0], L[in], L[it1], L[it2], L[4], R[0], R[in], R[it1], R[it2], R[4]);
+                Fr[f] = fl.r; Fmn[f] = fl.mn; Ft1[f] = fl.mt1; Ft2[f] = fl.mt2; FE[f] = fl.E;
+                int cl = sweep_cell(g, dir, iL, a, b), cr = sweep_cell(g, dir, iR, a, b);
+                Frc[f] = fl.r * (fl.r >= 0.0 ? rc[cl] / r[cl] : rc[cr] / r[cr]);
+            }
+            for (int p = 0; p < nL; p++) {
+                int c = sweep_cell(g, dir, p, a, b);
+                double w0, w1, inv;
+                if (axi) {
+                    w0 = p * g->dx;
+                    w1 = (p + 1) * g->dx;
+                    inv = 1.0 / (((p + 0.5) * g->dx) * g->dx);
+                } else {
+                    w0 = w1 = 1.0;
+                    inv = invdx;
+                }
+                d[D_R][c] += -(w1 * Fr[p + 1] - w0 * Fr[p]) * inv;
+                d[D_E][c] += -(w1 * FE[p + 1] - w0 * FE[p]) * inv;
+                d[D_RC][c] += -(w1 * Frc[p + 1] - w0 * Frc[p]) * inv;
+                double dmn = -(w1 * Fmn[p + 1] - w0 * Fmn[p]) * inv, dt1 = -(w1 * Ft1[p + 1] - w0 * Ft1[p]) * inv,
+                       dt2 = -(w1 * Ft2[p + 1] - w0 * Ft2[p]) * inv;
+                if (axi) dmn += eorc_pcell(g, c) / ((p + 0.5) * g->dx);
+                if (dir == 0) {
+                    d[D_MU][c] += dmn; d[D_MV][c] += dt1; d[D_MW][c] += dt2;
+                } else if (dir == 1) {
+                    d[D_MV][c] += dmn; d[D_MU][c] += dt1; d[D_MW][c] += dt2;
+                } else {
+                    d[D_MW][c] += dmn; d[D_MU][c] += dt1; d[D_MV][c] += dt2;
+                }
+            }
+        }
+}
+
+/* Upwind advection v . grad S of one cell, hydro_cpu.cpp:175-178. */
+static inline double adv(const eorc_grid* g, const double* S, int c, int i, int j, int k, int xm, int xp, int ym,
+                         int yp, int zm, int zp, double u, double v, double w) {
+    double ax = u > 0 ? (S[c] - S[xm]) / ((i > 0) ? g->dx : 1e30) : (S[xp] - S[c]) / ((i < g->nx - 1) ? g->dx : 1e30);
+    double ay = v > 0 ? (S[c] - S[ym]) / ((j > 0) ? g->dx : 1e30) : (S[yp] - S[c]) / ((j < g->ny - 1) ? g->dx : 1e30);
+    double az = w > 0 ? (S[c] - S[zm]) / ((k > 0) ? g->dx : 1e30) : (S[zp] - S[c]) / ((k < g->nz - 1) ? g->dx : 1e30);
+    return u * ax + v * ay + w * az;
+}
+
+/* Right-hand side of the conserved and material fields, hydro_cpu.cpp:98-214. */
+void eorc_lop(eorc_grid* g) {
+    const int n = g->n;
+    double** d = g->d;
+    for (int q = 0; q < ND; q++) memset(d[q], 0, sizeof(double) * (size_t)(n > 0 ? n : 1));
+    int nmax = imax2(g->nx, imax2(g->ny, g->nz)) + 1;
+    double* buf = (double*)malloc(sizeof(double) * 6 * (size_t)nmax);
+    for (int dir = 0; dir < 3; dir++)
+        sweep(g, dir, buf, buf + nmax, buf + 2 * nmax, buf + 3 * nmax, buf + 4 * nmax, buf + 5 * nmax);
+    free(buf);
+    const double GZ = g->p.gz, RHO_CFL = g->p.rho_cfl, ETA_AF = g->p.eta_af;
+    const double* r = g->f[F_R];
+    const double* mu = g->f[F_MU];
+    const double* mv = g->f[F_MV];
+    const double* mw = g->f[F_MW];
+    if (GZ != 0.0) /* hydro_cpu.cpp:137-138 (plain gravity body force) */
+        for (int c = 0; c < n; c++) {
+            d[D_MW][c] += -GZ * r[c];
+            d[D_E][c] += -GZ * g->f[F_MW][c];
+        }
+    const double G = g->mat.G;
+    if (G <= 0) return;
+    const double *Sxx = g->f[F_SXX], *Syy = g->f[F_SYY], *Szz = g->f[F_SZZ], *Sxy = g->f[F_SXY],
+                 *Sxz = g->f[F_SXZ], *Syz = g->f[F_SYZ];
+#define VX(cc) (mu[cc] / r[cc])
+#define VY(cc) (mv[cc] / r[cc])
+#define VZ(cc) (mw[cc] / r[cc])
+#define VOIDC(cc) (RHO_CFL > 0 && r[cc] < RHO_CFL)
+    for (int i = 0; i < g->nx; i++)
+        for (int j = 0; j < g->ny; j++)
+            for (int k = 0; k < g->nz; k++) {
+                int c = idx(g, i, j, k);
+                if (RHO_CFL > 0 && r[c] < RHO_CFL) continue;
+                int xm = idx(g, imax2(0, i - 1), j, k), xp = idx(g, imin2(g->nx - 1, i + 1), j, k),
+                    ym = idx(g, i, imax2(0, j - 1), k), yp = idx(g, i, imin2(g->ny - 1, j + 1), k),
+                    zm = idx(g, i, j, imax2(0, k - 1)), zp = idx(g, i, j, imin2(g->nz - 1, k + 1));
+                double hx = ((i > 0 && i < g->nx - 1) ? 2.0 : 1.0) * g->dx,
+                       hy = ((j > 0 && j < g->ny - 1) ? 2.0 : 1.0) * g->dx,
+                       hz = ((k > 0 && k < g->nz - 1) ? 2.0 : 1.0) * g->dx;
+                /* void neighbours take the centre velocity (traction-free surface) */
+#define VXW(cc) (VOIDC(cc) ? mu[c] / r[c] : mu[cc] / r[cc])
+#define VYW(cc) (VOIDC(cc) ? mv[c] / r[c] : mv[cc] / r[cc])
+#define VZW(cc) (VOIDC(cc) ? mw[c] / r[c] : mw[cc] / r[cc])
+                double Lxx = (VXW(xp) - VXW(xm)) / hx, Lxy = (VXW(yp) - VXW(ym)) / hy, Lxz = (VXW(zp) - VXW(zm)) / hz;
+                double Lyx = (VYW(xp) - VYW(xm)) / hx, Lyy = (VYW(yp) - VYW(ym)) / hy, Lyz = (VYW(zp) - VYW(zm)) / hz;
+                double Lzx = (VZW(xp) - VZW(xm)) / hx, Lzy = (VZW(yp) - VZW(ym)) / hy, Lzz = (VZW(zp) - VZW(zm)) / hz;
+                double rcyl = (i + 0.5) * g->dx;
+                double eyy = g->p.axisym ? (VX(c) / rcyl) : Lyy;
+                double exx = Lxx, ezz = Lzz, exy = 0.5 * (Lxy + Lyx), exz = 0.5 * (Lxz + Lzx), eyz = 0.5 * (Lyz + Lzy),
+                       tr = (exx + eyy + ezz) / 3.0;
+                double Wxy = 0.5 * (Lxy - Lyx), Wxz = 0.5 * (Lxz - Lzx), Wyz = 0.5 * (Lyz - Lzy);
+                double sxx = Sxx[c], syy = Syy[c], szz = Szz[c], sxy = Sxy[c], sxz = Sxz[c], syz = Syz[c];
+                double Sm[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}},
+                       Wm[3][3] = {{0, Wxy, Wxz}, {-Wxy, 0, Wyz}, {-Wxz, -Wyz, 0}}, Jm[3][3];
+                for (int aa = 0; aa < 3; aa++)
+                    for (int bb = 0; bb < 3; bb++) {
+                        double s = 0;
+                        for (int cc = 0; cc < 3; cc++) s += Sm[aa][cc] * Wm[cc][bb] - Wm[aa][cc] * Sm[cc][bb];
+                        Jm[aa][bb] = s;
+                    }
+                double u = VX(c), v = VY(c), w = VZ(c);
+#define ADV(S) adv(g, S, c, i, j, k, xm, xp, ym, yp, zm, zp, u, v, w)
+                d[D_SXX][c] += 2 * G * (exx - tr) + Jm[0][0] - ADV(Sxx);
+                d[D_SYY][c] += 2 * G * (eyy - tr) + Jm[1][1] - ADV(Syy);
+                d[D_SZZ][c] += 2 * G * (ezz - tr) + Jm[2][2] - ADV(Szz);
+                d[D_SXY][c] += 2 * G * exy + Jm[0][1] - ADV(Sxy);
+                d[D_SXZ][c] += 2 * G * exz + Jm[0][2] - ADV(Sxz);
+                d[D_SYZ][c] += 2 * G * eyz + Jm[1][2] - ADV(Syz);
+                d[D_D][c] += -ADV(g->f[F_D]);
+                d[D_VIB][c] += -ADV(g->f[F_VIB]);
+#undef ADV
+                double dSxx_x = (Sxx[xp] - Sxx[xm]) / hx, dSxy_y = (Sxy[yp] - Sxy[ym]) / hy,
+                       dSxz_z = (Sxz[zp] - Sxz[zm]) / hz;
+                double dSxy_x = (Sxy[xp] - Sxy[xm]) / hx, dSyy_y = (Syy[yp] - Syy[ym]) / hy,
+                       dSyz_z = (Syz[zp] - Syz[zm]) / hz;
+                double dSxz_x = (Sxz[xp] - Sxz[xm]) / hx, dSyz_y = (Syz[yp] - Syz[ym]) / hy,
+                       dSzz_z = (Szz[zp] - Szz[zm]) / hz;
+                d[D_MU][c] += dSxx_x + dSxy_y + dSxz_z;
+                d[D_MV][c] += dSxy_x + dSyy_y + dSyz_z;
+                d[D_MW][c] += dSxz_x + dSyz_y + dSzz_z;
+                if (g->p.axisym) {
+                    d[D_MU][c] += (Sxx[c] - Syy[c]) / rcyl;
+                    d[D_MW][c] += Sxz[c] / rcyl;
+                }
+                if (g->f[F_AF][c] > 0 && ETA_AF > 0) { /* explicit AF viscosity (VISC_IMP not restated) */
+                    double eta = g->f[F_AF][c] * ETA_AF, id2 = 1.0 / (g->dx * g->dx);
+                    d[D_MU][c] += eta * (VX(xp) + VX(xm) + VX(yp) + VX(ym) + VX(zp) + VX(zm) - 6 * VX(c)) * id2;
+                    d[D_MV][c] += eta * (VY(xp) + VY(xm) + VY(yp) + VY(ym) + VY(zp) + VY(zm) - 6 * VY(c)) * id2;
+                    d[D_MW][c] += eta * (VZ(xp) + VZ(xm) + VZ(yp) + VZ(ym) + VZ(zp) + VZ(zm) - 6 * VZ(c)) * id2;
+                    if (g->p.axisym) {
+                        d[D_MU][c] += eta * (Lxx / rcyl - VX(c) / (rcyl * rcyl));
+                        d[D_MW][c] += eta * (Lzx / rcyl);
+                    }
+                }
+#define SVX(cc) (Sxx[cc] * VX(cc) + Sxy[cc] * VY(cc) + Sxz[cc] * VZ(cc))
+#define SVY(cc) (Sxy[cc] * VX(cc) + Syy[cc] * VY(cc) + Syz[cc] * VZ(cc))
+#define SVZ(cc) (Sxz[cc] * VX(cc) + Syz[cc] * VY(cc) + Szz[cc] * VZ(cc))
+                d[D_E][c] += (SVX(xp) - SVX(xm)) / hx + (SVY(yp) - SVY(ym)) / hy + (SVZ(zp) - SVZ(zm)) / hz;
+                if (g->p.axisym) d[D_E][c] += SVX(c) / rcyl;
+#undef SVX
+#undef SVY
+#undef SVZ
+#undef VXW
+#undef VYW
+#undef VZW
+            }
+#undef VX
+#undef VY
+#undef VZ
+#undef VOIDC
+}
+
+/* Radial return to the yield surface, hydro_cpu.cpp:229-252. */
+void eorc_vonmises(eorc_grid* g, int reg) {
+    const eorc_params* P_ = &g->p;
+    const double Y0 = g->mat.Y;
+    if (Y0 <= 0 && !P_->rock) return;
+    double *Sxx = g->f[F_SXX], *Syy = g->f[F_SYY], *Szz = g->f[F_SZZ], *Sxy = g->f[F_SXY], *Sxz = g->f[F_SXZ],
+           *Syz = g->f[F_SYZ];
+    const double* r = g->f[F_R];
+    const double* D = g->f[F_D];
+    const double* af = g->f[F_AF];
+    double* vib = g->f[F_VIB];
+    for (int c = 0; c < g->n; c++) {
+        double Y;
+        if (P_->rock) {
+            double P = dmax2(eorc_pcell(g, c), 0.0);
+            double Peff = P;
+            if (P_->af_prel && vib[c] > 0) {
+                double p2, cs2;
+                eos_pc(&g->mat, r[c], eint(g, c), &p2, &cs2);
+                Peff = dmax2(P - r[c] * cs2 * vib[c], 0.0);
+            }
+            double Yi = P_->y_i0 + P_->mu_i * Peff / (1.0 + P_->mu_i * Peff / dmax2(P_->y_m - P_->y_i0, 1.0));
+            double Yd = dmin2(P_->y_d0 + P_->mu_d * Peff, P_->y_m);
+            double Yb = (1.0 - D[c]) * Yi + D[c] * Yd;
+            Y = P_->af_prel ? Yb : Yb * (1.0 - af[c]);
+            if (P_->y_bingham > 0 && af[c] > 1e-3) {
+                double Yf = dmin2(P_->y_bingham, Yb);
+                if (Y < Yf) Y = Yf;
+            }
+        } else {
+            Y = (1.0 - D[c]) * (1.0 - af[c]) * Y0;
+        }
+        double sxx = Sxx[c], syy = Syy[c], szz = Szz[c], sxy = Sxy[c], sxz = Sxz[c], syz = Syz[c];
+        double J2 = 0.5 * (sxx * sxx + syy * syy + szz * szz) + sxy * sxy + sxz * sxz + syz * syz;
+        double vm = sqrt(3.0 * J2);
+        if (vm > Y) {
+            double f = (vm > 0 ? Y / vm : 0.0);
+            Sxx[c] *= f; Syy[c] *= f; Szz[c] *= f; Sxy[c] *= f; Sxz[c] *= f; Syz[c] *= f;
+            if (P_->af_reg && reg && g->mat.G > 0 && (P_->rho_cfl <= 0 || r[c] > P_->rho_cfl)) {
+                double dW = (vm * vm - Y * Y) / (6.0 * g->mat.G);
+                vib[c] = sqrt(vib[c] * vib[c] + 2.0 * P_->c_reg * dW / r[c]);
+                g->f[F_E][c] -= P_->c_reg * dW;
+            }
+        }
+    }
+}
+
+/* Tensile damage growth from the weakest-flaw activation strain,
+ * hydro_cpu.cpp:253-258. */
+void eorc_grow_damage(eorc_grid* g, double dt) {
+    const double Em = g->mat.Emod, wk = g->mat.wk, wm = g->mat.wm;
+    if (Em <= 0 || wk <= 0) return;
+    const double dx = g->dx, eps_act = pow(1.0 / (wk * dx * dx * dx), 1.0 / wm);
+    double* D = g->f[F_D];
+    const double* r = g->f[F_R];
+    for (int c = 0; c < g->n; c++) {
+        if (D[c] >= 1.0) continue;
+        double P = eorc_pcell(g, c);
+        double sigmax = dmax2(-P + g->f[F_SXX][c], dmax2(-P + g->f[F_SYY][c], -P + g->f[F_SZZ][c]));
+        if (sigmax > 0.0 && sigmax / Em > eps_act) {
+            double cg = 0.4 * sqrt(Em / dmax2(r[c], 1e-30)), Rs = 0.5 * dx;
+            double d13 = pow(D[c], 1.0 / 3.0) + (cg / Rs) * dt;
+            D[c] = dmin2(1.0, d13 * d13 * d13);
+        }
+    }
+}
+
+/* Shock-activated acoustic fluidization, hydro_cpu.cpp:390-410. */
+void eorc_update_af(eorc_grid* g, double dt) {
+    const eorc_params* P_ = &g->p;
+    if (P_->c_act <= 0 || P_->tdec <= 0) return;
+    const double dec = exp(-dt / P_->tdec);
+    double *r = g->f[F_R], *vib = g->f[F_VIB], *Pmax = g->f[F_PMAX], *af = g->f[F_AF];
+    for (int c = 0; c < g->n; c++) {
+        double P = eorc_pcell(g, c);
+        double cs = orc_sound_speed(&g->mat, r[c], eint(g, c));
+        if (P > Pmax[c]) {
+            double dP = P - Pmax[c];
+            Pmax[c] = P;
+            if (dP > P_->p_act) {
+                double sp = P_->af_seeddp
+                                ? dP / (dmax2(r[c], 1e-30) * dmax2(cs, 1e-30))
+                                : sqrt(g->f[F_MU][c] * g->f[F_MU][c] + g->f[F_MV][c] * g->f[F_MV][c] +
+                                       g->f[F_MW][c] * g->f[F_MW][c]) / dmax2(r[c], 1e-30);
+                vib[c] = dmax2(vib[c], P_->c_act * sp);
+            }
+        }
+        double v0 = vib[c];
+        vib[c] *= dec;
+        double pov = dmax2(P, P_->p_coh);
+        if (P_->af_reg) {
+            if (r[c] > dmax2(P_->rho_cfl, 1e-12)) g->f[F_E][c] += 0.5 * r[c] * (v0 * v0 - vib[c] * vib[c]);
+            double vcap = P_->af_sat * pov / (dmax2(r[c], 1e-30) * dmax2(cs, 1e-30));
+            if (vib[c] > vcap) vib[c] = vcap;
+        }
+        double pvib = r[c] * cs * vib[c];
+        af[c] = pvib / (pvib + pov);
+    }
+}
+
+/* Largest signal speed |v| + sqrt(c^2 + 4G/(3 rho)), hydro_cpu.cpp:378-380. */
+double eorc_maxspeed(const eorc_grid* g) {
+    double s = 1e-30;
+    const double G = g->mat.G;
+    const double* r = g->f[F_R];
+    for (int c = 0; c < g->n; c++) {
+        if (r[c] < g->p.rho_cfl) continue;
+        double p, cs;
+        eos_pc(&g->mat, r[c], eint(g, c), &p, &cs);
+        double cel = sqrt(cs * cs + (G > 0 ? (4.0 / 3.0) * G / r[c] : 0.0));
+        double v = sqrt(g->f[F_MU][c] * g->f[F_MU][c] + g->f[F_MV][c] * g->f[F_MV][c] +
+                        g->f[F_MW][c] * g->f[F_MW][c]) / r[c];
+        s = dmax2(s, v + cel);
+    }
+    return s;
+}
+
+/* Near-void cells lose their momentum, hydro_cpu.cpp:272-273 (no frozen
+ * reference state). */
+static void void_cells(eorc_grid* g) {
+    if (g->p.rho_cfl <= 0) return;
+    for (int c = 0; c < g->n; c++)
+        if (g->f[F_R][c] < g->p.rho_cfl) g->f[F_MU][c] = g->f[F_MV][c] = g->f[F_MW][c] = 0;
+}
+
+static const int RK_FIELDS[ND] = {F_R, F_MU, F_MV, F_MW, F_E, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ, F_D, F_RC, F_VIB};
+
+/* Two-stage Runge-Kutta step, hydro_cpu.cpp:411-425. */
+void eorc_step_rk2(eorc_grid* g, double dt) {
+    const int n = g->n;
+    eorc_update_af(g, dt);
+    eorc_grid* g1 = eorc_create(g->nx, g->ny, g->nz, g->dx);
+    g1->mat = g->mat;
+    g1->p = g->p;
+    for (int q = 0; q < NF; q++) memcpy(g1->f[q], g->f[q], sizeof(double) * (size_t)n);
+    eorc_lop(g);
+    for (int q = 0; q < ND; q++) {
+        const double* x = g->f[RK_FIELDS[q]];
+        const double* dq = g->d[q];
+        double* y = g1->f[RK_FIELDS[q]];
+        for (int c = 0; c < n; c++) y[c] = x[c] + dt * dq[c];
+    }
+    void_cells(g1);
+    eorc_vonmises(g1, 0);
+    eorc_lop(g1);
+    for (int q = 0; q < ND; q++) {
+        double* x = g->f[RK_FIELDS[q]];
+        const double* y = g1->f[RK_FIELDS[q]];
+        const double* dq = g1->d[q];
+        for (int c = 0; c < n; c++) x[c] = 0.5 * (x[c] + y[c] + dt * dq[c]);
+    }
+    for (int q = 0; q < ND; q++) memcpy(g->d[q], g1->d[q], sizeof(double) * (size_t)n);
+    eorc_destroy(g1);
+    eorc_grow_damage(g, dt);
+    eorc_vonmises(g, 1);
+    if (g->p.damp < 1.0)
+        for (int c = 0; c < n; c++) {
+            g->f[F_MU][c] *= g->p.damp;
+            g->f[F_MV][c] *= g->p.damp;
+            g->f[F_MW][c] *= g->p.damp;
+        }
+    void_cells(g);
+}
+
+int eorc_run(eorc_grid* g, double cfl, double t_end, int max_steps, double* t_out) {
+    double t = 0;
+    int s = 0;
+    while (t < t_end && (max_steps < 0 || s < max_steps)) {
+        double dt = cfl * g->dx / eorc_maxspeed(g);
+        if (t + dt > t_end) dt = t_end - t;
+        eorc_step_rk2(g, dt);
+        t += dt;
+        s++;
+    }
+    if (t_out) *t_out = t;
+    return s;
+}
