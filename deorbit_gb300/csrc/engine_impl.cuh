@@ -1651,8 +1651,12 @@ public:
 
     // Levels of a graded impact: power-of-two bands of the reference smoothing
     // length h0 above its smallest value, each with cells 2^L base cells wide
-    // over the box of its particles (padded by a tenth of the domain per side,
-    // at least two level cells), when the h0 range spans more than a factor 2.
+    // over the box of its particles padded by two level cells per side, when
+    // the h0 range spans more than a factor 2.  A particle that later leaves
+    // its level's box is clamped into the border cells and flags the level, so
+    // searches never skip that level and never prune its border columns; tight
+    // boxes keep a coarse particle's search off the empty cells of the finer
+    // levels' boxes.
     void make_levels(ImpactD& I, const ImpactH& h, int64_t budget) {
         if (!levels_ || !h.use_h0 || h.per[0] || h.per[1] || h.per[2] || h.sh0.empty()) return;
         float h0min = 3.4e38f, h0max = 0.0f;
@@ -1688,7 +1692,7 @@ public:
             for (int a = 0; a < 3; a++) {
                 const int top = (I.nf[a] - 1) >> L;
                 if (lo[L][a] > hi[L][a]) { lo[L][a] = 0; hi[L][a] = 0; }  // an empty level: one cell
-                const int pad = std::max(2, (int)std::ceil(0.1 * (double)I.nf[a] / (double)(1 << L)));
+                const int pad = 2;
                 llo[L][a] = std::max(0, lo[L][a] - pad);
                 const int e = std::min(top, hi[L][a] + pad);
                 lnf[L][a] = e - llo[L][a] + 1;

@@ -1166,7 +1166,10 @@ int eu_run(eu_grid* h, double cfl, double t_end, int64_t max_steps, int64_t* ste
             if (limit >= 0) todo = (int)std::min<int64_t>(todo, limit - c.steps);
             for (int i = 0; i < todo; i++) EU_CUDA(cudaGraphLaunch(g->graph, g->st));
             g->launches += per_step * todo;
+            const double t_prev = c.t;
             c = g->read_ctl();
+            if (!(c.t > t_prev))  // dt collapsed (signal speed not finite): stop instead of spinning
+                throw SphError(SPH_ERR_STATE, "time step collapsed: no progress in t (non-finite state?)");
             chunk = std::min(chunk * 2, 64);
         }
         if (steps) *steps = c.steps - c0.steps;

@@ -4,9 +4,8 @@ sorted into cells of their own width (2^L base cells) over their own box, and
 every search visits the levels its sphere meets.  Checked on a crop of the
 graded slab (h0 spanning a factor > 2): the neighbour sets and reference cell
 lists are bit-exact with the oracle's, the FP64 trajectory matches the oracle
-to 1e-9, the results agree with the one-grid traversal to rounding of the
-summation order (FP64 1e-12), and the list build over the levels finds exactly
-the one-grid lists' entries on the same state."""
+to 1e-9, and the results agree with the one-grid traversal to rounding of the
+summation order (FP64 1e-12)."""
 import numpy as np
 import pytest
 
@@ -107,15 +106,34 @@ def test_levels_mixed_matches_one_grid(cuda_lib, graded):
     assert not bad, errs
 
 
+
 @pytest.mark.parametrize("precision", [0, 1])
-def test_level_lists_cover_the_one_grid_lists(cuda_lib, graded, precision):
-    """On the same state (right after init) the list build over the levels
-    finds exactly as many entries as the one-grid build: the superset lists
-    {j : r < 2 h_k (1 + slack)} do not depend on the traversal grid."""
+def test_level_sets_exact_with_particles_outside_their_boxes(cuda_lib, graded, precision):
+    """Level boxes are fixed when the impact is committed; particles written
+    far outside their level's box (fine surface particles moved deep into the
+    coarse region and up above the slab) are clamped into its border cells,
+    and the neighbour sets stay bit-exact with the oracle's."""
     from deorbit_gb300 import sph
-    entries = {}
-    for levels in (1, 0):
-        ctx, b = _run(sph, graded, precision, levels, 0)
-        entries[levels] = ctx.get_option("list_entries")
-        ctx.close()
-    assert entries[1] == entries[0] and entries[0] > 0, entries
+    ctx, b = _run(sph, graded, precision, 1, 1)
+    state = {k: ctx.read(b, k) for k in ("x", "y", "z", "hh")}
+    h0 = graded.h0
+    fine = np.flatnonzero(h0 < 1.5 * h0.min())
+    rng = np.random.default_rng(5)
+    pick = rng.choice(fine, size=max(8, fine.size // 50), replace=False)
+    depth = state["z"].max() - state["z"].min()
+    half = pick.size // 2
+    state["z"][pick[:half]] -= 0.6 * depth
+    state["z"][pick[half:]] += 0.3 * depth
+    for k, v in state.items():
+        ctx.write(b, k, v)
+    sets = [ctx.neighbors(b, kind) for kind in (0, 1)]
+    ctx.close()
+    orc = O.from_scenario(graded, threads=16)
+    for k, v in state.items():
+        orc.set_field(k, v)
+    orc.build_cells()
+    for kind, (cnt, nb) in enumerate(sets):
+        ocnt, onb = orc.neighbors(kind)
+        assert np.array_equal(cnt, ocnt), kind
+        assert np.array_equal(nb, _sorted_sets(ocnt, onb)), kind
+    orc.close()
