@@ -468,6 +468,81 @@ def halfspace_section(sph, ic, device, steps=200):
             "fp64_vs_oracle_rel_l2": err}
 
 
+# Compulsory state traffic of one grid cell-step (FP64): the 14 Runge-Kutta
+# fields (rho, momentum, energy, deviatoric stress, damage, tracer, vibration)
+# read and written once, the fluidization ratio read once.
+EULER_STEP_BYTES = 14 * 8 * 2 + 8
+
+
+def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32):
+    """The Euler grid solver (hydrocodes/euler/hydro_cpu.cpp step_rk2) on the
+    3-D half-space impact: N^3 cells of 50 m, basalt sphere at 30 deg, ROCK
+    yield, tensile damage, gravity, near-void cells.  Device loop (dt on the
+    device, steps replayed from a CUDA graph) timed with events; e2e through
+    the C ABI with every field written from and read back to pinned host
+    memory each step; the CPU oracle (the reference's algorithm, serial like
+    the reference) on a cropped grid; rel-L2 against the oracle."""
+    import torch
+    from deorbit_gb300 import euler as E, grid_ic as GI
+    from oracle import euler as EO
+
+    case = GI.impact3d(N)
+    g = E.from_case(case, device=device)
+    g.run(case.cfl, case.t_end, max(warmup, 3))
+    g.synchronize()
+    l0 = g.launches()
+    g.event_record(0)
+    s, t = g.run(case.cfl, case.t_end, steps)
+    g.event_record(1)
+    ms = g.event_elapsed(0, 1)
+    launches = g.launches() - l0
+    # e2e: host buffers every step
+    names = E.FIELDS
+    host = {k: torch.empty(case.n, dtype=torch.float64).pin_memory().numpy() for k in names}
+    g.read_many(names, [host[k] for k in names])
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.write_many(host)
+        g.run(case.cfl, case.t_end, 1)
+        g.read_many(names, [host[k] for k in names])
+    el = time.perf_counter() - t0
+    g.close()
+    nbytes = len(names) * 8 * case.n
+    hbm, hbm_kind = peaks()
+    value = case.n * s / (ms / 1000.0)
+    out = {"workload": f"3-D half-space impact, {N}^3 cells of 50 m, basalt sphere r = {N // 16} cells at 30 deg, "
+                       "8 km/s; ROCK yield, tensile damage, gravity 3.71, near-void < 100 kg/m^3",
+           "cells": case.n, "steps": s, "ms_per_step": ms / max(s, 1), "value": value, "unit": "cell-steps/s",
+           "dtype": "f64", "gpu_launches": launches,
+           "e2e": {"value": case.n * steps / el, "unit": "cell-steps/s", "h2d_bytes_per_step": nbytes,
+                   "d2h_bytes_per_step": nbytes, "pinned_host": True},
+           "step_roofline": {"alg_bytes_per_cell_step": EULER_STEP_BYTES,
+                             "achieved_gbs": EULER_STEP_BYTES * value / 1e9,
+                             "frac": EULER_STEP_BYTES * value / 1e9 / hbm, "peak_kind": f"{hbm_kind} copy bandwidth"}}
+    # CPU oracle on a smaller grid of the same workload (serial, as the reference)
+    small = GI.impact3d(cpu_n)
+    o = EO.from_case(small)
+    o.run(small.cfl, small.t_end, 1)
+    t0 = time.perf_counter()
+    so, _ = o.run(small.cfl, small.t_end, 2)
+    el = time.perf_counter() - t0
+    o.close()
+    out["cpu_baseline"] = {"value": small.n * so / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+                           "sample": f"the same impact on {cpu_n}^3 cells, {so} steps after one warm-up step"}
+    # parity on a small grid of the same workload
+    acc = GI.impact3d(acc_n)
+    a = E.from_case(acc, device=device)
+    a.run(acc.cfl, acc.t_end, 10)
+    o = EO.from_case(acc)
+    o.run(acc.cfl, acc.t_end, 10)
+    out["vs_oracle_rel_l2"] = {k: float(np.linalg.norm(a.read(k) - o.field(k)) / max(np.linalg.norm(o.field(k)), 1e-300))
+                               for k in ("r", "mu", "mw", "E", "Sxx", "Sxy", "D")}
+    out["vs_oracle_sample"] = f"{acc_n}^3 cells, 10 steps"
+    a.close()
+    o.close()
+    return out
+
+
 def serving_section(device, rates=(4.0, 8.0, 16.0), count=200, steps=300):
     """Poisson request streams through the continuous-batching server."""
     from deorbit_gb300 import serve, sph
@@ -515,6 +590,8 @@ def main():
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-halfspace", action="store_true")
+    ap.add_argument("--no-euler", action="store_true")
+    ap.add_argument("--euler-n", type=int, default=256)
     args = ap.parse_args()
     rank, world, local = rank_info()
 
@@ -623,6 +700,9 @@ def main():
     halfspace = None
     if rank == 0 and world == 1 and not args.no_halfspace:
         halfspace = halfspace_section(sph, ic, device)
+    euler = None
+    if rank == 0 and world == 1 and not args.no_euler:
+        euler = euler_section(device, args.steps, args.warmup, args.euler_n)
 
     # ---- accuracy of the mixed form against FP64 (same dt sequence), and of
     # both forms against the oracle on a bounded sample
@@ -694,7 +774,8 @@ def main():
                 "mixed_vs_fp64_rel_l2": err,
                 "accuracy_vs_oracle": acc,
                 "kernel_ms": {k: v[0] for k, v in kst.items()},
-                "batched": batched, "serving": serving, "large": large, "halfspace": halfspace}
+                "batched": batched, "serving": serving, "large": large, "halfspace": halfspace,
+                "euler": euler}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

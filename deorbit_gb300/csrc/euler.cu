@@ -485,8 +485,10 @@ static __global__ void __launch_bounds__(256) k_face(P p, Prim W, Faces F, const
 
 // Right-hand side of one cell (hydro_cpu.cpp:98-214): the three directions'
 // flux differences in the reference's order, gravity, strength sources.
-// s: the state Lop reads; af: its fluidization ratio.
-static __global__ void __launch_bounds__(256) k_rhs(P p, Fields s, const double* af, Faces F, Rhs d,
+// s: the state Lop reads; W: its primitives (k_prim), whose velocities mu/rho
+// are the very quotients the reference forms for every neighbour it reads;
+// af: the fluidization ratio.
+static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, Prim W, const double* af, Faces F, Rhs d,
                                                    const Ctl* ctl) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
@@ -516,7 +518,9 @@ static __global__ void __launch_bounds__(256) k_rhs(P p, Fields s, const double*
                 dmn = -(w1 * Fq[1][b] - w0 * Fq[1][a]) * inv;
                 dt1 = -(w1 * Fq[2][b] - w0 * Fq[2][a]) * inv;
                 dt2 = -(w1 * Fq[3][b] - w0 * Fq[3][a]) * inv;
-                dmn += pcell(p, s, c) / ((i + 0.5) * p.dx);
+                double pr, cs;
+                eos_pc(p.m, r[c], W.w[4][c], pr, cs);  // Pcell: EOS at the cell's internal energy
+                dmn += pr / ((i + 0.5) * p.dx);
             } else {  // face weights 1 (exact products)
                 const double inv = p.invdx;
                 vr = -(Fq[0][b] - Fq[0][a]) * inv;
@@ -550,11 +554,14 @@ static __global__ void __launch_bounds__(256) k_rhs(P p, Fields s, const double*
         const int64_t zm = c - (k > 0 ? 1 : 0), zp = c + (k < p.nz - 1 ? 1 : 0);
         const double hx = ((i > 0 && i < p.nx - 1) ? 2.0 : 1.0) * dx, hy = ((j > 0 && j < p.ny - 1) ? 2.0 : 1.0) * dx,
                      hz = ((k > 0 && k < p.nz - 1) ? 2.0 : 1.0) * dx;
-        const double vxc = mu[c] / r[c], vyc = mv[c] / r[c], vzc = mw[c] / r[c];
+        const double* Vx = W.w[1];  // mu / rho of every cell
+        const double* Vy = W.w[2];
+        const double* Vz = W.w[3];
+        const double vxc = Vx[c], vyc = Vy[c], vzc = Vz[c];
         const bool vd = p.rho_cfl > 0;
-        auto vxw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vxc : mu[q] / r[q]; };
-        auto vyw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vyc : mv[q] / r[q]; };
-        auto vzw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vzc : mw[q] / r[q]; };
+        auto vxw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vxc : Vx[q]; };
+        auto vyw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vyc : Vy[q]; };
+        auto vzw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vzc : Vz[q]; };
         const double Lxx = (vxw(xp) - vxw(xm)) / hx, Lxy = (vxw(yp) - vxw(ym)) / hy, Lxz = (vxw(zp) - vxw(zm)) / hz;
         const double Lyx = (vyw(xp) - vyw(xm)) / hx, Lyy = (vyw(yp) - vyw(ym)) / hy, Lyz = (vyw(zp) - vyw(zm)) / hz;
         const double Lzx = (vzw(xp) - vzw(xm)) / hx, Lzy = (vzw(yp) - vzw(ym)) / hy, Lzz = (vzw(zp) - vzw(zm)) / hz;
@@ -613,9 +620,9 @@ static __global__ void __launch_bounds__(256) k_rhs(P p, Fields s, const double*
         }
         if (af[c] > 0 && p.eta_af > 0) {  // explicit fluidization viscosity, hydro_cpu.cpp:190-197
             const double eta = af[c] * p.eta_af, id2 = 1.0 / (dx * dx);
-            auto vx = [&](int64_t q) { return mu[q] / r[q]; };
-            auto vy = [&](int64_t q) { return mv[q] / r[q]; };
-            auto vz = [&](int64_t q) { return mw[q] / r[q]; };
+            auto vx = [&](int64_t q) { return Vx[q]; };
+            auto vy = [&](int64_t q) { return Vy[q]; };
+            auto vz = [&](int64_t q) { return Vz[q]; };
             dmu += eta * (vx(xp) + vx(xm) + vx(yp) + vx(ym) + vx(zp) + vx(zm) - 6 * vx(c)) * id2;
             dmv += eta * (vy(xp) + vy(xm) + vy(yp) + vy(ym) + vy(zp) + vy(zm) - 6 * vy(c)) * id2;
             dmw += eta * (vz(xp) + vz(xm) + vz(yp) + vz(ym) + vz(zp) + vz(zm) - 6 * vz(c)) * id2;
@@ -625,9 +632,9 @@ static __global__ void __launch_bounds__(256) k_rhs(P p, Fields s, const double*
             }
         }
         // div(S.v) into energy, hydro_cpu.cpp:198-203
-        auto svx = [&](int64_t q) { return Sxx[q] * (mu[q] / r[q]) + Sxy[q] * (mv[q] / r[q]) + Sxz[q] * (mw[q] / r[q]); };
-        auto svy = [&](int64_t q) { return Sxy[q] * (mu[q] / r[q]) + Syy[q] * (mv[q] / r[q]) + Syz[q] * (mw[q] / r[q]); };
-        auto svz = [&](int64_t q) { return Sxz[q] * (mu[q] / r[q]) + Syz[q] * (mv[q] / r[q]) + Szz[q] * (mw[q] / r[q]); };
+        auto svx = [&](int64_t q) { return Sxx[q] * Vx[q] + Sxy[q] * Vy[q] + Sxz[q] * Vz[q]; };
+        auto svy = [&](int64_t q) { return Sxy[q] * Vx[q] + Syy[q] * Vy[q] + Syz[q] * Vz[q]; };
+        auto svz = [&](int64_t q) { return Sxz[q] * Vx[q] + Syz[q] * Vy[q] + Szz[q] * Vz[q]; };
         dE += (svx(xp) - svx(xm)) / hx + (svy(yp) - svy(ym)) / hy + (svz(zp) - svz(zm)) / hz;
         if (p.axisym) dE += svx(c) / rcyl;
     }
@@ -772,7 +779,7 @@ struct Grid {
         k_face<0><<<grid_of(face_count<0>(p.nx, p.ny, p.nz)), 256, 0, st>>>(p, W, F, ctl);
         k_face<1><<<grid_of(face_count<1>(p.nx, p.ny, p.nz)), 256, 0, st>>>(p, W, F, ctl);
         k_face<2><<<grid_of(face_count<2>(p.nx, p.ny, p.nz)), 256, 0, st>>>(p, W, F, ctl);
-        k_rhs<<<grid_of(n), 256, 0, st>>>(p, s, g.q[F_AF], F, d, ctl);
+        k_rhs<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(p, s, W, g.q[F_AF], F, d, ctl);
         launches += 5;
     }
 
