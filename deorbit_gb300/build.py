@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdeorbit_sph.so")
 
 SOURCES = ["scan_sort.cu", "engine_fp64.cu", "engine_mixed.cu", "capi.cu", "cell_sort_api.cu", "serve.cpp",
-           "euler.cu"]
+           "euler.cu", "euler_mixed.cu"]
 # Per-source flags: the grid solver evaluates every expression in the
 # reference's operation order, without fused multiply-adds.
 SOURCE_FLAGS = {"euler.cu": ["--fmad=false"]}

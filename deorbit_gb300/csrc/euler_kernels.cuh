@@ -1,0 +1,741 @@
+// euler_kernels.cuh -- device code of the Eulerian grid hydrocode (the
+// reference's hydrocodes/euler/hydro_cpu.cpp), shared by the two precision
+// forms:
+//   plain (FP64, euler.cu, compiled without fused multiply-adds): every
+//     expression in the reference's operation order;
+//   mixed (euler_mixed.cu): primitives, face fluxes and the right-hand side's
+//     sources in FP32 (the arithmetic of the reference's own GPU solver), the
+//     state, the Runge-Kutta stages, yield, damage, fluidization and the CFL
+//     speed in FP64.
+// The compute type R of the Lop kernels is the template parameter; state and
+// right-hand side are always FP64.  Literals are written as R(...) so that an
+// FP32 instantiation never promotes to FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace deu {
+
+// ---------------------------------------------------------------- materials
+
+template <class R>
+struct MatT {
+    int32_t ideal;
+    R gamma, rho0, a, b, A, B, alpha, beta, u0, uiv, ucv, G, Y, Emod, wm, wk;
+};
+using Mat = MatT<double>;
+
+template <class R>
+__host__ __device__ __forceinline__ MatT<R> mat_as(const Mat& m) {
+    return MatT<R>{m.ideal, R(m.gamma), R(m.rho0), R(m.a), R(m.b), R(m.A), R(m.B), R(m.alpha), R(m.beta),
+                   R(m.u0), R(m.uiv), R(m.ucv), R(m.G), R(m.Y), R(m.Emod), R(m.wm), R(m.wk)};
+}
+
+// Settings + material + grid geometry, passed by value to every kernel.
+struct P {
+    Mat m;
+    double gz, tdec, eta_af, c_act, p_coh, p_act, rho_cfl, damp, rho_vac;
+    double y_i0, mu_i, mu_d, y_d0, y_m, y_bingham, c_reg, af_sat;
+    int32_t axisym, rock, af_reg, af_prel, af_seeddp;
+    int32_t nx, ny, nz;
+    int64_t n;
+    double dx, invdx;
+    double eps_act;  // weakest-flaw activation strain, formed on the host as in hydro_cpu.cpp:254
+};
+
+template <class R> __device__ __forceinline__ R dmax2(R a, R b) { return a < b ? b : a; }  // std::max
+template <class R> __device__ __forceinline__ R dmin2(R a, R b) { return b < a ? b : a; }  // std::min
+
+// Tillotson pressure, eos.hpp:52-63.
+template <class R>
+__device__ R till(const MatT<R>& m, R rho, R u) {
+    if (rho <= R(0)) return R(0);
+    R eta = rho / m.rho0, mu = eta - R(1);
+    R w0 = u / (m.u0 * eta * eta) + R(1);
+    R Pc = (m.a + m.b / w0) * rho * u + m.A * mu + m.B * mu * mu;
+    if (rho >= m.rho0 || u <= m.uiv) return Pc;
+    R z = m.rho0 / rho - R(1);
+    R Pe = m.a * rho * u + (m.b * rho * u / w0 + m.A * mu * exp(-m.beta * z)) * exp(-m.alpha * z * z);
+    if (u >= m.ucv) return Pe;
+    return ((u - m.uiv) * Pe + (m.ucv - u) * Pc) / (m.ucv - m.uiv);
+}
+
+template <class R>
+__device__ __forceinline__ R pressure(const MatT<R>& m, R rho, R u) {  // eos.hpp:65-68
+    if (m.ideal) return (m.gamma - R(1)) * rho * u;
+    return till(m, rho, u);
+}
+
+// Condensed-branch value and analytic derivatives, eos.hpp:72-79.
+template <class R>
+__device__ void cond_d(const MatT<R>& m, R rho, R u, R& P, R& dPdr, R& dPdu) {
+    R eta = rho / m.rho0, mu = eta - R(1);
+    R w = R(1) + u / (m.u0 * eta * eta), aob = m.a + m.b / w;
+    P = aob * rho * u + m.A * mu + m.B * mu * mu;
+    dPdu = aob * rho - m.b * rho * u / (w * w * m.u0 * eta * eta);
+    R dwdr = R(-2) * u / (m.u0 * eta * eta * eta * m.rho0);
+    dPdr = aob * u + rho * u * (-m.b / (w * w)) * dwdr + m.A / m.rho0 + R(2) * m.B * mu / m.rho0;
+}
+
+// Expanded-branch value and analytic derivatives, eos.hpp:80-94.
+template <class R>
+__device__ void expd_d(const MatT<R>& m, R rho, R u, R& P, R& dPdr, R& dPdu) {
+    R eta = rho / m.rho0, mu = eta - R(1);
+    R w = R(1) + u / (m.u0 * eta * eta);
+    R z = m.rho0 / rho - R(1), dzdr = -m.rho0 / (rho * rho);
+    R E1 = exp(-m.alpha * z * z), E2 = exp(-m.beta * z);
+    R G = m.b * rho * u / w + m.A * mu * E2;
+    P = m.a * rho * u + G * E1;
+    R dwdr = R(-2) * u / (m.u0 * eta * eta * eta * m.rho0);
+    R dGu = m.b * rho / w - m.b * rho * u / (w * w * m.u0 * eta * eta);
+    dPdu = m.a * rho + dGu * E1;
+    R dbruw_dr = m.b * u / w + m.b * rho * u * (R(-1) / (w * w)) * dwdr;
+    R dGr = dbruw_dr + m.A * E2 / m.rho0 + m.A * mu * (E2 * (-m.beta) * dzdr);
+    R dE1dr = E1 * (-m.alpha * R(2) * z) * dzdr;
+    dPdr = m.a * u + dGr * E1 + G * dE1dr;
+}
+
+// Analytic sound speed, eos.hpp:95-113.
+template <class R>
+__device__ R sound_speed(const MatT<R>& m, R rho, R u) {
+    if (m.ideal) {
+        R Pi = (m.gamma - R(1)) * rho * u;
+        return sqrt(dmax2(m.gamma * Pi / dmax2(rho, R(1e-30)), R(1e-12)));
+    }
+    if (rho <= R(0)) return R(1e-3);
+    R Pp, dPdr, dPdu;
+    if (rho >= m.rho0 || u <= m.uiv) {
+        cond_d(m, rho, u, Pp, dPdr, dPdu);
+    } else if (u >= m.ucv) {
+        expd_d(m, rho, u, Pp, dPdr, dPdu);
+    } else {
+        R Pc, dPcr, dPcu, Pe, dPer, dPeu;
+        cond_d(m, rho, u, Pc, dPcr, dPcu);
+        expd_d(m, rho, u, Pe, dPer, dPeu);
+        R inv = R(1) / (m.ucv - m.uiv);
+        Pp = ((u - m.uiv) * Pe + (m.ucv - u) * Pc) * inv;
+        dPdu = ((Pe + (u - m.uiv) * dPeu) + (-Pc + (m.ucv - u) * dPcu)) * inv;
+        dPdr = ((u - m.uiv) * dPer + (m.ucv - u) * dPcr) * inv;
+    }
+    return sqrt(dmax2(dPdr + Pp / (rho * rho) * dPdu, R(1e-6)));
+}
+
+// hydro_cpu.cpp:38: pressure clamped at 0 and the sound speed.
+template <class R>
+__device__ __forceinline__ void eos_pc(const MatT<R>& m, R rho, R e, R& p, R& cs) {
+    p = pressure(m, rho, e);
+    if (p < R(0)) p = R(0);
+    cs = sound_speed(m, rho, e);
+}
+
+// ---------------------------------------------------------------- face flux
+
+template <class R>
+struct F5 {
+    R r, mn, mt1, mt2, E;
+};
+
+template <class R>
+__device__ __forceinline__ F5<R> flux_of(R r, R vn, R t1, R t2, R p, R E) {
+    return F5<R>{r * vn, r * vn * vn + p, r * vn * t1, r * vn * t2, (E + p) * vn};
+}
+
+// Exact rarefaction into vacuum sampled at the face, hydro_cpu.cpp:43-53.
+template <class R>
+__device__ F5<R> vac_flux(const MatT<R>& m, R rM, R vnM, R t1M, R t2M, R eM, int side) {
+    R pM, cM;
+    eos_pc(m, rM, eM, pM, cM);
+    R g = rM * cM * cM / dmax2(pM, R(1e-30));
+    if (g < R(1.01)) g = R(1.01);
+    if (g > R(1e5)) g = R(1e5);
+    R s = (R)side, vn = s * vnM;
+    if (vn - cM >= R(0)) {
+        R E = rM * eM + R(0.5) * rM * (vnM * vnM + t1M * t1M + t2M * t2M);
+        return F5<R>{rM * vnM, rM * vnM * vnM + pM, rM * vnM * t1M, rM * vnM * t2M, (E + pM) * vnM};
+    }
+    if (vn + R(2) * cM / (g - R(1)) <= R(0)) return F5<R>{R(0), R(0), R(0), R(0), R(0)};
+    R u0 = R(2) / (g + R(1)) * (cM + R(0.5) * (g - R(1)) * vn), c0 = u0;
+    R r0 = rM * pow(c0 / cM, R(2) / (g - R(1))), p0 = pM * pow(r0 / rM, g), e0 = p0 / ((g - R(1)) * r0),
+      un0 = s * u0;
+    R E0 = r0 * e0 + R(0.5) * r0 * (un0 * un0 + t1M * t1M + t2M * t2M);
+    return F5<R>{r0 * un0, r0 * un0 * un0 + p0, r0 * un0 * t1M, r0 * un0 * t2M, (E0 + p0) * un0};
+}
+
+template <class R>
+__device__ __forceinline__ F5<R> hllc_star(R r, R vn, R t1, R t2, R p, R E, R S, R Ss, F5<R> Fk) {
+    R f = r * (S - vn) / (S - Ss);
+    F5<R> Us{f, f * Ss, f * t1, f * t2, f * (E / r + (Ss - vn) * (Ss + p / (r * (S - vn))))};
+    F5<R> U{r, r * vn, r * t1, r * t2, E};
+    return F5<R>{Fk.r + S * (Us.r - U.r), Fk.mn + S * (Us.mn - U.mn), Fk.mt1 + S * (Us.mt1 - U.mt1),
+                 Fk.mt2 + S * (Us.mt2 - U.mt2), Fk.E + S * (Us.E - U.E)};
+}
+
+// HLLC, hydro_cpu.cpp:54-74.
+template <class R>
+__device__ F5<R> hllc(const MatT<R>& m, R rho_vac, R rL, R vnL, R t1L, R t2L, R eL, R rR, R vnR, R t1R, R t2R,
+                      R eR) {
+    if (rho_vac > R(0)) {
+        bool vL = rL < rho_vac, vR = rR < rho_vac;
+        if (vL && vR) return F5<R>{R(0), R(0), R(0), R(0), R(0)};
+        if (vR) return vac_flux(m, rL, vnL, t1L, t2L, eL, +1);
+        if (vL) return vac_flux(m, rR, vnR, t1R, t2R, eR, -1);
+    }
+    R pL, cL, pR, cR;
+    eos_pc(m, rL, eL, pL, cL);
+    eos_pc(m, rR, eR, pR, cR);
+    R SL = dmin2(vnL - cL, vnR - cR), SR = dmax2(vnL + cL, vnR + cR);
+    R Ss = (pR - pL + rL * vnL * (SL - vnL) - rR * vnR * (SR - vnR)) / (rL * (SL - vnL) - rR * (SR - vnR));
+    R EL = rL * eL + R(0.5) * rL * (vnL * vnL + t1L * t1L + t2L * t2L),
+      ER = rR * eR + R(0.5) * rR * (vnR * vnR + t1R * t1R + t2R * t2R);
+    if (SL >= R(0)) return flux_of(rL, vnL, t1L, t2L, pL, EL);
+    if (SR <= R(0)) return flux_of(rR, vnR, t1R, t2R, pR, ER);
+    if (Ss >= R(0)) return hllc_star(rL, vnL, t1L, t2L, pL, EL, SL, Ss, flux_of(rL, vnL, t1L, t2L, pL, EL));
+    return hllc_star(rR, vnR, t1R, t2R, pR, ER, SR, Ss, flux_of(rR, vnR, t1R, t2R, pR, ER));
+}
+
+template <class R>
+__device__ __forceinline__ R mm(R a, R b) {  // minmod, hydro_cpu.cpp:89
+    return (a * b <= R(0)) ? R(0) : (fabs(a) < fabs(b) ? a : b);
+}
+
+// ---------------------------------------------------------------- state
+
+enum { F_R, F_MU, F_MV, F_MW, F_E, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ, F_D, F_AF, F_RC, F_VIB, F_PMAX, NF };
+// Runge-Kutta fields (hydro_cpu.cpp:413-417) and the right-hand side, same order.
+enum { D_R, D_MU, D_MV, D_MW, D_E, D_SXX, D_SYY, D_SZZ, D_SXY, D_SXZ, D_SYZ, D_D, D_RC, D_VIB, ND };
+__host__ __device__ constexpr int rk_field(int q) {  // r .. Syz, D keep their index; rc, vib follow af
+    return q <= D_D ? q : (q == D_RC ? F_RC : F_VIB);
+}
+inline const char* const kFieldNames[NF] = {"r", "mu", "mv", "mw", "E", "Sxx", "Syy", "Szz",
+                                      "Sxy", "Sxz", "Syz", "D", "af", "rc", "vib", "Pmax"};
+inline const char* const kRhsNames[ND] = {"r", "mu", "mv", "mw", "E", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz", "D", "rc", "vib"};
+
+// One state of the grid: the 16 fields (a predictor state aliases af and Pmax
+// of the state it was formed from).
+struct Fields {
+    double* q[NF];
+};
+struct Rhs {
+    double* q[ND];
+};
+template <class R>
+struct PrimT {  // rho, vx, vy, vz, e, rc/rho in the Lop's compute type
+    R* w[6];
+};
+template <class R>
+struct FacesT {  // per direction: mass, normal / tangential momentum, energy, tracer fluxes
+    R* q[3][6];
+};
+
+// Device-resident step control (the drivers' loop of hydro_cpu.cpp:452).
+struct Ctl {
+    double dt, t, t_end, cfl;
+    int64_t steps, max_steps;
+    int32_t active, pad;
+    unsigned long long smax_bits;  // CFL speed of this step (positive doubles order as their bits)
+};
+
+static __device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+
+// hydro_cpu.cpp:94-95
+static __device__ __forceinline__ double eint_of(double r, double mu, double mv, double mw, double E) {
+    double ke = 0.5 * (mu * mu + mv * mv + mw * mw) / r;
+    return (E - ke) / r;
+}
+static __device__ __forceinline__ double pcell(const P& p, const Fields& s, int64_t c) {
+    double pr, cs;
+    const double r = s.q[F_R][c];
+    eos_pc(p.m, r, eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c]), pr, cs);
+    return pr;
+}
+
+// Acoustic fluidization of one cell, hydro_cpu.cpp:390-410.
+static __device__ void update_af_cell(const P& p, const Fields& g, int64_t c, double dt) {
+    const double dec = exp(-dt / p.tdec);
+    double* r = g.q[F_R];
+    double* vib = g.q[F_VIB];
+    double* Pmax = g.q[F_PMAX];
+    const double e = eint_of(r[c], g.q[F_MU][c], g.q[F_MV][c], g.q[F_MW][c], g.q[F_E][c]);
+    double Pc, cs;  // Pcell and MAT.sound_speed of the cell
+    eos_pc(p.m, r[c], e, Pc, cs);
+    if (Pc > Pmax[c]) {
+        double dP = Pc - Pmax[c];
+        Pmax[c] = Pc;
+        if (dP > p.p_act) {
+            double sp = p.af_seeddp ? dP / (dmax2(r[c], 1e-30) * dmax2(cs, 1e-30))
+                                    : sqrt(g.q[F_MU][c] * g.q[F_MU][c] + g.q[F_MV][c] * g.q[F_MV][c] +
+                                           g.q[F_MW][c] * g.q[F_MW][c]) / dmax2(r[c], 1e-30);
+            vib[c] = dmax2(vib[c], p.c_act * sp);
+        }
+    }
+    double v0 = vib[c];
+    vib[c] *= dec;
+    double pov = dmax2(Pc, p.p_coh);
+    if (p.af_reg) {
+        if (r[c] > dmax2(p.rho_cfl, 1e-12)) g.q[F_E][c] += 0.5 * r[c] * (v0 * v0 - vib[c] * vib[c]);
+        double vcap = p.af_sat * pov / (dmax2(r[c], 1e-30) * dmax2(cs, 1e-30));
+        if (vib[c] > vcap) vib[c] = vcap;
+    }
+    double pvib = r[c] * cs * vib[c];
+    g.q[F_AF][c] = pvib / (pvib + pov);
+}
+
+// Radial return of one cell, hydro_cpu.cpp:229-252 (s: the stress / energy /
+// vibration state; af from the state the step started from).
+static __device__ void vonmises_cell(const P& p, const Fields& s, const double* af, int64_t c, bool reg) {
+    if (p.m.Y <= 0 && !p.rock) return;
+    double Y;
+    const double r = s.q[F_R][c];
+    if (p.rock) {
+        double Pp = dmax2(pcell(p, s, c), 0.0);
+        double Peff = Pp;
+        if (p.af_prel && s.q[F_VIB][c] > 0) {
+            double p2, cs2;
+            eos_pc(p.m, r, eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c]), p2, cs2);
+            Peff = dmax2(Pp - r * cs2 * s.q[F_VIB][c], 0.0);
+        }
+        double Yi = p.y_i0 + p.mu_i * Peff / (1.0 + p.mu_i * Peff / dmax2(p.y_m - p.y_i0, 1.0));
+        double Yd = dmin2(p.y_d0 + p.mu_d * Peff, p.y_m);
+        const double D = s.q[F_D][c];
+        double Yb = (1.0 - D) * Yi + D * Yd;
+        Y = p.af_prel ? Yb : Yb * (1.0 - af[c]);
+        if (p.y_bingham > 0 && af[c] > 1e-3) {
+            double Yf = dmin2(p.y_bingham, Yb);
+            if (Y < Yf) Y = Yf;
+        }
+    } else {
+        Y = (1.0 - s.q[F_D][c]) * (1.0 - af[c]) * p.m.Y;
+    }
+    double sxx = s.q[F_SXX][c], syy = s.q[F_SYY][c], szz = s.q[F_SZZ][c], sxy = s.q[F_SXY][c], sxz = s.q[F_SXZ][c],
+           syz = s.q[F_SYZ][c];
+    double J2 = 0.5 * (sxx * sxx + syy * syy + szz * szz) + sxy * sxy + sxz * sxz + syz * syz;
+    double vm = sqrt(3.0 * J2);
+    if (vm > Y) {
+        double f = (vm > 0 ? Y / vm : 0.0);
+        s.q[F_SXX][c] = sxx * f; s.q[F_SYY][c] = syy * f; s.q[F_SZZ][c] = szz * f;
+        s.q[F_SXY][c] = sxy * f; s.q[F_SXZ][c] = sxz * f; s.q[F_SYZ][c] = syz * f;
+        if (p.af_reg && reg && p.m.G > 0 && (p.rho_cfl <= 0 || r > p.rho_cfl)) {
+            double dW = (vm * vm - Y * Y) / (6.0 * p.m.G);
+            s.q[F_VIB][c] = sqrt(s.q[F_VIB][c] * s.q[F_VIB][c] + 2.0 * p.c_reg * dW / r);
+            s.q[F_E][c] -= p.c_reg * dW;
+        }
+    }
+}
+
+// Tensile damage growth of one cell, hydro_cpu.cpp:253-258.
+static __device__ void grow_damage_cell(const P& p, const Fields& g, int64_t c, double dt) {
+    if (p.m.Emod <= 0 || p.m.wk <= 0) return;
+    double* D = g.q[F_D];
+    if (D[c] >= 1.0) return;
+    double Pp = pcell(p, g, c);
+    double sigmax = dmax2(-Pp + g.q[F_SXX][c], dmax2(-Pp + g.q[F_SYY][c], -Pp + g.q[F_SZZ][c]));
+    if (sigmax > 0.0 && sigmax / p.m.Emod > p.eps_act) {
+        double cg = 0.4 * sqrt(p.m.Emod / dmax2(g.q[F_R][c], 1e-30)), Rs = 0.5 * p.dx;
+        double d13 = pow(D[c], 1.0 / 3.0) + (cg / Rs) * dt;
+        D[c] = dmin2(1.0, d13 * d13 * d13);
+    }
+}
+
+
+// ---------------------------------------------------------------- kernels
+
+// Step start (drivers' loop): is there a step to take, and reset the speed.
+static __global__ void k_begin(Ctl* ctl) {
+    ctl->active = (ctl->t < ctl->t_end && (ctl->max_steps < 0 || ctl->steps < ctl->max_steps)) ? 1 : 0;
+    ctl->smax_bits = (unsigned long long)__double_as_longlong(1e-30);
+}
+
+// maxspeed (hydro_cpu.cpp:378-380): per-cell signal speed, block maximum, one
+// atomic per block on the ordered bits.
+static __global__ void __launch_bounds__(256) k_maxspeed(P p, Fields g, Ctl* ctl) {
+    __shared__ double red[8];
+    const int64_t c = gtid();
+    double s = 1e-30;
+    if (ctl->active && c < p.n) {
+        const double r = g.q[F_R][c];
+        if (!(r < p.rho_cfl)) {
+            const double mu = g.q[F_MU][c], mv = g.q[F_MV][c], mw = g.q[F_MW][c];
+            double pr, cs;
+            eos_pc(p.m, r, eint_of(r, mu, mv, mw, g.q[F_E][c]), pr, cs);
+            double cel = sqrt(cs * cs + (p.m.G > 0 ? (4.0 / 3.0) * p.m.G / r : 0.0));
+            double v = sqrt(mu * mu + mv * mv + mw * mw) / r;
+            s = dmax2(s, v + cel);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) s = dmax2(s, __shfl_xor_sync(0xffffffffu, s, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 1e-30;
+        for (int o = 16; o > 0; o >>= 1) s = dmax2(s, __shfl_xor_sync(0xffffffffu, s, o));
+        if (threadIdx.x == 0) atomicMax(&ctl->smax_bits, (unsigned long long)__double_as_longlong(s));
+    }
+}
+
+// dt = CFL dx / maxspeed, clipped at t_end (hydro_cpu.cpp:452).
+static __global__ void k_dt(P p, Ctl* ctl) {
+    if (!ctl->active) return;
+    double dt = ctl->cfl * p.dx / __longlong_as_double((long long)ctl->smax_bits);
+    if (ctl->t + dt > ctl->t_end) dt = ctl->t_end - ctl->t;
+    ctl->dt = dt;
+}
+
+static __global__ void k_end(Ctl* ctl) {
+    if (!ctl->active) return;
+    ctl->t += ctl->dt;
+    ctl->steps++;
+}
+
+// update_af before the stage (hydro_cpu.cpp:412).
+static __global__ void k_update_af(P p, Fields g, const Ctl* ctl) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    update_af_cell(p, g, c, ctl->dt);
+}
+
+// Primitives of one state (hydro_cpu.cpp:101) and the tracer ratio rc/rho,
+// formed in FP64 and stored in the Lop's compute type R.
+template <class R>
+static __global__ void k_prim(P p, Fields s, PrimT<R> W, const Ctl* ctl) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    const double r = s.q[F_R][c], mu = s.q[F_MU][c], mv = s.q[F_MV][c], mw = s.q[F_MW][c];
+    const double E = s.q[F_E][c], rc = s.q[F_RC][c];
+    W.w[0][c] = R(r);
+    W.w[1][c] = R(mu / r);
+    W.w[2][c] = R(mv / r);
+    W.w[3][c] = R(mw / r);
+    W.w[4][c] = R(eint_of(r, mu, mv, mw, E));
+    W.w[5][c] = R(rc / r);
+}
+
+// Face geometry of direction DIR: number of faces and, for face id, the face
+// position f along DIR and the cell of position p along DIR on its line.
+template <int DIR>
+struct FaceLine {
+    int64_t base, stride;  // cell(p) = base + p * stride
+    int f, nL;
+    __device__ __forceinline__ FaceLine(const P& p, int64_t id) {
+        if (DIR == 0) {
+            const int64_t plane = (int64_t)p.ny * p.nz;
+            f = (int)(id / plane);
+            base = id - (int64_t)f * plane;
+            stride = plane;
+            nL = p.nx;
+        } else if (DIR == 1) {
+            const int64_t row = (int64_t)(p.ny + 1) * p.nz;
+            const int64_t i = id / row, rem = id - i * row;
+            f = (int)(rem / p.nz);
+            base = i * (int64_t)p.ny * p.nz + (rem - (int64_t)f * p.nz);
+            stride = p.nz;
+            nL = p.ny;
+        } else {
+            const int64_t line = id / (p.nz + 1);
+            f = (int)(id - line * (p.nz + 1));
+            base = line * p.nz;
+            stride = 1;
+            nL = p.nz;
+        }
+    }
+    __device__ __forceinline__ int64_t cell(int q) const { return base + (int64_t)q * stride; }
+};
+
+template <int DIR>
+__host__ __device__ __forceinline__ int64_t face_count(int nx, int ny, int nz) {
+    return DIR == 0 ? (int64_t)(nx + 1) * ny * nz : (DIR == 1 ? (int64_t)nx * (ny + 1) * nz : (int64_t)nx * ny * (nz + 1));
+}
+
+// Face fluxes of direction DIR (hydro_cpu.cpp:109-121): MUSCL-minmod
+// reconstruction of the primitives, floors, HLLC / vacuum flux, tracer flux
+// upwinded by the mass flux.
+template <int DIR, class R>
+static __global__ void __launch_bounds__(256) k_face(P p, PrimT<R> W, FacesT<R> F, const Ctl* ctl) {
+    const int64_t id = gtid();
+    if (id >= face_count<DIR>(p.nx, p.ny, p.nz) || !ctl->active) return;
+    const FaceLine<DIR> ln(p, id);
+    const int f = ln.f, nL = ln.nL;
+    const int iL = max(0, f - 1), iR = min(nL - 1, f), iLL = max(0, f - 2), iRR = min(nL - 1, f + 1);
+    const int64_t cL = ln.cell(iL), cR = ln.cell(iR), cLL = ln.cell(iLL), cRR = ln.cell(iRR);
+    R L[5], Rr[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        const R* w = W.w[q];
+        const R A = w[cL], B = w[cR], AA = w[cLL], BB = w[cRR];
+        L[q] = A + R(0.5) * mm(A - AA, B - A);
+        Rr[q] = B - R(0.5) * mm(B - A, BB - B);
+        if (q == 0) {
+            if (L[0] < R(1e-9)) L[0] = A;
+            if (Rr[0] < R(1e-9)) Rr[0] = B;
+        }
+        if (q == 4) {
+            if (L[4] < R(0)) L[4] = A;
+            if (Rr[4] < R(0)) Rr[4] = B;
+        }
+    }
+    constexpr int in = DIR == 0 ? 1 : (DIR == 1 ? 2 : 3), it1 = DIR == 0 ? 2 : 1, it2 = DIR == 2 ? 2 : 3;
+    const MatT<R> m = mat_as<R>(p.m);
+    const F5<R> fl = hllc(m, R(p.rho_vac), L[0], L[in], L[it1], L[it2], L[4], Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4]);
+    F.q[DIR][0][id] = fl.r;
+    F.q[DIR][1][id] = fl.mn;
+    F.q[DIR][2][id] = fl.mt1;
+    F.q[DIR][3][id] = fl.mt2;
+    F.q[DIR][4][id] = fl.E;
+    F.q[DIR][5][id] = fl.r * (fl.r >= R(0) ? W.w[5][cL] : W.w[5][cR]);
+}
+
+// Right-hand side of one cell (hydro_cpu.cpp:98-214): the three directions'
+// flux differences in the reference's order, gravity, strength sources.
+// s: the state Lop reads; W: its primitives (k_prim), whose velocities mu/rho
+// are the very quotients the reference forms for every neighbour it reads;
+// af: the fluidization ratio.  Flux differences and strength sources are
+// formed in R and added to the FP64 right-hand side (with R = double: every
+// operation of the reference, in its order).
+template <class R>
+static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W, const double* af, FacesT<R> F,
+                                                      Rhs d, const Ctl* ctl) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    const int64_t plane = (int64_t)p.ny * p.nz;
+    const int i = (int)(c / plane);
+    const int64_t rem = c - (int64_t)i * plane;
+    const int j = (int)(rem / p.nz), k = (int)(rem - (int64_t)j * p.nz);
+    const double* r = s.q[F_R];
+    const double* mw = s.q[F_MW];
+    double dr = 0.0, dE = 0.0, drc = 0.0, dmu = 0.0, dmv = 0.0, dmw = 0.0;
+    // ---- hydro sweeps (hydro_cpu.cpp:122-133), x then y then z
+    {
+        const int64_t lo[3] = {c, ((int64_t)i * (p.ny + 1) + j) * p.nz + k, ((int64_t)i * p.ny + j) * (p.nz + 1) + k};
+        const int64_t up[3] = {(int64_t)p.ny * p.nz, p.nz, 1};
+#pragma unroll
+        for (int dir = 0; dir < 3; dir++) {
+            const int64_t a = lo[dir], b = lo[dir] + up[dir];
+            const R* const* Fq = F.q[dir];
+            R vr, vE, vrc, dmn, dt1, dt2;
+            if (dir == 0 && p.axisym) {
+                const R w0 = R(i * p.dx), w1 = R((i + 1) * p.dx), inv = R(1.0 / (((i + 0.5) * p.dx) * p.dx));
+                vr = -(w1 * Fq[0][b] - w0 * Fq[0][a]) * inv;
+                vE = -(w1 * Fq[4][b] - w0 * Fq[4][a]) * inv;
+                vrc = -(w1 * Fq[5][b] - w0 * Fq[5][a]) * inv;
+                dmn = -(w1 * Fq[1][b] - w0 * Fq[1][a]) * inv;
+                dt1 = -(w1 * Fq[2][b] - w0 * Fq[2][a]) * inv;
+                dt2 = -(w1 * Fq[3][b] - w0 * Fq[3][a]) * inv;
+                R pr, cs;
+                eos_pc(mat_as<R>(p.m), W.w[0][c], W.w[4][c], pr, cs);  // Pcell: EOS at the cell's internal energy
+                dmn += pr / R((i + 0.5) * p.dx);
+            } else {  // face weights 1 (exact products)
+                const R inv = R(p.invdx);
+                vr = -(Fq[0][b] - Fq[0][a]) * inv;
+                vE = -(Fq[4][b] - Fq[4][a]) * inv;
+                vrc = -(Fq[5][b] - Fq[5][a]) * inv;
+                dmn = -(Fq[1][b] - Fq[1][a]) * inv;
+                dt1 = -(Fq[2][b] - Fq[2][a]) * inv;
+                dt2 = -(Fq[3][b] - Fq[3][a]) * inv;
+            }
+            dr += double(vr);
+            dE += double(vE);
+            drc += double(vrc);
+            if (dir == 0) {
+                dmu += double(dmn); dmv += double(dt1); dmw += double(dt2);
+            } else if (dir == 1) {
+                dmv += double(dmn); dmu += double(dt1); dmw += double(dt2);
+            } else {
+                dmw += double(dmn); dmu += double(dt1); dmv += double(dt2);
+            }
+        }
+    }
+    if (p.gz != 0.0) {  // plain gravity body force, hydro_cpu.cpp:137-138
+        dmw += -p.gz * r[c];
+        dE += -p.gz * mw[c];
+    }
+    double dS[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, dD = 0.0, dvib = 0.0;
+    if (p.m.G > 0 && !(p.rho_cfl > 0 && r[c] < p.rho_cfl)) {  // strength sources, hydro_cpu.cpp:145-213
+        const R G = R(p.m.G), dx = R(p.dx);
+        const int64_t xm = c - (i > 0 ? plane : 0), xp = c + (i < p.nx - 1 ? plane : 0);
+        const int64_t ym = c - (j > 0 ? p.nz : 0), yp = c + (j < p.ny - 1 ? p.nz : 0);
+        const int64_t zm = c - (k > 0 ? 1 : 0), zp = c + (k < p.nz - 1 ? 1 : 0);
+        const R hx = ((i > 0 && i < p.nx - 1) ? R(2) : R(1)) * dx, hy = ((j > 0 && j < p.ny - 1) ? R(2) : R(1)) * dx,
+                hz = ((k > 0 && k < p.nz - 1) ? R(2) : R(1)) * dx;
+        const R* Vx = W.w[1];  // mu / rho of every cell
+        const R* Vy = W.w[2];
+        const R* Vz = W.w[3];
+        const R vxc = Vx[c], vyc = Vy[c], vzc = Vz[c];
+        const bool vd = p.rho_cfl > 0;
+        auto vxw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vxc : Vx[q]; };
+        auto vyw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vyc : Vy[q]; };
+        auto vzw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vzc : Vz[q]; };
+        const R Lxx = (vxw(xp) - vxw(xm)) / hx, Lxy = (vxw(yp) - vxw(ym)) / hy, Lxz = (vxw(zp) - vxw(zm)) / hz;
+        const R Lyx = (vyw(xp) - vyw(xm)) / hx, Lyy = (vyw(yp) - vyw(ym)) / hy, Lyz = (vyw(zp) - vyw(zm)) / hz;
+        const R Lzx = (vzw(xp) - vzw(xm)) / hx, Lzy = (vzw(yp) - vzw(ym)) / hy, Lzz = (vzw(zp) - vzw(zm)) / hz;
+        const R rcyl = R((i + 0.5) * p.dx);
+        const R eyy = p.axisym ? (vxc / rcyl) : Lyy;
+        const R exx = Lxx, ezz = Lzz, exy = R(0.5) * (Lxy + Lyx), exz = R(0.5) * (Lxz + Lzx),
+                eyz = R(0.5) * (Lyz + Lzy), tr = (exx + eyy + ezz) / R(3);
+        const R Wxy = R(0.5) * (Lxy - Lyx), Wxz = R(0.5) * (Lxz - Lzx), Wyz = R(0.5) * (Lyz - Lzy);
+        const double* Sxx = s.q[F_SXX];
+        const double* Syy = s.q[F_SYY];
+        const double* Szz = s.q[F_SZZ];
+        const double* Sxy = s.q[F_SXY];
+        const double* Sxz = s.q[F_SXZ];
+        const double* Syz = s.q[F_SYZ];
+        const R sxx = R(Sxx[c]), syy = R(Syy[c]), szz = R(Szz[c]), sxy = R(Sxy[c]), sxz = R(Sxz[c]), syz = R(Syz[c]);
+        const R Sm[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}};
+        const R Wm[3][3] = {{R(0), Wxy, Wxz}, {-Wxy, R(0), Wyz}, {-Wxz, -Wyz, R(0)}};
+        R Jm[3][3];
+#pragma unroll
+        for (int aa = 0; aa < 3; aa++)
+#pragma unroll
+            for (int bb = 0; bb < 3; bb++) {  // (S.W - W.S), hydro_cpu.cpp:172-173
+                R t = R(0);
+#pragma unroll
+                for (int cc = 0; cc < 3; cc++) t += Sm[aa][cc] * Wm[cc][bb] - Wm[aa][cc] * Sm[cc][bb];
+                Jm[aa][bb] = t;
+            }
+        const R u = vxc, v = vyc, w = vzc;
+        const R ix_ = i > 0 ? dx : R(1e30), ixp = i < p.nx - 1 ? dx : R(1e30);
+        const R iy_ = j > 0 ? dx : R(1e30), iyp = j < p.ny - 1 ? dx : R(1e30);
+        const R iz_ = k > 0 ? dx : R(1e30), izp = k < p.nz - 1 ? dx : R(1e30);
+        auto adv = [&](const double* S) {  // upwind v . grad S, hydro_cpu.cpp:175-178
+            const R sc = R(S[c]);
+            R ax = u > R(0) ? (sc - R(S[xm])) / ix_ : (R(S[xp]) - sc) / ixp;
+            R ay = v > R(0) ? (sc - R(S[ym])) / iy_ : (R(S[yp]) - sc) / iyp;
+            R az = w > R(0) ? (sc - R(S[zm])) / iz_ : (R(S[zp]) - sc) / izp;
+            return u * ax + v * ay + w * az;
+        };
+        dS[0] = 0.0 + double(R(2) * G * (exx - tr) + Jm[0][0] - adv(Sxx));
+        dS[1] = 0.0 + double(R(2) * G * (eyy - tr) + Jm[1][1] - adv(Syy));
+        dS[2] = 0.0 + double(R(2) * G * (ezz - tr) + Jm[2][2] - adv(Szz));
+        dS[3] = 0.0 + double(R(2) * G * exy + Jm[0][1] - adv(Sxy));
+        dS[4] = 0.0 + double(R(2) * G * exz + Jm[0][2] - adv(Sxz));
+        dS[5] = 0.0 + double(R(2) * G * eyz + Jm[1][2] - adv(Syz));
+        dD = 0.0 + double(-adv(s.q[F_D]));
+        dvib = 0.0 + double(-adv(s.q[F_VIB]));
+        // div S into momentum (central differences), hydro_cpu.cpp:183-186
+        auto cd = [&](const double* S, int64_t q1, int64_t q0, R h) { return (R(S[q1]) - R(S[q0])) / h; };
+        const R dSxx_x = cd(Sxx, xp, xm, hx), dSxy_y = cd(Sxy, yp, ym, hy), dSxz_z = cd(Sxz, zp, zm, hz);
+        const R dSxy_x = cd(Sxy, xp, xm, hx), dSyy_y = cd(Syy, yp, ym, hy), dSyz_z = cd(Syz, zp, zm, hz);
+        const R dSxz_x = cd(Sxz, xp, xm, hx), dSyz_y = cd(Syz, yp, ym, hy), dSzz_z = cd(Szz, zp, zm, hz);
+        dmu += double(dSxx_x + dSxy_y + dSxz_z);
+        dmv += double(dSxy_x + dSyy_y + dSyz_z);
+        dmw += double(dSxz_x + dSyz_y + dSzz_z);
+        if (p.axisym) {
+            dmu += double((sxx - syy) / rcyl);
+            dmw += double(sxz / rcyl);
+        }
+        if (af[c] > 0 && p.eta_af > 0) {  // explicit fluidization viscosity, hydro_cpu.cpp:190-197
+            const R eta = R(af[c] * p.eta_af), id2 = R(1.0 / (p.dx * p.dx));
+            auto vx = [&](int64_t q) { return Vx[q]; };
+            auto vy = [&](int64_t q) { return Vy[q]; };
+            auto vz = [&](int64_t q) { return Vz[q]; };
+            dmu += double(eta * (vx(xp) + vx(xm) + vx(yp) + vx(ym) + vx(zp) + vx(zm) - R(6) * vx(c)) * id2);
+            dmv += double(eta * (vy(xp) + vy(xm) + vy(yp) + vy(ym) + vy(zp) + vy(zm) - R(6) * vy(c)) * id2);
+            dmw += double(eta * (vz(xp) + vz(xm) + vz(yp) + vz(ym) + vz(zp) + vz(zm) - R(6) * vz(c)) * id2);
+            if (p.axisym) {
+                dmu += double(eta * (Lxx / rcyl - vxc / (rcyl * rcyl)));
+                dmw += double(eta * (Lzx / rcyl));
+            }
+        }
+        // div(S.v) into energy, hydro_cpu.cpp:198-203
+        auto svx = [&](int64_t q) { return R(Sxx[q]) * Vx[q] + R(Sxy[q]) * Vy[q] + R(Sxz[q]) * Vz[q]; };
+        auto svy = [&](int64_t q) { return R(Sxy[q]) * Vx[q] + R(Syy[q]) * Vy[q] + R(Syz[q]) * Vz[q]; };
+        auto svz = [&](int64_t q) { return R(Sxz[q]) * Vx[q] + R(Syz[q]) * Vy[q] + R(Szz[q]) * Vz[q]; };
+        dE += double((svx(xp) - svx(xm)) / hx + (svy(yp) - svy(ym)) / hy + (svz(zp) - svz(zm)) / hz);
+        if (p.axisym) dE += double(svx(c) / rcyl);
+    }
+    d.q[D_R][c] = dr;
+    d.q[D_MU][c] = dmu;
+    d.q[D_MV][c] = dmv;
+    d.q[D_MW][c] = dmw;
+    d.q[D_E][c] = dE;
+#pragma unroll
+    for (int q = 0; q < 6; q++) d.q[D_SXX + q][c] = dS[q];
+    d.q[D_D][c] = dD;
+    d.q[D_RC][c] = drc;
+    d.q[D_VIB][c] = dvib;
+}
+
+// Predictor (hydro_cpu.cpp:413-418): g1 = g + dt d, void-cell reset, radial
+// return without regeneration.
+static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    const double dt = ctl->dt;
+#pragma unroll
+    for (int q = 0; q < ND; q++) g1.q[rk_field(q)][c] = g.q[rk_field(q)][c] + dt * d.q[q][c];
+    if (p.rho_cfl > 0 && g1.q[F_R][c] < p.rho_cfl) g1.q[F_MU][c] = g1.q[F_MV][c] = g1.q[F_MW][c] = 0;
+    vonmises_cell(p, g1, g.q[F_AF], c, false);
+}
+
+// Corrector and the end of the step (hydro_cpu.cpp:419-424): trapezoidal
+// average, damage growth, radial return, damping, void-cell reset.
+static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    const double dt = ctl->dt;
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+        double* x = g.q[rk_field(q)];
+        x[c] = 0.5 * (x[c] + g1.q[rk_field(q)][c] + dt * d.q[q][c]);
+    }
+    grow_damage_cell(p, g, c, dt);
+    vonmises_cell(p, g, g.q[F_AF], c, true);
+    if (p.damp < 1.0) {
+        g.q[F_MU][c] *= p.damp;
+        g.q[F_MV][c] *= p.damp;
+        g.q[F_MW][c] *= p.damp;
+    }
+    if (p.rho_cfl > 0 && g.q[F_R][c] < p.rho_cfl) g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
+}
+
+// Single operators for the C ABI's unit calls.
+static __global__ void k_vonmises(P p, Fields g, int reg) {
+    const int64_t c = gtid();
+    if (c < p.n) vonmises_cell(p, g, g.q[F_AF], c, reg != 0);
+}
+static __global__ void k_grow_damage(P p, Fields g, double dt) {
+    const int64_t c = gtid();
+    if (c < p.n) grow_damage_cell(p, g, c, dt);
+}
+static __global__ void k_pressure(P p, Fields g, double* out) {
+    const int64_t c = gtid();
+    if (c < p.n) out[c] = pcell(p, g, c);
+}
+
+static __global__ void k_set_step(Ctl* ctl, double dt) {  // a step at a host dt
+    ctl->dt = dt;
+    ctl->active = 1;
+}
+static __global__ void k_set_run(Ctl* ctl, double cfl, double t_end, int64_t max_steps) {
+    ctl->cfl = cfl;
+    ctl->t_end = t_end;
+    ctl->max_steps = max_steps < 0 ? -1 : ctl->steps + max_steps;
+}
+static __global__ void k_set_time(Ctl* ctl, double t) { ctl->t = t; }
+static __global__ void k_maxspeed_begin(Ctl* ctl) {
+    ctl->active = 1;
+    ctl->smax_bits = (unsigned long long)__double_as_longlong(1e-30);
+}
+
+
+// ---------------------------------------------------------------- Lop launcher
+
+// One Lop (hydro_cpu.cpp:98-214) of state s in compute type R: primitives,
+// the three directions' face fluxes, the right-hand side.
+template <class R>
+inline void enqueue_lop_t(const P& p, const Fields& s, PrimT<R> W, const double* af, FacesT<R> F, Rhs d,
+                          const Ctl* ctl, cudaStream_t st) {
+    auto blocks = [](int64_t count, int b) { return (unsigned)((count + b - 1) / b); };
+    k_prim<R><<<blocks(p.n, 256), 256, 0, st>>>(p, s, W, ctl);
+    k_face<0, R><<<blocks(face_count<0>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
+    k_face<1, R><<<blocks(face_count<1>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
+    k_face<2, R><<<blocks(face_count<2>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
+    k_rhs<R><<<blocks(p.n, 128), 128, 0, st>>>(p, s, W, af, F, d, ctl);
+}
+
+// The FP32 instantiation lives in euler_mixed.cu (compiled with fused
+// multiply-adds); the FP64 one in euler.cu (compiled without).
+void enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* af, FacesT<float> F, Rhs d,
+                     const Ctl* ctl, cudaStream_t st);
+
+}  // namespace deu

@@ -19,6 +19,7 @@ import numpy as np
 from . import sph
 
 FIELDS = "r mu mv mw E Sxx Syy Szz Sxy Sxz Syz D af rc vib Pmax".split()
+FP64, MIXED = 0, 1  # eu_form: the Lop in FP64 (reference order) or in FP32 (state FP64)
 RHS = "r mu mv mw E Sxx Syy Szz Sxy Sxz Syz D rc vib".split()
 
 
@@ -35,6 +36,8 @@ _P = C.c_void_p
 _SIGS = {
     "eu_params_default": (None, [C.POINTER(Params)]),
     "eu_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(_P)]),
+    "eu_create_form": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.c_int32,
+                                 C.POINTER(_P)]),
     "eu_destroy": (C.c_int, [_P]),
     "eu_set_material": (C.c_int, [_P, C.POINTER(sph.Material)]),
     "eu_set_params": (C.c_int, [_P, C.POINTER(Params)]),
@@ -95,10 +98,11 @@ def _material(m) -> sph.Material:
 class Grid:
     """One Eulerian grid on one GPU (the reference's `Grid`, hydro_cpu.cpp:90-93)."""
 
-    def __init__(self, nx, ny, nz, dx, material=None, params=None, device=0):
+    def __init__(self, nx, ny, nz, dx, material=None, params=None, device=0, form=FP64):
         L = lib()
         h = _P()
-        sph.check(L.eu_create(int(nx), int(ny), int(nz), float(dx), int(device), C.byref(h)))
+        sph.check(L.eu_create_form(int(nx), int(ny), int(nz), float(dx), int(device), int(form), C.byref(h)))
+        self.form = int(form)
         self.h = h
         self.shape = (int(nx), int(ny), int(nz))
         self.n = int(nx) * int(ny) * int(nz)
@@ -235,8 +239,8 @@ class Grid:
             pass
 
 
-def from_case(case, device=0) -> Grid:
+def from_case(case, device=0, form=FP64) -> Grid:
     """A grid loaded with a workload case (grid_ic.Case)."""
-    g = Grid(*case.shape, case.dx, material=case.material, params=case.params, device=device)
+    g = Grid(*case.shape, case.dx, material=case.material, params=case.params, device=device, form=form)
     g.write_many(case.fields)
     return g

@@ -67,12 +67,22 @@ typedef struct eu_params {
 
 typedef struct eu_grid eu_grid;
 
+/* Arithmetic of the Lop (right-hand side).  EU_FP64: every operation in FP64,
+ * in the reference's order (the reference's CPU solver).  EU_MIXED: the state,
+ * the Runge-Kutta stages, yield, damage, fluidization and the CFL speed in
+ * FP64; primitives, face fluxes and the strength sources in FP32 (the
+ * arithmetic of the reference's own GPU solver, hydro.metal), at the FP32
+ * rate of the device. */
+enum eu_form { EU_FP64 = 0, EU_MIXED = 1 };
+
 /* Reference defaults of every setting (hydro_cpu.cpp:17-36, 222). */
 void eu_params_default(eu_params* out);
 
 /* Replaces Grid(X, Y, Z, d) (hydro_cpu.cpp:92): all fields zero, material
  * ideal gas gamma 1.4 (the reference's initial MAT, hydro_cpu.cpp:15). */
 int eu_create(int32_t nx, int32_t ny, int32_t nz, double dx, int32_t device, eu_grid** out);
+/* eu_create with the Lop's arithmetic chosen (eu_form). */
+int eu_create_form(int32_t nx, int32_t ny, int32_t nz, double dx, int32_t device, int32_t form, eu_grid** out);
 int eu_destroy(eu_grid* g);
 /* Replaces the global MAT (hydro_cpu.cpp:15); only the EOS, G, Y, Emod, wm and
  * wk fields are used (the SPH yield-model fields are ignored). */
