@@ -474,7 +474,7 @@ def halfspace_section(sph, ic, device, steps=200):
 EULER_STEP_BYTES = 14 * 8 * 2 + 8
 
 
-def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32):
+def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32, form=0, cpu=True, acc=True, e2e=True):
     """The Euler grid solver (hydrocodes/euler/hydro_cpu.cpp step_rk2) on the
     3-D half-space impact: N^3 cells of 50 m, basalt sphere at 30 deg, ROCK
     yield, tensile damage, gravity, near-void cells.  Device loop (dt on the
@@ -487,7 +487,7 @@ def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32):
     from oracle import euler as EO
 
     case = GI.impact3d(N)
-    g = E.from_case(case, device=device)
+    g = E.from_case(case, device=device, form=form)
     g.run(case.cfl, case.t_end, max(warmup, 3))
     g.synchronize()
     l0 = g.launches()
@@ -498,14 +498,16 @@ def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32):
     launches = g.launches() - l0
     # e2e: host buffers every step
     names = E.FIELDS
-    host = {k: torch.empty(case.n, dtype=torch.float64).pin_memory().numpy() for k in names}
-    g.read_many(names, [host[k] for k in names])
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        g.write_many(host)
-        g.run(case.cfl, case.t_end, 1)
+    el = None
+    if e2e:
+        host = {k: torch.empty(case.n, dtype=torch.float64).pin_memory().numpy() for k in names}
         g.read_many(names, [host[k] for k in names])
-    el = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            g.write_many(host)
+            g.run(case.cfl, case.t_end, 1)
+            g.read_many(names, [host[k] for k in names])
+        el = time.perf_counter() - t0
     g.close()
     nbytes = len(names) * 8 * case.n
     hbm, hbm_kind = peaks()
@@ -513,32 +515,38 @@ def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32):
     out = {"workload": f"3-D half-space impact, {N}^3 cells of 50 m, basalt sphere r = {N // 16} cells at 30 deg, "
                        "8 km/s; ROCK yield, tensile damage, gravity 3.71, near-void < 100 kg/m^3",
            "cells": case.n, "steps": s, "ms_per_step": ms / max(s, 1), "value": value, "unit": "cell-steps/s",
-           "dtype": "f64", "gpu_launches": launches,
-           "e2e": {"value": case.n * steps / el, "unit": "cell-steps/s", "h2d_bytes_per_step": nbytes,
-                   "d2h_bytes_per_step": nbytes, "pinned_host": True},
+           "form": "mixed (FP32 fluxes and sources, FP64 state)" if form else "fp64 (reference operation order)",
+           "dtype": "f32+f64" if form else "f64", "gpu_launches": launches,
+           "e2e": None if el is None else {"value": case.n * steps / el, "unit": "cell-steps/s",
+                                           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                                           "pinned_host": True},
            "step_roofline": {"alg_bytes_per_cell_step": EULER_STEP_BYTES,
                              "achieved_gbs": EULER_STEP_BYTES * value / 1e9,
                              "frac": EULER_STEP_BYTES * value / 1e9 / hbm, "peak_kind": f"{hbm_kind} copy bandwidth"}}
-    # CPU oracle on a smaller grid of the same workload (serial, as the reference)
-    small = GI.impact3d(cpu_n)
-    o = EO.from_case(small)
-    o.run(small.cfl, small.t_end, 1)
-    t0 = time.perf_counter()
-    so, _ = o.run(small.cfl, small.t_end, 2)
-    el = time.perf_counter() - t0
-    o.close()
-    out["cpu_baseline"] = {"value": small.n * so / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
-                           "sample": f"the same impact on {cpu_n}^3 cells, {so} steps after one warm-up step"}
+    if cpu:  # CPU oracle on a smaller grid of the same workload (serial, as the reference)
+        small = GI.impact3d(cpu_n)
+        o = EO.from_case(small)
+        o.run(small.cfl, small.t_end, 1)
+        t0 = time.perf_counter()
+        so, _ = o.run(small.cfl, small.t_end, 2)
+        el = time.perf_counter() - t0
+        o.close()
+        out["cpu_baseline"] = {"value": small.n * so / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+                               "sample": f"the same impact on {cpu_n}^3 cells, {so} steps after one warm-up step"}
+    if not acc:
+        return out
     # parity on a small grid of the same workload
     acc = GI.impact3d(acc_n)
-    a = E.from_case(acc, device=device)
+    keys = ("r", "mu", "mw", "E", "Sxx", "Sxy", "D")
+    a = E.from_case(acc, device=device, form=form)
     a.run(acc.cfl, acc.t_end, 10)
+    got = {k: a.read(k) for k in keys}
+    a.close()
     o = EO.from_case(acc)
     o.run(acc.cfl, acc.t_end, 10)
-    out["vs_oracle_rel_l2"] = {k: float(np.linalg.norm(a.read(k) - o.field(k)) / max(np.linalg.norm(o.field(k)), 1e-300))
-                               for k in ("r", "mu", "mw", "E", "Sxx", "Sxy", "D")}
+    out["vs_oracle_rel_l2"] = {k: float(np.linalg.norm(got[k] - o.field(k)) / max(np.linalg.norm(o.field(k)), 1e-300))
+                               for k in keys}
     out["vs_oracle_sample"] = f"{acc_n}^3 cells, 10 steps"
-    a.close()
     o.close()
     return out
 
@@ -592,8 +600,16 @@ def main():
     ap.add_argument("--no-halfspace", action="store_true")
     ap.add_argument("--no-euler", action="store_true")
     ap.add_argument("--euler-n", type=int, default=256)
+    ap.add_argument("--only-euler", action="store_true",
+                    help="run only the Euler grid section (both forms) and print its JSON")
     args = ap.parse_args()
     rank, world, local = rank_info()
+    if args.only_euler:
+        out = {f: euler_section(local, args.steps, args.warmup, args.euler_n, form=i, cpu=not args.no_cpu,
+                                acc=not args.no_acc, e2e=not args.no_e2e)
+               for i, f in enumerate(("fp64", "mixed"))}
+        print(json.dumps(out), flush=True)
+        return
 
     from deorbit_gb300 import ic
 
@@ -702,7 +718,8 @@ def main():
         halfspace = halfspace_section(sph, ic, device)
     euler = None
     if rank == 0 and world == 1 and not args.no_euler:
-        euler = euler_section(device, args.steps, args.warmup, args.euler_n)
+        euler = {"fp64": euler_section(device, args.steps, args.warmup, args.euler_n),
+                 "mixed": euler_section(device, args.steps, args.warmup, args.euler_n, form=1, cpu=False)}
 
     # ---- accuracy of the mixed form against FP64 (same dt sequence), and of
     # both forms against the oracle on a bounded sample
