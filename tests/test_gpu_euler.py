@@ -246,3 +246,78 @@ def test_gpu_gate_alimpact(E):
             hi = Us
     Phug = rho0 * 0.5 * (lo + hi) * up
     assert abs(Pmax - Phug) / Phug < 0.05
+
+
+# ---------------------------------------------------------------- mixed form
+
+GROUPS = {"rho": ["r"], "momentum": ["mu", "mv", "mw"], "E": ["E"],
+          "S": ["Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"], "D": ["D"], "rc": ["rc"]}
+
+
+def _group_err(got, ref, names):
+    a = np.concatenate([got[k] for k in names])
+    b = np.concatenate([ref[k] for k in names])
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+@pytest.mark.parametrize("case,steps", [(GI.sod(), 120), (GI.tracer(), 60), (GI.sedov(16), 12),
+                                        (GI.sedov_axi(16, 32), 15), (GI.atmos(50), 10), (GI.shear(200), 40),
+                                        (GI.yield_pulse(100), 40), (GI.vacuum(200), 40), (GI.bshock(100), 20),
+                                        (GI.tensile(), 20), (GI.alimpact(100), 40), (GI.impact3d(16), 8),
+                                        (GI.impact3d(16, af=True), 8)],
+                         ids=lambda x: getattr(x, "name", str(x)) + ("_af" if getattr(x, "params", {}).get("c_act") else ""))
+def test_mixed_runs_match_oracle(E, case, steps):
+    """The mixed form (FP32 fluxes and sources, FP64 state) against the FP64
+    oracle: rel-L2 of every field group (density, momentum vector, energy,
+    stress tensor, damage, tracer) <= 1e-4 over the run, same step count.
+    The fluidization ratio and vibration velocity are threshold quantities
+    (seeded when a pressure rise crosses P_ACT) and are left out."""
+    g = E.from_case(case, form=E.MIXED)
+    s, t = g.run(case.cfl, case.t_end, steps)
+    got = g.fields()
+    g.close()
+    o = EO.from_case(case)
+    so, to = o.run(case.cfl, case.t_end, steps)
+    ref = o.fields()
+    o.close()
+    assert s == so and abs(t - to) <= 1e-5 * abs(to)
+    errs = {k: _group_err(got, ref, names) for k, names in GROUPS.items()}
+    assert all(v <= 1e-4 for v in errs.values()), errs
+
+
+def test_mixed_gates(E):
+    """The reference's gates on the mixed form (as its own FP32 GPU solver is
+    held to them): Sod L1, 64^3 Sedov radius, shear speed, tensile damage,
+    free surface."""
+    from test_euler_oracle import _exact_sod
+    case = GI.sod()
+    g = E.from_case(case, form=E.MIXED)
+    g.run(case.cfl, case.t_end)
+    x = (np.arange(200) + 0.5) * case.dx
+    re = np.array([_exact_sod((xi - 0.5) / case.t_end)[0] for xi in x])
+    assert np.abs(g.read("r") - re).mean() < 0.007
+    case = GI.sedov(64)
+    g = E.from_case(case, form=E.MIXED)
+    g.run(case.cfl, case.t_end)
+    r = g.read("r").reshape(64, 64, 64)
+    i, j, k = np.unravel_index(np.argmax(r), r.shape)
+    dx, cen = case.dx, 32.5 * case.dx
+    rpk = math.sqrt(((i + .5) * dx - cen) ** 2 + ((j + .5) * dx - cen) ** 2 + ((k + .5) * dx - cen) ** 2)
+    Ran = (1.0 / 0.851) ** 0.2 * case.t_end ** 0.4
+    assert abs(rpk - Ran) / Ran < 0.10
+    case = GI.shear()
+    g = E.from_case(case, form=E.MIXED)
+    s, t = g.run(case.cfl, case.t_end)
+    vy = g.read("mv") / g.read("r")
+    ii = np.arange(int(0.3 * 400e3 / case.dx) + 3, case.shape[0] - 2)
+    cs = math.sqrt(2.27e10 / 2700.0)
+    assert abs(((ii[np.argmax(vy[ii])] + 0.5) * case.dx - 0.3 * 400e3) / t - cs) / cs < 0.03
+    case = GI.tensile()
+    g = E.from_case(case, form=E.MIXED)
+    g.run(case.cfl, case.t_end)
+    assert g.read("D")[20:80].max() > 0.9 and np.abs(g.read("Sxx")[20:80]).max() < 0.5 * 3.5e8
+    case = GI.surface()
+    g = E.from_case(case, form=E.MIXED)
+    g.run(case.cfl, case.t_end)
+    assert np.abs(g.read("mw") / g.read("r")).max() < 5.0
