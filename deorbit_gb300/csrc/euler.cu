@@ -120,7 +120,8 @@ struct Grid {
         const int64_t n = p.n;
         if (with_dt) {
             k_begin<<<1, 1, 0, st>>>(ctl);
-            k_maxspeed<<<grid_of(n), 256, 0, st>>>(p, g, ctl);
+            if (mixed) enqueue_maxspeed_f32(p, g, ctl, st);
+            else enqueue_maxspeed_t<double>(p, g, ctl, st);
             k_dt<<<1, 1, 0, st>>>(p, ctl);
             launches += 3;
         }
@@ -129,9 +130,11 @@ struct Grid {
             launches++;
         }
         enqueue_lop(g);
-        k_predict<<<grid_of(n), 256, 0, st>>>(p, g, g1, d, ctl);
+        if (mixed) enqueue_predict_f32(p, g, g1, d, ctl, st);
+        else enqueue_predict_t<double>(p, g, g1, d, ctl, st);
         enqueue_lop(g1);
-        k_correct<<<grid_of(n), 256, 0, st>>>(p, g, g1, d, ctl);
+        if (mixed) enqueue_correct_f32(p, g, g1, d, ctl, st);
+        else enqueue_correct_t<double>(p, g, g1, d, ctl, st);
         k_end<<<1, 1, 0, st>>>(ctl);
         launches += 3;
     }
@@ -447,7 +450,8 @@ int eu_maxspeed(eu_grid* h, double* out) {
         if (!out) throw SphError(SPH_ERR_ARG, "null output pointer");
         deu::DeviceScope ds(g->device);
         deu::k_maxspeed_begin<<<1, 1, 0, g->st>>>(g->ctl);
-        deu::k_maxspeed<<<g->grid_of(g->p.n), 256, 0, g->st>>>(g->p, g->g, g->ctl);
+        if (g->mixed) deu::enqueue_maxspeed_f32(g->p, g->g, g->ctl, g->st);
+        else deu::enqueue_maxspeed_t<double>(g->p, g->g, g->ctl, g->st);
         g->launches += 2;
         g->check();
         const deu::Ctl c = g->read_ctl();

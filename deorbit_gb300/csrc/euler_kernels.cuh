@@ -3,12 +3,12 @@
 // forms:
 //   plain (FP64, euler.cu, compiled without fused multiply-adds): every
 //     expression in the reference's operation order;
-//   mixed (euler_mixed.cu): primitives, face fluxes and the right-hand side's
-//     sources in FP32 (the arithmetic of the reference's own GPU solver), the
-//     state, the Runge-Kutta stages, yield, damage, fluidization and the CFL
-//     speed in FP64.
-// The compute type R of the Lop kernels is the template parameter; state and
-// right-hand side are always FP64.  Literals are written as R(...) so that an
+//   mixed (euler_mixed.cu): primitives, face fluxes, the right-hand side's
+//     sources, the yield surface, damage growth and the CFL speed in FP32 (the
+//     arithmetic of the reference's own GPU solver); the state and its
+//     Runge-Kutta updates, the fluidization update and dt in FP64.
+// The compute type R is the template parameter; state and right-hand side
+// are always FP64.  Literals are written as R(...) so that an
 // FP32 instantiation never promotes to FP64.
 #pragma once
 
@@ -284,57 +284,76 @@ static __device__ void update_af_cell(const P& p, const Fields& g, int64_t c, do
 
 // Radial return of one cell, hydro_cpu.cpp:229-252 (s: the stress / energy /
 // vibration state; af from the state the step started from).
+template <class R>
+static __device__ __forceinline__ double pcell_r(const P& p, const Fields& s, int64_t c) {
+    // Pcell (hydro_cpu.cpp:95) with the EOS evaluated in R: the clamped pressure
+    const double r = s.q[F_R][c];
+    R pr = pressure(mat_as<R>(p.m), R(r), R(eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
+    if (pr < R(0)) pr = R(0);
+    return double(pr);
+}
+
+// Radial return of one cell, hydro_cpu.cpp:229-252 (s: the stress / energy /
+// vibration state; af from the state the step started from).  The yield
+// surface and the return factor are formed in R; the state stays FP64.
+template <class R>
 static __device__ void vonmises_cell(const P& p, const Fields& s, const double* af, int64_t c, bool reg) {
     if (p.m.Y <= 0 && !p.rock) return;
-    double Y;
+    R Y;
     const double r = s.q[F_R][c];
+    const R afc = R(af[c]);
     if (p.rock) {
-        double Pp = dmax2(pcell(p, s, c), 0.0);
-        double Peff = Pp;
+        R Pp = R(dmax2(pcell_r<R>(p, s, c), 0.0));
+        R Peff = Pp;
         if (p.af_prel && s.q[F_VIB][c] > 0) {
-            double p2, cs2;
-            eos_pc(p.m, r, eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c]), p2, cs2);
-            Peff = dmax2(Pp - r * cs2 * s.q[F_VIB][c], 0.0);
+            R p2, cs2;
+            eos_pc(mat_as<R>(p.m), R(r), R(eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2,
+                   cs2);
+            Peff = dmax2(Pp - R(r) * cs2 * R(s.q[F_VIB][c]), R(0));
         }
-        double Yi = p.y_i0 + p.mu_i * Peff / (1.0 + p.mu_i * Peff / dmax2(p.y_m - p.y_i0, 1.0));
-        double Yd = dmin2(p.y_d0 + p.mu_d * Peff, p.y_m);
-        const double D = s.q[F_D][c];
-        double Yb = (1.0 - D) * Yi + D * Yd;
-        Y = p.af_prel ? Yb : Yb * (1.0 - af[c]);
-        if (p.y_bingham > 0 && af[c] > 1e-3) {
-            double Yf = dmin2(p.y_bingham, Yb);
+        R Yi = R(p.y_i0) + R(p.mu_i) * Peff / (R(1) + R(p.mu_i) * Peff / dmax2(R(p.y_m - p.y_i0), R(1)));
+        R Yd = dmin2(R(p.y_d0) + R(p.mu_d) * Peff, R(p.y_m));
+        const R D = R(s.q[F_D][c]);
+        R Yb = (R(1) - D) * Yi + D * Yd;
+        Y = p.af_prel ? Yb : Yb * (R(1) - afc);
+        if (p.y_bingham > 0 && afc > R(1e-3)) {
+            R Yf = dmin2(R(p.y_bingham), Yb);
             if (Y < Yf) Y = Yf;
         }
     } else {
-        Y = (1.0 - s.q[F_D][c]) * (1.0 - af[c]) * p.m.Y;
+        Y = (R(1) - R(s.q[F_D][c])) * (R(1) - afc) * R(p.m.Y);
     }
-    double sxx = s.q[F_SXX][c], syy = s.q[F_SYY][c], szz = s.q[F_SZZ][c], sxy = s.q[F_SXY][c], sxz = s.q[F_SXZ][c],
-           syz = s.q[F_SYZ][c];
-    double J2 = 0.5 * (sxx * sxx + syy * syy + szz * szz) + sxy * sxy + sxz * sxz + syz * syz;
-    double vm = sqrt(3.0 * J2);
+    const double sxx = s.q[F_SXX][c], syy = s.q[F_SYY][c], szz = s.q[F_SZZ][c], sxy = s.q[F_SXY][c],
+                 sxz = s.q[F_SXZ][c], syz = s.q[F_SYZ][c];
+    const R xx = R(sxx), yy = R(syy), zz = R(szz), xy = R(sxy), xz = R(sxz), yz = R(syz);
+    R J2 = R(0.5) * (xx * xx + yy * yy + zz * zz) + xy * xy + xz * xz + yz * yz;
+    R vm = sqrt(R(3) * J2);
     if (vm > Y) {
-        double f = (vm > 0 ? Y / vm : 0.0);
+        const double f = double(vm > R(0) ? Y / vm : R(0));
         s.q[F_SXX][c] = sxx * f; s.q[F_SYY][c] = syy * f; s.q[F_SZZ][c] = szz * f;
         s.q[F_SXY][c] = sxy * f; s.q[F_SXZ][c] = sxz * f; s.q[F_SYZ][c] = syz * f;
         if (p.af_reg && reg && p.m.G > 0 && (p.rho_cfl <= 0 || r > p.rho_cfl)) {
-            double dW = (vm * vm - Y * Y) / (6.0 * p.m.G);
-            s.q[F_VIB][c] = sqrt(s.q[F_VIB][c] * s.q[F_VIB][c] + 2.0 * p.c_reg * dW / r);
-            s.q[F_E][c] -= p.c_reg * dW;
+            R dW = (vm * vm - Y * Y) / (R(6) * R(p.m.G));
+            const R vb = R(s.q[F_VIB][c]);
+            s.q[F_VIB][c] = double(sqrt(vb * vb + R(2) * R(p.c_reg) * dW / R(r)));
+            s.q[F_E][c] -= double(R(p.c_reg) * dW);
         }
     }
 }
 
-// Tensile damage growth of one cell, hydro_cpu.cpp:253-258.
+// Tensile damage growth of one cell, hydro_cpu.cpp:253-258 (threshold and
+// growth formed in R).
+template <class R>
 static __device__ void grow_damage_cell(const P& p, const Fields& g, int64_t c, double dt) {
     if (p.m.Emod <= 0 || p.m.wk <= 0) return;
     double* D = g.q[F_D];
     if (D[c] >= 1.0) return;
-    double Pp = pcell(p, g, c);
-    double sigmax = dmax2(-Pp + g.q[F_SXX][c], dmax2(-Pp + g.q[F_SYY][c], -Pp + g.q[F_SZZ][c]));
-    if (sigmax > 0.0 && sigmax / p.m.Emod > p.eps_act) {
-        double cg = 0.4 * sqrt(p.m.Emod / dmax2(g.q[F_R][c], 1e-30)), Rs = 0.5 * p.dx;
-        double d13 = pow(D[c], 1.0 / 3.0) + (cg / Rs) * dt;
-        D[c] = dmin2(1.0, d13 * d13 * d13);
+    const R Pp = R(pcell_r<R>(p, g, c));
+    const R sigmax = dmax2(-Pp + R(g.q[F_SXX][c]), dmax2(-Pp + R(g.q[F_SYY][c]), -Pp + R(g.q[F_SZZ][c])));
+    if (sigmax > R(0) && sigmax / R(p.m.Emod) > R(p.eps_act)) {
+        R cg = R(0.4) * sqrt(R(p.m.Emod) / dmax2(R(g.q[F_R][c]), R(1e-30))), Rs = R(0.5) * R(p.dx);
+        R d13 = pow(R(D[c]), R(1) / R(3)) + (cg / Rs) * R(dt);
+        D[c] = double(dmin2(R(1), d13 * d13 * d13));
     }
 }
 
@@ -349,6 +368,7 @@ static __global__ void k_begin(Ctl* ctl) {
 
 // maxspeed (hydro_cpu.cpp:378-380): per-cell signal speed, block maximum, one
 // atomic per block on the ordered bits.
+template <class R>
 static __global__ void __launch_bounds__(256) k_maxspeed(P p, Fields g, Ctl* ctl) {
     __shared__ double red[8];
     const int64_t c = gtid();
@@ -357,11 +377,12 @@ static __global__ void __launch_bounds__(256) k_maxspeed(P p, Fields g, Ctl* ctl
         const double r = g.q[F_R][c];
         if (!(r < p.rho_cfl)) {
             const double mu = g.q[F_MU][c], mv = g.q[F_MV][c], mw = g.q[F_MW][c];
-            double pr, cs;
-            eos_pc(p.m, r, eint_of(r, mu, mv, mw, g.q[F_E][c]), pr, cs);
-            double cel = sqrt(cs * cs + (p.m.G > 0 ? (4.0 / 3.0) * p.m.G / r : 0.0));
-            double v = sqrt(mu * mu + mv * mv + mw * mw) / r;
-            s = dmax2(s, v + cel);
+            const R rr = R(r);
+            R pr, cs;
+            eos_pc(mat_as<R>(p.m), rr, R(eint_of(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
+            R cel = sqrt(cs * cs + (p.m.G > 0 ? R(4.0 / 3.0) * R(p.m.G) / rr : R(0)));
+            R v = sqrt(R(mu) * R(mu) + R(mv) * R(mv) + R(mw) * R(mw)) / rr;
+            s = dmax2(s, double(v + cel));
         }
     }
     for (int o = 16; o > 0; o >>= 1) s = dmax2(s, __shfl_xor_sync(0xffffffffu, s, o));
@@ -657,6 +678,7 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
 
 // Predictor (hydro_cpu.cpp:413-418): g1 = g + dt d, void-cell reset, radial
 // return without regeneration.
+template <class R>
 static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
@@ -664,11 +686,12 @@ static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
 #pragma unroll
     for (int q = 0; q < ND; q++) g1.q[rk_field(q)][c] = g.q[rk_field(q)][c] + dt * d.q[q][c];
     if (p.rho_cfl > 0 && g1.q[F_R][c] < p.rho_cfl) g1.q[F_MU][c] = g1.q[F_MV][c] = g1.q[F_MW][c] = 0;
-    vonmises_cell(p, g1, g.q[F_AF], c, false);
+    vonmises_cell<R>(p, g1, g.q[F_AF], c, false);
 }
 
 // Corrector and the end of the step (hydro_cpu.cpp:419-424): trapezoidal
 // average, damage growth, radial return, damping, void-cell reset.
+template <class R>
 static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
@@ -678,8 +701,8 @@ static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
         double* x = g.q[rk_field(q)];
         x[c] = 0.5 * (x[c] + g1.q[rk_field(q)][c] + dt * d.q[q][c]);
     }
-    grow_damage_cell(p, g, c, dt);
-    vonmises_cell(p, g, g.q[F_AF], c, true);
+    grow_damage_cell<R>(p, g, c, dt);
+    vonmises_cell<R>(p, g, g.q[F_AF], c, true);
     if (p.damp < 1.0) {
         g.q[F_MU][c] *= p.damp;
         g.q[F_MV][c] *= p.damp;
@@ -691,11 +714,11 @@ static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
 // Single operators for the C ABI's unit calls.
 static __global__ void k_vonmises(P p, Fields g, int reg) {
     const int64_t c = gtid();
-    if (c < p.n) vonmises_cell(p, g, g.q[F_AF], c, reg != 0);
+    if (c < p.n) vonmises_cell<double>(p, g, g.q[F_AF], c, reg != 0);
 }
 static __global__ void k_grow_damage(P p, Fields g, double dt) {
     const int64_t c = gtid();
-    if (c < p.n) grow_damage_cell(p, g, c, dt);
+    if (c < p.n) grow_damage_cell<double>(p, g, c, dt);
 }
 static __global__ void k_pressure(P p, Fields g, double* out) {
     const int64_t c = gtid();
@@ -733,9 +756,26 @@ inline void enqueue_lop_t(const P& p, const Fields& s, PrimT<R> W, const double*
     k_rhs<R><<<blocks(p.n, 128), 128, 0, st>>>(p, s, W, af, F, d, ctl);
 }
 
-// The FP32 instantiation lives in euler_mixed.cu (compiled with fused
-// multiply-adds); the FP64 one in euler.cu (compiled without).
+// The CFL speed reduction, the predictor and the corrector in compute type R.
+template <class R>
+inline void enqueue_maxspeed_t(const P& p, const Fields& g, Ctl* ctl, cudaStream_t st) {
+    k_maxspeed<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, ctl);
+}
+template <class R>
+inline void enqueue_predict_t(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st) {
+    k_predict<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, g1, d, ctl);
+}
+template <class R>
+inline void enqueue_correct_t(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st) {
+    k_correct<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, g1, d, ctl);
+}
+
+// The FP32 instantiations live in euler_mixed.cu (compiled with fused
+// multiply-adds); the FP64 ones in euler.cu (compiled without).
 void enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* af, FacesT<float> F, Rhs d,
                      const Ctl* ctl, cudaStream_t st);
+void enqueue_maxspeed_f32(const P& p, const Fields& g, Ctl* ctl, cudaStream_t st);
+void enqueue_predict_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st);
+void enqueue_correct_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st);
 
 }  // namespace deu

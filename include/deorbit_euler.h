@@ -67,12 +67,12 @@ typedef struct eu_params {
 
 typedef struct eu_grid eu_grid;
 
-/* Arithmetic of the Lop (right-hand side).  EU_FP64: every operation in FP64,
- * in the reference's order (the reference's CPU solver).  EU_MIXED: the state,
- * the Runge-Kutta stages, yield, damage, fluidization and the CFL speed in
- * FP64; primitives, face fluxes and the strength sources in FP32 (the
- * arithmetic of the reference's own GPU solver, hydro.metal), at the FP32
- * rate of the device. */
+/* Arithmetic of the step.  EU_FP64: every operation in FP64, in the
+ * reference's order (the reference's CPU solver).  EU_MIXED: the state and its
+ * Runge-Kutta updates, the fluidization update and dt in FP64; primitives,
+ * face fluxes, the strength sources, the yield surface, damage growth and the
+ * CFL speed in FP32 (the arithmetic of the reference's own GPU solver,
+ * hydro.metal), at the FP32 rate of the device. */
 enum eu_form { EU_FP64 = 0, EU_MIXED = 1 };
 
 /* Reference defaults of every setting (hydro_cpu.cpp:17-36, 222). */
