@@ -10,7 +10,8 @@
 // read back into host memory and its slot and memory released, which admits
 // the next one.
 //
-// A worker thread prepares queued requests on the host (flaw seeding: the
+// A pool of worker threads (half the host's hardware threads, at most 8)
+// prepares queued requests on the host, oldest first (flaw seeding: the
 // multi-flaw law draws ~N ln N thresholds) while the serving thread keeps the
 // GPU busy, so admission costs only the upload and the impact's first
 // evaluation.  All engine calls stay on the serving thread (the thread that
@@ -65,6 +66,7 @@ struct Req {
     // prepared by the worker
     std::vector<double> eps_act, feps;
     std::vector<int64_t> fptr;
+    bool claimed = false;  // a worker is preparing it
     bool ready = false;
     // lifecycle (serving thread)
     int32_t state = SPH_SERVE_QUEUED;
@@ -111,9 +113,11 @@ struct sph_server {
     std::map<int64_t, std::shared_ptr<Req>> all;   // every request not yet released
     int64_t next_id = 0;
     bool stop = false;
-    std::thread worker;
+    std::vector<std::thread> workers;  // flaw seeding of queued requests, in parallel
     // statistics
     double particle_steps = 0, busy_s = 0;
+    double admit_wait_s = 0;  // admission blocked on a request still being seeded
+    double host_s = 0;        // admission, initialisation and retirement between rounds
     double first_arrival = -1, last_finish = -1;
     std::vector<double> latencies;
     int64_t peak_bytes = 0;
@@ -123,11 +127,12 @@ struct sph_server {
         while (!stop) {
             std::shared_ptr<Req> r;
             for (auto& q : queue)
-                if (!q->ready) { r = q; break; }
+                if (!q->claimed) { r = q; break; }
             if (!r) {
                 cv.wait(lk);
                 continue;
             }
+            r->claimed = true;  // the oldest unclaimed request first
             lk.unlock();
             try {
                 prepare(*r);
@@ -195,9 +200,13 @@ int admit(sph_server* s, double now) {
             if (s->queue.empty()) break;
             r = s->queue.front();
             if (r->arrival > now) break;
-            // the worker is behind: wait for it rather than idle the GPU on a
-            // request that has arrived (bounded by the seeding time of one request)
-            s->cv.wait(lk, [&] { return r->ready; });
+            // the workers are behind: wait for them rather than idle the GPU on
+            // a request that has arrived (bounded by the seeding time of one request)
+            if (!r->ready) {
+                const auto w0 = std::chrono::steady_clock::now();
+                s->cv.wait(lk, [&] { return r->ready; });
+                s->admit_wait_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
+            }
         }
         const int64_t bytes = E.device_bytes_after_adding(r->n);
         if (!s->active.empty() && (double)bytes > s->budget) break;  // FIFO: wait for memory
@@ -263,7 +272,9 @@ int sph_serve_create(sph_ctx* ctx, double hbm_budget_bytes, int32_t chunk, const
         }
         s->t0 = std::chrono::steady_clock::now();
         sph_server* raw = s.get();
-        s->worker = std::thread([raw] { raw->work(); });
+        const unsigned hc = std::thread::hardware_concurrency();
+        const int nw = (int)std::max(1u, std::min(8u, hc > 2 ? hc / 2 : 1u));
+        for (int w = 0; w < nw; w++) s->workers.emplace_back([raw] { raw->work(); });
         *out = s.release();
     });
 }
@@ -276,7 +287,8 @@ int sph_serve_destroy(sph_server* s) {
             s->stop = true;
         }
         s->cv.notify_all();
-        if (s->worker.joinable()) s->worker.join();
+        for (auto& w : s->workers)
+            if (w.joinable()) w.join();
         if (s->ctx && s->ctx->eng) {
             DevScope dv(s->ctx->device);
             for (auto& kv : s->active) {
@@ -356,7 +368,12 @@ int sph_serve_poll(sph_server* s, double max_wait_s, int64_t* done_ids, int32_t 
         *ndone = 0;
         DevScope dv(s->ctx->device);
         EngineBase& E = *s->ctx->eng;
-        admit(s, now_s(s->t0));
+        const double th0 = now_s(s->t0);
+        admit(s, th0);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->host_s += now_s(s->t0) - th0;
+        }
         if (s->active.empty()) {
             // idle: wait (bounded) for the next arrival
             double next = -1;
@@ -387,6 +404,15 @@ int sph_serve_poll(sph_server* s, double max_wait_s, int64_t* done_ids, int32_t 
             s->particle_steps += (double)n_res * (double)steps;
         }
         // retire finished requests: results to host memory, slot and memory released
+        const double tr0 = now_s(s->t0);
+        struct HostTime {  // retirement time, added however the scope ends
+            sph_server* s;
+            double t0;
+            ~HostTime() {
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->host_s += now_s(s->t0) - t0;
+            }
+        } host_time{s, tr0};
         std::vector<int> fin;
         for (auto& kv : s->active)
             if (E.impact_info(kv.first).steps >= kv.second->steps) fin.push_back(kv.first);
@@ -492,6 +518,8 @@ int sph_serve_stats(sph_server* s, sph_serve_summary* out) {
         out->busy_throughput = s->busy_s > 0 ? s->particle_steps / s->busy_s : 0;
         out->busy_s = s->busy_s;
         out->peak_device_bytes = (double)s->peak_bytes;
+        out->admit_wait_s = s->admit_wait_s;
+        out->host_s = s->host_s;
     });
 }
 

@@ -170,6 +170,8 @@ class Server:
             "gpu_busy_particle_steps_per_s": st.busy_throughput or None,
             "particle_steps": st.particle_steps,
             "peak_device_bytes": st.peak_device_bytes,
+            "admit_wait_s": st.admit_wait_s,
+            "host_s": st.host_s,
         }
 
     def close(self):

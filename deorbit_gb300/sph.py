@@ -89,7 +89,8 @@ class ServeRecord(C.Structure):
 class ServeSummary(C.Structure):
     _fields_ = [("done", C.c_int64), ("queued", C.c_int64), ("resident", C.c_int64)] + [
         (k, C.c_double) for k in ("p50_latency_s", "p99_latency_s", "mean_latency_s", "particle_steps",
-                                  "throughput", "busy_throughput", "busy_s", "peak_device_bytes")]
+                                  "throughput", "busy_throughput", "busy_s", "peak_device_bytes",
+                                  "admit_wait_s", "host_s")]
 
 
 SERVE_FLAWS = {None: 0, "single": 1, "multi": 2}

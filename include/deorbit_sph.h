@@ -325,6 +325,8 @@ typedef struct sph_serve_summary {
     double busy_throughput;     /* particle-steps / time spent advancing */
     double busy_s;
     double peak_device_bytes;   /* largest engine allocation seen after an admission */
+    double admit_wait_s;        /* admission blocked on requests still being seeded */
+    double host_s;              /* admission, initialisation and retirement between rounds */
 } sph_serve_summary;
 /* fields: comma-separated field names kept for each finished request (NULL:
  * x,y,z,vx,vy,vz,u,rho,P,D); the server clock starts here. */
