@@ -76,6 +76,9 @@ public:
     virtual void compute_forces() = 0;
     virtual void synchronize() = 0;
     virtual int64_t impact_n(int b) = 0;
+    // Steps the impact has taken (host copy, current after every run / step;
+    // no device round trip, unlike impact_info).
+    virtual int64_t impact_steps(int b) = 0;
     virtual void read_field(int b, const char* name, double* out) = 0;
     virtual void write_field(int b, const char* name, const double* in) = 0;
     virtual void read_fields(int b, int nf, const char* const* names, double* const* outs) = 0;

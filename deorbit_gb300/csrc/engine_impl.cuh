@@ -628,6 +628,7 @@ public:
     }
 
     int64_t impact_n(int b) override { return imp(b).n; }
+    int64_t impact_steps(int b) override { return imp(b).steps; }
 
     // ------------------------------------------------------------- stepping
     void init() override {

@@ -77,6 +77,8 @@ struct Grid {
     FacesT<float> F32{};
     Ctl* ctl = nullptr;
     double* scratch = nullptr;  // pressure read-out
+    double* ref_r0 = nullptr;   // hydrostatic reference (set_ref), allocated on first use
+    double* ref_p0 = nullptr;
     std::vector<void*> allocs;
     int64_t bytes = 0;
     int64_t launches = 0;
@@ -206,6 +208,7 @@ void to_params(deu::P& p, const eu_params& e) {
     p.c_reg = e.c_reg; p.af_sat = e.af_sat;
     p.axisym = e.axisym != 0; p.rock = e.rock != 0; p.af_reg = e.af_reg != 0; p.af_prel = e.af_prel != 0;
     p.af_seeddp = e.af_seeddp != 0;
+    p.void_amb = e.void_amb;
 }
 
 // Weakest-flaw activation strain of grow_damage (hydro_cpu.cpp:254), formed
@@ -268,7 +271,7 @@ int eu_create_form(int32_t nx, int32_t ny, int32_t nz, double dx, int32_t device
             for (int q = 0; q < deu::ND; q++) g->g1.q[deu::rk_field(q)] = g->alloc(n);
             for (int q = 0; q < deu::ND; q++) g->d.q[q] = g->alloc(n);
             g->mixed = form == EU_MIXED;
-            for (int q = 0; q < 6; q++) {
+            for (int q = 0; q < 7; q++) {
                 if (g->mixed) g->W32.w[q] = g->alloc<float>(n);
                 else g->W.w[q] = g->alloc(n);
             }
@@ -331,8 +334,48 @@ int eu_set_params(eu_grid* h, const eu_params* e) {
         if (!e) throw SphError(SPH_ERR_ARG, "null params");
         if (e->axisym && g->p.ny != 1) throw SphError(SPH_ERR_ARG, "axisym needs ny == 1");
         if (!(e->damp >= 0) || !(e->damp <= 1.0)) throw SphError(SPH_ERR_ARG, "damp must be in [0, 1]");
+        if (!(e->void_amb >= 0)) throw SphError(SPH_ERR_ARG, "void_amb must be >= 0");
         to_params(g->p, *e);
         g->graph_valid = false;
+    });
+}
+
+int eu_set_ref(eu_grid* h) {
+    return guard([&] {
+        deu::Grid* g = G(h);
+        deu::DeviceScope ds(g->device);
+        if (!g->ref_r0) {
+            g->ref_r0 = g->alloc(g->p.n);
+            g->ref_p0 = g->alloc(g->p.n);
+        }
+        deu::k_set_ref<<<g->grid_of(g->p.n), 256, 0, g->st>>>(g->p, g->g, g->ref_r0, g->ref_p0);
+        g->launches++;
+        g->check();
+        EU_CUDA(cudaStreamSynchronize(g->st));
+        g->p.ref_r0 = g->ref_r0;
+        g->p.ref_p0 = g->ref_p0;
+        g->graph_valid = false;
+    });
+}
+
+int eu_clear_ref(eu_grid* h) {
+    return guard([&] {
+        deu::Grid* g = G(h);
+        g->p.ref_r0 = nullptr;
+        g->p.ref_p0 = nullptr;
+        g->graph_valid = false;
+    });
+}
+
+int eu_read_ref(eu_grid* h, double* r0, double* p0, int64_t n) {
+    return guard([&] {
+        deu::Grid* g = G(h);
+        deu::need_n(g, n);
+        if (!g->p.ref_r0) throw SphError(SPH_ERR_STATE, "no reference state (eu_set_ref)");
+        deu::DeviceScope ds(g->device);
+        if (r0) EU_CUDA(cudaMemcpyAsync(r0, g->ref_r0, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, g->st));
+        if (p0) EU_CUDA(cudaMemcpyAsync(p0, g->ref_p0, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, g->st));
+        EU_CUDA(cudaStreamSynchronize(g->st));
     });
 }
 

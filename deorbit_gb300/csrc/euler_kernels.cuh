@@ -43,6 +43,11 @@ struct P {
     int64_t n;
     double dx, invdx;
     double eps_act;  // weakest-flaw activation strain, formed on the host as in hydro_cpu.cpp:254
+    // hydrostatic reference of set_ref (hydro_cpu.cpp:259-261), null when off:
+    // the well-balanced z-sweep and gravity source and the void-cell reset
+    const double* ref_r0;
+    const double* ref_p0;
+    double void_amb;  // VOID_AMB: void cells reset to this density instead of the reference's
 };
 
 template <class R> __device__ __forceinline__ R dmax2(R a, R b) { return a < b ? b : a; }  // std::max
@@ -195,6 +200,23 @@ __device__ F5<R> hllc(const MatT<R>& m, R rho_vac, R rL, R vnL, R t1L, R t2L, R 
     return hllc_star(rR, vnR, t1R, t2R, pR, ER, SR, Ss, flux_of(rR, vnR, t1R, t2R, pR, ER));
 }
 
+// HLLC with the face pressures given (the well-balanced z-sweep), hydro_cpu.cpp:75-88.
+template <class R>
+__device__ F5<R> hllc_p(const MatT<R>& m, R rL, R vnL, R t1L, R t2L, R eL, R pL, R rR, R vnR, R t1R, R t2R, R eR,
+                        R pR) {
+    R cL = sound_speed(m, rL, eL), cR = sound_speed(m, rR, eR);
+    if (pL < R(0)) pL = R(0);
+    if (pR < R(0)) pR = R(0);
+    R SL = dmin2(vnL - cL, vnR - cR), SR = dmax2(vnL + cL, vnR + cR);
+    R Ss = (pR - pL + rL * vnL * (SL - vnL) - rR * vnR * (SR - vnR)) / (rL * (SL - vnL) - rR * (SR - vnR));
+    R EL = rL * eL + R(0.5) * rL * (vnL * vnL + t1L * t1L + t2L * t2L),
+      ER = rR * eR + R(0.5) * rR * (vnR * vnR + t1R * t1R + t2R * t2R);
+    if (SL >= R(0)) return flux_of(rL, vnL, t1L, t2L, pL, EL);
+    if (SR <= R(0)) return flux_of(rR, vnR, t1R, t2R, pR, ER);
+    if (Ss >= R(0)) return hllc_star(rL, vnL, t1L, t2L, pL, EL, SL, Ss, flux_of(rL, vnL, t1L, t2L, pL, EL));
+    return hllc_star(rR, vnR, t1R, t2R, pR, ER, SR, Ss, flux_of(rR, vnR, t1R, t2R, pR, ER));
+}
+
 template <class R>
 __device__ __forceinline__ R mm(R a, R b) {  // minmod, hydro_cpu.cpp:89
     return (a * b <= R(0)) ? R(0) : (fabs(a) < fabs(b) ? a : b);
@@ -221,8 +243,8 @@ struct Rhs {
     double* q[ND];
 };
 template <class R>
-struct PrimT {  // rho, vx, vy, vz, e, rc/rho in the Lop's compute type
-    R* w[6];
+struct PrimT {  // rho, vx, vy, vz, e, rc/rho in the Lop's compute type, and (with a
+    R* w[7];    // reference state) the pressure deviation Pcell - REF_P0 formed in FP64
 };
 template <class R>
 struct FacesT {  // per direction: mass, normal / tangential momentum, energy, tracer fluxes
@@ -428,8 +450,14 @@ static __global__ void k_prim(P p, Fields s, PrimT<R> W, const Ctl* ctl) {
     W.w[1][c] = R(mu / r);
     W.w[2][c] = R(mv / r);
     W.w[3][c] = R(mw / r);
-    W.w[4][c] = R(eint_of(r, mu, mv, mw, E));
+    const double e = eint_of(r, mu, mv, mw, E);
+    W.w[4][c] = R(e);
     W.w[5][c] = R(rc / r);
+    if (p.ref_p0) {  // Pcell - REF_P0 (hydro_cpu.cpp:116)
+        double pr = pressure(p.m, r, e);
+        if (pr < 0) pr = 0;
+        W.w[6][c] = R(pr - p.ref_p0[c]);
+    }
 }
 
 // Face geometry of direction DIR: number of faces and, for face id, the face
@@ -497,7 +525,18 @@ static __global__ void __launch_bounds__(256) k_face(P p, PrimT<R> W, FacesT<R> 
     }
     constexpr int in = DIR == 0 ? 1 : (DIR == 1 ? 2 : 3), it1 = DIR == 0 ? 2 : 1, it2 = DIR == 2 ? 2 : 3;
     const MatT<R> m = mat_as<R>(p.m);
-    const F5<R> fl = hllc(m, R(p.rho_vac), L[0], L[in], L[it1], L[it2], L[4], Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4]);
+    F5<R> fl;
+    if (DIR == 2 && p.ref_p0) {  // well-balanced: reconstruct the deviation from the reference (hydro_cpu.cpp:114-119)
+        const R* dv = W.w[6];
+        const R dLL = dv[cLL], dL = dv[cL], dR = dv[cR], dRR = dv[cRR];
+        const R dLf = dL + R(0.5) * mm(dL - dLL, dR - dL), dRf = dR - R(0.5) * mm(dR - dL, dRR - dR);
+        double p0f = pressure(p.m, 0.5 * (p.ref_r0[cL] + p.ref_r0[cR]), 0.0);
+        if (p0f < 0) p0f = 0;
+        fl = hllc_p(m, L[0], L[in], L[it1], L[it2], L[4], R(p0f) + dLf, Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4],
+                    R(p0f) + dRf);
+    } else {
+        fl = hllc(m, R(p.rho_vac), L[0], L[in], L[it1], L[it2], L[4], Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4]);
+    }
     F.q[DIR][0][id] = fl.r;
     F.q[DIR][1][id] = fl.mn;
     F.q[DIR][2][id] = fl.mt1;
@@ -566,9 +605,21 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
             }
         }
     }
-    if (p.gz != 0.0) {  // plain gravity body force, hydro_cpu.cpp:137-138
-        dmw += -p.gz * r[c];
-        dE += -p.gz * mw[c];
+    if (p.gz != 0.0) {
+        if (!p.ref_r0) {  // plain gravity body force, hydro_cpu.cpp:137-138
+            dmw += -p.gz * r[c];
+            dE += -p.gz * mw[c];
+        } else {  // well-balanced source against the reference, hydro_cpu.cpp:139-143
+            const double* R0 = p.ref_r0;
+            const int64_t ct = c + (k < p.nz - 1 ? 1 : 0), cb = c - (k > 0 ? 1 : 0);
+            double r0t = 0.5 * (R0[c] + R0[ct]), r0b = 0.5 * (R0[cb] + R0[c]);
+            double p0t = pressure(p.m, r0t, 0.0);
+            if (p0t < 0) p0t = 0;
+            double p0b = pressure(p.m, r0b, 0.0);
+            if (p0b < 0) p0b = 0;
+            dmw += -p.gz * (r[c] - R0[c]) + (p0t - p0b) * p.invdx;
+            dE += -p.gz * mw[c];
+        }
     }
     double dS[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, dD = 0.0, dvib = 0.0;
     if (p.m.G > 0 && !(p.rho_cfl > 0 && r[c] < p.rho_cfl)) {  // strength sources, hydro_cpu.cpp:145-213
@@ -676,6 +727,28 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
     d.q[D_VIB][c] = dvib;
 }
 
+// Near-void cell: momentum zeroed; with a reference state also reset to the
+// reference (or ambient) density with no energy, stress or tracer,
+// hydro_cpu.cpp:272-290 (not the conservative transfer).
+static __device__ __forceinline__ void void_cell(const P& p, const Fields& g, int64_t c) {
+    if (!(p.rho_cfl > 0 && g.q[F_R][c] < p.rho_cfl)) return;
+    g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
+    if (p.ref_r0) {
+        g.q[F_R][c] = (p.void_amb > 0 ? p.void_amb : p.ref_r0[c]);
+        g.q[F_E][c] = 0;
+        g.q[F_SXX][c] = g.q[F_SYY][c] = g.q[F_SZZ][c] = g.q[F_SXY][c] = g.q[F_SXZ][c] = g.q[F_SYZ][c] = 0;
+        g.q[F_RC][c] = 0;
+    }
+}
+
+// set_ref (hydro_cpu.cpp:259-261): density and pressure frozen as the reference.
+static __global__ void k_set_ref(P p, Fields g, double* r0, double* p0) {
+    const int64_t c = gtid();
+    if (c >= p.n) return;
+    r0[c] = g.q[F_R][c];
+    p0[c] = pcell(p, g, c);
+}
+
 // Predictor (hydro_cpu.cpp:413-418): g1 = g + dt d, void-cell reset, radial
 // return without regeneration.
 template <class R>
@@ -685,7 +758,7 @@ static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
     const double dt = ctl->dt;
 #pragma unroll
     for (int q = 0; q < ND; q++) g1.q[rk_field(q)][c] = g.q[rk_field(q)][c] + dt * d.q[q][c];
-    if (p.rho_cfl > 0 && g1.q[F_R][c] < p.rho_cfl) g1.q[F_MU][c] = g1.q[F_MV][c] = g1.q[F_MW][c] = 0;
+    void_cell(p, g1, c);
     vonmises_cell<R>(p, g1, g.q[F_AF], c, false);
 }
 
@@ -708,7 +781,7 @@ static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
         g.q[F_MV][c] *= p.damp;
         g.q[F_MW][c] *= p.damp;
     }
-    if (p.rho_cfl > 0 && g.q[F_R][c] < p.rho_cfl) g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
+    void_cell(p, g, c);
 }
 
 // Single operators for the C ABI's unit calls.

@@ -389,10 +389,9 @@ int sph_serve_poll(sph_server* s, double max_wait_s, int64_t* done_ids, int32_t 
         }
         int64_t steps = s->chunk;
         int64_t n_res = 0;
-        for (auto& kv : s->active) {
-            const sph_impact_info inf = E.impact_info(kv.first);
-            steps = std::min<int64_t>(steps, kv.second->steps - inf.steps);
-            n_res += inf.n;
+        for (auto& kv : s->active) {  // host step counts: no device round trip per impact
+            steps = std::min<int64_t>(steps, kv.second->steps - E.impact_steps(kv.first));
+            n_res += E.impact_n(kv.first);
         }
         steps = std::max<int64_t>(steps, 1);
         const double tb = now_s(s->t0);
@@ -415,7 +414,7 @@ int sph_serve_poll(sph_server* s, double max_wait_s, int64_t* done_ids, int32_t 
         } host_time{s, tr0};
         std::vector<int> fin;
         for (auto& kv : s->active)
-            if (E.impact_info(kv.first).steps >= kv.second->steps) fin.push_back(kv.first);
+            if (E.impact_steps(kv.first) >= kv.second->steps) fin.push_back(kv.first);
         for (int b : fin) {
             auto r = s->active[b];
             const int nf = (int)s->fields.size();

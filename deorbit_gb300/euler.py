@@ -28,7 +28,7 @@ class Params(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
                                           "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
-        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp reserved".split()]
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp reserved".split()] + [("void_amb", C.c_double)]
 
 
 _D = C.POINTER(C.c_double)
@@ -62,6 +62,9 @@ _SIGS = {
     "eu_event_elapsed": (C.c_int, [_P, C.c_int32, C.c_int32, _D]),
     "eu_device_bytes": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "eu_launches": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "eu_set_ref": (C.c_int, [_P]),
+    "eu_clear_ref": (C.c_int, [_P]),
+    "eu_read_ref": (C.c_int, [_P, _D, _D, C.c_int64]),
 }
 _declared = False
 
@@ -158,6 +161,19 @@ class Grid:
     def fields(self, names=FIELDS):
         return self.read_many(names)
 
+    def set_ref(self):
+        """set_ref (hydro_cpu.cpp:259-261): the current density and pressure
+        become the hydrostatic reference (well-balanced sweep, void reset)."""
+        sph.check(lib().eu_set_ref(self.h))
+
+    def clear_ref(self):
+        sph.check(lib().eu_clear_ref(self.h))
+
+    def reference(self):
+        r0, p0 = np.empty(self.n), np.empty(self.n)
+        sph.check(lib().eu_read_ref(self.h, r0.ctypes.data_as(_D), p0.ctypes.data_as(_D), self.n))
+        return r0, p0
+
     def pressure(self):
         out = np.empty(self.n)
         sph.check(lib().eu_read_pressure(self.h, out.ctypes.data_as(_D), self.n))
@@ -243,4 +259,33 @@ def from_case(case, device=0, form=FP64) -> Grid:
     """A grid loaded with a workload case (grid_ic.Case)."""
     g = Grid(*case.shape, case.dx, material=case.material, params=case.params, device=device, form=form)
     g.write_many(case.fields)
+    if getattr(case, "set_ref", False):
+        g.set_ref()
+        if case.post_ref:
+            g.write_many(case.post_ref)
     return g
+
+
+def run_case(g, case, steps):
+    """The drivers' loop on a grid built from `case` with the case's floor pin
+    after every step (hydro_cpu.cpp:855); without a pin, Grid.run."""
+    if not case.pin_floor:
+        return g.run(case.cfl, case.t_end, steps)
+    nx, ny, nz = case.shape
+    base = case.fields["r"].reshape(nx, ny, nz)
+    t, s = g.time(), 0
+    while t < case.t_end and s < steps:
+        dt = case.cfl * case.dx / g.maxspeed()
+        if t + dt > case.t_end:
+            dt = case.t_end - t
+        g.step(dt)
+        f = g.read_many(["r", "mu", "mv", "mw", "E"])
+        f = {k: v.reshape(nx, ny, nz) for k, v in f.items()}
+        f["r"][:, :, :case.pin_floor] = base[:, :, :case.pin_floor]
+        for k in ("mu", "mv", "mw", "E"):
+            f[k][:, :, :case.pin_floor] = 0.0
+        g.write_many({k: v.reshape(-1) for k, v in f.items()})
+        t += dt
+        s += 1
+    g.set_time(t)
+    return s, t

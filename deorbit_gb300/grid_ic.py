@@ -29,6 +29,9 @@ class Case:
     fields: dict = field(default_factory=dict)
     cfl: float = 0.4
     t_end: float = 0.0
+    set_ref: bool = False      # freeze `fields` as the hydrostatic reference (set_ref) ...
+    post_ref: dict = field(default_factory=dict)  # ... then write these over them
+    pin_floor: int = 0         # driver: the lowest pin_floor z-layers return to the reference each step
 
     @property
     def n(self):
@@ -212,6 +215,46 @@ def impact3d(N=64, a_cells=None, speed=8000.0, angle_deg=30.0, af=False, t_end=N
     if t_end is None:
         t_end = 4.0 * a * dx / speed
     return Case(f"impact3d_{N}", (N, N, N), dx, ic.basalt(), prm, f, 0.3, t_end)
+
+
+def substrate(N=60):
+    """hydro_cpu.cpp:847-859: a gravity-loaded lithostatic basalt substrate
+    under the well-balanced reconstruction must stay at rest (t_end 200 s,
+    the two deepest layers pinned to the reference after every step)."""
+    gz, rho0, A, dx, zsurf = 3.71, 2700.0, 2.67e10, 500.0, 20e3
+    z = _centres(N, dx)
+    col = np.where(z < zsurf, rho0 * (1.0 + rho0 * gz * (zsurf - z) / A), 0.27)
+    r = np.tile(col, N)  # (i, k) with k fastest
+    return Case("substrate", (N, 1, N), dx, ic.basalt(), {"gz": gz, "damp": 1.0, "rho_cfl": 100.0},
+                {"r": r, "E": np.zeros(N * N)}, 0.4, 200.0, set_ref=True, pin_floor=2)
+
+
+def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0, gz=3.71, t_end=None):
+    """hydro_cpu.cpp:557-597: the axisymmetric vertical impact crater -- a
+    basalt sphere of radius a on the axis, tangent to the surface, at U m/s
+    into a lithostatic basalt half-space under gravity, with the frozen
+    pre-impact column as the well-balanced reference, ROCK yield, near-void
+    and vacuum-aware faces, and (tdec > 0) shock-activated fluidization with
+    the crater defaults (acoustic seeding, overburden relief).  The driver's
+    far-field floor pin and radial sponge are not part of the case."""
+    rho0, Abulk = 2700.0, 2.67e10
+    dx = a / cppr
+    Nr, Nz = int(Rfac * a / dx + 0.5), int(Zfac * a / dx + 0.5)
+    zsurf = Nz * dx - 5.0 * a
+    rr = _centres(Nr, dx)[:, None]
+    zz = _centres(Nz, dx)[None, :]
+    r = np.where(zz < zsurf, rho0 * (1.0 + rho0 * gz * (zsurf - zz) / Abulk), 0.27) * np.ones_like(rr)
+    zc = zsurf + a
+    sph_ = np.sqrt(rr * rr + (zz - zc) * (zz - zc)) < a
+    post = {"r": np.where(sph_, rho0, r).reshape(-1), "mw": np.where(sph_, -rho0 * U, 0.0).reshape(-1),
+            "E": np.where(sph_, 0.5 * rho0 * U * U, 0.0).reshape(-1)}
+    prm = {"axisym": 1, "rho_cfl": 100.0, "rho_vac": 100.0, "rock": 1, "gz": gz}
+    if tdec > 0:
+        prm.update(tdec=tdec, eta_af=eta_af, c_act=0.5, p_coh=1.0e6, p_act=1.0e8, af_seeddp=1, af_prel=1)
+    if t_end is None:
+        t_end = 2.0 * math.sqrt((Rfac * a) / gz)
+    return Case(f"crater_{cppr}", (Nr, 1, Nz), dx, ic.basalt(), prm,
+                {"r": r.reshape(-1), "E": np.zeros(Nr * Nz)}, 0.4, t_end, set_ref=True, post_ref=post)
 
 
 GATES = {"sod": sod, "tracer": tracer, "sedov": sedov, "sedov_axi": sedov_axi, "shear": shear,

@@ -18,9 +18,9 @@
  * differently from the host library's.
  *
  * Not provided (the reference's options for them must stay off): the
- * well-balanced hydrostatic reconstruction and the void-cell reset against a
- * frozen reference state (set_ref, REF_R0 / REF_P0, VOID_AMB, VOID_CONS) and
- * the implicit viscous solve (VISC_IMP).  eu_set_params has no field for them.
+ * conservative void-cell transfer (VOID_CONS: excess mass moved to the densest
+ * neighbour cell by cell in index order, a serial dependency) and the implicit
+ * viscous solve (VISC_IMP).  eu_set_params has no field for them.
  *
  * Fields are host arrays of nx*ny*nz doubles, cell (i,j,k) at
  * (i*ny + j)*nz + k, exactly the reference's layout.  Names: r mu mv mw E Sxx
@@ -63,6 +63,8 @@ typedef struct eu_params {
     int32_t af_prel;  /* AF_PREL: overburden-relief form */
     int32_t af_seeddp;/* AF_SEEDDP: seed from the acoustic velocity of the jump */
     int32_t reserved;
+    double void_amb;  /* VOID_AMB: with a reference state, void cells reset to this
+                         density instead of the reference's (0 = the reference's) */
 } eu_params;
 
 typedef struct eu_grid eu_grid;
@@ -90,6 +92,15 @@ int eu_set_material(eu_grid* g, const sph_material* m);
 /* Replaces the file-scope settings; rejects axisym with ny != 1. */
 int eu_set_params(eu_grid* g, const eu_params* p);
 int eu_get_shape(const eu_grid* g, int32_t shape[3], double* dx);
+
+/* set_ref (hydro_cpu.cpp:259-261): the current density and pressure become the
+ * hydrostatic reference of the well-balanced z-sweep and gravity source
+ * (hydro_cpu.cpp:75-88, 114-119, 139-143) and of the void-cell reset
+ * (272-290: near-void cells return to the reference, or VOID_AMB, density).
+ * eu_clear_ref drops it; eu_read_ref reads it (either pointer may be NULL). */
+int eu_set_ref(eu_grid* g);
+int eu_clear_ref(eu_grid* g);
+int eu_read_ref(eu_grid* g, double* r0, double* p0, int64_t n);
 
 /* Field i/o of one named field (n = nx*ny*nz doubles), or of several in one
  * call (copies overlap on the grid's stream, one synchronisation). */

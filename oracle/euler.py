@@ -30,7 +30,7 @@ class Params(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
                                           "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
-        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()]
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()] + [("void_amb", C.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad_"}
@@ -56,6 +56,8 @@ def _declare(lib, p):
         f"{p}step_rk2": (None, [C.c_void_p, C.c_double]),
         f"{p}run": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _D]),
         f"{p}pcell": (C.c_double, [C.c_void_p, C.c_int]),
+        f"{p}set_ref": (None, [C.c_void_p]),
+        f"{p}clear_ref": (None, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -167,6 +169,13 @@ class _Grid:
     def pcell(self, c) -> float:
         return self._f("pcell")(self.h, int(c))
 
+    def set_ref(self):
+        """set_ref: the current density and pressure become the hydrostatic reference."""
+        self._f("set_ref")(self.h)
+
+    def clear_ref(self):
+        self._f("clear_ref")(self.h)
+
     def close(self):
         if self.h:
             self._f("destroy")(self.h)
@@ -200,4 +209,33 @@ def from_case(case, cls=OracleGrid):
     g = cls(*case.shape, case.dx, material=O.material_from_dict(case.material), params=case.params)
     for k, v in case.fields.items():
         g.set_field(k, v)
+    if getattr(case, "set_ref", False):
+        g.set_ref()
+        for k, v in case.post_ref.items():
+            g.set_field(k, v)
     return g
+
+
+def run_case(g, case, steps):
+    """The drivers' loop on a grid built from `case` (steps of step_rk2 at
+    dt = cfl dx / maxspeed clipped at t_end), with the case's floor pin after
+    every step (hydro_cpu.cpp:855): returns (steps, t)."""
+    if not case.pin_floor:
+        return g.run(case.cfl, case.t_end, steps)
+    nx, ny, nz = case.shape
+    base = case.fields["r"].reshape(nx, ny, nz)  # the reference density of the pinned layers
+    t, s = 0.0, 0
+    while t < case.t_end and s < steps:
+        dt = case.cfl * case.dx / g.maxspeed()
+        if t + dt > case.t_end:
+            dt = case.t_end - t
+        g.step(dt)
+        f = {k: g.field(k).reshape(nx, ny, nz) for k in ("r", "mu", "mv", "mw", "E")}
+        f["r"][:, :, :case.pin_floor] = base[:, :, :case.pin_floor]
+        for k in ("mu", "mv", "mw", "E"):
+            f[k][:, :, :case.pin_floor] = 0.0
+        for k, v in f.items():
+            g.set_field(k, v)
+        t += dt
+        s += 1
+    return s, t

@@ -24,6 +24,7 @@ struct eorc_grid {
     double* d[ND];
     orc_material mat;
     eorc_params p;
+    double *ref_r0, *ref_p0; /* hydrostatic reference (set_ref), NULL when off */
 };
 
 static inline double dmax2(double a, double b) { return a < b ? b : a; } /* std::max */
@@ -55,6 +56,8 @@ eorc_grid* eorc_create(int nx, int ny, int nz, double dx) {
 
 void eorc_destroy(eorc_grid* g) {
     if (!g) return;
+    free(g->ref_r0);
+    free(g->ref_p0);
     for (int q = 0; q < NF; q++) free(g->f[q]);
     for (int q = 0; q < ND; q++) free(g->d[q]);
     free(g);
@@ -165,6 +168,23 @@ static F5 hllc(const eorc_grid* gr, double rL, double vnL, double t1L, double t2
     return hllc_star(rR, vnR, t1R, t2R, pR, ER, SR, Ss, flux_of(rR, vnR, t1R, t2R, pR, ER));
 }
 
+/* HLLC with the face pressures given (well-balanced z-sweep), hydro_cpu.cpp:75-88. */
+static F5 hllc_p(const eorc_grid* gr, double rL, double vnL, double t1L, double t2L, double eL, double pL, double rR,
+                 double vnR, double t1R, double t2R, double eR, double pR) {
+    const orc_material* m = &gr->mat;
+    double cL = orc_sound_speed(m, rL, eL), cR = orc_sound_speed(m, rR, eR);
+    if (pL < 0) pL = 0;
+    if (pR < 0) pR = 0;
+    double SL = dmin2(vnL - cL, vnR - cR), SR = dmax2(vnL + cL, vnR + cR);
+    double Ss = (pR - pL + rL * vnL * (SL - vnL) - rR * vnR * (SR - vnR)) / (rL * (SL - vnL) - rR * (SR - vnR));
+    double EL = rL * eL + 0.5 * rL * (vnL * vnL + t1L * t1L + t2L * t2L),
+           ER = rR * eR + 0.5 * rR * (vnR * vnR + t1R * t1R + t2R * t2R);
+    if (SL >= 0) return flux_of(rL, vnL, t1L, t2L, pL, EL);
+    if (SR <= 0) return flux_of(rR, vnR, t1R, t2R, pR, ER);
+    if (Ss >= 0) return hllc_star(rL, vnL, t1L, t2L, pL, EL, SL, Ss, flux_of(rL, vnL, t1L, t2L, pL, EL));
+    return hllc_star(rR, vnR, t1R, t2R, pR, ER, SR, Ss, flux_of(rR, vnR, t1R, t2R, pR, ER));
+}
+
 static inline double mm(double a, double b) { /* hydro_cpu.cpp:89 */
     return (a * b <= 0) ? 0.0 : (fabs(a) < fabs(b) ? a : b);
 }
@@ -210,7 +230,20 @@ static void sweep(const eorc_grid* g, int dir, double* Fr, double* Fmn, double* 
                 if (R[0] < 1e-9) R[0] = B[0];
                 if (L[4] < 0) L[4] = A[4];
                 if (R[4] < 0) R[4] = B[4];
-                F5 fl = hllc(g, L[0], L[in], L[it1], L[it2], L[4], R[0], R[in], R[it1], R[it2], R[4]);
+                F5 fl;
+                if (dir == 2 && g->ref_r0) { /* well-balanced: the pressure deviation from the reference */
+                    int cLL = sweep_cell(g, dir, iLL, a, b), cL = sweep_cell(g, dir, iL, a, b),
+                        cR = sweep_cell(g, dir, iR, a, b), cRR = sweep_cell(g, dir, iRR, a, b);
+                    double dLL = eorc_pcell(g, cLL) - g->ref_p0[cLL], dL = eorc_pcell(g, cL) - g->ref_p0[cL],
+                           dR = eorc_pcell(g, cR) - g->ref_p0[cR], dRR = eorc_pcell(g, cRR) - g->ref_p0[cRR];
+                    double dLf = dL + 0.5 * mm(dL - dLL, dR - dL), dRf = dR - 0.5 * mm(dR - dL, dRR - dR);
+                    double p0f = orc_pressure(&g->mat, 0.5 * (g->ref_r0[cL] + g->ref_r0[cR]), 0.0);
+                    if (p0f < 0) p0f = 0;
+                    fl = hllc_p(g, L[0], L[in], L[it1], L[it2], L[4], p0f + dLf, R[0], R[in], R[it1], R[it2], R[4],
+                                p0f + dRf);
+                } else {
+                    fl = hllc(g, L[0], L[in], L[it1], L[it2], L[4], R[0], R[in], R[it1], R[it2], R[4]);
+                }
                 Fr[f] = fl.r; Fmn[f] = fl.mn; Ft1[f] = fl.mt1; Ft2[f] = fl.mt2; FE[f] = fl.E;
                 int cl = sweep_cell(g, dir, iL, a, b), cr = sweep_cell(g, dir, iR, a, b);
                 Frc[f] = fl.r * (fl.r >= 0.0 ? rc[cl] / r[cl] : rc[cr] / r[cr]);
@@ -267,11 +300,30 @@ void eorc_lop(eorc_grid* g) {
     const double* mu = g->f[F_MU];
     const double* mv = g->f[F_MV];
     const double* mw = g->f[F_MW];
-    if (GZ != 0.0) /* hydro_cpu.cpp:137-138 (plain gravity body force) */
-        for (int c = 0; c < n; c++) {
-            d[D_MW][c] += -GZ * r[c];
-            d[D_E][c] += -GZ * g->f[F_MW][c];
+    if (GZ != 0.0) {
+        if (!g->ref_r0) { /* hydro_cpu.cpp:137-138 (plain gravity body force) */
+            for (int c = 0; c < n; c++) {
+                d[D_MW][c] += -GZ * r[c];
+                d[D_E][c] += -GZ * g->f[F_MW][c];
+            }
+        } else { /* hydro_cpu.cpp:139-143 (well-balanced source against the reference) */
+            const double invdx = 1.0 / g->dx;
+            const double* R0 = g->ref_r0;
+            for (int i = 0; i < g->nx; i++)
+                for (int j = 0; j < g->ny; j++)
+                    for (int k = 0; k < g->nz; k++) {
+                        int c = idx(g, i, j, k);
+                        double r0t = 0.5 * (R0[c] + R0[idx(g, i, j, imin2(g->nz - 1, k + 1))]),
+                               r0b = 0.5 * (R0[idx(g, i, j, imax2(0, k - 1))] + R0[c]);
+                        double p0t = orc_pressure(&g->mat, r0t, 0.0);
+                        if (p0t < 0) p0t = 0;
+                        double p0b = orc_pressure(&g->mat, r0b, 0.0);
+                        if (p0b < 0) p0b = 0;
+                        d[D_MW][c] += -GZ * (r[c] - R0[c]) + (p0t - p0b) * invdx;
+                        d[D_E][c] += -GZ * g->f[F_MW][c];
+                    }
         }
+    }
     const double G = g->mat.G;
     if (G <= 0) return;
     const double *Sxx = g->f[F_SXX], *Syy = g->f[F_SYY], *Szz = g->f[F_SZZ], *Sxy = g->f[F_SXY],
@@ -481,12 +533,36 @@ double eorc_maxspeed(const eorc_grid* g) {
     return s;
 }
 
-/* Near-void cells lose their momentum, hydro_cpu.cpp:272-273 (no frozen
- * reference state). */
+/* Near-void cells lose their momentum and, with a reference state, are reset
+ * to the reference density (or the ambient VOID_AMB) with no energy, stress or
+ * tracer, hydro_cpu.cpp:272-290 (not the conservative transfer). */
 static void void_cells(eorc_grid* g) {
     if (g->p.rho_cfl <= 0) return;
     for (int c = 0; c < g->n; c++)
-        if (g->f[F_R][c] < g->p.rho_cfl) g->f[F_MU][c] = g->f[F_MV][c] = g->f[F_MW][c] = 0;
+        if (g->f[F_R][c] < g->p.rho_cfl) {
+            g->f[F_MU][c] = g->f[F_MV][c] = g->f[F_MW][c] = 0;
+            if (g->ref_r0) {
+                g->f[F_R][c] = (g->p.void_amb > 0 ? g->p.void_amb : g->ref_r0[c]);
+                g->f[F_E][c] = 0;
+                g->f[F_SXX][c] = g->f[F_SYY][c] = g->f[F_SZZ][c] = g->f[F_SXY][c] = g->f[F_SXZ][c] = g->f[F_SYZ][c] = 0;
+                g->f[F_RC][c] = 0;
+            }
+        }
+}
+
+void eorc_set_ref(eorc_grid* g) { /* hydro_cpu.cpp:259-261 */
+    if (!g->ref_r0) g->ref_r0 = (double*)calloc((size_t)(g->n > 0 ? g->n : 1), sizeof(double));
+    if (!g->ref_p0) g->ref_p0 = (double*)calloc((size_t)(g->n > 0 ? g->n : 1), sizeof(double));
+    for (int c = 0; c < g->n; c++) {
+        g->ref_r0[c] = g->f[F_R][c];
+        g->ref_p0[c] = eorc_pcell(g, c);
+    }
+}
+
+void eorc_clear_ref(eorc_grid* g) {
+    free(g->ref_r0);
+    free(g->ref_p0);
+    g->ref_r0 = g->ref_p0 = NULL;
 }
 
 static const int RK_FIELDS[ND] = {F_R, F_MU, F_MV, F_MW, F_E, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ, F_D, F_RC, F_VIB};
@@ -498,6 +574,8 @@ void eorc_step_rk2(eorc_grid* g, double dt) {
     eorc_grid* g1 = eorc_create(g->nx, g->ny, g->nz, g->dx);
     g1->mat = g->mat;
     g1->p = g->p;
+    g1->ref_r0 = g->ref_r0; /* shared, not owned */
+    g1->ref_p0 = g->ref_p0;
     for (int q = 0; q < NF; q++) memcpy(g1->f[q], g->f[q], sizeof(double) * (size_t)n);
     eorc_lop(g);
     for (int q = 0; q < ND; q++) {
@@ -516,6 +594,7 @@ void eorc_step_rk2(eorc_grid* g, double dt) {
         for (int c = 0; c < n; c++) x[c] = 0.5 * (x[c] + y[c] + dt * dq[c]);
     }
     for (int q = 0; q < ND; q++) memcpy(g->d[q], g1->d[q], sizeof(double) * (size_t)n);
+    g1->ref_r0 = g1->ref_p0 = NULL;
     eorc_destroy(g1);
     eorc_grow_damage(g, dt);
     eorc_vonmises(g, 1);

@@ -3,17 +3,19 @@
  * A plain C restatement of the reference's CPU Euler solver
  * (hydrocodes/euler/hydro_cpu.cpp): unsplit MUSCL-minmod + HLLC hydro sweeps
  * with a passive material tracer (hydro_cpu.cpp:54-74,98-136), the
- * vacuum-aware face flux (43-53), plain gravity (137-144), elastic-plastic
+ * vacuum-aware face flux (43-53), gravity (137-144), elastic-plastic
  * strength with the Jaumann rate, upwind stress advection, div S and div(S.v)
  * in Cartesian or cylindrical (r, z) geometry (145-214), von Mises and the
  * pressure-dependent ROCK yield (229-252), tensile damage growth (253-258),
- * the near-void momentum reset (272-273), acoustic fluidization activation
- * (390-410), the CFL speed (378-380) and the two-stage Runge-Kutta step
- * (411-425).  Every expression keeps the reference's floating-point operation
- * order; the library is built with -ffp-contract=off.  The well-balanced
- * hydrostatic reconstruction, the void-cell reset against a frozen reference
- * state and the implicit viscous solve are not restated (the CUDA grid solver
- * does not provide them either).
+ * the frozen hydrostatic reference of set_ref (259-261) with the well-balanced
+ * z-sweep and gravity source against it (75-88, 114-119, 139-143), the
+ * near-void reset to that reference or to an ambient density (272-290; not the
+ * conservative transfer), acoustic fluidization activation (390-410), the CFL
+ * speed (378-380) and the two-stage Runge-Kutta step (411-425).  Every
+ * expression keeps the reference's floating-point operation order; the
+ * library is built with -ffp-contract=off.  The conservative void transfer
+ * (VOID_CONS) and the implicit viscous solve (VISC_IMP) are not restated (the
+ * CUDA grid solver does not provide them either).
  *
  * The oracle is test infrastructure: only tests/, the smoke check and the
  * bench's CPU legs call it, never the product path.
@@ -47,6 +49,7 @@ typedef struct {
     int af_prel;      /* overburden relief constitutive form */
     int af_seeddp;    /* seed vibrations from the acoustic velocity of the jump */
     int pad_;
+    double void_amb;  /* void cells reset to this ambient density instead of the reference's */
 } eorc_params;
 
 void eorc_params_default(eorc_params* p);
@@ -66,6 +69,11 @@ double* eorc_field(eorc_grid* g, const char* name);
  * Sxy Sxz Syz D rc vib). */
 double* eorc_rhs(eorc_grid* g, const char* name);
 
+/* set_ref (hydro_cpu.cpp:259-261): the current density and pressure become
+ * the hydrostatic reference of the well-balanced sweep and the void reset;
+ * eorc_clear_ref drops it. */
+void eorc_set_ref(eorc_grid* g);
+void eorc_clear_ref(eorc_grid* g);
 void eorc_lop(eorc_grid* g);                    /* hydro_cpu.cpp:98-214 */
 void eorc_vonmises(eorc_grid* g, int reg);      /* 229-252 */
 void eorc_grow_damage(eorc_grid* g, double dt); /* 253-258 */

@@ -25,6 +25,7 @@ struct RefGrid {
     DU d;
     orc_material mat;
     eorc_params prm;
+    std::vector<double> ref_r0, ref_p0;  // this grid's hydrostatic reference (set_ref), empty when off
     RefGrid(int nx, int ny, int nz, double dx) : g(nx, ny, nz, dx), d(nx * ny * nz) {}
 };
 
@@ -48,8 +49,10 @@ void load(const RefGrid* R) {
     RHO_CFL = p.rho_cfl; DAMP = p.damp; RHO_VAC = p.rho_vac; AXISYM = p.axisym != 0; ROCK = p.rock != 0;
     Y_I0 = p.y_i0; MU_I = p.mu_i; MU_D = p.mu_d; Y_D0 = p.y_d0; Y_M = p.y_m; Y_BINGHAM = p.y_bingham;
     VISC_IMP = false;
-    REF_R0.clear();
-    REF_P0.clear();
+    VOID_CONS = false;
+    VOID_AMB = p.void_amb;
+    REF_R0 = R->ref_r0;
+    REF_P0 = R->ref_p0;
     AF_REG = p.af_reg != 0; C_REG = p.c_reg; AF_SAT = p.af_sat; AF_PREL = p.af_prel != 0;
     AF_SEEDDP = p.af_seeddp != 0;
 }
@@ -101,6 +104,7 @@ eorc_params capture_defaults() {
     p.rho_cfl = RHO_CFL; p.damp = DAMP; p.rho_vac = RHO_VAC; p.axisym = AXISYM; p.rock = ROCK;
     p.y_i0 = Y_I0; p.mu_i = MU_I; p.mu_d = MU_D; p.y_d0 = Y_D0; p.y_m = Y_M; p.y_bingham = Y_BINGHAM;
     p.af_reg = AF_REG; p.c_reg = C_REG; p.af_sat = AF_SAT; p.af_prel = AF_PREL; p.af_seeddp = AF_SEEDDP;
+    p.void_amb = VOID_AMB;
     return p;
 }
 const eorc_params kDefaults = capture_defaults();
@@ -175,6 +179,18 @@ int eref_run(void* h, double cfl, double t_end, int max_steps, double* t_out) {
     }
     if (t_out) *t_out = t;
     return s;
+}
+void eref_set_ref(void* h) {
+    RefGrid* R = (RefGrid*)h;
+    load(R);
+    set_ref(R->g);
+    R->ref_r0 = REF_R0;
+    R->ref_p0 = REF_P0;
+}
+void eref_clear_ref(void* h) {
+    RefGrid* R = (RefGrid*)h;
+    R->ref_r0.clear();
+    R->ref_p0.clear();
 }
 double eref_pcell(void* h, int c) {
     RefGrid* R = (RefGrid*)h;

@@ -34,7 +34,9 @@ OUT = os.path.join(HERE, "euler_gates.npz")
 RUNS = [(GI.sod(), 60), (GI.tracer(), 40), (GI.sedov(12), 8), (GI.sedov_axi(16, 32), 10),
         (GI.shear(200), 30), (GI.yield_pulse(100), 40), (GI.vacuum(200), 40), (GI.bshock(100), 20),
         (GI.freefall(), 20), (GI.atmos(50), 10), (GI.tensile(), 20), (GI.alimpact(100), 30),
-        (GI.surface(), 20), (GI.impact3d(12), 6), (GI.impact3d(12, af=True), 6)]
+        (GI.surface(), 20), (GI.impact3d(12), 6), (GI.impact3d(12, af=True), 6),
+        (GI.substrate(), 30), (GI.crater(), 20), (GI.crater(tdec=2.0, eta_af=1e8), 20),
+        (GI.crater(cppr=3, U=6000.0), 15)]
 
 
 def perturbed_state(seed, shape, strength=True):
@@ -79,16 +81,18 @@ def main():
     out = {}
     for case, steps in RUNS:
         g = EO.from_case(case, EO.RefGrid)
-        s, t = g.run(case.cfl, case.t_end, steps)
+        s, t = EO.run_case(g, case, steps)
         key = case.name + ("_af" if case.params.get("c_act") else "")
         for k, v in case.fields.items():
             out[f"{key}/in/{k}"] = np.asarray(v, dtype=np.float64)
+        for k, v in case.post_ref.items():
+            out[f"{key}/post/{k}"] = np.asarray(v, dtype=np.float64)
         for k, v in g.fields().items():
             out[f"{key}/out/{k}"] = v
         out[f"{key}/meta"] = np.array(json.dumps({
             "kind": "run", "shape": list(case.shape), "dx": case.dx, "material": case.material,
             "params": case.params, "cfl": case.cfl, "t_end": case.t_end, "max_steps": steps,
-            "steps": s, "t": t}))
+            "steps": s, "t": t, "set_ref": case.set_ref, "pin_floor": case.pin_floor}))
         g.close()
         print(key, s, t)
     for i, (name, shape, dx, prm, op, arg) in enumerate(OPS):

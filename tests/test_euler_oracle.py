@@ -31,22 +31,28 @@ def _cases():
     return z, keys
 
 
-def _grid_from(z, key):
+def case_from(z, key):
+    """The workload case a fixture was made from (fields, reference state, pin)."""
     meta = json.loads(str(z[f"{key}/meta"]))
-    g = EO.OracleGrid(*meta["shape"], meta["dx"], material=O.material_from_dict(meta["material"]),
-                      params=meta["params"])
-    for k in z.files:
-        if k.startswith(key + "/in/"):
-            g.set_field(k.split("/")[-1], z[k])
-    return g, meta
+    ins = {k.split("/")[-1]: z[k] for k in z.files if k.startswith(key + "/in/")}
+    post = {k.split("/")[-1]: z[k] for k in z.files if k.startswith(key + "/post/")}
+    case = GI.Case(key, tuple(meta["shape"]), meta["dx"], meta["material"], meta["params"], ins,
+                   meta.get("cfl", 0.4), meta.get("t_end", 0.0), meta.get("set_ref", False), post,
+                   meta.get("pin_floor", 0))
+    return case, meta
+
+
+def _grid_from(z, key):
+    case, meta = case_from(z, key)
+    return EO.from_case(case), meta, case
 
 
 @pytest.mark.parametrize("key", _cases()[1])
 def test_oracle_reproduces_reference_bit_for_bit(key):
     z = np.load(GOLD)
-    g, meta = _grid_from(z, key)
+    g, meta, case = _grid_from(z, key)
     if meta["kind"] == "run":
-        s, t = g.run(meta["cfl"], meta["t_end"], meta["max_steps"])
+        s, t = EO.run_case(g, case, meta["max_steps"])
         assert s == meta["steps"] and t == meta["t"]
         got = g.fields()
     else:

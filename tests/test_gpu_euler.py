@@ -42,12 +42,12 @@ def rel_l2(a, b):
 
 def _pair(E, case, steps):
     g = E.from_case(case)
-    s, t = g.run(case.cfl, case.t_end, steps)
+    s, t = E.run_case(g, case, steps)
     got = g.fields()
     n_launch = g.launches()
     g.close()
     o = EO.from_case(case)
-    so, to = o.run(case.cfl, case.t_end, steps)
+    so, to = EO.run_case(o, case, steps)
     ref = o.fields()
     o.close()
     return (s, t, got, n_launch), (so, to, ref)
@@ -66,7 +66,9 @@ def test_ideal_gas_runs_bit_exact(E, case, steps):
 
 @pytest.mark.parametrize("case,steps", [(GI.shear(200), 40), (GI.yield_pulse(100), 40), (GI.vacuum(200), 40),
                                         (GI.bshock(100), 20), (GI.tensile(), 20), (GI.alimpact(100), 40),
-                                        (GI.surface(), 20), (GI.impact3d(16), 8), (GI.impact3d(16, af=True), 8)],
+                                        (GI.surface(), 20), (GI.impact3d(16), 8), (GI.impact3d(16, af=True), 8),
+                                        (GI.substrate(), 30), (GI.crater(), 20),
+                                        (GI.crater(tdec=2.0, eta_af=1e8), 20)],
                          ids=lambda x: getattr(x, "name", str(x)) + ("_af" if getattr(x, "params", {}).get("c_act") else ""))
 def test_tillotson_runs_match_oracle(E, case, steps):
     (s, t, got, _), (so, to, ref) = _pair(E, case, steps)
@@ -265,7 +267,7 @@ def _group_err(got, ref, names):
                                         (GI.sedov_axi(16, 32), 15), (GI.atmos(50), 10), (GI.shear(200), 40),
                                         (GI.yield_pulse(100), 40), (GI.vacuum(200), 40), (GI.bshock(100), 20),
                                         (GI.tensile(), 20), (GI.alimpact(100), 40), (GI.impact3d(16), 8),
-                                        (GI.impact3d(16, af=True), 8)],
+                                        (GI.impact3d(16, af=True), 8), (GI.substrate(), 30), (GI.crater(), 20)],
                          ids=lambda x: getattr(x, "name", str(x)) + ("_af" if getattr(x, "params", {}).get("c_act") else ""))
 def test_mixed_runs_match_oracle(E, case, steps):
     """The mixed form (FP32 fluxes and sources, FP64 state) against the FP64
@@ -274,11 +276,11 @@ def test_mixed_runs_match_oracle(E, case, steps):
     The fluidization ratio and vibration velocity are threshold quantities
     (seeded when a pressure rise crosses P_ACT) and are left out."""
     g = E.from_case(case, form=E.MIXED)
-    s, t = g.run(case.cfl, case.t_end, steps)
+    s, t = E.run_case(g, case, steps)
     got = g.fields()
     g.close()
     o = EO.from_case(case)
-    so, to = o.run(case.cfl, case.t_end, steps)
+    so, to = EO.run_case(o, case, steps)
     ref = o.fields()
     o.close()
     assert s == so and abs(t - to) <= 1e-5 * abs(to)
@@ -321,3 +323,47 @@ def test_mixed_gates(E):
     g = E.from_case(case, form=E.MIXED)
     g.run(case.cfl, case.t_end)
     assert np.abs(g.read("mw") / g.read("r")).max() < 5.0
+
+
+def test_gpu_gate_substrate(E):
+    """hydro_cpu.cpp:847-859 (a CI gate of the reference): the gravity-loaded
+    substrate under the well-balanced reconstruction settles (max |v| < 5 m/s
+    over the basalt cells at t = 200 s) with no rarefaction (basalt cells
+    stay above 97 % of their initial count), the deep floor pinned to the
+    reference after every step as the reference's driver does."""
+    case = GI.substrate()
+    g = E.from_case(case)
+    r0, p0 = g.reference()
+    assert np.array_equal(r0, case.fields["r"])
+    nb0 = int((case.fields["r"] > 1350.0).sum())
+    s, t = E.run_case(g, case, 1 << 30)
+    f = g.read_many(["r", "mu", "mv", "mw"])
+    dense = f["r"] > 1350.0
+    v = np.sqrt(f["mu"] ** 2 + f["mv"] ** 2 + f["mw"] ** 2)[dense] / f["r"][dense]
+    assert t == case.t_end and s > 1000
+    assert v.max() < 5.0 and dense.sum() > 0.97 * nb0
+    g.close()
+
+
+def test_reference_state_calls(E):
+    """eu_set_ref freezes density and pressure; eu_clear_ref returns to the
+    plain sweep and plain gravity (the same state as a grid that never had a
+    reference); reading a reference that is not set is an error."""
+    from deorbit_gb300 import sph
+    case = GI.crater(cppr=3)
+    a = E.from_case(case)
+    r0, p0 = a.reference()
+    assert np.array_equal(r0, case.fields["r"]) and np.all(p0 >= 0)
+    a.clear_ref()
+    with pytest.raises(sph.SphError):
+        a.reference()
+    b = E.Grid(*case.shape, case.dx, material=case.material, params=case.params)
+    b.write_many(case.fields)
+    b.write_many(case.post_ref)
+    a.run(case.cfl, case.t_end, 3)
+    b.run(case.cfl, case.t_end, 3)
+    fa, fb = a.fields(), b.fields()
+    for k in FIELDS:
+        assert np.array_equal(fa[k], fb[k]), k
+    a.close()
+    b.close()
