@@ -93,6 +93,7 @@ struct Counting : dsph::EngineBase {
     void compute_forces() override { unused(__func__); }
     void synchronize() override {}
     int64_t impact_n(int b) override { return imps.at(b).n; }
+    int64_t impact_steps(int b) override { return imps.at(b).steps; }
     void read_field(int, const char*, double*) override { unused(__func__); }
     void write_field(int, const char*, const double*) override { unused(__func__); }
     void read_fields(int b, int nf, const char* const*, double* const* outs) override {
