@@ -805,7 +805,6 @@ public:
         const int64_t shape = N_ * 65536 + (int64_t)imp_.size();
         cudaGraphExec_t& ge = graph_exec_[kind][p];
         if (ge && graph_key_[kind][p] == layout_epoch_ && graph_n_[kind][p] == shape) return ge;
-        if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
         const int nimp = (int)imp_.size();
         const int64_t l0 = launches_;
         const uint64_t epoch0 = layout_epoch_;
@@ -817,7 +816,21 @@ public:
         }
         cudaGraph_t g = nullptr;
         DSPH_CUDA(cudaStreamEndCapture(st_, &g));
-        DSPH_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        // A new particle count or impact table usually changes only kernel
+        // parameters and grid sizes: update the executable graph in place
+        // (cheaper than a fresh instantiation) and instantiate only when the
+        // topology changed.
+        bool updated = false;
+        if (ge) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(ge, g, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(ge);
+                ge = nullptr;
+            }
+        }
+        if (!updated) DSPH_CUDA(cudaGraphInstantiate(&ge, g, 0));
         cudaGraphDestroy(g);
         graph_launches_[kind][p] = launches_ - l0;
         launches_ = l0;

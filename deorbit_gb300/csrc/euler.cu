@@ -209,6 +209,7 @@ void to_params(deu::P& p, const eu_params& e) {
     p.axisym = e.axisym != 0; p.rock = e.rock != 0; p.af_reg = e.af_reg != 0; p.af_prel = e.af_prel != 0;
     p.af_seeddp = e.af_seeddp != 0;
     p.void_amb = e.void_amb;
+    p.void_cons = e.void_cons != 0;
 }
 
 // Weakest-flaw activation strain of grow_damage (hydro_cpu.cpp:254), formed
@@ -553,7 +554,8 @@ int eu_run(eu_grid* h, double cfl, double t_end, int64_t max_steps, int64_t* ste
             g->launches = l0;
             g->graph_valid = true;
         }
-        const int64_t per_step = 16 + ((g->p.c_act > 0 && g->p.tdec > 0) ? 1 : 0);
+        const int64_t per_step = 16 + ((g->p.c_act > 0 && g->p.tdec > 0) ? 1 : 0) +
+                                 ((g->p.void_cons && g->p.ref_r0 && g->p.rho_cfl > 0) ? 3 : 0);
         const int64_t limit = c0.max_steps;  // absolute step count, -1 = none
         deu::Ctl c = c0;
         // replay in chunks; steps past the end are no-ops (inactive control)

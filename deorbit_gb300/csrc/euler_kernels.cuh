@@ -48,6 +48,7 @@ struct P {
     const double* ref_r0;
     const double* ref_p0;
     double void_amb;  // VOID_AMB: void cells reset to this density instead of the reference's
+    int32_t void_cons, pad_vc;  // VOID_CONS: the reset moves the excess mass to a neighbour first
 };
 
 template <class R> __device__ __forceinline__ R dmax2(R a, R b) { return a < b ? b : a; }  // std::max
@@ -732,6 +733,7 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
 // hydro_cpu.cpp:272-290 (not the conservative transfer).
 static __device__ __forceinline__ void void_cell(const P& p, const Fields& g, int64_t c) {
     if (!(p.rho_cfl > 0 && g.q[F_R][c] < p.rho_cfl)) return;
+    if (p.void_cons && p.ref_r0) return;  // the serial conservative pass (k_void_cons) does it
     g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
     if (p.ref_r0) {
         g.q[F_R][c] = (p.void_amb > 0 ? p.void_amb : p.ref_r0[c]);
@@ -739,6 +741,76 @@ static __device__ __forceinline__ void void_cell(const P& p, const Fields& g, in
         g.q[F_SXX][c] = g.q[F_SYY][c] = g.q[F_SZZ][c] = g.q[F_SXY][c] = g.q[F_SXZ][c] = g.q[F_SYZ][c] = 0;
         g.q[F_RC][c] = 0;
     }
+}
+
+// The conservative void reset (VOID_CONS, hydro_cpu.cpp:272-290): every
+// near-void cell, in index order, zeroes its momentum, moves its excess over
+// the ambient density to the densest face neighbour above RHO_CFL (candidates
+// x-, x+, z-, z+, then y-, y+ when ny > 1; first of equals; volume-weighted in
+// cylindrical geometry) and is reset.  The choice of neighbour depends on the
+// transfers of the cells before it, so one thread walks the cells in order;
+// the block loads each 1024-cell chunk's densities in parallel first.  A cell
+// below RHO_CFL is never a transfer target (targets exceed RHO_CFL and only
+// grow), so whether a cell is void and its own density are unchanged from the
+// chunk's load until its turn.
+static __global__ void __launch_bounds__(1024) k_void_cons(P p, Fields g, const Ctl* ctl) {
+    if (!ctl->active) return;
+    __shared__ double rs[1024];
+    double* r = g.q[F_R];
+    const int64_t plane = (int64_t)p.ny * p.nz;
+    for (int64_t base = 0; base < p.n; base += 1024) {
+        const int64_t c0 = base + threadIdx.x;
+        rs[threadIdx.x] = c0 < p.n ? r[c0] : 1e300;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int m = (int)(p.n - base < 1024 ? p.n - base : 1024);
+            for (int t = 0; t < m; t++) {
+                if (!(rs[t] < p.rho_cfl)) continue;
+                const int64_t c = base + t;
+                g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
+                const double amb = (p.void_amb > 0 ? p.void_amb : 0.27), exc = rs[t] - amb;
+                if (exc > 0) {
+                    const int i = (int)(c / plane), j = (int)((c / p.nz) % p.ny), k = (int)(c % p.nz);
+                    int64_t nb = -1;
+                    double rbest = p.rho_cfl;
+                    const int cand[6][3] = {{i - 1, j, k}, {i + 1, j, k}, {i, j, k - 1},
+                                            {i, j, k + 1}, {i, j - 1, k}, {i, j + 1, k}};
+                    const int nc = p.ny > 1 ? 6 : 4;
+                    for (int q = 0; q < nc; q++) {
+                        const int ii = cand[q][0], jj = cand[q][1], kk = cand[q][2];
+                        if (ii < 0 || ii >= p.nx || jj < 0 || jj >= p.ny || kk < 0 || kk >= p.nz) continue;
+                        const int64_t cc = ((int64_t)ii * p.ny + jj) * p.nz + kk;
+                        if (r[cc] > rbest) {
+                            rbest = r[cc];
+                            nb = cc;
+                        }
+                    }
+                    if (nb >= 0) {
+                        double w = 1.0;
+                        if (p.axisym) {
+                            const int inb = (int)(nb / plane);
+                            w = (i + 0.5) / (inb + 0.5);
+                        }
+                        r[nb] += exc * w;
+                    }
+                }
+                r[c] = (p.void_amb > 0 ? p.void_amb : p.ref_r0[c]);
+                g.q[F_E][c] = 0;
+                g.q[F_SXX][c] = g.q[F_SYY][c] = g.q[F_SZZ][c] = g.q[F_SXY][c] = g.q[F_SXZ][c] = g.q[F_SYZ][c] = 0;
+                g.q[F_RC][c] = 0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// The predictor's radial return when the conservative void pass runs between
+// the update and the return.
+template <class R>
+static __global__ void k_yield_stage(P p, Fields g1, const double* af, const Ctl* ctl) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    vonmises_cell<R>(p, g1, af, c, false);
 }
 
 // set_ref (hydro_cpu.cpp:259-261): density and pressure frozen as the reference.
@@ -759,7 +831,7 @@ static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
 #pragma unroll
     for (int q = 0; q < ND; q++) g1.q[rk_field(q)][c] = g.q[rk_field(q)][c] + dt * d.q[q][c];
     void_cell(p, g1, c);
-    vonmises_cell<R>(p, g1, g.q[F_AF], c, false);
+    if (!(p.void_cons && p.ref_r0)) vonmises_cell<R>(p, g1, g.q[F_AF], c, false);  // else after k_void_cons
 }
 
 // Corrector and the end of the step (hydro_cpu.cpp:419-424): trapezoidal
@@ -837,10 +909,15 @@ inline void enqueue_maxspeed_t(const P& p, const Fields& g, Ctl* ctl, cudaStream
 template <class R>
 inline void enqueue_predict_t(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st) {
     k_predict<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, g1, d, ctl);
+    if (p.void_cons && p.ref_r0 && p.rho_cfl > 0) {  // void_cells(g1) in order, then vonmises(g1, false)
+        k_void_cons<<<1, 1024, 0, st>>>(p, g1, ctl);
+        k_yield_stage<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g1, g.q[F_AF], ctl);
+    }
 }
 template <class R>
 inline void enqueue_correct_t(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st) {
     k_correct<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, g1, d, ctl);
+    if (p.void_cons && p.ref_r0 && p.rho_cfl > 0) k_void_cons<<<1, 1024, 0, st>>>(p, g, ctl);  // void_cells(g) last
 }
 
 // The FP32 instantiations live in euler_mixed.cu (compiled with fused

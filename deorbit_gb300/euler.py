@@ -28,7 +28,7 @@ class Params(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
                                           "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
-        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp reserved".split()] + [("void_amb", C.c_double)]
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp reserved".split()] + [("void_amb", C.c_double), ("void_cons", C.c_int32), ("reserved2", C.c_int32)]
 
 
 _D = C.POINTER(C.c_double)

@@ -229,14 +229,17 @@ def substrate(N=60):
                 {"r": r, "E": np.zeros(N * N)}, 0.4, 200.0, set_ref=True, pin_floor=2)
 
 
-def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0, gz=3.71, t_end=None):
+def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0, gz=3.71, t_end=None,
+           void_cons=0, void_amb=0.0):
     """hydro_cpu.cpp:557-597: the axisymmetric vertical impact crater -- a
     basalt sphere of radius a on the axis, tangent to the surface, at U m/s
     into a lithostatic basalt half-space under gravity, with the frozen
     pre-impact column as the well-balanced reference, ROCK yield, near-void
     and vacuum-aware faces, and (tdec > 0) shock-activated fluidization with
-    the crater defaults (acoustic seeding, overburden relief).  The driver's
-    far-field floor pin and radial sponge are not part of the case."""
+    the crater defaults (acoustic seeding, overburden relief); void_cons /
+    void_amb select the conservative and ambient void resets (its arguments 17
+    and 14).  The driver's far-field floor pin and radial sponge are not part
+    of the case."""
     rho0, Abulk = 2700.0, 2.67e10
     dx = a / cppr
     Nr, Nz = int(Rfac * a / dx + 0.5), int(Zfac * a / dx + 0.5)
@@ -251,9 +254,12 @@ def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0,
     prm = {"axisym": 1, "rho_cfl": 100.0, "rho_vac": 100.0, "rock": 1, "gz": gz}
     if tdec > 0:
         prm.update(tdec=tdec, eta_af=eta_af, c_act=0.5, p_coh=1.0e6, p_act=1.0e8, af_seeddp=1, af_prel=1)
+    if void_cons or void_amb:
+        prm.update(void_cons=int(void_cons), void_amb=float(void_amb))
     if t_end is None:
         t_end = 2.0 * math.sqrt((Rfac * a) / gz)
-    return Case(f"crater_{cppr}", (Nr, 1, Nz), dx, ic.basalt(), prm,
+    name = f"crater_{cppr}" + ("_vc" if void_cons else "") + ("_amb" if void_amb else "")
+    return Case(name, (Nr, 1, Nz), dx, ic.basalt(), prm,
                 {"r": r.reshape(-1), "E": np.zeros(Nr * Nz)}, 0.4, t_end, set_ref=True, post_ref=post)
 
 

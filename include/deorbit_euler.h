@@ -17,10 +17,8 @@
  * bit; Tillotson grids differ only where the device's exp / pow round
  * differently from the host library's.
  *
- * Not provided (the reference's options for them must stay off): the
- * conservative void-cell transfer (VOID_CONS: excess mass moved to the densest
- * neighbour cell by cell in index order, a serial dependency) and the implicit
- * viscous solve (VISC_IMP).  eu_set_params has no field for them.
+ * Not provided (the reference's option for it must stay off): the implicit
+ * viscous solve (VISC_IMP).  eu_set_params has no field for it.
  *
  * Fields are host arrays of nx*ny*nz doubles, cell (i,j,k) at
  * (i*ny + j)*nz + k, exactly the reference's layout.  Names: r mu mv mw E Sxx
@@ -65,6 +63,9 @@ typedef struct eu_params {
     int32_t reserved;
     double void_amb;  /* VOID_AMB: with a reference state, void cells reset to this
                          density instead of the reference's (0 = the reference's) */
+    int32_t void_cons;/* VOID_CONS: with a reference state, a void cell's excess mass
+                         first moves to its densest neighbour (serial pass, index order) */
+    int32_t reserved2;
 } eu_params;
 
 typedef struct eu_grid eu_grid;

@@ -30,10 +30,10 @@ class Params(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
                                           "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
-        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()] + [("void_amb", C.c_double)]
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()] + [("void_amb", C.c_double), ("void_cons", C.c_int32), ("pad2_", C.c_int32)]
 
     def as_dict(self):
-        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad_"}
+        return {n: getattr(self, n) for n, _ in self._fields_ if not n.startswith("pad")}
 
 
 _D = C.POINTER(C.c_double)

@@ -535,14 +535,43 @@ double eorc_maxspeed(const eorc_grid* g) {
 
 /* Near-void cells lose their momentum and, with a reference state, are reset
  * to the reference density (or the ambient VOID_AMB) with no energy, stress or
- * tracer, hydro_cpu.cpp:272-290 (not the conservative transfer). */
+ * tracer; with VOID_CONS the excess over the ambient density first moves to
+ * the densest face neighbour above RHO_CFL (volume-weighted in cylindrical
+ * geometry), cell by cell in index order, hydro_cpu.cpp:272-290. */
 static void void_cells(eorc_grid* g) {
     if (g->p.rho_cfl <= 0) return;
+    double* r = g->f[F_R];
     for (int c = 0; c < g->n; c++)
-        if (g->f[F_R][c] < g->p.rho_cfl) {
+        if (r[c] < g->p.rho_cfl) {
             g->f[F_MU][c] = g->f[F_MV][c] = g->f[F_MW][c] = 0;
             if (g->ref_r0) {
-                g->f[F_R][c] = (g->p.void_amb > 0 ? g->p.void_amb : g->ref_r0[c]);
+                if (g->p.void_cons) {
+                    double amb = (g->p.void_amb > 0 ? g->p.void_amb : 0.27), exc = r[c] - amb;
+                    if (exc > 0) {
+                        int i = c / (g->ny * g->nz), j = (c / g->nz) % g->ny, k = c % g->nz, nb = -1;
+                        double rbest = g->p.rho_cfl;
+                        int ci[6][3] = {{i - 1, j, k}, {i + 1, j, k}, {i, j, k - 1}, {i, j, k + 1}, {i, j - 1, k}, {i, j + 1, k}};
+                        int ncand = g->ny > 1 ? 6 : 4;
+                        for (int q = 0; q < ncand; q++) {
+                            int ii = ci[q][0], jj = ci[q][1], kk = ci[q][2];
+                            if (ii < 0 || ii >= g->nx || jj < 0 || jj >= g->ny || kk < 0 || kk >= g->nz) continue;
+                            int cc = idx(g, ii, jj, kk);
+                            if (r[cc] > rbest) {
+                                rbest = r[cc];
+                                nb = cc;
+                            }
+                        }
+                        if (nb >= 0) {
+                            double w = 1.0;
+                            if (g->p.axisym) {
+                                int inb = nb / (g->ny * g->nz);
+                                w = (i + 0.5) / (inb + 0.5);
+                            }
+                            r[nb] += exc * w;
+                        }
+                    }
+                }
+                r[c] = (g->p.void_amb > 0 ? g->p.void_amb : g->ref_r0[c]);
                 g->f[F_E][c] = 0;
                 g->f[F_SXX][c] = g->f[F_SYY][c] = g->f[F_SZZ][c] = g->f[F_SXY][c] = g->f[F_SXZ][c] = g->f[F_SYZ][c] = 0;
                 g->f[F_RC][c] = 0;

@@ -9,13 +9,12 @@
  * pressure-dependent ROCK yield (229-252), tensile damage growth (253-258),
  * the frozen hydrostatic reference of set_ref (259-261) with the well-balanced
  * z-sweep and gravity source against it (75-88, 114-119, 139-143), the
- * near-void reset to that reference or to an ambient density (272-290; not the
- * conservative transfer), acoustic fluidization activation (390-410), the CFL
+ * near-void reset to that reference or to an ambient density, optionally
+ * conservative (272-290), acoustic fluidization activation (390-410), the CFL
  * speed (378-380) and the two-stage Runge-Kutta step (411-425).  Every
  * expression keeps the reference's floating-point operation order; the
- * library is built with -ffp-contract=off.  The conservative void transfer
- * (VOID_CONS) and the implicit viscous solve (VISC_IMP) are not restated (the
- * CUDA grid solver does not provide them either).
+ * library is built with -ffp-contract=off.  The implicit viscous solve
+ * (VISC_IMP) is not restated.
  *
  * The oracle is test infrastructure: only tests/, the smoke check and the
  * bench's CPU legs call it, never the product path.
@@ -50,6 +49,8 @@ typedef struct {
     int af_seeddp;    /* seed vibrations from the acoustic velocity of the jump */
     int pad_;
     double void_amb;  /* void cells reset to this ambient density instead of the reference's */
+    int void_cons;    /* conservative reset: excess mass to the densest neighbour first */
+    int pad2_;
 } eorc_params;
 
 void eorc_params_default(eorc_params* p);

@@ -49,7 +49,7 @@ void load(const RefGrid* R) {
     RHO_CFL = p.rho_cfl; DAMP = p.damp; RHO_VAC = p.rho_vac; AXISYM = p.axisym != 0; ROCK = p.rock != 0;
     Y_I0 = p.y_i0; MU_I = p.mu_i; MU_D = p.mu_d; Y_D0 = p.y_d0; Y_M = p.y_m; Y_BINGHAM = p.y_bingham;
     VISC_IMP = false;
-    VOID_CONS = false;
+    VOID_CONS = p.void_cons != 0;
     VOID_AMB = p.void_amb;
     REF_R0 = R->ref_r0;
     REF_P0 = R->ref_p0;
@@ -105,6 +105,7 @@ eorc_params capture_defaults() {
     p.y_i0 = Y_I0; p.mu_i = MU_I; p.mu_d = MU_D; p.y_d0 = Y_D0; p.y_m = Y_M; p.y_bingham = Y_BINGHAM;
     p.af_reg = AF_REG; p.c_reg = C_REG; p.af_sat = AF_SAT; p.af_prel = AF_PREL; p.af_seeddp = AF_SEEDDP;
     p.void_amb = VOID_AMB;
+    p.void_cons = VOID_CONS;
     return p;
 }
 const eorc_params kDefaults = capture_defaults();

@@ -36,7 +36,8 @@ RUNS = [(GI.sod(), 60), (GI.tracer(), 40), (GI.sedov(12), 8), (GI.sedov_axi(16, 
         (GI.freefall(), 20), (GI.atmos(50), 10), (GI.tensile(), 20), (GI.alimpact(100), 30),
         (GI.surface(), 20), (GI.impact3d(12), 6), (GI.impact3d(12, af=True), 6),
         (GI.substrate(), 30), (GI.crater(), 20), (GI.crater(tdec=2.0, eta_af=1e8), 20),
-        (GI.crater(cppr=3, U=6000.0), 15)]
+        (GI.crater(cppr=3, U=6000.0), 15), (GI.crater(cppr=3, U=6000.0, void_cons=1), 25),
+        (GI.crater(cppr=3, U=6000.0, void_amb=0.27), 25)]
 
 
 def perturbed_state(seed, shape, strength=True):

@@ -68,7 +68,9 @@ def test_ideal_gas_runs_bit_exact(E, case, steps):
                                         (GI.bshock(100), 20), (GI.tensile(), 20), (GI.alimpact(100), 40),
                                         (GI.surface(), 20), (GI.impact3d(16), 8), (GI.impact3d(16, af=True), 8),
                                         (GI.substrate(), 30), (GI.crater(), 20),
-                                        (GI.crater(tdec=2.0, eta_af=1e8), 20)],
+                                        (GI.crater(tdec=2.0, eta_af=1e8), 20),
+                                        (GI.crater(cppr=3, U=6000.0, void_cons=1), 25),
+                                        (GI.crater(cppr=3, U=6000.0, void_amb=0.27), 25)],
                          ids=lambda x: getattr(x, "name", str(x)) + ("_af" if getattr(x, "params", {}).get("c_act") else ""))
 def test_tillotson_runs_match_oracle(E, case, steps):
     (s, t, got, _), (so, to, ref) = _pair(E, case, steps)
@@ -267,7 +269,7 @@ def _group_err(got, ref, names):
                                         (GI.sedov_axi(16, 32), 15), (GI.atmos(50), 10), (GI.shear(200), 40),
                                         (GI.yield_pulse(100), 40), (GI.vacuum(200), 40), (GI.bshock(100), 20),
                                         (GI.tensile(), 20), (GI.alimpact(100), 40), (GI.impact3d(16), 8),
-                                        (GI.impact3d(16, af=True), 8), (GI.substrate(), 30), (GI.crater(), 20)],
+                                        (GI.impact3d(16, af=True), 8), (GI.crater(), 20)],
                          ids=lambda x: getattr(x, "name", str(x)) + ("_af" if getattr(x, "params", {}).get("c_act") else ""))
 def test_mixed_runs_match_oracle(E, case, steps):
     """The mixed form (FP32 fluxes and sources, FP64 state) against the FP64
@@ -367,3 +369,21 @@ def test_reference_state_calls(E):
         assert np.array_equal(fa[k], fb[k]), k
     a.close()
     b.close()
+
+
+def test_mixed_substrate_stays_at_rest(E):
+    """The well-balanced substrate in the mixed form: the FP64 oracle keeps it
+    at rest to 1e-13 m/s, so field-relative errors are meaningless there; the
+    mixed form must keep it at rest to well below the gate's 5 m/s (1e-2 m/s
+    after 30 steps) with densities within 1e-6 of the oracle's."""
+    case = GI.substrate()
+    g = E.from_case(case, form=E.MIXED)
+    E.run_case(g, case, 30)
+    f = g.read_many(["r", "mu", "mv", "mw"])
+    g.close()
+    o = EO.from_case(case)
+    EO.run_case(o, case, 30)
+    v = np.sqrt(f["mu"] ** 2 + f["mv"] ** 2 + f["mw"] ** 2) / f["r"]
+    assert v.max() < 1e-2
+    assert rel_l2(f["r"], o.field("r")) <= 1e-6
+    o.close()
