@@ -314,6 +314,7 @@ public:
         bool multi = false;
         std::vector<int64_t> flaw_ptr;
         std::vector<double> flaw_eps;
+        bool flaws_on_device = false;  // its segment of the device flaw pool is current
         double t = 0, dt_last = 0;
         int64_t steps = 0;
         int64_t step_limit = 0;
@@ -472,6 +473,8 @@ public:
 
     int64_t impact_seed_flaws_multi(int b, double dx, uint32_t seed) override {
         ImpactH& h = imp(b);
+        if (h.flaws_on_device) flaw_live_ -= (int64_t)h.flaw_eps.size();  // the old segment is dead
+        h.flaws_on_device = false;
         std::vector<double> eps(h.n);
         h.flaw_ptr.assign(h.n + 1, 0);
         double* fe = nullptr;
@@ -488,7 +491,7 @@ public:
             pull_table();
             fill_params(tab_[b], h);
             push_table();
-            upload_flaws();
+            sync_flaws();
         }
         return nf;
     }
@@ -581,6 +584,7 @@ public:
         ImpactH& h = imp(b);
         bool was_committed = h.committed;
         h.alive = false;
+        if (h.flaws_on_device) flaw_live_ -= (int64_t)h.flaw_eps.size();  // its pool segment is dead
         if (was_committed) {
             pull_table();
             tab_[b].alive = 0;
@@ -593,7 +597,6 @@ public:
         if (was_committed) {
             assign_cell_bases();
             push_table();
-            if (any_multi()) upload_flaws();
         }
     }
 
@@ -1186,16 +1189,17 @@ public:
     int64_t debug_flaws(int b, int64_t* ptr, double* eps, int64_t cap) override {
         ImpactH& h = imp(b);
         commit();
-        if (!(h.multi && flaw_ptr_d_)) {
+        if (!(h.multi && h.flaws_on_device) || h.n == 0) {
             for (int64_t l = 0; l <= h.n; l++) ptr[l] = 0;
             return 0;
         }
-        std::vector<int64_t> dptr(h.n + 1);
-        DSPH_CUDA(cudaMemcpyAsync(dptr.data(), flaw_ptr_d_ + h.gid_base, sizeof(int64_t) * (h.n + 1),
-                                  cudaMemcpyDeviceToHost, st_));
+        std::vector<int64_t> db(h.n), de(h.n);
+        DSPH_CUDA(cudaMemcpyAsync(db.data(), flaw_beg_d_ + h.gid_base, sizeof(int64_t) * h.n, cudaMemcpyDeviceToHost, st_));
+        DSPH_CUDA(cudaMemcpyAsync(de.data(), flaw_end_d_ + h.gid_base, sizeof(int64_t) * h.n, cudaMemcpyDeviceToHost, st_));
         DSPH_CUDA(cudaStreamSynchronize(st_));
-        const int64_t base = dptr[0], total = dptr[h.n] - base;
-        for (int64_t l = 0; l <= h.n; l++) ptr[l] = dptr[l] - base;
+        const int64_t base = db[0], total = de[h.n - 1] - base;
+        for (int64_t l = 0; l < h.n; l++) ptr[l] = db[l] - base;
+        ptr[h.n] = total;
         if (eps && total > cap) throw SphError(SPH_ERR_CAPACITY, "flaw buffer too small");
         if (eps && total > 0) {
             std::vector<R> e(total);
@@ -1517,7 +1521,8 @@ public:
         v.flags = flags_d_;
         v.imps = tab_d_;
         v.mats = mats_d_;
-        v.flaw_ptr = flaw_ptr_d_;
+        v.flaw_beg = flaw_beg_d_;
+        v.flaw_end = flaw_end_d_;
         v.flaw_eps = flaw_eps_d_;
         return v;
     }
@@ -1899,7 +1904,7 @@ public:
         }
         assign_cell_bases();
         push_table();
-        if (any_multi()) upload_flaws();
+        if (any_multi()) sync_flaws();
         grid_valid_ = false;
     }
 
@@ -2004,31 +2009,76 @@ public:
         N_ += n;
     }
 
-    void upload_flaws() {
-        std::vector<int64_t> ptr(G_ + 1, 0);
-        std::vector<R> eps;
-        // per gid counts
-        std::vector<int64_t> cnt(G_, 0);
-        for (auto& h : imp_) {
-            if (!(h.used && h.alive && h.committed && h.multi)) continue;
-            for (int64_t l = 0; l < h.n; l++) cnt[h.gid_base + l] = h.flaw_ptr[l + 1] - h.flaw_ptr[l];
+    // Multi-flaw thresholds on the device: one pool of thresholds (engine
+    // precision) holding a segment per impact, and per particle id the begin /
+    // end of its thresholds in the pool.  A committed impact's segment is
+    // appended once; a removed impact's segment turns dead and stays until the
+    // pool has to grow while more than half of it is dead, when the live
+    // segments are rewritten compactly.  Admitting or retiring an impact thus
+    // moves only that impact's thresholds.
+    void sync_flaws() {
+        if (G_ > flaw_gcap_) {  // per-id ranges follow the id space
+            const int64_t nc = std::max<int64_t>(G_, (int64_t)(flaw_gcap_ * 1.5) + 1024);
+            int64_t* nb = dalloc<int64_t>(nc);
+            int64_t* ne = dalloc<int64_t>(nc);
+            if (flaw_gcap_ > 0) {
+                DSPH_CUDA(cudaMemcpyAsync(nb, flaw_beg_d_, sizeof(int64_t) * flaw_gcap_, cudaMemcpyDeviceToDevice, st_));
+                DSPH_CUDA(cudaMemcpyAsync(ne, flaw_end_d_, sizeof(int64_t) * flaw_gcap_, cudaMemcpyDeviceToDevice, st_));
+            }
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+            dfree(flaw_beg_d_);
+            dfree(flaw_end_d_);
+            flaw_beg_d_ = nb;
+            flaw_end_d_ = ne;
+            flaw_gcap_ = nc;
         }
-        for (int64_t g = 0; g < G_; g++) ptr[g + 1] = ptr[g] + cnt[g];
-        eps.resize(std::max<int64_t>(ptr[G_], 1));
-        for (auto& h : imp_) {
-            if (!(h.used && h.alive && h.committed && h.multi)) continue;
-            for (int64_t l = 0; l < h.n; l++) {
-                int64_t o = ptr[h.gid_base + l];
-                for (int64_t q = h.flaw_ptr[l]; q < h.flaw_ptr[l + 1]; q++) eps[o++] = (R)h.flaw_eps[q];
+        int64_t need = 0;
+        for (auto& h : imp_)
+            if (h.used && h.alive && h.committed && h.multi && !h.flaws_on_device) need += (int64_t)h.flaw_eps.size();
+        if (need == 0) return;
+        if (flaw_used_ + need > flaw_cap_) {
+            const bool compact = flaw_used_ - flaw_live_ > flaw_live_;  // more than half dead
+            const int64_t keep = compact ? flaw_live_ : flaw_used_;
+            const int64_t nc = std::max<int64_t>(keep + need, (int64_t)((keep + need) * 1.5) + 4096);
+            R* np = dalloc<R>(nc);
+            if (!compact && flaw_used_ > 0)
+                DSPH_CUDA(cudaMemcpyAsync(np, flaw_eps_d_, sizeof(R) * flaw_used_, cudaMemcpyDeviceToDevice, st_));
+            DSPH_CUDA(cudaStreamSynchronize(st_));
+            dfree(flaw_eps_d_);
+            flaw_eps_d_ = np;
+            flaw_cap_ = nc;
+            if (compact) {  // every live segment is written again below
+                flaw_used_ = 0;
+                flaw_live_ = 0;
+                for (auto& h : imp_) h.flaws_on_device = false;
             }
         }
-        dfree(flaw_ptr_d_);
-        dfree(flaw_eps_d_);
-        flaw_ptr_d_ = dalloc<int64_t>(ptr.size());
-        flaw_eps_d_ = dalloc<R>(eps.size());
-        DSPH_CUDA(cudaMemcpyAsync(flaw_ptr_d_, ptr.data(), sizeof(int64_t) * ptr.size(), cudaMemcpyHostToDevice, st_));
-        DSPH_CUDA(cudaMemcpyAsync(flaw_eps_d_, eps.data(), sizeof(R) * eps.size(), cudaMemcpyHostToDevice, st_));
-        DSPH_CUDA(cudaStreamSynchronize(st_));
+        std::vector<R> seg;
+        std::vector<int64_t> beg, end;
+        for (auto& h : imp_) {
+            if (!(h.used && h.alive && h.committed && h.multi) || h.flaws_on_device) continue;
+            const int64_t nf = (int64_t)h.flaw_eps.size(), off = flaw_used_;
+            seg.resize(std::max<int64_t>(nf, 1));
+            for (int64_t q = 0; q < nf; q++) seg[q] = (R)h.flaw_eps[q];
+            beg.resize(h.n);
+            end.resize(h.n);
+            for (int64_t l = 0; l < h.n; l++) {
+                beg[l] = off + h.flaw_ptr[l];
+                end[l] = off + h.flaw_ptr[l + 1];
+            }
+            if (nf > 0)
+                DSPH_CUDA(cudaMemcpyAsync(flaw_eps_d_ + off, seg.data(), sizeof(R) * nf, cudaMemcpyHostToDevice, st_));
+            if (h.n > 0) {
+                DSPH_CUDA(cudaMemcpyAsync(flaw_beg_d_ + h.gid_base, beg.data(), sizeof(int64_t) * h.n,
+                                          cudaMemcpyHostToDevice, st_));
+                DSPH_CUDA(cudaMemcpyAsync(flaw_end_d_ + h.gid_base, end.data(), sizeof(int64_t) * h.n,
+                                          cudaMemcpyHostToDevice, st_));
+            }
+            DSPH_CUDA(cudaStreamSynchronize(st_));  // the staging vectors are reused
+            flaw_used_ += nf;
+            flaw_live_ += nf;
+            h.flaws_on_device = true;
+        }
     }
 
     void set_masks(const std::vector<int32_t>& mask, const std::vector<double>* dt,
@@ -2346,8 +2396,11 @@ public:
     int64_t stage_cap_ = 0;
     char* mask_buf_ = nullptr;
     size_t mask_buf_bytes_ = 0;
-    int64_t* flaw_ptr_d_ = nullptr;
-    R* flaw_eps_d_ = nullptr;
+    int64_t* flaw_beg_d_ = nullptr;  // per particle id: its thresholds in the pool
+    int64_t* flaw_end_d_ = nullptr;
+    int64_t flaw_gcap_ = 0;
+    R* flaw_eps_d_ = nullptr;        // the pool of thresholds
+    int64_t flaw_cap_ = 0, flaw_used_ = 0, flaw_live_ = 0;
     int block_ = 128;
     double cell_factor_ = 1.0;
     double cell_factor_z_ = 1.0;  // z cell height relative to the x / y width

@@ -117,7 +117,8 @@ struct View {
     int32_t* flags;     // [0] list overflow max, [1] any impact still in a density round
     ImpactD* imps;
     const MatT<R>* mats;
-    const int64_t* flaw_ptr;   // by gid, multi-flaw extension
+    const int64_t* flaw_beg;   // by gid: first / past-last threshold in flaw_eps (multi-flaw extension)
+    const int64_t* flaw_end;
     const R* flaw_eps;
 };
 
@@ -2079,7 +2080,7 @@ static __global__ void k_damage(View<R> v) {
         v.D[k] = rmin(R(1), d13 * d13 * d13);
     } else {
         int64_t g = v.gid[k];
-        int64_t b = v.flaw_ptr[g], e = v.flaw_ptr[g + 1];
+        int64_t b = v.flaw_beg[g], e = v.flaw_end[g];
         if (e <= b) return;
         int64_t nact = 0;
         for (int64_t q = b; q < e; q++)

@@ -136,3 +136,43 @@ def test_remove_in_the_middle(cuda_lib):
         alone.close()
         for k in NAMES:
             assert np.array_equal(g[k], ref[k]), k
+
+
+def test_flaw_pool_through_admissions_and_retirements(cuda_lib):
+    """Multi-flaw thresholds live in one device pool with a segment per impact:
+    impacts retired and admitted over several cycles (reusing particle ids and
+    growing, then compacting, the pool) keep exactly the thresholds and the
+    damage they have alone."""
+    from deorbit_gb300 import sph
+    scs = ic.batch_impacts(count=9, lo=1200, hi=2600, seed=7)
+    ctx = sph.Context(sph.MIXED)
+    mids = {}
+    live = {}
+    for s in scs[:3]:
+        live[ic.to_context(ctx, s, material_ids=mids)] = s
+    ctx.init()
+    ctx.run(2)
+    for cyc, s in enumerate(scs[3:]):
+        ctx.remove(sorted(live)[cyc % len(live)])
+        live.pop(sorted(live)[cyc % len(live)])
+        b = ic.to_context(ctx, s, material_ids=mids)
+        live[b] = s
+        ctx.init()
+        ctx.run(2)
+    ctx.run(2)
+    got = {b: (ctx.flaws(b), read_all(ctx, b, NAMES + ["D"])) for b in live}
+    ctx.close()
+    for b, s in live.items():
+        alone = sph.Context(sph.MIXED)
+        a = ic.to_context(alone, s)
+        alone.init()
+        ptr, eps = alone.flaws(a)
+        assert len(eps) > 0
+        assert np.array_equal(got[b][0][0], ptr) and np.array_equal(got[b][0][1], eps), b
+        if s is scs[-1]:  # admitted last: two rounds of two steps in the mix
+            alone.run(2)
+            alone.run(2)
+            ref = read_all(alone, a, NAMES + ["D"])
+            for k in ref:
+                assert np.array_equal(got[b][1][k], ref[k]), k
+        alone.close()
