@@ -551,6 +551,44 @@ def euler_section(device, steps, warmup, N=256, cpu_n=64, acc_n=32, form=0, cpu=
     return out
 
 
+def crater_visc_section(device, steps=20, warmup=3, cpu_steps=3):
+    """The reference driver's crater mode at its default size (hydro_cpu.cpp:
+    557-597: a = 500 m, U = 12 km/s, 5 cells per radius, a 30 x 22 radii
+    cylindrical domain) with shock-activated fluidization and the implicit
+    fluidization viscosity (its argument 16; eta = 1e9 Pa s): device time per
+    step of both forms (steps issued directly: the viscosity's cooperative
+    launch is not replayed from a graph), conjugate-gradient iterations per
+    step, and the serial CPU oracle on the same grid."""
+    from deorbit_gb300 import euler as E, grid_ic as GI
+    from oracle import euler as EO
+
+    case = GI.crater(cppr=5, Rfac=30.0, Zfac=22.0, tdec=2.0, eta_af=1e9, visc_imp=1)
+    out = {"workload": f"axisymmetric crater, {case.shape[0]} x {case.shape[2]} cells of {case.dx:.0f} m, "
+                       "12 km/s, fluidization with the implicit viscosity (eta 1e9 Pa s)", "cells": case.n}
+    for form, name in ((E.FP64, "fp64"), (E.MIXED, "mixed")):
+        g = E.from_case(case, device=device, form=form)
+        g.run(case.cfl, case.t_end, warmup)
+        g.synchronize()
+        it0, l0 = g.visc_iters(), g.launches()
+        g.event_record(0)
+        s, _ = g.run(case.cfl, case.t_end, steps)
+        g.event_record(1)
+        ms = g.event_elapsed(0, 1)
+        out[name] = {"ms_per_step": ms / max(s, 1), "value": case.n * s / (ms / 1000.0), "unit": "cell-steps/s",
+                     "cg_iters_per_step": (g.visc_iters() - it0) / max(s, 1),
+                     "gpu_launches_per_step": (g.launches() - l0) / max(s, 1)}
+        g.close()
+    o = EO.from_case(case)
+    EO.run_case(o, case, warmup)
+    t0 = time.perf_counter()
+    so, _ = EO.run_case(o, case, cpu_steps)
+    el = time.perf_counter() - t0
+    o.close()
+    out["cpu_baseline"] = {"value": case.n * so / el, "unit": "cell-steps/s", "ms_per_step": 1e3 * el / so,
+                           "cores": 1, "kind": "port", "sample": f"the same crater, {so} steps after {warmup}"}
+    return out
+
+
 def serving_section(device, rates=(4.0, 8.0, 16.0), count=200, steps=300):
     """Poisson request streams through the continuous-batching server."""
     from deorbit_gb300 import serve, sph
@@ -608,6 +646,7 @@ def main():
         out = {f: euler_section(local, args.steps, args.warmup, args.euler_n, form=i, cpu=not args.no_cpu,
                                 acc=not args.no_acc, e2e=not args.no_e2e)
                for i, f in enumerate(("fp64", "mixed"))}
+        out["crater_visc"] = crater_visc_section(local)
         print(json.dumps(out), flush=True)
         return
 
@@ -719,7 +758,8 @@ def main():
     euler = None
     if rank == 0 and world == 1 and not args.no_euler:
         euler = {"fp64": euler_section(device, args.steps, args.warmup, args.euler_n),
-                 "mixed": euler_section(device, args.steps, args.warmup, args.euler_n, form=1, cpu=False)}
+                 "mixed": euler_section(device, args.steps, args.warmup, args.euler_n, form=1, cpu=False),
+                 "crater_visc": crater_visc_section(device)}
 
     # ---- accuracy of the mixed form against FP64 (same dt sequence), and of
     # both forms against the oracle on a bounded sample

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -42,6 +43,347 @@ void set_error_message(const std::string& m);
 namespace deu {
 
 using dsph::SphError;
+
+// ---------------------------------------------------------------- implicit viscosity
+
+// implicit_visc (hydro_cpu.cpp:286-377): backward Euler for
+// d(rho v)/dt = div(eta grad v), eta = af ETA_AF in fluidized cells, each
+// velocity component solved by Jacobi-preconditioned conjugate gradients to a
+// relative residual of 1e-8, the kinetic energy removed returned as heat.
+//
+// One persistent cooperative launch does the whole update: the face
+// coefficients and the diagonal, the three solves and the heating, separated
+// by grid-wide barriers (two per CG iteration: after A p with its p.Ap sum,
+// after the x / r / z update with its r.r and r.z sums).  Every per-cell
+// expression is the reference's, in its order; the direction update
+// p = z + beta p is formed again at each stencil point of A p (the same bits
+// as the stored value), which saves a third barrier per iteration.  Sums are
+// per-block partials combined in block order by every block alike, so every
+// block holds the same scalars and the result does not depend on timing (the
+// partials alternate between two sets: a block that has passed the next
+// barrier cannot overwrite a set another block is still reading); the
+// order differs from the reference's serial sums, so the solution agrees with
+// the reference to the solver's tolerance, not bit for bit.
+
+struct Visc {
+    double *eta, *cfx, *cfy, *cfz, *dax, *dsum;
+    double* x[3];  // u1 v1 w1
+    double *rr, *zz, *pp[2], *qq;
+    double* part;  // per-block partial sums, two sets of [3][nblk] used in turn
+    int nblk;
+};
+
+// Polls of the barrier generation before a block gives up (~0.1-1 s).
+constexpr long long kBarrierPolls = 1ll << 21;
+
+// Grid-wide barrier of the persistent launch; all blocks are co-resident (the
+// launch is cooperative).  The wait is bounded: a block whose poll limit runs
+// out records the error, any block that sees the error stops waiting, and the
+// kernel returns; the host reads the flag after the step.
+static __device__ bool grid_barrier(Ctl* ctl, unsigned nblk) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &ctl->bar_gen;
+        volatile int* err = &ctl->visc_err;
+        const unsigned g0 = *gen;
+        __threadfence();
+        if (atomicAdd(&ctl->bar_count, 1u) == nblk - 1) {
+            atomicExch(&ctl->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&ctl->bar_gen, 1u);
+        } else {
+            long long polls = 0;
+            while (*gen == g0 && *err == 0) {
+                if (++polls > kBarrierPolls) {
+                    atomicExch(&ctl->visc_err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = *err == 0;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// The block's sums of K per-thread values into part[k * nblk + block].
+template <int K>
+static __device__ void block_partials(const double (&v)[K], double* part, unsigned nblk) {
+    __shared__ double sh[K][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double s = v[k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sh[k][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < K; k++) {
+            double s = sh[k][0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); w++) s += sh[k][w];
+            part[(int64_t)k * nblk + blockIdx.x] = s;
+        }
+}
+
+// Grid total of partial k, the same value in every thread of every block.
+static __device__ double grid_total(const double* part, int k, unsigned nblk) {
+    const int lane = threadIdx.x & 31;
+    double s = 0;
+    for (unsigned b = lane; b < nblk; b += 32) s += __ldcg(part + (int64_t)k * nblk + b);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
+static __device__ __forceinline__ double harmonic(double a, double b) {
+    return (a > 0 && b > 0) ? 2.0 * a * b / (a + b) : 0.0;
+}
+
+static __global__ void __launch_bounds__(256, 3) k_implicit_visc(P p, Fields g, Visc w, Ctl* ctl) {
+    if (!ctl->active) return;
+    const double dt = ctl->dt, dx = p.dx, rmin = dmax2(p.rho_cfl, 1e-12);
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const bool ax = p.axisym != 0;
+    const int64_t n = p.n, sx = (int64_t)ny * nz, sy = nz;
+    const unsigned nb = gridDim.x;
+    const int64_t c0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)nb * blockDim.x;
+    const double* r = g.q[F_R];
+    int ph = 0;  // the partial set of the next sum
+    auto sums = [&]() {
+        double* s = w.part + (int64_t)ph * 3 * nb;
+        ph ^= 1;
+        return s;
+    };
+    auto ijk = [&](int64_t c, int& i, int& j, int& k) {
+        i = (int)(c / sx);
+        j = (int)((c / nz) % ny);
+        k = (int)(c % nz);
+    };
+    auto cell_volume = [&](int i) {  // hydro_cpu.cpp:309
+        const double rc = (i + 0.5) * dx, wV = ax ? rc : dx;
+        return wV * dx * dx;
+    };
+
+    // fluidized cells and their viscosity
+    {
+        double v[1] = {0};
+        for (int64_t c = c0; c < n; c += stride) {
+            const bool on = r[c] > rmin && g.q[F_AF][c] > 1e-3;
+            w.eta[c] = on ? g.q[F_AF][c] * p.eta_af : 0.0;
+            v[0] += on ? 1.0 : 0.0;
+        }
+        double* part = sums();
+        block_partials<1>(v, part, nb);
+        if (!grid_barrier(ctl, nb)) return;
+        if (grid_total(part, 0, nb) == 0) return;  // nothing fluidized: no change
+    }
+    // face coefficients dt A_f eta_f / dx and the curvature diagonal
+    for (int64_t c = c0; c < n; c += stride) {
+        int i, j, k;
+        ijk(c, i, j, k);
+        const double e = __ldcg(w.eta + c), rc = (i + 0.5) * dx, wV = ax ? rc : dx, Vc = wV * dx * dx;
+        w.cfx[c] = i < nx - 1 ? dt * (ax ? (i + 1) * dx : dx) * harmonic(e, __ldcg(w.eta + c + sx)) : 0.0;
+        w.cfy[c] = (ny > 1 && j < ny - 1) ? dt * dx * harmonic(e, __ldcg(w.eta + c + sy)) : 0.0;
+        w.cfz[c] = k < nz - 1 ? dt * wV * harmonic(e, __ldcg(w.eta + c + 1)) : 0.0;
+        w.dax[c] = ax ? dt * e * Vc / (rc * rc) : 0.0;
+    }
+    if (!grid_barrier(ctl, nb)) return;
+    // diagonal: the cell's mass and every face coefficient it touches, added
+    // in the order of the reference's scatter loop (hydro_cpu.cpp:315-319)
+    for (int64_t c = c0; c < n; c += stride) {
+        int i, j, k;
+        ijk(c, i, j, k);
+        double s = r[c] * cell_volume(i);
+        if (i > 0) s += __ldcg(w.cfx + c - sx);
+        if (ny > 1 && j > 0) s += __ldcg(w.cfy + c - sy);
+        if (k > 0) s += __ldcg(w.cfz + c - 1);
+        if (i < nx - 1) s += __ldcg(w.cfx + c);
+        if (ny > 1 && j < ny - 1) s += __ldcg(w.cfy + c);
+        if (k < nz - 1) s += __ldcg(w.cfz + c);
+        w.dsum[c] = s;
+    }
+    if (!grid_barrier(ctl, nb)) return;
+
+    // y = A x at cell c (hydro_cpu.cpp:321-331), x given per cell by xv
+    auto amul = [&](int64_t c, int i, int j, int k, bool wd, auto xv) {
+        double s = (__ldcg(w.dsum + c) + (wd ? __ldcg(w.dax + c) : 0.0)) * xv(c);
+        if (i < nx - 1) s -= __ldcg(w.cfx + c) * xv(c + sx);
+        if (i > 0) s -= __ldcg(w.cfx + c - sx) * xv(c - sx);
+        if (ny > 1) {
+            if (j < ny - 1) s -= __ldcg(w.cfy + c) * xv(c + sy);
+            if (j > 0) s -= __ldcg(w.cfy + c - sy) * xv(c - sy);
+        }
+        if (k < nz - 1) s -= __ldcg(w.cfz + c) * xv(c + 1);
+        if (k > 0) s -= __ldcg(w.cfz + c - 1) * xv(c - 1);
+        return s;
+    };
+    auto diag = [&](int64_t c, bool wd) { return __ldcg(w.dsum + c) + (wd ? __ldcg(w.dax + c) : 0.0); };
+
+    for (int m = 0; m < 3; m++) {  // u and the hoop component carry -v/r^2, w does not
+        const bool wd = m < 2 && ax;
+        double* x = m == 0 ? w.x[0] : (m == 1 ? w.x[1] : w.x[2]);
+        const double* mom = m == 0 ? g.q[F_MU] : (m == 1 ? g.q[F_MV] : g.q[F_MW]);
+        double bn, rn, rz;
+        {  // initial guess: the current velocity; right-hand side Vc (rho v)
+            double v[1] = {0};
+            for (int64_t c = c0; c < n; c += stride) {
+                const double b = cell_volume((int)(c / sx)) * mom[c];
+                x[c] = mom[c] / r[c];
+                v[0] += b * b;
+            }
+            double* part = sums();
+            block_partials<1>(v, part, nb);
+            if (!grid_barrier(ctl, nb)) return;
+            bn = grid_total(part, 0, nb);
+        }
+        if (bn <= 0) {
+            for (int64_t c = c0; c < n; c += stride) x[c] = 0;
+            continue;
+        }
+        {  // r = b - A x, z = r / diag, p = z
+            double v[2] = {0, 0};
+            for (int64_t c = c0; c < n; c += stride) {
+                int i, j, k;
+                ijk(c, i, j, k);
+                const double q = amul(c, i, j, k, wd, [&](int64_t cc) { return __ldcg(x + cc); });
+                const double rv = cell_volume(i) * mom[c] - q;
+                const double zv = rv / diag(c, wd);
+                w.rr[c] = rv;
+                w.zz[c] = zv;
+                w.pp[0][c] = zv;
+                v[0] += rv * rv;
+                v[1] += rv * zv;
+            }
+            double* part = sums();
+            block_partials<2>(v, part, nb);
+            if (!grid_barrier(ctl, nb)) return;
+            rn = grid_total(part, 0, nb);
+            rz = grid_total(part, 1, nb);
+        }
+        const double tol2 = 1e-16 * bn;
+        int cur = 0;
+        double be = 0;
+        for (int it = 0; it < 800 && rn > tol2; it++) {
+            double pq;
+            {  // p = z + beta p (after the first iteration), q = A p
+                const double* po = cur ? w.pp[1] : w.pp[0];
+                double* pn = cur ? w.pp[0] : w.pp[1];
+                const bool first = it == 0;
+                auto pv = [&](int64_t cc) {
+                    return first ? __ldcg(po + cc) : __ldcg(w.zz + cc) + be * __ldcg(po + cc);
+                };
+                double v[1] = {0};
+                for (int64_t c = c0; c < n; c += stride) {
+                    int i, j, k;
+                    ijk(c, i, j, k);
+                    const double pc = pv(c);
+                    if (!first) pn[c] = pc;
+                    const double q = amul(c, i, j, k, wd, pv);
+                    w.qq[c] = q;
+                    v[0] += pc * q;
+                }
+                if (!first) cur ^= 1;
+                double* part = sums();
+                block_partials<1>(v, part, nb);
+                if (!grid_barrier(ctl, nb)) return;
+                pq = grid_total(part, 0, nb);
+            }
+            if (pq <= 0) break;
+            const double al = rz / pq;
+            double rz2;
+            {  // x += alpha p, r -= alpha q, z = r / diag
+                const double* pc = cur ? w.pp[1] : w.pp[0];
+                double v[2] = {0, 0};
+                for (int64_t c = c0; c < n; c += stride) {
+                    x[c] += al * pc[c];
+                    const double rv = w.rr[c] - al * w.qq[c];
+                    w.rr[c] = rv;
+                    const double zv = rv / diag(c, wd);
+                    w.zz[c] = zv;
+                    v[0] += rv * rv;
+                    v[1] += rv * zv;
+                }
+                double* part = sums();
+                block_partials<2>(v, part, nb);
+                if (!grid_barrier(ctl, nb)) return;
+                rn = grid_total(part, 0, nb);
+                rz2 = grid_total(part, 1, nb);
+            }
+            if (blockIdx.x == 0 && threadIdx.x == 0) ctl->visc_iters++;
+            if (rn <= tol2) break;
+            be = rz2 / rz;
+            rz = rz2;
+        }
+    }
+    if (!grid_barrier(ctl, nb)) return;  // every cell's new velocity in place
+
+    // heating: the kinetic energy removed, spread over the cells in
+    // proportion to the dissipation of their faces (hydro_cpu.cpp:355-376)
+    const double *u1 = w.x[0], *v1 = w.x[1], *w1 = w.x[2];
+    auto face_heat = [&](int64_t a, int64_t b, double cf) {  // a is the lower cell
+        const double du = __ldcg(u1 + a) - __ldcg(u1 + b), dv = __ldcg(v1 + a) - __ldcg(v1 + b),
+                     dw = __ldcg(w1 + a) - __ldcg(w1 + b);
+        return cf * (du * du + dv * dv + dw * dw);
+    };
+    double sc;
+    {
+        double v[3] = {0, 0, 0};
+        for (int64_t c = c0; c < n; c += stride) {
+            int i, j, k;
+            ijk(c, i, j, k);
+            const double rho = r[c], mu = g.q[F_MU][c], mv = g.q[F_MV][c], mw = g.q[F_MW][c];
+            const double uc = __ldcg(u1 + c), vc = __ldcg(v1 + c), wc = __ldcg(w1 + c), Vc = cell_volume(i);
+            const double keo = 0.5 * (mu * mu + mv * mv + mw * mw) / rho;
+            const double ken = 0.5 * rho * (uc * uc + vc * vc + wc * wc);
+            v[0] += keo * Vc;
+            v[1] += ken * Vc;
+            const double fx = __ldcg(w.cfx + c), fy = __ldcg(w.cfy + c), fz = __ldcg(w.cfz + c), fa = __ldcg(w.dax + c);
+            if (i < nx - 1 && fx > 0) v[2] += face_heat(c, c + sx, fx);
+            if (ny > 1 && j < ny - 1 && fy > 0) v[2] += face_heat(c, c + sy, fy);
+            if (k < nz - 1 && fz > 0) v[2] += face_heat(c, c + 1, fz);
+            if (ax && fa > 0) v[2] += fa * (uc * uc + vc * vc);
+        }
+        double* part = sums();
+        block_partials<3>(v, part, nb);
+        if (!grid_barrier(ctl, nb)) return;
+        const double totold = grid_total(part, 0, nb), totnew = grid_total(part, 1, nb),
+                     htot = grid_total(part, 2, nb);
+        const double loss = totold - totnew;
+        sc = (loss > 0 && htot > 0) ? loss / htot : 0.0;
+    }
+    for (int64_t c = c0; c < n; c += stride) {
+        int i, j, k;
+        ijk(c, i, j, k);
+        // this cell's share of its faces' dissipation, in the reference's order
+        double hr = 0;
+        if (i > 0 && __ldcg(w.cfx + c - sx) > 0) hr += 0.5 * face_heat(c - sx, c, __ldcg(w.cfx + c - sx));
+        if (ny > 1 && j > 0 && __ldcg(w.cfy + c - sy) > 0) hr += 0.5 * face_heat(c - sy, c, __ldcg(w.cfy + c - sy));
+        if (k > 0 && __ldcg(w.cfz + c - 1) > 0) hr += 0.5 * face_heat(c - 1, c, __ldcg(w.cfz + c - 1));
+        if (i < nx - 1 && __ldcg(w.cfx + c) > 0) hr += 0.5 * face_heat(c, c + sx, __ldcg(w.cfx + c));
+        if (ny > 1 && j < ny - 1 && __ldcg(w.cfy + c) > 0) hr += 0.5 * face_heat(c, c + sy, __ldcg(w.cfy + c));
+        if (k < nz - 1 && __ldcg(w.cfz + c) > 0) hr += 0.5 * face_heat(c, c + 1, __ldcg(w.cfz + c));
+        const double uc = __ldcg(u1 + c), vc = __ldcg(v1 + c), wc = __ldcg(w1 + c);
+        if (ax && __ldcg(w.dax + c) > 0) hr += __ldcg(w.dax + c) * (uc * uc + vc * vc);
+        const double rho = r[c];
+        double& mu = g.q[F_MU][c];
+        double& mv = g.q[F_MV][c];
+        double& mw = g.q[F_MW][c];
+        const double keo = 0.5 * (mu * mu + mv * mv + mw * mw) / rho;
+        mu = rho * uc;
+        mv = rho * vc;
+        mw = rho * wc;
+        const double ken = 0.5 * (mu * mu + mv * mv + mw * mw) / rho;
+        double q = sc * hr / cell_volume(i);
+        if (p.af_reg && q > 0) {  // C_REG of the dissipation regenerates vibrations
+            g.q[F_VIB][c] = sqrt(g.q[F_VIB][c] * g.q[F_VIB][c] + 2.0 * p.c_reg * q / rho);
+            q *= (1.0 - p.c_reg);
+        }
+        g.q[F_E][c] += (ken - keo) + q;
+    }
+}
 
 // ---------------------------------------------------------------- host engine
 
@@ -85,6 +427,8 @@ struct Grid {
     cudaEvent_t ev[8] = {};
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    int64_t graph_launches = 0;  // kernels per replay of the step graph
+    Visc vw{};                   // implicit viscosity work arrays, allocated on first use
 
     template <class T = double>
     T* alloc(int64_t count) {
@@ -109,6 +453,40 @@ struct Grid {
     }
 
     unsigned grid_of(int64_t count) const { return (unsigned)((count + 255) / 256); }
+
+    bool visc_on() const { return p.visc_imp && p.eta_af > 0; }
+
+    // The persistent launch's blocks: as many as fit on the device at once
+    // (a cooperative launch needs all of them resident), at most one per 256
+    // cells.
+    void ensure_visc() {
+        if (vw.eta) return;
+        int dev_coop = 0, nsm = 0, per_sm = 0;
+        EU_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, device));
+        if (!dev_coop) throw SphError(SPH_ERR_CUDA, "the implicit viscosity needs cooperative launches");
+        EU_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+        EU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_implicit_visc, 256, 0));
+        if (per_sm < 1) throw SphError(SPH_ERR_CUDA, "implicit viscosity kernel does not fit on an SM");
+        const int64_t want = std::max<int64_t>(1, (p.n + 255) / 256);
+        vw.nblk = (int)std::min<int64_t>(want, (int64_t)per_sm * nsm);
+        for (double** a : {&vw.eta, &vw.cfx, &vw.cfy, &vw.cfz, &vw.dax, &vw.dsum, &vw.x[0], &vw.x[1], &vw.x[2],
+                           &vw.rr, &vw.zz, &vw.pp[0], &vw.pp[1], &vw.qq})
+            *a = alloc(p.n);
+        vw.part = alloc(6 * (int64_t)vw.nblk);
+    }
+
+    void enqueue_visc() {
+        ensure_visc();
+        static_assert(offsetof(Ctl, visc_err) == offsetof(Ctl, bar_count) + 4, "barrier fields are adjacent");
+        EU_CUDA(cudaMemsetAsync(&ctl->bar_count, 0, 8, st));  // barrier count and error flag
+        P pv = p;
+        Fields gv = g;
+        Visc wv = vw;
+        Ctl* cv = ctl;
+        void* args[] = {&pv, &gv, &wv, &cv};
+        EU_CUDA(cudaLaunchCooperativeKernel((const void*)k_implicit_visc, dim3((unsigned)vw.nblk), dim3(256), args, 0, st));
+        launches++;
+    }
 
     void enqueue_lop(const Fields& s) {
         if (mixed) enqueue_lop_f32(p, s, W32, g.q[F_AF], F32, d, ctl, st);
@@ -135,10 +513,23 @@ struct Grid {
         if (mixed) enqueue_predict_f32(p, g, g1, d, ctl, st);
         else enqueue_predict_t<double>(p, g, g1, d, ctl, st);
         enqueue_lop(g1);
-        if (mixed) enqueue_correct_f32(p, g, g1, d, ctl, st);
-        else enqueue_correct_t<double>(p, g, g1, d, ctl, st);
+        const bool vi = visc_on();
+        if (mixed) enqueue_correct_f32(p, g, g1, d, ctl, st, vi ? 1 : 0);
+        else enqueue_correct_t<double>(p, g, g1, d, ctl, st, vi ? 1 : 0);
+        if (vi) {  // implicit_visc between the average and the rest (hydro_cpu.cpp:420)
+            enqueue_visc();
+            if (mixed) enqueue_correct_f32(p, g, g1, d, ctl, st, 2);
+            else enqueue_correct_t<double>(p, g, g1, d, ctl, st, 2);
+            launches++;
+        }
         k_end<<<1, 1, 0, st>>>(ctl);
         launches += 3;
+        if (p.void_cons && p.ref_r0 && p.rho_cfl > 0) launches += 3;
+    }
+
+    void check_visc(const Ctl& c) {
+        if (c.visc_err)
+            throw SphError(SPH_ERR_STATE, "implicit viscosity: a grid-wide barrier wait ran out (device busy?)");
     }
 
     Ctl read_ctl() {
@@ -210,6 +601,7 @@ void to_params(deu::P& p, const eu_params& e) {
     p.af_seeddp = e.af_seeddp != 0;
     p.void_amb = e.void_amb;
     p.void_cons = e.void_cons != 0;
+    p.visc_imp = e.visc_imp != 0;
 }
 
 // Weakest-flaw activation strain of grow_damage (hydro_cpu.cpp:254), formed
@@ -527,6 +919,32 @@ int eu_step(eu_grid* h, double dt) {
         g->enqueue_step(false);
         g->check();
         EU_CUDA(cudaStreamSynchronize(g->st));
+        if (g->visc_on()) g->check_visc(g->read_ctl());
+    });
+}
+
+int eu_implicit_visc(eu_grid* h, double dt) {
+    return guard([&] {
+        deu::Grid* g = G(h);
+        if (!(dt >= 0) || !std::isfinite(dt)) throw SphError(SPH_ERR_ARG, "dt must be finite and >= 0");
+        deu::DeviceScope ds(g->device);
+        if (g->visc_on()) {  // implicit_visc returns at once otherwise (hydro_cpu.cpp:302)
+            deu::k_set_step<<<1, 1, 0, g->st>>>(g->ctl, dt);
+            g->launches++;
+            g->enqueue_visc();
+        }
+        g->check();
+        EU_CUDA(cudaStreamSynchronize(g->st));
+        g->check_visc(g->read_ctl());
+    });
+}
+
+int eu_visc_iterations(eu_grid* h, int64_t* iters) {
+    return guard([&] {
+        deu::Grid* g = G(h);
+        if (!iters) throw SphError(SPH_ERR_ARG, "null output pointer");
+        deu::DeviceScope ds(g->device);
+        *iters = g->read_ctl().visc_iters;
     });
 }
 
@@ -539,7 +957,10 @@ int eu_run(eu_grid* h, double cfl, double t_end, int64_t max_steps, int64_t* ste
         deu::k_set_run<<<1, 1, 0, g->st>>>(g->ctl, cfl, t_end, max_steps);
         g->launches++;
         const deu::Ctl c0 = g->read_ctl();
-        if (!g->graph_valid) {  // one driver step, captured once per settings
+        // The implicit viscosity's cooperative launch is issued directly, not
+        // from a graph: steps with it are enqueued one by one.
+        const bool direct = g->visc_on();
+        if (!direct && !g->graph_valid) {  // one driver step, captured once per settings
             if (g->graph) cudaGraphExecDestroy(g->graph);
             g->graph = nullptr;
             cudaGraph_t gr = nullptr;
@@ -551,11 +972,10 @@ int eu_run(eu_grid* h, double cfl, double t_end, int64_t max_steps, int64_t* ste
             e = cudaGraphInstantiate(&g->graph, gr, 0);
             cudaGraphDestroy(gr);
             if (e != cudaSuccess) throw SphError(SPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+            g->graph_launches = g->launches - l0;
             g->launches = l0;
             g->graph_valid = true;
         }
-        const int64_t per_step = 16 + ((g->p.c_act > 0 && g->p.tdec > 0) ? 1 : 0) +
-                                 ((g->p.void_cons && g->p.ref_r0 && g->p.rho_cfl > 0) ? 3 : 0);
         const int64_t limit = c0.max_steps;  // absolute step count, -1 = none
         deu::Ctl c = c0;
         // replay in chunks; steps past the end are no-ops (inactive control)
@@ -563,10 +983,17 @@ int eu_run(eu_grid* h, double cfl, double t_end, int64_t max_steps, int64_t* ste
         while (c.t < c.t_end && (limit < 0 || c.steps < limit)) {
             int todo = chunk;
             if (limit >= 0) todo = (int)std::min<int64_t>(todo, limit - c.steps);
-            for (int i = 0; i < todo; i++) EU_CUDA(cudaGraphLaunch(g->graph, g->st));
-            g->launches += per_step * todo;
+            for (int i = 0; i < todo; i++) {
+                if (direct) {
+                    g->enqueue_step(true);
+                } else {
+                    EU_CUDA(cudaGraphLaunch(g->graph, g->st));
+                    g->launches += g->graph_launches;
+                }
+            }
             const double t_prev = c.t;
             c = g->read_ctl();
+            g->check_visc(c);
             if (!(c.t > t_prev))  // dt collapsed (signal speed not finite): stop instead of spinning
                 throw SphError(SPH_ERR_STATE, "time step collapsed: no progress in t (non-finite state?)");
             chunk = std::min(chunk * 2, 64);

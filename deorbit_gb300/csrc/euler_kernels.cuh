@@ -48,7 +48,8 @@ struct P {
     const double* ref_r0;
     const double* ref_p0;
     double void_amb;  // VOID_AMB: void cells reset to this density instead of the reference's
-    int32_t void_cons, pad_vc;  // VOID_CONS: the reset moves the excess mass to a neighbour first
+    int32_t void_cons;  // VOID_CONS: the reset moves the excess mass to a neighbour first
+    int32_t visc_imp;   // VISC_IMP: fluidization viscosity by the implicit solve, not in the Lop
 };
 
 template <class R> __device__ __forceinline__ R dmax2(R a, R b) { return a < b ? b : a; }  // std::max
@@ -258,6 +259,13 @@ struct Ctl {
     int64_t steps, max_steps;
     int32_t active, pad;
     unsigned long long smax_bits;  // CFL speed of this step (positive doubles order as their bits)
+    // implicit viscosity: grid barrier of its persistent launch, a wait that
+    // ran out (error), conjugate-gradient iterations so far
+    unsigned int bar_count;
+    int32_t visc_err;  // bar_count and visc_err are cleared together before each launch
+    unsigned int bar_gen;
+    int32_t pad2;
+    long long visc_iters;
 };
 
 static __device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
@@ -696,7 +704,7 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
             dmu += double((sxx - syy) / rcyl);
             dmw += double(sxz / rcyl);
         }
-        if (af[c] > 0 && p.eta_af > 0) {  // explicit fluidization viscosity, hydro_cpu.cpp:190-197
+        if (af[c] > 0 && p.eta_af > 0 && !p.visc_imp) {  // explicit fluidization viscosity, hydro_cpu.cpp:190-197
             const R eta = R(af[c] * p.eta_af), id2 = R(1.0 / (p.dx * p.dx));
             auto vx = [&](int64_t q) { return Vx[q]; };
             auto vy = [&](int64_t q) { return Vy[q]; };
@@ -835,16 +843,21 @@ static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
 }
 
 // Corrector and the end of the step (hydro_cpu.cpp:419-424): trapezoidal
-// average, damage growth, radial return, damping, void-cell reset.
+// average, damage growth, radial return, damping, void-cell reset.  With the
+// implicit viscosity, which runs between the average and the rest, stage 1 is
+// the average alone and stage 2 the rest; stage 0 is all of it.
 template <class R>
-static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl) {
+static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl, int stage) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
     const double dt = ctl->dt;
+    if (stage != 2) {
 #pragma unroll
-    for (int q = 0; q < ND; q++) {
-        double* x = g.q[rk_field(q)];
-        x[c] = 0.5 * (x[c] + g1.q[rk_field(q)][c] + dt * d.q[q][c]);
+        for (int q = 0; q < ND; q++) {
+            double* x = g.q[rk_field(q)];
+            x[c] = 0.5 * (x[c] + g1.q[rk_field(q)][c] + dt * d.q[q][c]);
+        }
+        if (stage == 1) return;
     }
     grow_damage_cell<R>(p, g, c, dt);
     vonmises_cell<R>(p, g, g.q[F_AF], c, true);
@@ -915,9 +928,11 @@ inline void enqueue_predict_t(const P& p, const Fields& g, const Fields& g1, Rhs
     }
 }
 template <class R>
-inline void enqueue_correct_t(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st) {
-    k_correct<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, g1, d, ctl);
-    if (p.void_cons && p.ref_r0 && p.rho_cfl > 0) k_void_cons<<<1, 1024, 0, st>>>(p, g, ctl);  // void_cells(g) last
+inline void enqueue_correct_t(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st,
+                              int stage) {
+    k_correct<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p, g, g1, d, ctl, stage);
+    if (stage != 1 && p.void_cons && p.ref_r0 && p.rho_cfl > 0)
+        k_void_cons<<<1, 1024, 0, st>>>(p, g, ctl);  // void_cells(g) last
 }
 
 // The FP32 instantiations live in euler_mixed.cu (compiled with fused
@@ -926,6 +941,7 @@ void enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* 
                      const Ctl* ctl, cudaStream_t st);
 void enqueue_maxspeed_f32(const P& p, const Fields& g, Ctl* ctl, cudaStream_t st);
 void enqueue_predict_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st);
-void enqueue_correct_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st);
+void enqueue_correct_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st,
+                         int stage);
 
 }  // namespace deu

@@ -20,8 +20,9 @@ void enqueue_predict_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, c
     enqueue_predict_t<float>(p, g, g1, d, ctl, st);
 }
 
-void enqueue_correct_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st) {
-    enqueue_correct_t<float>(p, g, g1, d, ctl, st);
+void enqueue_correct_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st,
+                         int stage) {
+    enqueue_correct_t<float>(p, g, g1, d, ctl, st, stage);
 }
 
 }  // namespace deu

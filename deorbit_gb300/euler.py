@@ -28,7 +28,7 @@ class Params(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
                                           "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
-        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp reserved".split()] + [("void_amb", C.c_double), ("void_cons", C.c_int32), ("reserved2", C.c_int32)]
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp reserved".split()] + [("void_amb", C.c_double), ("void_cons", C.c_int32), ("visc_imp", C.c_int32)]
 
 
 _D = C.POINTER(C.c_double)
@@ -65,6 +65,8 @@ _SIGS = {
     "eu_set_ref": (C.c_int, [_P]),
     "eu_clear_ref": (C.c_int, [_P]),
     "eu_read_ref": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "eu_implicit_visc": (C.c_int, [_P, C.c_double]),
+    "eu_visc_iterations": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 }
 _declared = False
 
@@ -196,6 +198,16 @@ class Grid:
 
     def update_af(self, dt):
         sph.check(lib().eu_update_af(self.h, float(dt)))
+
+    def implicit_visc(self, dt):
+        """implicit_visc(g, dt): the backward-Euler fluidization viscosity."""
+        sph.check(lib().eu_implicit_visc(self.h, float(dt)))
+
+    def visc_iters(self) -> int:
+        """Conjugate-gradient iterations of the implicit viscosity so far."""
+        v = C.c_int64()
+        sph.check(lib().eu_visc_iterations(self.h, C.byref(v)))
+        return v.value
 
     def maxspeed(self) -> float:
         v = C.c_double()

@@ -230,7 +230,7 @@ def substrate(N=60):
 
 
 def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0, gz=3.71, t_end=None,
-           void_cons=0, void_amb=0.0):
+           void_cons=0, void_amb=0.0, visc_imp=0):
     """hydro_cpu.cpp:557-597: the axisymmetric vertical impact crater -- a
     basalt sphere of radius a on the axis, tangent to the surface, at U m/s
     into a lithostatic basalt half-space under gravity, with the frozen
@@ -238,8 +238,8 @@ def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0,
     and vacuum-aware faces, and (tdec > 0) shock-activated fluidization with
     the crater defaults (acoustic seeding, overburden relief); void_cons /
     void_amb select the conservative and ambient void resets (its arguments 17
-    and 14).  The driver's far-field floor pin and radial sponge are not part
-    of the case."""
+    and 14), visc_imp the implicit fluidization viscosity (argument 16).  The
+    driver's far-field floor pin and radial sponge are not part of the case."""
     rho0, Abulk = 2700.0, 2.67e10
     dx = a / cppr
     Nr, Nz = int(Rfac * a / dx + 0.5), int(Zfac * a / dx + 0.5)
@@ -256,11 +256,99 @@ def crater(cppr=4, Rfac=8.0, Zfac=8.0, a=500.0, U=12000.0, tdec=0.0, eta_af=0.0,
         prm.update(tdec=tdec, eta_af=eta_af, c_act=0.5, p_coh=1.0e6, p_act=1.0e8, af_seeddp=1, af_prel=1)
     if void_cons or void_amb:
         prm.update(void_cons=int(void_cons), void_amb=float(void_amb))
+    if visc_imp:
+        prm.update(visc_imp=1)
     if t_end is None:
         t_end = 2.0 * math.sqrt((Rfac * a) / gz)
-    name = f"crater_{cppr}" + ("_vc" if void_cons else "") + ("_amb" if void_amb else "")
+    name = f"crater_{cppr}" + ("_vc" if void_cons else "") + ("_amb" if void_amb else "") + ("_vi" if visc_imp else "")
     return Case(name, (Nr, 1, Nz), dx, ic.basalt(), prm,
                 {"r": r.reshape(-1), "E": np.zeros(Nr * Nz)}, 0.4, t_end, set_ref=True, post_ref=post)
+
+
+def visc_mode(N=256, m=4, nu=1.0):
+    """hydro_cpu.cpp:907-929 (visc_diff A): a fluidized ideal-gas slab of N
+    unit cells, rho 1, eta = nu, carrying the transverse cosine mode
+    v_y = cos(k x), v_z = v_y / 2 (k = m pi / L, the discrete Neumann
+    eigenmode); the gate applies the implicit viscosity at 20x the explicit
+    limit."""
+    dx, rho0 = 1.0, 1.0
+    kk = m * math.pi / (N * dx)
+    vy = np.cos(kk * (np.arange(N) + 0.5) * dx)  # k (i + 1/2) dx, the reference's order
+    mv, mw = rho0 * vy, 0.5 * rho0 * vy
+    f = {"r": np.full(N, rho0), "af": np.ones(N), "mv": mv, "mw": mw,
+         "E": 1e5 + 0.5 * (mv * mv + mw * mw) / rho0}
+    return Case("visc_mode", (N, 1, 1), dx, ic.ideal_gas(GAM), {"visc_imp": 1, "eta_af": nu * rho0}, f, 0.4, 0.0)
+
+
+def visc_axi(Nr=64, Nz=8, A0=1e-2, W0=3.0, nu=1.0):
+    """hydro_cpu.cpp:930-944 (visc_diff B): cylindrical, v_r = A0 r (an exact
+    null mode of the discrete operator) and v_z = W0 in a fluidized ideal gas."""
+    dx, rho0 = 1.0, 1.0
+    rr = _centres(Nr, dx)[:, None] * np.ones((1, Nz))
+    mu, mw = rho0 * A0 * rr, rho0 * W0 * np.ones_like(rr)
+    f = {"r": np.full(Nr * Nz, rho0), "af": np.ones(Nr * Nz), "mu": mu.reshape(-1), "mw": mw.reshape(-1),
+         "E": (1e5 + 0.5 * (mu * mu + mw * mw) / rho0).reshape(-1)}
+    return Case("visc_axi", (Nr, 1, Nz), dx, ic.ideal_gas(GAM), {"visc_imp": 1, "eta_af": nu * rho0, "axisym": 1},
+                f, 0.4, 0.0)
+
+
+def visc_slab(eta=1e8, A0=1.0, t_end=25.0, N=256, m=24, visc_imp=1):
+    """hydro_cpu.cpp:947-987 (visc_agree, visc_energy): a fluidized basalt
+    slab (af = 1, so no strength) of N 500 m cells carrying a transverse cosine
+    shear mode of amplitude A0 m/s, viscosity eta, CFL 0.4; visc_imp 0 runs the
+    Lop's explicit viscosity instead."""
+    dx = 500.0
+    rho0 = 2700.0
+    kk = m * math.pi / (N * dx)
+    vy = A0 * np.cos(kk * (np.arange(N) + 0.5) * dx)
+    f = {"r": np.full(N, rho0), "af": np.ones(N), "mv": rho0 * vy, "E": 0.5 * rho0 * vy * vy}
+    return Case(f"visc_slab_{'imp' if visc_imp else 'exp'}_{eta:.0e}", (N, 1, 1), dx, ic.basalt(),
+                {"visc_imp": int(visc_imp), "eta_af": float(eta)}, f, 0.4, t_end)
+
+
+def vib_slab(case=2, t_end=40.0, N=256, m=24):
+    """hydro_cpu.cpp:988-1027 (vib_regen): a yielding-soft basalt slab
+    (Y = 1 MPa) with vibrations vib0 = 10 m/s, a 10 m/s cosine shear mode,
+    implicit viscosity 5e8 Pa s, decay time 2 s, no shock re-seeding; case 0
+    without regeneration bookkeeping, 1 with it at C_REG = 0, 2 with
+    C_REG = 1."""
+    dx, A0, vib0 = 500.0, 10.0, 10.0
+    mat = dict(ic.basalt())
+    mat["Y"] = 1e6
+    rho0 = mat["rho0"]
+    kk = m * math.pi / (N * dx)
+    vy = A0 * np.cos(kk * (np.arange(N) + 0.5) * dx)
+    f = {"r": np.full(N, rho0), "vib": np.full(N, vib0), "Pmax": np.full(N, 1e30), "mv": rho0 * vy,
+         "E": 0.5 * rho0 * vy * vy}
+    prm = {"visc_imp": 1, "eta_af": 5e8, "tdec": 2.0, "c_act": 0.5, "p_act": 1e30, "p_coh": 1e6,
+           "af_reg": int(case > 0), "c_reg": 0.0 if case < 2 else 1.0, "af_sat": 1e9}
+    return Case(f"vib_slab_{case}", (N, 1, 1), dx, mat, prm, f, 0.4, t_end)
+
+
+def bingham_heap(case=1, NX=112, NZ=20):
+    """hydro_cpu.cpp:1028-1077 (bingham_slope): a fluidized triangular basalt
+    heap (H 2 km, half-width 6 km) on an intact lithostatic substrate in x-z,
+    gravity 3.71, ROCK yield, implicit viscosity 5e7 Pa s, voids reset to the
+    ambient density, and the Bingham floor Y_B of the case: 0 static
+    (2.5 x the peak flank stress), 1 arrest (0.2 x), 2 Newtonian control (0);
+    run for 400 / 1200 / 600 s with the two deepest layers pinned to the
+    reference."""
+    rho0, Ab, gz, dx = 2700.0, 2.67e10, 3.71, 250.0
+    z0, H, W = 1500.0, 2000.0, 6000.0
+    xc = 0.5 * NX * dx
+    taumax = rho0 * gz * H * (H / W)
+    yb = (2.5 * math.sqrt(3.0) * taumax, 0.2 * math.sqrt(3.0) * taumax, 0.0)[case]
+    x = _centres(NX, dx)[:, None]
+    z = _centres(NZ, dx)[None, :]
+    xx = np.abs(x - xc)
+    zs = z0 + np.where(xx < W, H * (1.0 - xx / W), 0.0)
+    r = np.where(z < zs, rho0 * (1.0 + rho0 * gz * (zs - z) / Ab), 0.27) * np.ones((NX, NZ))
+    af = np.where(z > z0, 1.0, 0.0) * np.ones((NX, NZ))
+    prm = {"gz": gz, "rock": 1, "rho_cfl": 100.0, "rho_vac": 100.0, "visc_imp": 1, "eta_af": 5e7,
+           "void_amb": 0.27, "y_bingham": yb}
+    return Case(f"bingham_{case}", (NX, 1, NZ), dx, ic.basalt(), prm,
+                {"r": r.reshape(-1), "E": np.zeros(NX * NZ), "af": af.reshape(-1)}, 0.4,
+                (400.0, 1200.0, 600.0)[case], set_ref=True, pin_floor=2)
 
 
 GATES = {"sod": sod, "tracer": tracer, "sedov": sedov, "sedov_axi": sedov_axi, "shear": shear,

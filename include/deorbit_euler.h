@@ -6,7 +6,8 @@
  * (hydrocodes/euler/hydro_cpu.cpp): the `Grid` of conserved and material
  * fields (hydro_cpu.cpp:90-93), its right-hand side `Lop` (98-214), the
  * radial return `vonmises` (229-252), `grow_damage` (253-258), the
- * acoustic-fluidization update `update_af` (390-410), the CFL speed
+ * acoustic-fluidization update `update_af` (390-410), the implicit
+ * fluidization viscosity `implicit_visc` (286-377), the CFL speed
  * `maxspeed` (378-380), the two-stage Runge-Kutta step `step_rk2`
  * (411-425) and the drivers' time loop (e.g. hydro_cpu.cpp:452).  The
  * reference's file-scope settings (hydro_cpu.cpp:15-36, 222-223) become the
@@ -15,10 +16,10 @@
  * All arithmetic is FP64, in the reference's operation order, with no fused
  * multiply-adds: on ideal-gas grids the results equal the reference's bit for
  * bit; Tillotson grids differ only where the device's exp / pow round
- * differently from the host library's.
- *
- * Not provided (the reference's option for it must stay off): the implicit
- * viscous solve (VISC_IMP).  eu_set_params has no field for it.
+ * differently from the host library's.  The implicit viscosity's
+ * conjugate-gradient sums are parallel reductions (fixed order, so runs
+ * repeat exactly) instead of the reference's serial sums: its solutions agree
+ * with the reference's to the solver's tolerance (relative residual 1e-8).
  *
  * Fields are host arrays of nx*ny*nz doubles, cell (i,j,k) at
  * (i*ny + j)*nz + k, exactly the reference's layout.  Names: r mu mv mw E Sxx
@@ -65,7 +66,8 @@ typedef struct eu_params {
                          density instead of the reference's (0 = the reference's) */
     int32_t void_cons;/* VOID_CONS: with a reference state, a void cell's excess mass
                          first moves to its densest neighbour (serial pass, index order) */
-    int32_t reserved2;
+    int32_t visc_imp; /* VISC_IMP: the fluidization viscosity by the implicit solve
+                         after the Runge-Kutta average instead of the Lop's explicit term */
 } eu_params;
 
 typedef struct eu_grid eu_grid;
@@ -119,6 +121,12 @@ int eu_read_rhs(eu_grid* g, const char* name, double* host, int64_t n);
 int eu_vonmises(eu_grid* g, int32_t reg);
 int eu_grow_damage(eu_grid* g, double dt);
 int eu_update_af(eu_grid* g, double dt);
+/* implicit_visc(g, dt) (286-377) applied to the current state: a no-op unless
+ * visc_imp is set and eta_af > 0.  eu_visc_iterations reads the
+ * conjugate-gradient iterations taken since the grid was created (the
+ * reference's VISC_IT). */
+int eu_implicit_visc(eu_grid* g, double dt);
+int eu_visc_iterations(eu_grid* g, int64_t* iters);
 /* maxspeed(g) (378-380), reduced on the device. */
 int eu_maxspeed(eu_grid* g, double* out);
 /* Pressure of every cell (Pcell, hydro_cpu.cpp:95) into host[n]. */

@@ -30,7 +30,7 @@ class Params(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("gz tdec eta_af c_act p_coh p_act rho_cfl damp rho_vac "
                                           "y_i0 mu_i mu_d y_d0 y_m y_bingham c_reg af_sat").split()] + [
-        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()] + [("void_amb", C.c_double), ("void_cons", C.c_int32), ("pad2_", C.c_int32)]
+        (n, C.c_int32) for n in "axisym rock af_reg af_prel af_seeddp pad_".split()] + [("void_amb", C.c_double), ("void_cons", C.c_int32), ("visc_imp", C.c_int32)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if not n.startswith("pad")}
@@ -58,6 +58,8 @@ def _declare(lib, p):
         f"{p}pcell": (C.c_double, [C.c_void_p, C.c_int]),
         f"{p}set_ref": (None, [C.c_void_p]),
         f"{p}clear_ref": (None, [C.c_void_p]),
+        f"{p}implicit_visc": (None, [C.c_void_p, C.c_double]),
+        f"{p}visc_iters": (C.c_long, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -175,6 +177,14 @@ class _Grid:
 
     def clear_ref(self):
         self._f("clear_ref")(self.h)
+
+    def implicit_visc(self, dt):
+        """implicit_visc(g, dt): the backward-Euler fluidization viscosity."""
+        self._f("implicit_visc")(self.h, float(dt))
+
+    def visc_iters(self) -> int:
+        """Conjugate-gradient iterations of the implicit viscosity so far."""
+        return int(self._f("visc_iters")(self.h))
 
     def close(self):
         if self.h:

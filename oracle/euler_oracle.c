@@ -25,6 +25,7 @@ struct eorc_grid {
     orc_material mat;
     eorc_params p;
     double *ref_r0, *ref_p0; /* hydrostatic reference (set_ref), NULL when off */
+    long visc_iters;         /* conjugate-gradient iterations of the implicit viscosity */
 };
 
 static inline double dmax2(double a, double b) { return a < b ? b : a; } /* std::max */
@@ -388,7 +389,7 @@ void eorc_lop(eorc_grid* g) {
                     d[D_MU][c] += (Sxx[c] - Syy[c]) / rcyl;
                     d[D_MW][c] += Sxz[c] / rcyl;
                 }
-                if (g->f[F_AF][c] > 0 && ETA_AF > 0) { /* explicit AF viscosity (VISC_IMP not restated) */
+                if (g->f[F_AF][c] > 0 && ETA_AF > 0 && !g->p.visc_imp) { /* explicit AF viscosity */
                     double eta = g->f[F_AF][c] * ETA_AF, id2 = 1.0 / (g->dx * g->dx);
                     d[D_MU][c] += eta * (VX(xp) + VX(xm) + VX(yp) + VX(ym) + VX(zp) + VX(zm) - 6 * VX(c)) * id2;
                     d[D_MV][c] += eta * (VY(xp) + VY(xm) + VY(yp) + VY(ym) + VY(zp) + VY(zm) - 6 * VY(c)) * id2;
@@ -594,6 +595,198 @@ void eorc_clear_ref(eorc_grid* g) {
     g->ref_r0 = g->ref_p0 = NULL;
 }
 
+/* ---- implicit fluidization viscosity, hydro_cpu.cpp:286-377 ----
+ * Backward Euler for d(rho v)/dt = div(eta grad v) with eta = af * ETA_AF in
+ * fluidized cells (af > 1e-3, rho above RHO_CFL): a finite-volume operator
+ * with face-harmonic eta (a face with a non-fluidized side carries no flux),
+ * face-area weights and the -v/r^2 diagonal of the r and hoop components in
+ * cylindrical geometry; each component solved by Jacobi-preconditioned
+ * conjugate gradients to a relative residual of 1e-8 (at most 800
+ * iterations); the kinetic energy removed comes back as heat, spread in
+ * proportion to each face's dissipation and scaled so that total energy is
+ * conserved. */
+typedef struct {
+    int nx, ny, nz, n, axisym;
+    const double *cfx, *cfy, *cfz, *dsum, *dax;
+} visc_op;
+
+static double visc_diag(const visc_op* A, int c, int wdax) { return A->dsum[c] + (wdax ? A->dax[c] : 0.0); }
+
+/* y = A x (hydro_cpu.cpp:321-331). */
+static void visc_apply(const visc_op* A, const double* x, double* y, int wdax) {
+    const int nx = A->nx, ny = A->ny, nz = A->nz;
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const int c = (i * ny + j) * nz + k;
+                double s = visc_diag(A, c, wdax) * x[c];
+                if (i < nx - 1) s -= A->cfx[c] * x[c + ny * nz];
+                if (i > 0) s -= A->cfx[c - ny * nz] * x[c - ny * nz];
+                if (ny > 1) {
+                    if (j < ny - 1) s -= A->cfy[c] * x[c + nz];
+                    if (j > 0) s -= A->cfy[c - nz] * x[c - nz];
+                }
+                if (k < nz - 1) s -= A->cfz[c] * x[c + 1];
+                if (k > 0) s -= A->cfz[c - 1] * x[c - 1];
+                y[c] = s;
+            }
+}
+
+/* Jacobi-preconditioned CG from the initial guess in x (hydro_cpu.cpp:332-351);
+ * every sum runs over the cells in index order. */
+static void visc_cg(const visc_op* A, double* x, const double* b, int wdax, double* rr, double* zz, double* pp,
+                    double* qq, long* iters) {
+    const int n = A->n;
+    double bn = 0;
+    for (int c = 0; c < n; c++) bn += b[c] * b[c];
+    if (bn <= 0) {
+        for (int c = 0; c < n; c++) x[c] = 0;
+        return;
+    }
+    visc_apply(A, x, qq, wdax);
+    double rn = 0;
+    for (int c = 0; c < n; c++) {
+        rr[c] = b[c] - qq[c];
+        rn += rr[c] * rr[c];
+    }
+    const double tol2 = 1e-16 * bn;
+    double rz = 0;
+    for (int c = 0; c < n; c++) {
+        zz[c] = rr[c] / visc_diag(A, c, wdax);
+        pp[c] = zz[c];
+        rz += rr[c] * zz[c];
+    }
+    for (int it = 0; it < 800 && rn > tol2; it++) {
+        visc_apply(A, pp, qq, wdax);
+        double pq = 0;
+        for (int c = 0; c < n; c++) pq += pp[c] * qq[c];
+        if (pq <= 0) break;
+        const double al = rz / pq;
+        rn = 0;
+        for (int c = 0; c < n; c++) {
+            x[c] += al * pp[c];
+            rr[c] -= al * qq[c];
+            rn += rr[c] * rr[c];
+        }
+        (*iters)++;
+        if (rn <= tol2) break;
+        double rz2 = 0;
+        for (int c = 0; c < n; c++) {
+            zz[c] = rr[c] / visc_diag(A, c, wdax);
+            rz2 += rr[c] * zz[c];
+        }
+        const double be = rz2 / rz;
+        rz = rz2;
+        for (int c = 0; c < n; c++) pp[c] = zz[c] + be * pp[c];
+    }
+}
+
+static double harmonic(double a, double b) { return (a > 0 && b > 0) ? 2.0 * a * b / (a + b) : 0.0; }
+
+void eorc_implicit_visc(eorc_grid* g, double dt) {
+    if (!g->p.visc_imp || g->p.eta_af <= 0) return;
+    const int nx = g->nx, ny = g->ny, nz = g->nz, n = g->n, ax = g->p.axisym;
+    const double dx = g->dx, rmin = dmax2(g->p.rho_cfl, 1e-12);
+    double** f = g->f;
+    double* eta = (double*)calloc((size_t)n, sizeof(double));
+    int any = 0;
+    for (int c = 0; c < n; c++)
+        if (f[F_R][c] > rmin && f[F_AF][c] > 1e-3) {
+            eta[c] = f[F_AF][c] * g->p.eta_af;
+            any = 1;
+        }
+    if (!any) {
+        free(eta);
+        return;
+    }
+    enum { VC, CFX, CFY, CFZ, DSUM, DAX, RR, ZZ, PP, QQ, U1, V1, W1, BB, HR, NBUF };
+    double* w[NBUF];
+    for (int q = 0; q < NBUF; q++) w[q] = (double*)calloc((size_t)n, sizeof(double));
+    double *Vc = w[VC], *cfx = w[CFX], *cfy = w[CFY], *cfz = w[CFZ], *dsum = w[DSUM], *dax = w[DAX];
+    const int sx = ny * nz, sy = nz;
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const int c = idx(g, i, j, k);
+                const double rc = (i + 0.5) * dx, wV = ax ? rc : dx;
+                Vc[c] = wV * dx * dx;
+                dsum[c] = f[F_R][c] * Vc[c];
+                if (i < nx - 1) cfx[c] = dt * (ax ? (i + 1) * dx : dx) * harmonic(eta[c], eta[c + sx]);
+                if (ny > 1 && j < ny - 1) cfy[c] = dt * dx * harmonic(eta[c], eta[c + sy]);
+                if (k < nz - 1) cfz[c] = dt * wV * harmonic(eta[c], eta[c + 1]);
+                if (ax) dax[c] = dt * eta[c] * Vc[c] / (rc * rc);
+            }
+    /* each face coefficient enters the diagonal of both its cells, in the
+     * reference's scatter order (hydro_cpu.cpp:315-319) */
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const int c = idx(g, i, j, k);
+                if (i < nx - 1) { dsum[c] += cfx[c]; dsum[c + sx] += cfx[c]; }
+                if (ny > 1 && j < ny - 1) { dsum[c] += cfy[c]; dsum[c + sy] += cfy[c]; }
+                if (k < nz - 1) { dsum[c] += cfz[c]; dsum[c + 1] += cfz[c]; }
+            }
+    const visc_op A = {nx, ny, nz, n, ax, cfx, cfy, cfz, dsum, dax};
+    const int mom[3] = {F_MU, F_MV, F_MW}, xq[3] = {U1, V1, W1};
+    for (int m = 0; m < 3; m++) { /* u and the hoop component carry -v/r^2; w does not */
+        double *x = w[xq[m]], *b = w[BB];
+        for (int c = 0; c < n; c++) {
+            x[c] = f[mom[m]][c] / f[F_R][c];
+            b[c] = Vc[c] * f[mom[m]][c];
+        }
+        visc_cg(&A, x, b, m < 2 ? ax : 0, w[RR], w[ZZ], w[PP], w[QQ], &g->visc_iters);
+    }
+    const double *u1 = w[U1], *v1 = w[V1], *w1 = w[W1];
+    double* hr = w[HR];
+    double totold = 0, totnew = 0, htot = 0;
+#define FACE_HEAT(cn, cf)                                                              \
+    do {                                                                               \
+        const double du = u1[c] - u1[cn], dv = v1[c] - v1[cn], dw = w1[c] - w1[cn];    \
+        const double h = (cf) * (du * du + dv * dv + dw * dw);                         \
+        hr[c] += 0.5 * h;                                                              \
+        hr[cn] += 0.5 * h;                                                             \
+        htot += h;                                                                     \
+    } while (0)
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const int c = idx(g, i, j, k);
+                const double r = f[F_R][c];
+                const double keo = 0.5 * (f[F_MU][c] * f[F_MU][c] + f[F_MV][c] * f[F_MV][c] + f[F_MW][c] * f[F_MW][c]) / r;
+                const double ken = 0.5 * r * (u1[c] * u1[c] + v1[c] * v1[c] + w1[c] * w1[c]);
+                totold += keo * Vc[c];
+                totnew += ken * Vc[c];
+                if (i < nx - 1 && cfx[c] > 0) FACE_HEAT(c + sx, cfx[c]);
+                if (ny > 1 && j < ny - 1 && cfy[c] > 0) FACE_HEAT(c + sy, cfy[c]);
+                if (k < nz - 1 && cfz[c] > 0) FACE_HEAT(c + 1, cfz[c]);
+                if (ax && dax[c] > 0) {
+                    const double h = dax[c] * (u1[c] * u1[c] + v1[c] * v1[c]);
+                    hr[c] += h;
+                    htot += h;
+                }
+            }
+#undef FACE_HEAT
+    const double loss = totold - totnew, sc = (loss > 0 && htot > 0) ? loss / htot : 0.0;
+    for (int c = 0; c < n; c++) {
+        const double r = f[F_R][c];
+        const double keo = 0.5 * (f[F_MU][c] * f[F_MU][c] + f[F_MV][c] * f[F_MV][c] + f[F_MW][c] * f[F_MW][c]) / r;
+        f[F_MU][c] = r * u1[c];
+        f[F_MV][c] = r * v1[c];
+        f[F_MW][c] = r * w1[c];
+        const double ken = 0.5 * (f[F_MU][c] * f[F_MU][c] + f[F_MV][c] * f[F_MV][c] + f[F_MW][c] * f[F_MW][c]) / r;
+        double q = sc * hr[c] / Vc[c];
+        if (g->p.af_reg && q > 0) { /* C_REG of the dissipation regenerates vibrations */
+            f[F_VIB][c] = sqrt(f[F_VIB][c] * f[F_VIB][c] + 2.0 * g->p.c_reg * q / r);
+            q *= (1.0 - g->p.c_reg);
+        }
+        f[F_E][c] += (ken - keo) + q;
+    }
+    for (int q = 0; q < NBUF; q++) free(w[q]);
+    free(eta);
+}
+
+long eorc_visc_iters(const eorc_grid* g) { return g->visc_iters; }
+
 static const int RK_FIELDS[ND] = {F_R, F_MU, F_MV, F_MW, F_E, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ, F_D, F_RC, F_VIB};
 
 /* Two-stage Runge-Kutta step, hydro_cpu.cpp:411-425. */
@@ -625,6 +818,7 @@ void eorc_step_rk2(eorc_grid* g, double dt) {
     for (int q = 0; q < ND; q++) memcpy(g->d[q], g1->d[q], sizeof(double) * (size_t)n);
     g1->ref_r0 = g1->ref_p0 = NULL;
     eorc_destroy(g1);
+    eorc_implicit_visc(g, dt);
     eorc_grow_damage(g, dt);
     eorc_vonmises(g, 1);
     if (g->p.damp < 1.0)

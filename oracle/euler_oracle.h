@@ -11,10 +11,11 @@
  * z-sweep and gravity source against it (75-88, 114-119, 139-143), the
  * near-void reset to that reference or to an ambient density, optionally
  * conservative (272-290), acoustic fluidization activation (390-410), the CFL
- * speed (378-380) and the two-stage Runge-Kutta step (411-425).  Every
- * expression keeps the reference's floating-point operation order; the
- * library is built with -ffp-contract=off.  The implicit viscous solve
- * (VISC_IMP) is not restated.
+ * speed (378-380), the implicit fluidization viscosity (VISC_IMP: backward
+ * Euler, Jacobi-preconditioned conjugate gradients, dissipation returned as
+ * heat, 286-377) and the two-stage Runge-Kutta step (411-425).  Every
+ * expression keeps the reference's floating-point operation order, sums
+ * included; the library is built with -ffp-contract=off.
  *
  * The oracle is test infrastructure: only tests/, the smoke check and the
  * bench's CPU legs call it, never the product path.
@@ -50,7 +51,7 @@ typedef struct {
     int pad_;
     double void_amb;  /* void cells reset to this ambient density instead of the reference's */
     int void_cons;    /* conservative reset: excess mass to the densest neighbour first */
-    int pad2_;
+    int visc_imp;     /* fluidization viscosity by the implicit solve instead of the Lop term */
 } eorc_params;
 
 void eorc_params_default(eorc_params* p);
@@ -80,6 +81,11 @@ void eorc_vonmises(eorc_grid* g, int reg);      /* 229-252 */
 void eorc_grow_damage(eorc_grid* g, double dt); /* 253-258 */
 void eorc_update_af(eorc_grid* g, double dt);   /* 390-410 */
 double eorc_maxspeed(const eorc_grid* g);       /* 378-380 */
+/* implicit_visc(g, dt) (hydro_cpu.cpp:301-377): a no-op unless visc_imp is set
+ * and eta_af > 0; eorc_visc_iters counts its conjugate-gradient iterations
+ * since the grid was created (the reference's VISC_IT). */
+void eorc_implicit_visc(eorc_grid* g, double dt);
+long eorc_visc_iters(const eorc_grid* g);
 void eorc_step_rk2(eorc_grid* g, double dt);    /* 411-425 */
 /* The reference drivers' loop (hydro_cpu.cpp:452 and every mode): dt =
  * cfl*dx/maxspeed, clipped at t_end; runs until t_end or max_steps steps.

@@ -6,7 +6,7 @@
 // includes), read where it lies; nothing from the reference is copied into
 // this repository.  The reference's driver `main` is renamed so that its
 // solver functions (Lop, vonmises, grow_damage, update_af, maxspeed,
-// step_rk2) and file-scope settings can be driven on arbitrary grids.  The
+// step_rk2, implicit_visc) and file-scope settings can be driven on arbitrary grids.  The
 // resulting oracle/_ref/libeulerref.so lets the golden-vector generator and
 // the oracle tests run the reference and the C oracle on the same inputs.
 #define main deorbit_hydro_cpu_main
@@ -26,6 +26,7 @@ struct RefGrid {
     orc_material mat;
     eorc_params prm;
     std::vector<double> ref_r0, ref_p0;  // this grid's hydrostatic reference (set_ref), empty when off
+    long visc_iters = 0;                 // this grid's share of the reference's VISC_IT counter
     RefGrid(int nx, int ny, int nz, double dx) : g(nx, ny, nz, dx), d(nx * ny * nz) {}
 };
 
@@ -48,7 +49,7 @@ void load(const RefGrid* R) {
     GZ = p.gz; TDEC = p.tdec; ETA_AF = p.eta_af; C_ACT = p.c_act; P_COH = p.p_coh; P_ACT = p.p_act;
     RHO_CFL = p.rho_cfl; DAMP = p.damp; RHO_VAC = p.rho_vac; AXISYM = p.axisym != 0; ROCK = p.rock != 0;
     Y_I0 = p.y_i0; MU_I = p.mu_i; MU_D = p.mu_d; Y_D0 = p.y_d0; Y_M = p.y_m; Y_BINGHAM = p.y_bingham;
-    VISC_IMP = false;
+    VISC_IMP = p.visc_imp != 0;
     VOID_CONS = p.void_cons != 0;
     VOID_AMB = p.void_amb;
     REF_R0 = R->ref_r0;
@@ -106,6 +107,7 @@ eorc_params capture_defaults() {
     p.af_reg = AF_REG; p.c_reg = C_REG; p.af_sat = AF_SAT; p.af_prel = AF_PREL; p.af_seeddp = AF_SEEDDP;
     p.void_amb = VOID_AMB;
     p.void_cons = VOID_CONS;
+    p.visc_imp = VISC_IMP;
     return p;
 }
 const eorc_params kDefaults = capture_defaults();
@@ -164,13 +166,24 @@ double eref_maxspeed(void* h) {
 void eref_step_rk2(void* h, double dt) {
     RefGrid* R = (RefGrid*)h;
     load(R);
+    const long it0 = VISC_IT;
     step_rk2(R->g, dt);
+    R->visc_iters += VISC_IT - it0;
 }
+void eref_implicit_visc(void* h, double dt) {
+    RefGrid* R = (RefGrid*)h;
+    load(R);
+    const long it0 = VISC_IT;
+    implicit_visc(R->g, dt);
+    R->visc_iters += VISC_IT - it0;
+}
+long eref_visc_iters(void* h) { return ((RefGrid*)h)->visc_iters; }
 int eref_run(void* h, double cfl, double t_end, int max_steps, double* t_out) {
     RefGrid* R = (RefGrid*)h;
     load(R);
     double t = 0;
     int s = 0;
+    const long it0 = VISC_IT;
     while (t < t_end && (max_steps < 0 || s < max_steps)) {  // the drivers' loop, hydro_cpu.cpp:452
         double dt = cfl * R->g.dx / maxspeed(R->g);
         if (t + dt > t_end) dt = t_end - t;
@@ -178,6 +191,7 @@ int eref_run(void* h, double cfl, double t_end, int max_steps, double* t_out) {
         t += dt;
         s++;
     }
+    R->visc_iters += VISC_IT - it0;
     if (t_out) *t_out = t;
     return s;
 }

@@ -6,7 +6,8 @@ oracle/Makefile into oracle/_ref/libeulerref.so, on the gate workloads of
 deorbit_gb300.grid_ic (small sizes, a bounded number of steps of the drivers'
 loop) and on single-operator cases (Lop with every source term, the ROCK
 yield with damage and fluidization forms, damage growth, fluidization
-activation).  Inputs, settings and outputs are stored as one compressed .npz;
+activation, the implicit viscosity).  The conjugate-gradient iteration
+counts of the implicit viscosity are recorded too.  Inputs, settings and outputs are stored as one compressed .npz;
 the tests reproduce them with the C oracle bit for bit, without the
 reference tree.
 
@@ -37,7 +38,9 @@ RUNS = [(GI.sod(), 60), (GI.tracer(), 40), (GI.sedov(12), 8), (GI.sedov_axi(16, 
         (GI.surface(), 20), (GI.impact3d(12), 6), (GI.impact3d(12, af=True), 6),
         (GI.substrate(), 30), (GI.crater(), 20), (GI.crater(tdec=2.0, eta_af=1e8), 20),
         (GI.crater(cppr=3, U=6000.0), 15), (GI.crater(cppr=3, U=6000.0, void_cons=1), 25),
-        (GI.crater(cppr=3, U=6000.0, void_amb=0.27), 25)]
+        (GI.crater(cppr=3, U=6000.0, void_amb=0.27), 25),
+        (GI.visc_slab(), 20), (GI.visc_slab(eta=5e11, A0=2.0, t_end=5.0), 12), (GI.vib_slab(2), 20),
+        (GI.bingham_heap(1, NX=60, NZ=16), 10), (GI.crater(cppr=3, U=6000.0, tdec=2.0, eta_af=1e9, visc_imp=1), 15)]
 
 
 def perturbed_state(seed, shape, strength=True):
@@ -73,6 +76,8 @@ OPS = [
     ("af", (5, 4, 6), 50.0, {"tdec": 2.0, "c_act": 0.1, "p_act": 1e6}, "update_af", 1e-2),
     ("af_reg", (5, 4, 6), 50.0, {"tdec": 2.0, "c_act": 0.1, "af_reg": 1, "af_seeddp": 1, "rho_cfl": 100.0},
      "update_af", 1e-2),
+    ("visc_cart", (6, 5, 7), 50.0, {"visc_imp": 1, "eta_af": 1e9, "rho_cfl": 100.0}, "implicit_visc", 0.05),
+    ("visc_cyl", (9, 1, 8), 50.0, {"visc_imp": 1, "eta_af": 1e9, "axisym": 1, "af_reg": 1}, "implicit_visc", 0.05),
 ]
 
 
@@ -93,7 +98,8 @@ def main():
         out[f"{key}/meta"] = np.array(json.dumps({
             "kind": "run", "shape": list(case.shape), "dx": case.dx, "material": case.material,
             "params": case.params, "cfl": case.cfl, "t_end": case.t_end, "max_steps": steps,
-            "steps": s, "t": t, "set_ref": case.set_ref, "pin_floor": case.pin_floor}))
+            "steps": s, "t": t, "set_ref": case.set_ref, "pin_floor": case.pin_floor,
+            "visc_iters": g.visc_iters()}))
         g.close()
         print(key, s, t)
     for i, (name, shape, dx, prm, op, arg) in enumerate(OPS):
@@ -114,7 +120,7 @@ def main():
             out[f"{name}/out/{k}"] = v
         out[f"{name}/meta"] = np.array(json.dumps({
             "kind": "op", "op": op, "arg": arg, "shape": list(shape), "dx": dx, "material": GI.ic.basalt(),
-            "params": prm}))
+            "params": prm, "visc_iters": g.visc_iters()}))
         g.close()
         print(name, op)
     np.savez_compressed(OUT, **out)

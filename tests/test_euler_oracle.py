@@ -10,6 +10,8 @@
   the CI list) evaluated on the oracle's full runs.
 * The library's default settings equal the oracle's (and, where the reference
   tree is present, the reference's own).
+* The reference's implicit-viscosity gates (visc_diff, visc_agree,
+  visc_energy, vib_regen; tests/visc_gates.py) on the oracle.
 """
 import json
 import math
@@ -63,11 +65,19 @@ def test_oracle_reproduces_reference_bit_for_bit(key):
             getattr(g, meta["op"])(meta["arg"])
             got = g.fields()
         got["maxspeed"] = np.array([g.maxspeed()])
+    assert g.visc_iters() == meta.get("visc_iters", 0)
     for k in z.files:
         if k.startswith(key + "/out/"):
             name = k.split("/")[-1]
             assert np.array_equal(got[name], z[k]), (key, name)
     g.close()
+
+
+@pytest.mark.parametrize("gate", ["visc_diff", "visc_agree", "visc_energy", "vib_regen"])
+def test_oracle_passes_viscosity_gates(gate):
+    import visc_gates as VG
+    ok, info = VG.GATES[gate](VG.OracleGrid)
+    assert ok, info
 
 
 def test_default_settings_agree():

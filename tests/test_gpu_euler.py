@@ -80,8 +80,12 @@ def test_tillotson_runs_match_oracle(E, case, steps):
 
 
 def _op_cases():
+    """The single-operator fixtures held to 1e-12 (the implicit viscosity's,
+    a converged linear solve, are checked in test_gpu_euler_visc.py)."""
     z = np.load(GOLD)
-    return sorted({k.split("/")[0] for k in z.files if json.loads(str(z[k.split("/")[0] + "/meta"]))["kind"] == "op"})
+    keys = sorted({k.split("/")[0] for k in z.files})
+    metas = {k: json.loads(str(z[k + "/meta"])) for k in keys}
+    return [k for k in keys if metas[k]["kind"] == "op" and metas[k]["op"] != "implicit_visc"]
 
 
 @pytest.mark.parametrize("key", _op_cases())
