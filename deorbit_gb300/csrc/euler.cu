@@ -429,6 +429,8 @@ struct Grid {
     bool graph_valid = false;
     int64_t graph_launches = 0;  // kernels per replay of the step graph
     Visc vw{};                   // implicit viscosity work arrays, allocated on first use
+    int pin_floor = 0;           // driver adjustments after each step (eu_set_driver)
+    int sponge_from = -1;
 
     template <class T = double>
     T* alloc(int64_t count) {
@@ -520,6 +522,11 @@ struct Grid {
             enqueue_visc();
             if (mixed) enqueue_correct_f32(p, g, g1, d, ctl, st, 2);
             else enqueue_correct_t<double>(p, g, g1, d, ctl, st, 2);
+            launches++;
+        }
+        if (pin_floor > 0 || sponge_from >= 0) {
+            if (!p.ref_r0) throw SphError(SPH_ERR_STATE, "the floor pin and sponge need a reference state (eu_set_ref)");
+            k_driver<<<grid_of(p.n), 256, 0, st>>>(p, g, ctl, pin_floor, sponge_from);
             launches++;
         }
         k_end<<<1, 1, 0, st>>>(ctl);
@@ -754,6 +761,8 @@ int eu_set_ref(eu_grid* h) {
 int eu_clear_ref(eu_grid* h) {
     return guard([&] {
         deu::Grid* g = G(h);
+        g->pin_floor = 0;  // the driver adjustments relax toward the reference
+        g->sponge_from = -1;
         g->p.ref_r0 = nullptr;
         g->p.ref_p0 = nullptr;
         g->graph_valid = false;
@@ -920,6 +929,19 @@ int eu_step(eu_grid* h, double dt) {
         g->check();
         EU_CUDA(cudaStreamSynchronize(g->st));
         if (g->visc_on()) g->check_visc(g->read_ctl());
+    });
+}
+
+int eu_set_driver(eu_grid* h, int32_t pin_floor, int32_t sponge_from) {
+    return guard([&] {
+        deu::Grid* g = G(h);
+        if (pin_floor < 0 || pin_floor > g->p.nz) throw SphError(SPH_ERR_ARG, "pin_floor must be in [0, nz]");
+        if (sponge_from >= g->p.nx) throw SphError(SPH_ERR_ARG, "sponge_from must be < nx (or negative: off)");
+        if ((pin_floor > 0 || sponge_from >= 0) && !g->p.ref_r0)
+            throw SphError(SPH_ERR_STATE, "the floor pin and sponge need a reference state (eu_set_ref)");
+        g->pin_floor = pin_floor;
+        g->sponge_from = sponge_from < 0 ? -1 : sponge_from;
+        g->graph_valid = false;
     });
 }
 

@@ -869,6 +869,31 @@ static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
     void_cell(p, g, c);
 }
 
+// A driver's adjustments after each step, against the hydrostatic reference:
+// the lowest `pin` z-layers return to the reference density at rest with no
+// energy, then columns i >= isp relax toward the reference with weight
+// ((i - isp) / max(1, nx - 1 - isp))^2 (the crater mode's far-field floor pin
+// and radial sponge, hydro_cpu.cpp:634-637; isp < 0: no sponge).
+static __global__ void k_driver(P p, Fields g, const Ctl* ctl, int pin, int isp) {
+    const int64_t c = gtid();
+    if (c >= p.n || !ctl->active) return;
+    const int i = (int)(c / ((int64_t)p.ny * p.nz)), k = (int)(c % p.nz);
+    if (k < pin) {
+        g.q[F_R][c] = p.ref_r0[c];
+        g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
+        g.q[F_E][c] = 0;
+    }
+    if (isp >= 0 && i >= isp) {
+        const int span = p.nx - 1 - isp;
+        const double xi = (double)(i - isp) / (span > 1 ? span : 1), sp = xi * xi;
+        g.q[F_R][c] = (1 - sp) * g.q[F_R][c] + sp * p.ref_r0[c];
+        g.q[F_MU][c] *= (1 - sp);
+        g.q[F_MV][c] *= (1 - sp);
+        g.q[F_MW][c] *= (1 - sp);
+        g.q[F_E][c] *= (1 - sp);
+    }
+}
+
 // Single operators for the C ABI's unit calls.
 static __global__ void k_vonmises(P p, Fields g, int reg) {
     const int64_t c = gtid();

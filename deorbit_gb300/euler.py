@@ -66,6 +66,7 @@ _SIGS = {
     "eu_clear_ref": (C.c_int, [_P]),
     "eu_read_ref": (C.c_int, [_P, _D, _D, C.c_int64]),
     "eu_implicit_visc": (C.c_int, [_P, C.c_double]),
+    "eu_set_driver": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "eu_visc_iterations": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 }
 _declared = False
@@ -170,6 +171,11 @@ class Grid:
 
     def clear_ref(self):
         sph.check(lib().eu_clear_ref(self.h))
+
+    def set_driver(self, pin_floor=0, sponge_from=-1):
+        """Per-step floor pin and radial sponge against the reference state,
+        applied on the device after every step (eu_set_driver)."""
+        sph.check(lib().eu_set_driver(self.h, int(pin_floor), int(sponge_from)))
 
     def reference(self):
         r0, p0 = np.empty(self.n), np.empty(self.n)
@@ -279,25 +285,9 @@ def from_case(case, device=0, form=FP64) -> Grid:
 
 
 def run_case(g, case, steps):
-    """The drivers' loop on a grid built from `case` with the case's floor pin
-    after every step (hydro_cpu.cpp:855); without a pin, Grid.run."""
-    if not case.pin_floor:
-        return g.run(case.cfl, case.t_end, steps)
-    nx, ny, nz = case.shape
-    base = case.fields["r"].reshape(nx, ny, nz)
-    t, s = g.time(), 0
-    while t < case.t_end and s < steps:
-        dt = case.cfl * case.dx / g.maxspeed()
-        if t + dt > case.t_end:
-            dt = case.t_end - t
-        g.step(dt)
-        f = g.read_many(["r", "mu", "mv", "mw", "E"])
-        f = {k: v.reshape(nx, ny, nz) for k, v in f.items()}
-        f["r"][:, :, :case.pin_floor] = base[:, :, :case.pin_floor]
-        for k in ("mu", "mv", "mw", "E"):
-            f[k][:, :, :case.pin_floor] = 0.0
-        g.write_many({k: v.reshape(-1) for k, v in f.items()})
-        t += dt
-        s += 1
-    g.set_time(t)
-    return s, t
+    """The drivers' loop on a grid built from `case`, with the case's floor pin
+    and radial sponge applied on the device after every step
+    (hydro_cpu.cpp:634-637, 855)."""
+    if case.pin_floor or case.sponge_from >= 0:
+        g.set_driver(case.pin_floor, case.sponge_from)
+    return g.run(case.cfl, case.t_end, steps)

@@ -32,6 +32,7 @@ class Case:
     set_ref: bool = False      # freeze `fields` as the hydrostatic reference (set_ref) ...
     post_ref: dict = field(default_factory=dict)  # ... then write these over them
     pin_floor: int = 0         # driver: the lowest pin_floor z-layers return to the reference each step
+    sponge_from: int = -1      # driver: columns i >= sponge_from relax toward the reference each step
 
     @property
     def n(self):

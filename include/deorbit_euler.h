@@ -105,6 +105,16 @@ int eu_set_ref(eu_grid* g);
 int eu_clear_ref(eu_grid* g);
 int eu_read_ref(eu_grid* g, double* r0, double* p0, int64_t n);
 
+/* A driver's adjustments applied on the device after every step of eu_step /
+ * eu_run, against the reference state: the lowest pin_floor z-layers return
+ * to the reference density at rest with no energy; columns i >= sponge_from
+ * relax toward it with weight ((i - sponge_from) / max(1, nx - 1 -
+ * sponge_from))^2 (density blended, momentum and energy scaled).  The crater
+ * mode's far-field floor pin and radial sponge (hydro_cpu.cpp:634-637: pin 2,
+ * sponge from (int)(0.85 nx)); the substrate gate pins 2 layers.  0 / -1:
+ * off (the default); eu_clear_ref turns both off. */
+int eu_set_driver(eu_grid* g, int32_t pin_floor, int32_t sponge_from);
+
 /* Field i/o of one named field (n = nx*ny*nz doubles), or of several in one
  * call (copies overlap on the grid's stream, one synchronisation). */
 int eu_write_field(eu_grid* g, const char* name, const double* host, int64_t n);

@@ -226,26 +226,87 @@ def from_case(case, cls=OracleGrid):
     return g
 
 
+def drive(g, case, pin=None, isp=None):
+    """The crater / substrate drivers' adjustments after a step
+    (hydro_cpu.cpp:634-637, 855): the lowest `pin` (default case.pin_floor)
+    z-layers back to the reference density at rest with no energy, then
+    columns i >= isp (default case.sponge_from) relaxed toward the reference
+    with weight ((i - isp) / max(1, nx - 1 - isp))^2.  The reference density
+    is the case's pre-impact field (what set_ref froze)."""
+    nx, ny, nz = case.shape
+    pin = case.pin_floor if pin is None else pin
+    isp = getattr(case, "sponge_from", -1) if isp is None else isp
+    if not pin and isp < 0:
+        return
+    ref = np.asarray(case.fields["r"], dtype=np.float64).reshape(nx, ny, nz)
+    f = {k: g.field(k).reshape(nx, ny, nz) for k in ("r", "mu", "mv", "mw", "E")}
+    if pin:
+        f["r"][:, :, :pin] = ref[:, :, :pin]
+        for k in ("mu", "mv", "mw", "E"):
+            f[k][:, :, :pin] = 0.0
+    if isp >= 0:
+        for i in range(isp, nx):
+            xi = float(i - isp) / max(1, nx - 1 - isp)
+            sp = xi * xi
+            f["r"][i] = (1 - sp) * f["r"][i] + sp * ref[i]
+            for k in ("mu", "mv", "mw", "E"):
+                f[k][i] *= (1 - sp)
+    for k, v in f.items():
+        g.set_field(k, v)
+
+
 def run_case(g, case, steps):
     """The drivers' loop on a grid built from `case` (steps of step_rk2 at
-    dt = cfl dx / maxspeed clipped at t_end), with the case's floor pin after
-    every step (hydro_cpu.cpp:855): returns (steps, t)."""
-    if not case.pin_floor:
+    dt = cfl dx / maxspeed clipped at t_end), with the case's floor pin and
+    sponge after every step (hydro_cpu.cpp:634-637, 855): returns (steps, t)."""
+    if not case.pin_floor and getattr(case, "sponge_from", -1) < 0:
         return g.run(case.cfl, case.t_end, steps)
-    nx, ny, nz = case.shape
-    base = case.fields["r"].reshape(nx, ny, nz)  # the reference density of the pinned layers
     t, s = 0.0, 0
     while t < case.t_end and s < steps:
         dt = case.cfl * case.dx / g.maxspeed()
         if t + dt > case.t_end:
             dt = case.t_end - t
         g.step(dt)
-        f = {k: g.field(k).reshape(nx, ny, nz) for k in ("r", "mu", "mv", "mw", "E")}
-        f["r"][:, :, :case.pin_floor] = base[:, :, :case.pin_floor]
-        for k in ("mu", "mv", "mw", "E"):
-            f[k][:, :, :case.pin_floor] = 0.0
-        for k, v in f.items():
-            g.set_field(k, v)
+        drive(g, case)
         t += dt
         s += 1
     return s, t
+
+
+class DrivenGrid:
+    """An oracle (or reference) grid behind the interface the crater driver
+    (deorbit_gb300.crater.run) uses: the drivers' loop from the grid's own
+    time with the floor pin and sponge after every step."""
+
+    def __init__(self, case, cls=OracleGrid):
+        self.case = case
+        self.g = from_case(case, cls)
+        self.t = 0.0
+        self.pin, self.isp = 0, -1
+
+    def set_driver(self, pin_floor=0, sponge_from=-1):
+        self.pin, self.isp = int(pin_floor), int(sponge_from)
+
+    def reference(self):
+        return np.asarray(self.case.fields["r"], dtype=np.float64).copy(), None
+
+    def run(self, cfl, t_end, max_steps=-1):
+        s = 0
+        while self.t < t_end and (max_steps < 0 or s < max_steps):
+            dt = cfl * self.g.dx / self.g.maxspeed()
+            if self.t + dt > t_end:
+                dt = t_end - self.t
+            self.g.step(dt)
+            drive(self.g, self.case, self.pin, self.isp)
+            self.t += dt
+            s += 1
+        return s, self.t
+
+    def read(self, name):
+        return self.g.field(name)
+
+    def pressure(self):
+        return np.array([self.g.pcell(c) for c in range(self.g.n)])
+
+    def close(self):
+        self.g.close()

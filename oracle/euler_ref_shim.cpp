@@ -207,6 +207,10 @@ void eref_clear_ref(void* h) {
     R->ref_r0.clear();
     R->ref_p0.clear();
 }
+// The reference driver itself (its renamed main): a mode with its command
+// line, printing to stdout as the reference binary does.
+int eref_main(int argc, char** argv) { return deorbit_hydro_cpu_main(argc, argv); }
+
 double eref_pcell(void* h, int c) {
     RefGrid* R = (RefGrid*)h;
     load(R);

@@ -99,6 +99,7 @@ def main():
             "kind": "run", "shape": list(case.shape), "dx": case.dx, "material": case.material,
             "params": case.params, "cfl": case.cfl, "t_end": case.t_end, "max_steps": steps,
             "steps": s, "t": t, "set_ref": case.set_ref, "pin_floor": case.pin_floor,
+            "sponge_from": case.sponge_from,
             "visc_iters": g.visc_iters()}))
         g.close()
         print(key, s, t)

@@ -40,7 +40,7 @@ def case_from(z, key):
     post = {k.split("/")[-1]: z[k] for k in z.files if k.startswith(key + "/post/")}
     case = GI.Case(key, tuple(meta["shape"]), meta["dx"], meta["material"], meta["params"], ins,
                    meta.get("cfl", 0.4), meta.get("t_end", 0.0), meta.get("set_ref", False), post,
-                   meta.get("pin_floor", 0))
+                   meta.get("pin_floor", 0), meta.get("sponge_from", -1))
     return case, meta
 
 

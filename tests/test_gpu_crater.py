@@ -1,0 +1,57 @@
+"""The crater driver on the CUDA grid solver against the reference's own
+crater mode (tests/golden/crater_modes.json: what the reference's compiled
+driver printed and wrote).  FP64 form: the same number of steps, every crater
+measure and every profile value within 1e-6 of its scale (plus half a unit in
+the last printed digit); the device's exp / pow make the fields differ from
+the reference's by ~1e-10 per step.  Mixed form: the same crater to 1e-3 of
+its diameter."""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from deorbit_gb300 import crater
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "crater_modes.json")
+MODES = json.load(open(GOLD))
+
+
+def _result(line):
+    return [float(v) for v in line.split()[1:]]
+
+
+def _steps(lines):
+    return int(re.search(r"steps=(\d+)", lines[0]).group(1))
+
+
+def _profile(text):
+    return np.array([[float(v) for v in ln.split()] for ln in text.splitlines() if not ln.startswith("#")])
+
+
+@pytest.mark.parametrize("mode", MODES, ids=lambda m: "_".join(m["args"][:7]))
+def test_fp64_driver_matches_reference_mode(cuda_lib, mode, tmp_path):
+    st, _ = crater.setup_from_args(mode["args"], env={})
+    res = crater.run(st, form=0)
+    assert res["steps"] == _steps(mode["lines"])
+    got, ref = _result(res["result_line"]), _result(mode["lines"][-1])
+    for g, r in zip(got, ref):
+        assert abs(g - r) <= 1e-6 * max(abs(r), 1.0) + 5e-5, (got, ref)
+    prof = tmp_path / "p.txt"
+    crater.write_profile(str(prof), st, res)
+    a, b = _profile(prof.read_text()), _profile(mode["profile"])
+    assert a.shape == b.shape and np.abs(a - b).max() <= 1e-6 * np.abs(b).max() + 5e-4
+    assert res["finite"]
+
+
+@pytest.mark.parametrize("mode", MODES[:2], ids=lambda m: "_".join(m["args"][:7]))
+def test_mixed_driver_matches_reference_mode(cuda_lib, mode):
+    st, _ = crater.setup_from_args(mode["args"], env={})
+    res = crater.run(st, form=1)
+    got, ref = _result(res["result_line"]), _result(mode["lines"][-1])
+    D = ref[1]
+    for g, r in zip(got[1:4], ref[1:4]):  # diameter, depth, transient depth
+        assert abs(g - r) <= 1e-3 * D, (got, ref)
