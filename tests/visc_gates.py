@@ -1,9 +1,11 @@
 """The reference driver's implicit-viscosity gates (hydrocodes/euler/
-hydro_cpu.cpp modes visc_diff, visc_agree, visc_energy, vib_regen), at its
-sizes and with its pass criteria, for any grid with the deorbit_gb300.euler
-Grid interface (read, write, set_params, implicit_visc, update_af, run from
-the grid's own time, visc_iters, close).  The GPU tests run them on the CUDA
-solver; the oracle tests on the oracle through `OracleGrid` below.
+hydro_cpu.cpp modes visc_diff, visc_agree, visc_energy, vib_regen,
+bingham_slope), at its sizes and with its pass criteria, for any grid with
+the deorbit_gb300.euler Grid interface (read, write, set_params, set_driver,
+implicit_visc, update_af, run from the grid's own time, visc_iters, close).
+The GPU tests run them all on the CUDA solver; the oracle tests run the first
+four on the oracle through `OracleGrid` below (bingham_slope takes ~10^5
+steps).
 
 Each gate returns (passed, the measured quantities).
 """
@@ -20,8 +22,13 @@ class OracleGrid:
 
     def __init__(self, case):
         from oracle import euler as EO
+        self.EO, self.case = EO, case
         self.g = EO.from_case(case)
         self.t = 0.0
+        self.pin, self.isp = 0, -1
+
+    def set_driver(self, pin_floor=0, sponge_from=-1):
+        self.pin, self.isp = pin_floor, sponge_from
 
     def read(self, name):
         return self.g.field(name)
@@ -48,6 +55,7 @@ class OracleGrid:
             if self.t + dt > t_end:
                 dt = t_end - self.t
             self.g.step(dt)
+            self.EO.drive(self.g, self.case, self.pin, self.isp)
             self.t += dt
             s += 1
         return s, self.t
@@ -203,4 +211,67 @@ def sound_speed(mat, rho, u):
     return float(f(C.byref(m), float(rho), float(u)))
 
 
-GATES = {"visc_diff": visc_diff, "visc_agree": visc_agree, "visc_energy": visc_energy, "vib_regen": vib_regen}
+def bingham_slope(make):
+    """hydro_cpu.cpp:1028-1077: a fluidized heap on an intact substrate with
+    the implicit viscosity: (A) with the Bingham floor at 2.5x the peak flank
+    stress the peak holds (> 92 % of H after 400 s); (B) at 0.2x it flows
+    (peak < 75 % of H) and then arrests (peak decay over the last 400 s of
+    1200 s below 15 % of the first 400 s, steepest flank stress within 8x the
+    yield envelope); (C) with no floor (Newtonian control) it keeps
+    collapsing (late decay > 3x case B's, lower peak).  The heap height is the
+    column mass above the substrate plane, sampled at the first step end past
+    every 100 s."""
+    res = []
+    for cs in range(3):
+        case = GI.bingham_heap(cs)
+        nx, _, nz = case.shape
+        dx, rho0, z0, H = case.dx, case.material["rho0"], 1500.0, 2000.0
+        gz = case.params["gz"]
+        yb = case.params["y_bingham"]
+        tauy = yb / math.sqrt(3.0) if yb > 0 else 1e30
+        g = make(case)
+        g.set_driver(case.pin_floor, -1)
+
+        def surf(r):
+            r = r.reshape(nx, nz)
+            m = np.cumsum(np.where(r > 100.0, r, 0.0), axis=1)[:, -1]
+            return m * dx / rho0
+
+        def peak(r):
+            hm = 0.0
+            for v in surf(r)[2:nx - 2] - z0:
+                hm = max(hm, float(v))
+            return hm
+
+        hsamp, t, nlog, tc = [H], 0.0, 100.0, case.t_end
+        dt_last = None
+        while t < tc:
+            k = 1 if dt_last is None else max(1, int(0.9 * (nlog - t) / dt_last))
+            t0 = t
+            n, t = g.run(case.cfl, tc, k)
+            if n == 0:
+                break
+            dt_last = (t - t0) / n
+            if t >= nlog:
+                hsamp.append(peak(g.read("r")))
+                nlog += 100.0
+        r = g.read("r")
+        g.close()
+        h = surf(r) - z0
+        hmax, ratio = 0.0, 0.0
+        for i in range(2, nx - 2):
+            hmax = max(hmax, float(h[i]))
+            if h[i] > 500.0:
+                ratio = max(ratio, rho0 * gz * h[i] * abs(h[i + 1] - h[i - 1]) / (2 * dx) / tauy)
+        ns = len(hsamp)
+        early = hsamp[0] - hsamp[min(4, ns - 1)]
+        late = hsamp[max(0, ns - 5)] - hsamp[ns - 1]
+        res.append((hmax / H, early, late, ratio))
+    ok_a = res[0][0] > 0.92
+    ok_b = res[1][0] < 0.75 and res[1][2] < 0.15 * res[1][1] and res[1][3] < 8.0
+    ok_c = res[2][2] > 3.0 * res[1][2] and res[2][0] < res[1][0]
+    return ok_a and ok_b and ok_c, {"static": res[0], "arrest": res[1], "control": res[2]}
+
+
+GATES = {"visc_diff": visc_diff, "visc_agree": visc_agree, "visc_energy": visc_energy, "vib_regen": vib_regen,
+         "bingham_slope": bingham_slope}
