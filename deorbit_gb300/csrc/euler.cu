@@ -421,6 +421,7 @@ struct Grid {
     double* scratch = nullptr;  // pressure read-out
     double* ref_r0 = nullptr;   // hydrostatic reference (set_ref), allocated on first use
     double* ref_p0 = nullptr;
+    double* ref_dp = nullptr;   // its well-balanced gravity face-pressure difference
     std::vector<void*> allocs;
     int64_t bytes = 0;
     int64_t launches = 0;
@@ -675,6 +676,10 @@ int eu_create_form(int32_t nx, int32_t ny, int32_t nz, double dx, int32_t device
                 if (g->mixed) g->W32.w[q] = g->alloc<float>(n);
                 else g->W.w[q] = g->alloc(n);
             }
+            if (g->mixed) {  // FP32 strength fields and near-void flags of the right-hand side
+                for (int q = 0; q < 8; q++) g->W32.sq[q] = g->alloc<float>(n);
+                g->W32.vd = g->alloc<uint8_t>(n);
+            }
             const int64_t nfc[3] = {deu::face_count<0>(nx, ny, nz), deu::face_count<1>(nx, ny, nz),
                                     deu::face_count<2>(nx, ny, nz)};
             for (int dir = 0; dir < 3; dir++)
@@ -724,6 +729,13 @@ int eu_set_material(eu_grid* h, const sph_material* m) {
         M.alpha = m->alpha; M.beta = m->beta; M.u0 = m->u0; M.uiv = m->uiv; M.ucv = m->ucv;
         M.G = m->G; M.Y = m->Y; M.Emod = m->Emod; M.wm = m->wm; M.wk = m->wk;
         derive(g->p);
+        if (g->p.ref_r0) {  // the gravity source's reference pressures follow the material
+            deu::DeviceScope ds(g->device);
+            deu::k_ref_dp<<<g->grid_of(g->p.n), 256, 0, g->st>>>(g->p, g->ref_r0, g->ref_dp);
+            g->launches++;
+            g->check();
+            EU_CUDA(cudaStreamSynchronize(g->st));
+        }
         g->graph_valid = false;
     });
 }
@@ -747,13 +759,16 @@ int eu_set_ref(eu_grid* h) {
         if (!g->ref_r0) {
             g->ref_r0 = g->alloc(g->p.n);
             g->ref_p0 = g->alloc(g->p.n);
+            g->ref_dp = g->alloc(g->p.n);
         }
         deu::k_set_ref<<<g->grid_of(g->p.n), 256, 0, g->st>>>(g->p, g->g, g->ref_r0, g->ref_p0);
-        g->launches++;
+        deu::k_ref_dp<<<g->grid_of(g->p.n), 256, 0, g->st>>>(g->p, g->ref_r0, g->ref_dp);
+        g->launches += 2;
         g->check();
         EU_CUDA(cudaStreamSynchronize(g->st));
         g->p.ref_r0 = g->ref_r0;
         g->p.ref_p0 = g->ref_p0;
+        g->p.ref_dp = g->ref_dp;
         g->graph_valid = false;
     });
 }
@@ -765,6 +780,7 @@ int eu_clear_ref(eu_grid* h) {
         g->sponge_from = -1;
         g->p.ref_r0 = nullptr;
         g->p.ref_p0 = nullptr;
+        g->p.ref_dp = nullptr;
         g->graph_valid = false;
     });
 }

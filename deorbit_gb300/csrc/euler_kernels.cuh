@@ -47,6 +47,7 @@ struct P {
     // the well-balanced z-sweep and gravity source and the void-cell reset
     const double* ref_r0;
     const double* ref_p0;
+    const double* ref_dp;  // per cell p0(top face) - p0(bottom face) of the well-balanced gravity source
     double void_amb;  // VOID_AMB: void cells reset to this density instead of the reference's
     int32_t void_cons;  // VOID_CONS: the reset moves the excess mass to a neighbour first
     int32_t visc_imp;   // VISC_IMP: fluidization viscosity by the implicit solve, not in the Lop
@@ -247,6 +248,11 @@ struct Rhs {
 template <class R>
 struct PrimT {  // rho, vx, vy, vz, e, rc/rho in the Lop's compute type, and (with a
     R* w[7];    // reference state) the pressure deviation Pcell - REF_P0 formed in FP64
+    // Sxx Syy Szz Sxy Sxz Syz D vib as the right-hand side reads them: in FP64
+    // the state's own arrays; in FP32 copies converted once per Lop by k_prim
+    // (the same values the conversion at every stencil read gave)
+    R* sq[8];
+    uint8_t* vd;  // FP32 form: near-void flag per cell (rho < RHO_CFL), formed in FP64
 };
 template <class R>
 struct FacesT {  // per direction: mass, normal / tangential momentum, energy, tracer fluxes
@@ -448,13 +454,38 @@ static __global__ void k_update_af(P p, Fields g, const Ctl* ctl) {
 }
 
 // Primitives of one state (hydro_cpu.cpp:101) and the tracer ratio rc/rho,
-// formed in FP64 and stored in the Lop's compute type R.
+// formed in FP64 and stored in the Lop's compute type R.  FP64: the
+// reference's quotients, one division each.  FP32: one FP64 reciprocal of
+// rho, the velocities, kinetic energy and internal energy from it in FP64
+// (E - ke cancels in kinetic-dominated cells), rounded to FP32; also the
+// strength fields in FP32 and the near-void flags for the right-hand side.
 template <class R>
 static __global__ void k_prim(P p, Fields s, PrimT<R> W, const Ctl* ctl) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
     const double r = s.q[F_R][c], mu = s.q[F_MU][c], mv = s.q[F_MV][c], mw = s.q[F_MW][c];
     const double E = s.q[F_E][c], rc = s.q[F_RC][c];
+    if constexpr (sizeof(R) == 4) {
+        const double inv = 1.0 / r, vx = mu * inv, vy = mv * inv, vz = mw * inv;
+        const double e = (E - 0.5 * (mu * vx + mv * vy + mw * vz)) * inv;
+        W.w[0][c] = R(r);
+        W.w[1][c] = R(vx);
+        W.w[2][c] = R(vy);
+        W.w[3][c] = R(vz);
+        W.w[4][c] = R(e);
+        W.w[5][c] = R(rc * inv);
+        if (p.ref_p0) {
+            double pr = pressure(p.m, r, e);
+            if (pr < 0) pr = 0;
+            W.w[6][c] = R(pr - p.ref_p0[c]);
+        }
+#pragma unroll
+        for (int q = 0; q < 6; q++) W.sq[q][c] = R(s.q[F_SXX + q][c]);
+        W.sq[6][c] = R(s.q[F_D][c]);
+        W.sq[7][c] = R(s.q[F_VIB][c]);
+        W.vd[c] = (p.rho_cfl > 0 && r < p.rho_cfl) ? 1 : 0;
+        return;
+    }
     W.w[0][c] = R(r);
     W.w[1][c] = R(mu / r);
     W.w[2][c] = R(mv / r);
@@ -620,18 +651,17 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
             dE += -p.gz * mw[c];
         } else {  // well-balanced source against the reference, hydro_cpu.cpp:139-143
             const double* R0 = p.ref_r0;
-            const int64_t ct = c + (k < p.nz - 1 ? 1 : 0), cb = c - (k > 0 ? 1 : 0);
-            double r0t = 0.5 * (R0[c] + R0[ct]), r0b = 0.5 * (R0[cb] + R0[c]);
-            double p0t = pressure(p.m, r0t, 0.0);
-            if (p0t < 0) p0t = 0;
-            double p0b = pressure(p.m, r0b, 0.0);
-            if (p0b < 0) p0b = 0;
-            dmw += -p.gz * (r[c] - R0[c]) + (p0t - p0b) * p.invdx;
+            dmw += -p.gz * (r[c] - R0[c]) + p.ref_dp[c] * p.invdx;  // ref_dp: k_ref_dp
             dE += -p.gz * mw[c];
         }
     }
     double dS[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, dD = 0.0, dvib = 0.0;
-    if (p.m.G > 0 && !(p.rho_cfl > 0 && r[c] < p.rho_cfl)) {  // strength sources, hydro_cpu.cpp:145-213
+    // near-void cell (rho < RHO_CFL): the FP32 form reads k_prim's flags
+    auto is_void = [&](int64_t q) -> bool {
+        if constexpr (sizeof(R) == 4) return W.vd[q] != 0;
+        else return p.rho_cfl > 0 && r[q] < p.rho_cfl;
+    };
+    if (p.m.G > 0 && !is_void(c)) {  // strength sources, hydro_cpu.cpp:145-213
         const R G = R(p.m.G), dx = R(p.dx);
         const int64_t xm = c - (i > 0 ? plane : 0), xp = c + (i < p.nx - 1 ? plane : 0);
         const int64_t ym = c - (j > 0 ? p.nz : 0), yp = c + (j < p.ny - 1 ? p.nz : 0);
@@ -642,10 +672,9 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
         const R* Vy = W.w[2];
         const R* Vz = W.w[3];
         const R vxc = Vx[c], vyc = Vy[c], vzc = Vz[c];
-        const bool vd = p.rho_cfl > 0;
-        auto vxw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vxc : Vx[q]; };
-        auto vyw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vyc : Vy[q]; };
-        auto vzw = [&](int64_t q) { return (vd && r[q] < p.rho_cfl) ? vzc : Vz[q]; };
+        auto vxw = [&](int64_t q) { return is_void(q) ? vxc : Vx[q]; };
+        auto vyw = [&](int64_t q) { return is_void(q) ? vyc : Vy[q]; };
+        auto vzw = [&](int64_t q) { return is_void(q) ? vzc : Vz[q]; };
         const R Lxx = (vxw(xp) - vxw(xm)) / hx, Lxy = (vxw(yp) - vxw(ym)) / hy, Lxz = (vxw(zp) - vxw(zm)) / hz;
         const R Lyx = (vyw(xp) - vyw(xm)) / hx, Lyy = (vyw(yp) - vyw(ym)) / hy, Lyz = (vyw(zp) - vyw(zm)) / hz;
         const R Lzx = (vzw(xp) - vzw(xm)) / hx, Lzy = (vzw(yp) - vzw(ym)) / hy, Lzz = (vzw(zp) - vzw(zm)) / hz;
@@ -654,12 +683,12 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
         const R exx = Lxx, ezz = Lzz, exy = R(0.5) * (Lxy + Lyx), exz = R(0.5) * (Lxz + Lzx),
                 eyz = R(0.5) * (Lyz + Lzy), tr = (exx + eyy + ezz) / R(3);
         const R Wxy = R(0.5) * (Lxy - Lyx), Wxz = R(0.5) * (Lxz - Lzx), Wyz = R(0.5) * (Lyz - Lzy);
-        const double* Sxx = s.q[F_SXX];
-        const double* Syy = s.q[F_SYY];
-        const double* Szz = s.q[F_SZZ];
-        const double* Sxy = s.q[F_SXY];
-        const double* Sxz = s.q[F_SXZ];
-        const double* Syz = s.q[F_SYZ];
+        const R* Sxx = W.sq[0];
+        const R* Syy = W.sq[1];
+        const R* Szz = W.sq[2];
+        const R* Sxy = W.sq[3];
+        const R* Sxz = W.sq[4];
+        const R* Syz = W.sq[5];
         const R sxx = R(Sxx[c]), syy = R(Syy[c]), szz = R(Szz[c]), sxy = R(Sxy[c]), sxz = R(Sxz[c]), syz = R(Syz[c]);
         const R Sm[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}};
         const R Wm[3][3] = {{R(0), Wxy, Wxz}, {-Wxy, R(0), Wyz}, {-Wxz, -Wyz, R(0)}};
@@ -677,7 +706,7 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
         const R ix_ = i > 0 ? dx : R(1e30), ixp = i < p.nx - 1 ? dx : R(1e30);
         const R iy_ = j > 0 ? dx : R(1e30), iyp = j < p.ny - 1 ? dx : R(1e30);
         const R iz_ = k > 0 ? dx : R(1e30), izp = k < p.nz - 1 ? dx : R(1e30);
-        auto adv = [&](const double* S) {  // upwind v . grad S, hydro_cpu.cpp:175-178
+        auto adv = [&](const R* S) {  // upwind v . grad S, hydro_cpu.cpp:175-178
             const R sc = R(S[c]);
             R ax = u > R(0) ? (sc - R(S[xm])) / ix_ : (R(S[xp]) - sc) / ixp;
             R ay = v > R(0) ? (sc - R(S[ym])) / iy_ : (R(S[yp]) - sc) / iyp;
@@ -690,10 +719,10 @@ static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W
         dS[3] = 0.0 + double(R(2) * G * exy + Jm[0][1] - adv(Sxy));
         dS[4] = 0.0 + double(R(2) * G * exz + Jm[0][2] - adv(Sxz));
         dS[5] = 0.0 + double(R(2) * G * eyz + Jm[1][2] - adv(Syz));
-        dD = 0.0 + double(-adv(s.q[F_D]));
-        dvib = 0.0 + double(-adv(s.q[F_VIB]));
+        dD = 0.0 + double(-adv(W.sq[6]));
+        dvib = 0.0 + double(-adv(W.sq[7]));
         // div S into momentum (central differences), hydro_cpu.cpp:183-186
-        auto cd = [&](const double* S, int64_t q1, int64_t q0, R h) { return (R(S[q1]) - R(S[q0])) / h; };
+        auto cd = [&](const R* S, int64_t q1, int64_t q0, R h) { return (R(S[q1]) - R(S[q0])) / h; };
         const R dSxx_x = cd(Sxx, xp, xm, hx), dSxy_y = cd(Sxy, yp, ym, hy), dSxz_z = cd(Sxz, zp, zm, hz);
         const R dSxy_x = cd(Sxy, xp, xm, hx), dSyy_y = cd(Syy, yp, ym, hy), dSyz_z = cd(Syz, zp, zm, hz);
         const R dSxz_x = cd(Sxz, xp, xm, hx), dSyz_y = cd(Syz, yp, ym, hy), dSzz_z = cd(Szz, zp, zm, hz);
@@ -821,6 +850,25 @@ static __global__ void k_yield_stage(P p, Fields g1, const double* af, const Ctl
     vonmises_cell<R>(p, g1, af, c, false);
 }
 
+// The reference state's face-pressure difference of the well-balanced gravity
+// source (hydro_cpu.cpp:139-143): p0 at the averaged reference densities of the
+// cell's top and bottom faces (zero internal energy, clamped at 0), in the
+// reference's operation order.  It depends only on the frozen reference and the
+// material, so it is formed once per reference (and material) instead of in
+// every right-hand side.
+static __global__ void k_ref_dp(P p, const double* R0, double* dp) {
+    const int64_t c = gtid();
+    if (c >= p.n) return;
+    const int k = (int)(c % p.nz);
+    const int64_t ct = c + (k < p.nz - 1 ? 1 : 0), cb = c - (k > 0 ? 1 : 0);
+    double r0t = 0.5 * (R0[c] + R0[ct]), r0b = 0.5 * (R0[cb] + R0[c]);
+    double p0t = pressure(p.m, r0t, 0.0);
+    if (p0t < 0) p0t = 0;
+    double p0b = pressure(p.m, r0b, 0.0);
+    if (p0b < 0) p0b = 0;
+    dp[c] = p0t - p0b;
+}
+
 // set_ref (hydro_cpu.cpp:259-261): density and pressure frozen as the reference.
 static __global__ void k_set_ref(P p, Fields g, double* r0, double* p0) {
     const int64_t c = gtid();
@@ -932,6 +980,13 @@ template <class R>
 inline void enqueue_lop_t(const P& p, const Fields& s, PrimT<R> W, const double* af, FacesT<R> F, Rhs d,
                           const Ctl* ctl, cudaStream_t st) {
     auto blocks = [](int64_t count, int b) { return (unsigned)((count + b - 1) / b); };
+    if constexpr (sizeof(R) == 8) {  // FP64: the right-hand side reads the state's own strength fields
+#pragma unroll
+        for (int q = 0; q < 6; q++) W.sq[q] = s.q[F_SXX + q];
+        W.sq[6] = s.q[F_D];
+        W.sq[7] = s.q[F_VIB];
+        W.vd = nullptr;
+    }
     k_prim<R><<<blocks(p.n, 256), 256, 0, st>>>(p, s, W, ctl);
     k_face<0, R><<<blocks(face_count<0>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
     k_face<1, R><<<blocks(face_count<1>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
