@@ -319,32 +319,61 @@ static __device__ void update_af_cell(const P& p, const Fields& g, int64_t c, do
     g.q[F_AF][c] = pvib / (pvib + pov);
 }
 
-// Radial return of one cell, hydro_cpu.cpp:229-252 (s: the stress / energy /
-// vibration state; af from the state the step started from).
+// Specific internal energy for an EOS evaluated in R: FP64, the reference's
+// two quotients (eint_of); FP32, one FP64 reciprocal of rho (E - ke cancels in
+// kinetic-dominated cells, so the difference stays FP64), the result rounded
+// to FP32 by the caller.
+template <class R>
+static __device__ __forceinline__ double eint_r(double r, double mu, double mv, double mw, double E) {
+    if constexpr (sizeof(R) == 8) {
+        return eint_of(r, mu, mv, mw, E);
+    } else {
+        const double inv = 1.0 / r;
+        return (E - 0.5 * (mu * mu + mv * mv + mw * mw) * inv) * inv;
+    }
+}
+
+// Pcell (hydro_cpu.cpp:95) with the EOS evaluated in R: the clamped pressure.
 template <class R>
 static __device__ __forceinline__ double pcell_r(const P& p, const Fields& s, int64_t c) {
-    // Pcell (hydro_cpu.cpp:95) with the EOS evaluated in R: the clamped pressure
     const double r = s.q[F_R][c];
-    R pr = pressure(mat_as<R>(p.m), R(r), R(eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
+    R pr = pressure(mat_as<R>(p.m), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
     if (pr < R(0)) pr = R(0);
     return double(pr);
 }
+
+// A cell's Pcell formed at most once per state and shared by the damage
+// growth and the radial return that follow each other in a stage (damage
+// growth changes only D, so both see the same pressure).
+template <class R>
+struct PcellOnce {
+    bool have = false;
+    double v = 0.0;
+    __device__ __forceinline__ double get(const P& p, const Fields& s, int64_t c) {
+        if (!have) {
+            v = pcell_r<R>(p, s, c);
+            have = true;
+        }
+        return v;
+    }
+};
 
 // Radial return of one cell, hydro_cpu.cpp:229-252 (s: the stress / energy /
 // vibration state; af from the state the step started from).  The yield
 // surface and the return factor are formed in R; the state stays FP64.
 template <class R>
-static __device__ void vonmises_cell(const P& p, const Fields& s, const double* af, int64_t c, bool reg) {
+static __device__ void vonmises_cell(const P& p, const Fields& s, const double* af, int64_t c, bool reg,
+                                     PcellOnce<R>& pc) {
     if (p.m.Y <= 0 && !p.rock) return;
     R Y;
     const double r = s.q[F_R][c];
     const R afc = R(af[c]);
     if (p.rock) {
-        R Pp = R(dmax2(pcell_r<R>(p, s, c), 0.0));
+        R Pp = R(dmax2(pc.get(p, s, c), 0.0));
         R Peff = Pp;
         if (p.af_prel && s.q[F_VIB][c] > 0) {
             R p2, cs2;
-            eos_pc(mat_as<R>(p.m), R(r), R(eint_of(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2,
+            eos_pc(mat_as<R>(p.m), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2,
                    cs2);
             Peff = dmax2(Pp - R(r) * cs2 * R(s.q[F_VIB][c]), R(0));
         }
@@ -381,11 +410,11 @@ static __device__ void vonmises_cell(const P& p, const Fields& s, const double* 
 // Tensile damage growth of one cell, hydro_cpu.cpp:253-258 (threshold and
 // growth formed in R).
 template <class R>
-static __device__ void grow_damage_cell(const P& p, const Fields& g, int64_t c, double dt) {
+static __device__ void grow_damage_cell(const P& p, const Fields& g, int64_t c, double dt, PcellOnce<R>& pc) {
     if (p.m.Emod <= 0 || p.m.wk <= 0) return;
     double* D = g.q[F_D];
     if (D[c] >= 1.0) return;
-    const R Pp = R(pcell_r<R>(p, g, c));
+    const R Pp = R(pc.get(p, g, c));
     const R sigmax = dmax2(-Pp + R(g.q[F_SXX][c]), dmax2(-Pp + R(g.q[F_SYY][c]), -Pp + R(g.q[F_SZZ][c])));
     if (sigmax > R(0) && sigmax / R(p.m.Emod) > R(p.eps_act)) {
         R cg = R(0.4) * sqrt(R(p.m.Emod) / dmax2(R(g.q[F_R][c]), R(1e-30))), Rs = R(0.5) * R(p.dx);
@@ -416,7 +445,7 @@ static __global__ void __launch_bounds__(256) k_maxspeed(P p, Fields g, Ctl* ctl
             const double mu = g.q[F_MU][c], mv = g.q[F_MV][c], mw = g.q[F_MW][c];
             const R rr = R(r);
             R pr, cs;
-            eos_pc(mat_as<R>(p.m), rr, R(eint_of(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
+            eos_pc(mat_as<R>(p.m), rr, R(eint_r<R>(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
             R cel = sqrt(cs * cs + (p.m.G > 0 ? R(4.0 / 3.0) * R(p.m.G) / rr : R(0)));
             R v = sqrt(R(mu) * R(mu) + R(mv) * R(mv) + R(mw) * R(mw)) / rr;
             s = dmax2(s, double(v + cel));
@@ -592,9 +621,16 @@ static __global__ void __launch_bounds__(256) k_face(P p, PrimT<R> W, FacesT<R> 
 // af: the fluidization ratio.  Flux differences and strength sources are
 // formed in R and added to the FP64 right-hand side (with R = double: every
 // operation of the reference, in its order).
+// Resident blocks per SM asked of the right-hand side (launch bounds) in the
+// FP32 form; the FP64 form keeps 3.  The FP32 form waits on neighbour loads at
+// low occupancy: 256^3 impact, mixed step 21.0 / 19.1 / 18.3 / 17.7 / 17.4 ms at
+// 3 / 4 / 5 / 6 / 7 blocks (141 registers; 128, 96, 80, 72 with spills).
+#ifndef DEU_RHS_MINB_F32
+#define DEU_RHS_MINB_F32 7
+#endif
 template <class R>
-static __global__ void __launch_bounds__(128, 3) k_rhs(P p, Fields s, PrimT<R> W, const double* af, FacesT<R> F,
-                                                      Rhs d, const Ctl* ctl) {
+static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 : 3)
+    k_rhs(P p, Fields s, PrimT<R> W, const double* af, FacesT<R> F, Rhs d, const Ctl* ctl) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
     const int64_t plane = (int64_t)p.ny * p.nz;
@@ -847,7 +883,8 @@ template <class R>
 static __global__ void k_yield_stage(P p, Fields g1, const double* af, const Ctl* ctl) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
-    vonmises_cell<R>(p, g1, af, c, false);
+    PcellOnce<R> pc;
+    vonmises_cell<R>(p, g1, af, c, false, pc);
 }
 
 // The reference state's face-pressure difference of the well-balanced gravity
@@ -887,7 +924,10 @@ static __global__ void k_predict(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
 #pragma unroll
     for (int q = 0; q < ND; q++) g1.q[rk_field(q)][c] = g.q[rk_field(q)][c] + dt * d.q[q][c];
     void_cell(p, g1, c);
-    if (!(p.void_cons && p.ref_r0)) vonmises_cell<R>(p, g1, g.q[F_AF], c, false);  // else after k_void_cons
+    if (!(p.void_cons && p.ref_r0)) {  // else after k_void_cons
+        PcellOnce<R> pc;
+        vonmises_cell<R>(p, g1, g.q[F_AF], c, false, pc);
+    }
 }
 
 // Corrector and the end of the step (hydro_cpu.cpp:419-424): trapezoidal
@@ -907,8 +947,9 @@ static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
         }
         if (stage == 1) return;
     }
-    grow_damage_cell<R>(p, g, c, dt);
-    vonmises_cell<R>(p, g, g.q[F_AF], c, true);
+    PcellOnce<R> pc;
+    grow_damage_cell<R>(p, g, c, dt, pc);
+    vonmises_cell<R>(p, g, g.q[F_AF], c, true, pc);
     if (p.damp < 1.0) {
         g.q[F_MU][c] *= p.damp;
         g.q[F_MV][c] *= p.damp;
@@ -945,11 +986,13 @@ static __global__ void k_driver(P p, Fields g, const Ctl* ctl, int pin, int isp)
 // Single operators for the C ABI's unit calls.
 static __global__ void k_vonmises(P p, Fields g, int reg) {
     const int64_t c = gtid();
-    if (c < p.n) vonmises_cell<double>(p, g, g.q[F_AF], c, reg != 0);
+    PcellOnce<double> pc;
+    if (c < p.n) vonmises_cell<double>(p, g, g.q[F_AF], c, reg != 0, pc);
 }
 static __global__ void k_grow_damage(P p, Fields g, double dt) {
     const int64_t c = gtid();
-    if (c < p.n) grow_damage_cell<double>(p, g, c, dt);
+    PcellOnce<double> pc;
+    if (c < p.n) grow_damage_cell<double>(p, g, c, dt, pc);
 }
 static __global__ void k_pressure(P p, Fields g, double* out) {
     const int64_t c = gtid();
