@@ -36,6 +36,10 @@
 #include "engine.hpp"
 #include "euler_kernels.cuh"
 
+static_assert(EU_DRIVER_PIN_STRESS == deu::DRV_PIN_STRESS && EU_DRIVER_VOID_AMBIENT == deu::DRV_VOID_AMBIENT &&
+                  EU_DRIVER_TRACK_PMAX == deu::DRV_TRACK_PMAX,
+              "driver flags of the C ABI and the kernel agree");
+
 namespace dsph {
 void set_error_message(const std::string& m);
 }
@@ -432,6 +436,7 @@ struct Grid {
     Visc vw{};                   // implicit viscosity work arrays, allocated on first use
     int pin_floor = 0;           // driver adjustments after each step (eu_set_driver)
     int sponge_from = -1;
+    int driver_flags = 0;
 
     template <class T = double>
     T* alloc(int64_t count) {
@@ -525,9 +530,10 @@ struct Grid {
             else enqueue_correct_t<double>(p, g, g1, d, ctl, st, 2);
             launches++;
         }
-        if (pin_floor > 0 || sponge_from >= 0) {
-            if (!p.ref_r0) throw SphError(SPH_ERR_STATE, "the floor pin and sponge need a reference state (eu_set_ref)");
-            k_driver<<<grid_of(p.n), 256, 0, st>>>(p, g, ctl, pin_floor, sponge_from);
+        if (pin_floor > 0 || sponge_from >= 0 || driver_flags) {
+            if ((pin_floor > 0 || sponge_from >= 0) && !p.ref_r0)
+                throw SphError(SPH_ERR_STATE, "the floor pin and sponge need a reference state (eu_set_ref)");
+            k_driver<<<grid_of(p.n), 256, 0, st>>>(p, g, ctl, pin_floor, sponge_from, driver_flags);
             launches++;
         }
         k_end<<<1, 1, 0, st>>>(ctl);
@@ -776,7 +782,7 @@ int eu_set_ref(eu_grid* h) {
 int eu_clear_ref(eu_grid* h) {
     return guard([&] {
         deu::Grid* g = G(h);
-        g->pin_floor = 0;  // the driver adjustments relax toward the reference
+        g->pin_floor = 0;  // the floor pin and sponge act toward the reference
         g->sponge_from = -1;
         g->p.ref_r0 = nullptr;
         g->p.ref_p0 = nullptr;
@@ -948,15 +954,18 @@ int eu_step(eu_grid* h, double dt) {
     });
 }
 
-int eu_set_driver(eu_grid* h, int32_t pin_floor, int32_t sponge_from) {
+int eu_set_driver(eu_grid* h, int32_t pin_floor, int32_t sponge_from, int32_t flags) {
     return guard([&] {
         deu::Grid* g = G(h);
         if (pin_floor < 0 || pin_floor > g->p.nz) throw SphError(SPH_ERR_ARG, "pin_floor must be in [0, nz]");
         if (sponge_from >= g->p.nx) throw SphError(SPH_ERR_ARG, "sponge_from must be < nx (or negative: off)");
+        if (flags & ~(EU_DRIVER_PIN_STRESS | EU_DRIVER_VOID_AMBIENT | EU_DRIVER_TRACK_PMAX))
+            throw SphError(SPH_ERR_ARG, "unknown driver flag");
         if ((pin_floor > 0 || sponge_from >= 0) && !g->p.ref_r0)
             throw SphError(SPH_ERR_STATE, "the floor pin and sponge need a reference state (eu_set_ref)");
         g->pin_floor = pin_floor;
         g->sponge_from = sponge_from < 0 ? -1 : sponge_from;
+        g->driver_flags = flags;
         g->graph_valid = false;
     });
 }

@@ -958,12 +958,20 @@ static __global__ void k_correct(P p, Fields g, Fields g1, Rhs d, const Ctl* ctl
     void_cell(p, g, c);
 }
 
-// A driver's adjustments after each step, against the hydrostatic reference:
-// the lowest `pin` z-layers return to the reference density at rest with no
-// energy, then columns i >= isp relax toward the reference with weight
-// ((i - isp) / max(1, nx - 1 - isp))^2 (the crater mode's far-field floor pin
-// and radial sponge, hydro_cpu.cpp:634-637; isp < 0: no sponge).
-static __global__ void k_driver(P p, Fields g, const Ctl* ctl, int pin, int isp) {
+// Driver adjustments after each step (eu_set_driver), in this order:
+//   pin:   the lowest `pin` z-layers return to the reference density at rest
+//          with no energy (DRV_PIN_STRESS: and no deviatoric stress);
+//   isp:   columns i >= isp relax toward the reference with weight
+//          ((i - isp) / max(1, nx - 1 - isp))^2 (isp < 0: none);
+//   DRV_VOID_AMBIENT: near-void cells (rho < RHO_CFL) become ambient gas
+//          (0.27 kg/m^3) at rest with no energy and no stress;
+//   DRV_TRACK_PMAX: Pmax = max(Pmax, Pcell) per cell.
+// The crater mode's floor pin and radial sponge (hydro_cpu.cpp:634-637), the
+// collapse demo's held floor (893-894), the Prater run's void cleanup
+// (823-824) and the Pierazzo run's peak-pressure record (769).
+enum { DRV_PIN_STRESS = 1, DRV_VOID_AMBIENT = 2, DRV_TRACK_PMAX = 4 };
+
+static __global__ void k_driver(P p, Fields g, const Ctl* ctl, int pin, int isp, int flags) {
     const int64_t c = gtid();
     if (c >= p.n || !ctl->active) return;
     const int i = (int)(c / ((int64_t)p.ny * p.nz)), k = (int)(c % p.nz);
@@ -971,6 +979,8 @@ static __global__ void k_driver(P p, Fields g, const Ctl* ctl, int pin, int isp)
         g.q[F_R][c] = p.ref_r0[c];
         g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
         g.q[F_E][c] = 0;
+        if (flags & DRV_PIN_STRESS)
+            g.q[F_SXX][c] = g.q[F_SYY][c] = g.q[F_SZZ][c] = g.q[F_SXY][c] = g.q[F_SXZ][c] = g.q[F_SYZ][c] = 0;
     }
     if (isp >= 0 && i >= isp) {
         const int span = p.nx - 1 - isp;
@@ -980,6 +990,16 @@ static __global__ void k_driver(P p, Fields g, const Ctl* ctl, int pin, int isp)
         g.q[F_MV][c] *= (1 - sp);
         g.q[F_MW][c] *= (1 - sp);
         g.q[F_E][c] *= (1 - sp);
+    }
+    if ((flags & DRV_VOID_AMBIENT) && g.q[F_R][c] < p.rho_cfl) {
+        g.q[F_R][c] = 0.27;
+        g.q[F_MU][c] = g.q[F_MV][c] = g.q[F_MW][c] = 0;
+        g.q[F_E][c] = 0;
+        g.q[F_SXX][c] = g.q[F_SYY][c] = g.q[F_SZZ][c] = g.q[F_SXY][c] = g.q[F_SXZ][c] = g.q[F_SYZ][c] = 0;
+    }
+    if (flags & DRV_TRACK_PMAX) {
+        const double P = pcell(p, g, c);
+        if (P > g.q[F_PMAX][c]) g.q[F_PMAX][c] = P;
     }
 }
 

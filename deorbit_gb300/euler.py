@@ -20,6 +20,8 @@ from . import sph
 
 FIELDS = "r mu mv mw E Sxx Syy Szz Sxy Sxz Syz D af rc vib Pmax".split()
 FP64, MIXED = 0, 1  # eu_form: the Lop in FP64 (reference order) or in FP32 (state FP64)
+# eu_set_driver flags
+DRIVER_PIN_STRESS, DRIVER_VOID_AMBIENT, DRIVER_TRACK_PMAX = 1, 2, 4
 RHS = "r mu mv mw E Sxx Syy Szz Sxy Sxz Syz D rc vib".split()
 
 
@@ -66,7 +68,7 @@ _SIGS = {
     "eu_clear_ref": (C.c_int, [_P]),
     "eu_read_ref": (C.c_int, [_P, _D, _D, C.c_int64]),
     "eu_implicit_visc": (C.c_int, [_P, C.c_double]),
-    "eu_set_driver": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "eu_set_driver": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "eu_visc_iterations": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 }
 _declared = False
@@ -172,10 +174,10 @@ class Grid:
     def clear_ref(self):
         sph.check(lib().eu_clear_ref(self.h))
 
-    def set_driver(self, pin_floor=0, sponge_from=-1):
-        """Per-step floor pin and radial sponge against the reference state,
-        applied on the device after every step (eu_set_driver)."""
-        sph.check(lib().eu_set_driver(self.h, int(pin_floor), int(sponge_from)))
+    def set_driver(self, pin_floor=0, sponge_from=-1, flags=0):
+        """Per-step driver adjustments applied on the device after every step
+        (eu_set_driver): floor pin, radial sponge, DRIVER_* flags."""
+        sph.check(lib().eu_set_driver(self.h, int(pin_floor), int(sponge_from), int(flags)))
 
     def reference(self):
         r0, p0 = np.empty(self.n), np.empty(self.n)
@@ -288,6 +290,6 @@ def run_case(g, case, steps):
     """The drivers' loop on a grid built from `case`, with the case's floor pin
     and radial sponge applied on the device after every step
     (hydro_cpu.cpp:634-637, 855)."""
-    if case.pin_floor or case.sponge_from >= 0:
-        g.set_driver(case.pin_floor, case.sponge_from)
+    if case.pin_floor or case.sponge_from >= 0 or case.driver_flags:
+        g.set_driver(case.pin_floor, case.sponge_from, case.driver_flags)
     return g.run(case.cfl, case.t_end, steps)

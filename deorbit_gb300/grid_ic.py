@@ -33,6 +33,7 @@ class Case:
     post_ref: dict = field(default_factory=dict)  # ... then write these over them
     pin_floor: int = 0         # driver: the lowest pin_floor z-layers return to the reference each step
     sponge_from: int = -1      # driver: columns i >= sponge_from relax toward the reference each step
+    driver_flags: int = 0      # driver: euler.DRIVER_* steps after each step
 
     @property
     def n(self):
@@ -350,6 +351,132 @@ def bingham_heap(case=1, NX=112, NZ=20):
     return Case(f"bingham_{case}", (NX, 1, NZ), dx, ic.basalt(), prm,
                 {"r": r.reshape(-1), "E": np.zeros(NX * NZ), "af": af.reshape(-1)}, 0.4,
                 (400.0, 1200.0, 600.0)[case], set_ref=True, pin_floor=2)
+
+
+def lame_hoop(Nr=40, edot=1e-6):
+    """hydro_cpu.cpp:490-501 (lame A): a cylindrical basalt column in uniform
+    radial expansion u = edot r, unstressed; one Lop gives the hoop strain
+    rate's stress rates."""
+    dx, rho0 = 500.0, ic.basalt()["rho0"]
+    mu = rho0 * edot * ((np.arange(Nr) + 0.5) * dx)
+    return Case("lame_hoop", (Nr, 1, 1), dx, ic.basalt(), {"axisym": 1},
+                {"r": np.full(Nr, rho0), "E": np.zeros(Nr), "mu": mu})
+
+
+def lame_equilibrium(Nr=200, ia=20, ib=180):
+    """hydro_cpu.cpp:502-516 (lame B): the deviatoric stress of a thick
+    cylinder under internal pressure (S_rr = -B/r^2, S_thth = B/r^2) at rest;
+    one Lop's radial momentum balance."""
+    dx, rho0 = 500.0, ic.basalt()["rho0"]
+    ia_r = (ia + 0.5) * dx
+    bc = 2.0e6 * ia_r * ia_r
+    rr = (np.arange(Nr) + 0.5) * dx
+    inside = (np.arange(Nr) >= ia) & (np.arange(Nr) <= ib)
+    sxx = np.where(inside, -bc / (rr * rr), 0.0)
+    syy = np.where(inside, bc / (rr * rr), 0.0)
+    return Case("lame_equilibrium", (Nr, 1, 1), dx, ic.basalt(), {"axisym": 1},
+                {"r": np.full(Nr, rho0), "E": np.zeros(Nr), "Sxx": sxx, "Syy": syy})
+
+
+def af_visc_column(af, Nr=120, A=1e-9, eta=1e9):
+    """hydro_cpu.cpp:519-529 (af_visc): u = A r^2 in a cylindrical basalt
+    column, fluidized (af = 1) or not, explicit fluidization viscosity eta."""
+    dx, rho0 = 500.0, ic.basalt()["rho0"]
+    r = (np.arange(Nr) + 0.5) * dx
+    return Case(f"af_visc_{af}", (Nr, 1, 1), dx, ic.basalt(), {"axisym": 1, "eta_af": eta},
+                {"r": np.full(Nr, rho0), "E": np.zeros(Nr), "mu": rho0 * A * r * r, "af": np.full(Nr, float(af))})
+
+
+def vib_advect(N=200, v0=2000.0):
+    """hydro_cpu.cpp:530-539 (vib_advect): a Gaussian vibration bump in basalt
+    moving uniformly at v0 for 20 km (CFL 0.4)."""
+    dx, rho0 = 500.0, ic.basalt()["rho0"]
+    x0, wid = 0.3 * N * dx, 8e3
+    x = (np.arange(N) + 0.5) * dx
+    return Case("vib_advect", (N, 1, 1), dx, ic.basalt(), {},
+                {"r": np.full(N, rho0), "mu": np.full(N, rho0 * v0), "E": np.full(N, 0.5 * rho0 * v0 * v0),
+                 "vib": np.exp(-((x - x0) / wid) * ((x - x0) / wid))}, 0.4, 20e3 / v0)
+
+
+def af_shock(N=200, V=2000.0):
+    """hydro_cpu.cpp:865-873 (af_activate A): the left half of a basalt bar
+    moving at V into the right half, fluidization seeding on (TDEC 10 s,
+    C_ACT 0.5), for 3 s."""
+    dx, rho0 = 500.0, ic.basalt()["rho0"]
+    mu = np.where(np.arange(N) < N // 2, rho0 * V, 0.0)
+    return Case("af_shock", (N, 1, 1), dx, ic.basalt(), {"tdec": 10.0, "c_act": 0.5, "eta_af": 0.0},
+                {"r": np.full(N, rho0), "E": np.zeros(N), "mu": mu}, 0.4, 3.0)
+
+
+def af_decay(M=50, vib0=80.0):
+    """hydro_cpu.cpp:874-880 (af_activate B): basalt at rest with vibrations
+    vib0 (TDEC 0.5 s, C_ACT 0.5), for 5 s."""
+    dx, rho0 = 500.0, ic.basalt()["rho0"]
+    return Case("af_decay", (M, 1, 1), dx, ic.basalt(), {"tdec": 0.5, "c_act": 0.5, "eta_af": 0.0},
+                {"r": np.full(M, rho0), "E": np.zeros(M), "vib": np.full(M, vib0)}, 0.4, 5.0)
+
+
+def collapse(af_on, NX=80, NZ=40):
+    """hydro_cpu.cpp:883-900 (collapse): a lithostatic basalt step (14 km /
+    10 km) under gravity 3.71 with its column as the reference, fluidized
+    (af = 1, TDEC 1e6, explicit viscosity 1e9) or not, for 8 s with the two
+    lowest layers held (stress included)."""
+    rho0, A, gz, dx = 2700.0, 2.67e10, 3.71, 500.0
+    zlo, zhi = 10e3, 14e3
+    x = ((np.arange(NX) + 0.5) * dx)[:, None]
+    z = ((np.arange(NZ) + 0.5) * dx)[None, :]
+    zs = np.where(x < 0.5 * NX * dx, zhi, zlo)
+    solid = z < zs
+    r = np.where(solid, rho0 * (1.0 + rho0 * gz * (zs - z) / A), 0.27)
+    prm = {"gz": gz, "rho_cfl": 100.0, "rho_vac": 100.0, "tdec": 1e6 if af_on else 0.0,
+           "eta_af": 1e9 if af_on else 0.0}
+    f = {"r": r.reshape(-1), "E": np.zeros(NX * NZ)}
+    if af_on:
+        f["af"] = np.where(solid, 1.0, 0.0).reshape(-1)
+    return Case(f"collapse_{'af' if af_on else 'rigid'}", (NX, 1, NZ), dx, ic.basalt(), prm, f, 0.4, 8.0,
+                set_ref=True, pin_floor=2, driver_flags=1)
+
+
+def pierazzo2d(cppr=12.0, reach=12.0, U=5000.0, t_end=-1.0):
+    """hydro_cpu.cpp:753-798 (pierazzo2d): Pierazzo et al. 2008's Al-on-Al
+    benchmark, axisymmetric: an aluminium sphere of radius 1 m (no gravity:
+    scale-free) at U into an aluminium half-space, strengthless, ambient gas
+    above; CFL 0.3 until the shock has crossed 1.3 reach radii; the peak
+    pressure of every cell recorded after each step."""
+    mat = aluminum()
+    a, dx, rho0 = 1.0, 1.0 / cppr, mat["rho0"]
+    zsurf, zc = reach * a, reach * a + a
+    nr, nz = int(reach * a / dx + 0.5), int((reach + 3.0) * a / dx + 0.5)
+    r = ((np.arange(nr) + 0.5) * dx)[:, None]
+    z = ((np.arange(nz) + 0.5) * dx)[None, :]
+    proj = np.sqrt(r * r + (z - zc) * (z - zc)) < a
+    dens = np.where(proj | (z < zsurf), rho0, 0.27) * np.ones((nr, nz))
+    f = {"r": dens.reshape(-1), "mw": np.where(proj, -rho0 * U, 0.0).reshape(-1),
+         "E": np.where(proj, 0.5 * rho0 * U * U, 0.0).reshape(-1)}
+    c0 = math.sqrt(mat["A"] / rho0)
+    return Case(f"pierazzo2d_{U:.0f}", (nr, 1, nz), dx, mat, {"axisym": 1}, f, 0.3,
+                t_end if t_end > 0 else 1.3 * reach * a / c0, driver_flags=4)
+
+
+def prater(cppr=10.0, U=7000.0, Y=414e6, G=27.6e9, Rfac=8.0, t_end=70e-6, rho_cfl=100.0):
+    """hydro_cpu.cpp:799-846 (prater): Prater 1970's aluminium crater growth,
+    axisymmetric: a 3.175 mm aluminium sphere at U into aluminium with von
+    Mises strength Y and shear modulus G, vacuum-aware faces, CFL 0.3, the
+    near-void cells reset to ambient gas after each step, for t_end."""
+    mat = dict(aluminum())
+    mat["Y"], mat["G"] = float(Y), float(G)
+    a = 3.175e-3
+    dx, rho0 = a / cppr, mat["rho0"]
+    nr, nz = int(Rfac * a / dx + 0.5), int((Rfac + 3.0) * a / dx + 0.5)
+    zsurf, zc = Rfac * a, Rfac * a + a
+    r = ((np.arange(nr) + 0.5) * dx)[:, None]
+    z = ((np.arange(nz) + 0.5) * dx)[None, :]
+    proj = np.sqrt(r * r + (z - zc) * (z - zc)) < a
+    dens = np.where(proj | (z < zsurf), rho0, 0.27) * np.ones((nr, nz))
+    f = {"r": dens.reshape(-1), "mw": np.where(proj, -rho0 * U, 0.0).reshape(-1),
+         "E": np.where(proj, 0.5 * rho0 * U * U, 0.0).reshape(-1)}
+    return Case(f"prater_{cppr:g}", (nr, 1, nz), dx, mat, {"axisym": 1, "rho_vac": 100.0, "rho_cfl": float(rho_cfl)},
+                f, 0.3, t_end, driver_flags=2)
 
 
 GATES = {"sod": sod, "tracer": tracer, "sedov": sedov, "sedov_axi": sedov_axi, "shear": shear,

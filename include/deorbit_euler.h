@@ -106,14 +106,22 @@ int eu_clear_ref(eu_grid* g);
 int eu_read_ref(eu_grid* g, double* r0, double* p0, int64_t n);
 
 /* A driver's adjustments applied on the device after every step of eu_step /
- * eu_run, against the reference state: the lowest pin_floor z-layers return
- * to the reference density at rest with no energy; columns i >= sponge_from
- * relax toward it with weight ((i - sponge_from) / max(1, nx - 1 -
- * sponge_from))^2 (density blended, momentum and energy scaled).  The crater
- * mode's far-field floor pin and radial sponge (hydro_cpu.cpp:634-637: pin 2,
- * sponge from (int)(0.85 nx)); the substrate gate pins 2 layers.  0 / -1:
- * off (the default); eu_clear_ref turns both off. */
-int eu_set_driver(eu_grid* g, int32_t pin_floor, int32_t sponge_from);
+ * eu_run, in this order: the lowest pin_floor z-layers return to the
+ * reference density at rest with no energy (EU_DRIVER_PIN_STRESS: and no
+ * deviatoric stress); columns i >= sponge_from relax toward the reference
+ * with weight ((i - sponge_from) / max(1, nx - 1 - sponge_from))^2 (density
+ * blended, momentum and energy scaled); EU_DRIVER_VOID_AMBIENT: cells below
+ * rho_cfl become ambient gas (0.27 kg/m^3) at rest with no energy and stress;
+ * EU_DRIVER_TRACK_PMAX: each cell's Pmax keeps the largest pressure seen.
+ * These are the reference drivers' own per-step steps: the crater mode's
+ * floor pin and radial sponge (hydro_cpu.cpp:634-637: pin 2, sponge from
+ * (int)(0.85 nx)), the substrate gate's pin (855), the collapse demo's held
+ * floor (893-894), the Prater run's void cleanup (823-824) and the Pierazzo
+ * run's peak-pressure record (769).  The pin and the sponge need a reference
+ * state (eu_set_ref); eu_clear_ref turns them off.  0, -1, 0: none (the
+ * default). */
+enum { EU_DRIVER_PIN_STRESS = 1, EU_DRIVER_VOID_AMBIENT = 2, EU_DRIVER_TRACK_PMAX = 4 };
+int eu_set_driver(eu_grid* g, int32_t pin_floor, int32_t sponge_from, int32_t flags);
 
 /* Field i/o of one named field (n = nx*ny*nz doubles), or of several in one
  * call (copies overlap on the grid's stream, one synchronisation). */

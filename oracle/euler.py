@@ -226,23 +226,32 @@ def from_case(case, cls=OracleGrid):
     return g
 
 
-def drive(g, case, pin=None, isp=None):
-    """The crater / substrate drivers' adjustments after a step
-    (hydro_cpu.cpp:634-637, 855): the lowest `pin` (default case.pin_floor)
-    z-layers back to the reference density at rest with no energy, then
-    columns i >= isp (default case.sponge_from) relaxed toward the reference
-    with weight ((i - isp) / max(1, nx - 1 - isp))^2.  The reference density
-    is the case's pre-impact field (what set_ref froze)."""
+PIN_STRESS, VOID_AMBIENT, TRACK_PMAX = 1, 2, 4  # the C ABI's EU_DRIVER_* flags
+
+
+def drive(g, case, pin=None, isp=None, flags=None):
+    """The reference drivers' own adjustments after a step, in the order the
+    CUDA solver's eu_set_driver applies them: the lowest `pin` (default
+    case.pin_floor) z-layers back to the reference density at rest with no
+    energy (PIN_STRESS: no deviatoric stress either; hydro_cpu.cpp:634, 855,
+    893-894); columns i >= isp (default case.sponge_from) relaxed toward the
+    reference with weight ((i - isp) / max(1, nx - 1 - isp))^2 (635-637);
+    VOID_AMBIENT: cells below RHO_CFL to ambient gas at rest, no energy and
+    stress (823-824); TRACK_PMAX: Pmax = max(Pmax, Pcell) (769).  The
+    reference density is the case's pre-impact field (what set_ref froze)."""
     nx, ny, nz = case.shape
     pin = case.pin_floor if pin is None else pin
     isp = getattr(case, "sponge_from", -1) if isp is None else isp
-    if not pin and isp < 0:
+    flags = getattr(case, "driver_flags", 0) if flags is None else flags
+    if not pin and isp < 0 and not flags:
         return
-    ref = np.asarray(case.fields["r"], dtype=np.float64).reshape(nx, ny, nz)
-    f = {k: g.field(k).reshape(nx, ny, nz) for k in ("r", "mu", "mv", "mw", "E")}
+    names = ("r", "mu", "mv", "mw", "E", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz")
+    f = {k: g.field(k).reshape(nx, ny, nz) for k in names}
+    if pin or isp >= 0:
+        ref = np.asarray(case.fields["r"], dtype=np.float64).reshape(nx, ny, nz)
     if pin:
         f["r"][:, :, :pin] = ref[:, :, :pin]
-        for k in ("mu", "mv", "mw", "E"):
+        for k in ("mu", "mv", "mw", "E") + (names[5:] if flags & PIN_STRESS else ()):
             f[k][:, :, :pin] = 0.0
     if isp >= 0:
         for i in range(isp, nx):
@@ -251,15 +260,24 @@ def drive(g, case, pin=None, isp=None):
             f["r"][i] = (1 - sp) * f["r"][i] + sp * ref[i]
             for k in ("mu", "mv", "mw", "E"):
                 f[k][i] *= (1 - sp)
-    for k, v in f.items():
-        g.set_field(k, v)
+    if flags & VOID_AMBIENT:
+        v = f["r"] < g.params.rho_cfl
+        f["r"][v] = 0.27
+        for k in names[1:]:
+            f[k][v] = 0.0
+    for k, a in f.items():
+        g.set_field(k, a)
+    if flags & TRACK_PMAX:
+        pm = g.field("Pmax")
+        P = np.array([g.pcell(c) for c in range(g.n)])
+        g.set_field("Pmax", np.where(P > pm, P, pm))
 
 
 def run_case(g, case, steps):
     """The drivers' loop on a grid built from `case` (steps of step_rk2 at
     dt = cfl dx / maxspeed clipped at t_end), with the case's floor pin and
     sponge after every step (hydro_cpu.cpp:634-637, 855): returns (steps, t)."""
-    if not case.pin_floor and getattr(case, "sponge_from", -1) < 0:
+    if not case.pin_floor and getattr(case, "sponge_from", -1) < 0 and not getattr(case, "driver_flags", 0):
         return g.run(case.cfl, case.t_end, steps)
     t, s = 0.0, 0
     while t < case.t_end and s < steps:
@@ -282,10 +300,10 @@ class DrivenGrid:
         self.case = case
         self.g = from_case(case, cls)
         self.t = 0.0
-        self.pin, self.isp = 0, -1
+        self.pin, self.isp, self.flags = 0, -1, 0
 
-    def set_driver(self, pin_floor=0, sponge_from=-1):
-        self.pin, self.isp = int(pin_floor), int(sponge_from)
+    def set_driver(self, pin_floor=0, sponge_from=-1, flags=0):
+        self.pin, self.isp, self.flags = int(pin_floor), int(sponge_from), int(flags)
 
     def reference(self):
         return np.asarray(self.case.fields["r"], dtype=np.float64).copy(), None
@@ -297,7 +315,7 @@ class DrivenGrid:
             if self.t + dt > t_end:
                 dt = t_end - self.t
             self.g.step(dt)
-            drive(self.g, self.case, self.pin, self.isp)
+            drive(self.g, self.case, self.pin, self.isp, self.flags)
             self.t += dt
             s += 1
         return s, self.t

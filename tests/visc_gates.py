@@ -25,10 +25,10 @@ class OracleGrid:
         self.EO, self.case = EO, case
         self.g = EO.from_case(case)
         self.t = 0.0
-        self.pin, self.isp = 0, -1
+        self.pin, self.isp, self.flags = 0, -1, 0
 
-    def set_driver(self, pin_floor=0, sponge_from=-1):
-        self.pin, self.isp = pin_floor, sponge_from
+    def set_driver(self, pin_floor=0, sponge_from=-1, flags=0):
+        self.pin, self.isp, self.flags = pin_floor, sponge_from, flags
 
     def read(self, name):
         return self.g.field(name)
@@ -48,6 +48,15 @@ class OracleGrid:
     def visc_iters(self):
         return self.g.visc_iters()
 
+    def lop(self):
+        self.g.lop()
+
+    def rhs(self, name):
+        return self.g.rhs(name)
+
+    def pressure(self):
+        return np.array([self.g.pcell(c) for c in range(self.g.n)])
+
     def run(self, cfl, t_end, max_steps=-1):
         s = 0
         while self.t < t_end and (max_steps < 0 or s < max_steps):
@@ -55,7 +64,7 @@ class OracleGrid:
             if self.t + dt > t_end:
                 dt = t_end - self.t
             self.g.step(dt)
-            self.EO.drive(self.g, self.case, self.pin, self.isp)
+            self.EO.drive(self.g, self.case, self.pin, self.isp, self.flags)
             self.t += dt
             s += 1
         return s, self.t
