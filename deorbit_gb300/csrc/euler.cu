@@ -622,6 +622,7 @@ void to_params(deu::P& p, const eu_params& e) {
 // on the host with the host library's pow.
 void derive(deu::P& p) {
     const deu::Mat& m = p.m;
+    p.mf = deu::mat_as<float>(m);
     p.eps_act = (m.Emod > 0 && m.wk > 0) ? std::pow(1.0 / (m.wk * p.dx * p.dx * p.dx), 1.0 / m.wm) : 0.0;
     p.invdx = 1.0 / p.dx;
 }

@@ -36,6 +36,7 @@ __host__ __device__ __forceinline__ MatT<R> mat_as(const Mat& m) {
 // Settings + material + grid geometry, passed by value to every kernel.
 struct P {
     Mat m;
+    MatT<float> mf;  // the material rounded to FP32 once on the host (for the FP32 form)
     double gz, tdec, eta_af, c_act, p_coh, p_act, rho_cfl, damp, rho_vac;
     double y_i0, mu_i, mu_d, y_d0, y_m, y_bingham, c_reg, af_sat;
     int32_t axisym, rock, af_reg, af_prel, af_seeddp;
@@ -52,6 +53,15 @@ struct P {
     int32_t void_cons;  // VOID_CONS: the reset moves the excess mass to a neighbour first
     int32_t visc_imp;   // VISC_IMP: fluidization viscosity by the implicit solve, not in the Lop
 };
+
+// The material in the compute type R: FP64 as given, FP32 as rounded once on
+// the host (the same values a per-thread conversion gives, without the
+// per-thread conversions, which run on the FP64 pipe).
+template <class R>
+__device__ __forceinline__ MatT<R> mat_of(const P& p) {
+    if constexpr (sizeof(R) == 4) return p.mf;
+    else return p.m;
+}
 
 template <class R> __device__ __forceinline__ R dmax2(R a, R b) { return a < b ? b : a; }  // std::max
 template <class R> __device__ __forceinline__ R dmin2(R a, R b) { return b < a ? b : a; }  // std::min
@@ -337,7 +347,7 @@ static __device__ __forceinline__ double eint_r(double r, double mu, double mv, 
 template <class R>
 static __device__ __forceinline__ double pcell_r(const P& p, const Fields& s, int64_t c) {
     const double r = s.q[F_R][c];
-    R pr = pressure(mat_as<R>(p.m), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
+    R pr = pressure(mat_of<R>(p), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
     if (pr < R(0)) pr = R(0);
     return double(pr);
 }
@@ -373,7 +383,7 @@ static __device__ void vonmises_cell(const P& p, const Fields& s, const double* 
         R Peff = Pp;
         if (p.af_prel && s.q[F_VIB][c] > 0) {
             R p2, cs2;
-            eos_pc(mat_as<R>(p.m), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2,
+            eos_pc(mat_of<R>(p), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2,
                    cs2);
             Peff = dmax2(Pp - R(r) * cs2 * R(s.q[F_VIB][c]), R(0));
         }
@@ -445,7 +455,7 @@ static __global__ void __launch_bounds__(256) k_maxspeed(P p, Fields g, Ctl* ctl
             const double mu = g.q[F_MU][c], mv = g.q[F_MV][c], mw = g.q[F_MW][c];
             const R rr = R(r);
             R pr, cs;
-            eos_pc(mat_as<R>(p.m), rr, R(eint_r<R>(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
+            eos_pc(mat_of<R>(p), rr, R(eint_r<R>(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
             R cel = sqrt(cs * cs + (p.m.G > 0 ? R(4.0 / 3.0) * R(p.m.G) / rr : R(0)));
             R v = sqrt(R(mu) * R(mu) + R(mv) * R(mv) + R(mw) * R(mw)) / rr;
             s = dmax2(s, double(v + cel));
@@ -593,7 +603,7 @@ static __global__ void __launch_bounds__(256) k_face(P p, PrimT<R> W, FacesT<R> 
         }
     }
     constexpr int in = DIR == 0 ? 1 : (DIR == 1 ? 2 : 3), it1 = DIR == 0 ? 2 : 1, it2 = DIR == 2 ? 2 : 3;
-    const MatT<R> m = mat_as<R>(p.m);
+    const MatT<R> m = mat_of<R>(p);
     F5<R> fl;
     if (DIR == 2 && p.ref_p0) {  // well-balanced: reconstruct the deviation from the reference (hydro_cpu.cpp:114-119)
         const R* dv = W.w[6];
@@ -623,10 +633,10 @@ static __global__ void __launch_bounds__(256) k_face(P p, PrimT<R> W, FacesT<R> 
 // operation of the reference, in its order).
 // Resident blocks per SM asked of the right-hand side (launch bounds) in the
 // FP32 form; the FP64 form keeps 3.  The FP32 form waits on neighbour loads at
-// low occupancy: 256^3 impact, mixed step 21.0 / 19.1 / 18.3 / 17.7 / 17.4 ms at
-// 3 / 4 / 5 / 6 / 7 blocks (141 registers; 128, 96, 80, 72 with spills).
+// low occupancy: 256^3 impact, mixed step 16.2 / 15.3 / 15.0 ms at 5 / 7 / 8
+// blocks (80 / 72 / 64 registers, with spills to L1).
 #ifndef DEU_RHS_MINB_F32
-#define DEU_RHS_MINB_F32 7
+#define DEU_RHS_MINB_F32 8
 #endif
 template <class R>
 static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 : 3)
@@ -639,7 +649,11 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
     const int j = (int)(rem / p.nz), k = (int)(rem - (int64_t)j * p.nz);
     const double* r = s.q[F_R];
     const double* mw = s.q[F_MW];
-    double dr = 0.0, dE = 0.0, drc = 0.0, dmu = 0.0, dmv = 0.0, dmw = 0.0;
+    // Sums of the right-hand side: FP64 in the FP64 form (the reference's
+    // additions); in the FP32 form the terms are FP32 already and are summed
+    // in FP32 (in the same order) and widened once at the store.
+    using A = R;
+    A dr = A(0), dE = A(0), drc = A(0), dmu = A(0), dmv = A(0), dmw = A(0);
     // ---- hydro sweeps (hydro_cpu.cpp:122-133), x then y then z
     {
         const int64_t lo[3] = {c, ((int64_t)i * (p.ny + 1) + j) * p.nz + k, ((int64_t)i * p.ny + j) * (p.nz + 1) + k};
@@ -658,7 +672,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
                 dt1 = -(w1 * Fq[2][b] - w0 * Fq[2][a]) * inv;
                 dt2 = -(w1 * Fq[3][b] - w0 * Fq[3][a]) * inv;
                 R pr, cs;
-                eos_pc(mat_as<R>(p.m), W.w[0][c], W.w[4][c], pr, cs);  // Pcell: EOS at the cell's internal energy
+                eos_pc(mat_of<R>(p), W.w[0][c], W.w[4][c], pr, cs);  // Pcell: EOS at the cell's internal energy
                 dmn += pr / R((i + 0.5) * p.dx);
             } else {  // face weights 1 (exact products)
                 const R inv = R(p.invdx);
@@ -669,29 +683,29 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
                 dt1 = -(Fq[2][b] - Fq[2][a]) * inv;
                 dt2 = -(Fq[3][b] - Fq[3][a]) * inv;
             }
-            dr += double(vr);
-            dE += double(vE);
-            drc += double(vrc);
+            dr += A(vr);
+            dE += A(vE);
+            drc += A(vrc);
             if (dir == 0) {
-                dmu += double(dmn); dmv += double(dt1); dmw += double(dt2);
+                dmu += A(dmn); dmv += A(dt1); dmw += A(dt2);
             } else if (dir == 1) {
-                dmv += double(dmn); dmu += double(dt1); dmw += double(dt2);
+                dmv += A(dmn); dmu += A(dt1); dmw += A(dt2);
             } else {
-                dmw += double(dmn); dmu += double(dt1); dmv += double(dt2);
+                dmw += A(dmn); dmu += A(dt1); dmv += A(dt2);
             }
         }
     }
     if (p.gz != 0.0) {
         if (!p.ref_r0) {  // plain gravity body force, hydro_cpu.cpp:137-138
-            dmw += -p.gz * r[c];
-            dE += -p.gz * mw[c];
+            dmw += A(-p.gz * r[c]);
+            dE += A(-p.gz * mw[c]);
         } else {  // well-balanced source against the reference, hydro_cpu.cpp:139-143
             const double* R0 = p.ref_r0;
-            dmw += -p.gz * (r[c] - R0[c]) + p.ref_dp[c] * p.invdx;  // ref_dp: k_ref_dp
-            dE += -p.gz * mw[c];
+            dmw += A(-p.gz * (r[c] - R0[c]) + p.ref_dp[c] * p.invdx);  // ref_dp: k_ref_dp
+            dE += A(-p.gz * mw[c]);
         }
     }
-    double dS[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, dD = 0.0, dvib = 0.0;
+    A dS[6] = {A(0), A(0), A(0), A(0), A(0), A(0)}, dD = A(0), dvib = A(0);
     // near-void cell (rho < RHO_CFL): the FP32 form reads k_prim's flags
     auto is_void = [&](int64_t q) -> bool {
         if constexpr (sizeof(R) == 4) return W.vd[q] != 0;
@@ -749,45 +763,45 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
             R az = w > R(0) ? (sc - R(S[zm])) / iz_ : (R(S[zp]) - sc) / izp;
             return u * ax + v * ay + w * az;
         };
-        dS[0] = 0.0 + double(R(2) * G * (exx - tr) + Jm[0][0] - adv(Sxx));
-        dS[1] = 0.0 + double(R(2) * G * (eyy - tr) + Jm[1][1] - adv(Syy));
-        dS[2] = 0.0 + double(R(2) * G * (ezz - tr) + Jm[2][2] - adv(Szz));
-        dS[3] = 0.0 + double(R(2) * G * exy + Jm[0][1] - adv(Sxy));
-        dS[4] = 0.0 + double(R(2) * G * exz + Jm[0][2] - adv(Sxz));
-        dS[5] = 0.0 + double(R(2) * G * eyz + Jm[1][2] - adv(Syz));
-        dD = 0.0 + double(-adv(W.sq[6]));
-        dvib = 0.0 + double(-adv(W.sq[7]));
+        dS[0] = A(0) + A(R(2) * G * (exx - tr) + Jm[0][0] - adv(Sxx));
+        dS[1] = A(0) + A(R(2) * G * (eyy - tr) + Jm[1][1] - adv(Syy));
+        dS[2] = A(0) + A(R(2) * G * (ezz - tr) + Jm[2][2] - adv(Szz));
+        dS[3] = A(0) + A(R(2) * G * exy + Jm[0][1] - adv(Sxy));
+        dS[4] = A(0) + A(R(2) * G * exz + Jm[0][2] - adv(Sxz));
+        dS[5] = A(0) + A(R(2) * G * eyz + Jm[1][2] - adv(Syz));
+        dD = A(0) + A(-adv(W.sq[6]));
+        dvib = A(0) + A(-adv(W.sq[7]));
         // div S into momentum (central differences), hydro_cpu.cpp:183-186
         auto cd = [&](const R* S, int64_t q1, int64_t q0, R h) { return (R(S[q1]) - R(S[q0])) / h; };
         const R dSxx_x = cd(Sxx, xp, xm, hx), dSxy_y = cd(Sxy, yp, ym, hy), dSxz_z = cd(Sxz, zp, zm, hz);
         const R dSxy_x = cd(Sxy, xp, xm, hx), dSyy_y = cd(Syy, yp, ym, hy), dSyz_z = cd(Syz, zp, zm, hz);
         const R dSxz_x = cd(Sxz, xp, xm, hx), dSyz_y = cd(Syz, yp, ym, hy), dSzz_z = cd(Szz, zp, zm, hz);
-        dmu += double(dSxx_x + dSxy_y + dSxz_z);
-        dmv += double(dSxy_x + dSyy_y + dSyz_z);
-        dmw += double(dSxz_x + dSyz_y + dSzz_z);
+        dmu += A(dSxx_x + dSxy_y + dSxz_z);
+        dmv += A(dSxy_x + dSyy_y + dSyz_z);
+        dmw += A(dSxz_x + dSyz_y + dSzz_z);
         if (p.axisym) {
-            dmu += double((sxx - syy) / rcyl);
-            dmw += double(sxz / rcyl);
+            dmu += A((sxx - syy) / rcyl);
+            dmw += A(sxz / rcyl);
         }
         if (af[c] > 0 && p.eta_af > 0 && !p.visc_imp) {  // explicit fluidization viscosity, hydro_cpu.cpp:190-197
             const R eta = R(af[c] * p.eta_af), id2 = R(1.0 / (p.dx * p.dx));
             auto vx = [&](int64_t q) { return Vx[q]; };
             auto vy = [&](int64_t q) { return Vy[q]; };
             auto vz = [&](int64_t q) { return Vz[q]; };
-            dmu += double(eta * (vx(xp) + vx(xm) + vx(yp) + vx(ym) + vx(zp) + vx(zm) - R(6) * vx(c)) * id2);
-            dmv += double(eta * (vy(xp) + vy(xm) + vy(yp) + vy(ym) + vy(zp) + vy(zm) - R(6) * vy(c)) * id2);
-            dmw += double(eta * (vz(xp) + vz(xm) + vz(yp) + vz(ym) + vz(zp) + vz(zm) - R(6) * vz(c)) * id2);
+            dmu += A(eta * (vx(xp) + vx(xm) + vx(yp) + vx(ym) + vx(zp) + vx(zm) - R(6) * vx(c)) * id2);
+            dmv += A(eta * (vy(xp) + vy(xm) + vy(yp) + vy(ym) + vy(zp) + vy(zm) - R(6) * vy(c)) * id2);
+            dmw += A(eta * (vz(xp) + vz(xm) + vz(yp) + vz(ym) + vz(zp) + vz(zm) - R(6) * vz(c)) * id2);
             if (p.axisym) {
-                dmu += double(eta * (Lxx / rcyl - vxc / (rcyl * rcyl)));
-                dmw += double(eta * (Lzx / rcyl));
+                dmu += A(eta * (Lxx / rcyl - vxc / (rcyl * rcyl)));
+                dmw += A(eta * (Lzx / rcyl));
             }
         }
         // div(S.v) into energy, hydro_cpu.cpp:198-203
         auto svx = [&](int64_t q) { return R(Sxx[q]) * Vx[q] + R(Sxy[q]) * Vy[q] + R(Sxz[q]) * Vz[q]; };
         auto svy = [&](int64_t q) { return R(Sxy[q]) * Vx[q] + R(Syy[q]) * Vy[q] + R(Syz[q]) * Vz[q]; };
         auto svz = [&](int64_t q) { return R(Sxz[q]) * Vx[q] + R(Syz[q]) * Vy[q] + R(Szz[q]) * Vz[q]; };
-        dE += double((svx(xp) - svx(xm)) / hx + (svy(yp) - svy(ym)) / hy + (svz(zp) - svz(zm)) / hz);
-        if (p.axisym) dE += double(svx(c) / rcyl);
+        dE += A((svx(xp) - svx(xm)) / hx + (svy(yp) - svy(ym)) / hy + (svz(zp) - svz(zm)) / hz);
+        if (p.axisym) dE += A(svx(c) / rcyl);
     }
     d.q[D_R][c] = dr;
     d.q[D_MU][c] = dmu;
