@@ -964,10 +964,12 @@ int eu_set_driver(eu_grid* h, int32_t pin_floor, int32_t sponge_from, int32_t fl
             throw SphError(SPH_ERR_ARG, "unknown driver flag");
         if ((pin_floor > 0 || sponge_from >= 0) && !g->p.ref_r0)
             throw SphError(SPH_ERR_STATE, "the floor pin and sponge need a reference state (eu_set_ref)");
+        const int isp = sponge_from < 0 ? -1 : sponge_from;
+        if (pin_floor == g->pin_floor && isp == g->sponge_from && flags == g->driver_flags) return;
         g->pin_floor = pin_floor;
-        g->sponge_from = sponge_from < 0 ? -1 : sponge_from;
+        g->sponge_from = isp;
         g->driver_flags = flags;
-        g->graph_valid = false;
+        g->graph_valid = false;  // the step graph holds the adjustments
     });
 }
 
