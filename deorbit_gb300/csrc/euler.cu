@@ -625,6 +625,10 @@ void derive(deu::P& p) {
     p.mf = deu::mat_as<float>(m);
     p.eps_act = (m.Emod > 0 && m.wk > 0) ? std::pow(1.0 / (m.wk * p.dx * p.dx * p.dx), 1.0 / m.wm) : 0.0;
     p.invdx = 1.0 / p.dx;
+    p.cf.y_i0 = (float)p.y_i0; p.cf.mu_i = (float)p.mu_i; p.cf.ymi = (float)(p.y_m - p.y_i0);
+    p.cf.y_d0 = (float)p.y_d0; p.cf.mu_d = (float)p.mu_d; p.cf.y_m = (float)p.y_m;
+    p.cf.y_bingham = (float)p.y_bingham; p.cf.c_reg = (float)p.c_reg; p.cf.eps_act = (float)p.eps_act;
+    p.cf.dx = (float)p.dx; p.cf.invdx = (float)p.invdx; p.cf.rho_vac = (float)p.rho_vac;
 }
 
 }  // namespace
@@ -755,6 +759,7 @@ int eu_set_params(eu_grid* h, const eu_params* e) {
         if (!(e->damp >= 0) || !(e->damp <= 1.0)) throw SphError(SPH_ERR_ARG, "damp must be in [0, 1]");
         if (!(e->void_amb >= 0)) throw SphError(SPH_ERR_ARG, "void_amb must be >= 0");
         to_params(g->p, *e);
+        derive(g->p);  // the FP32 copies of the settings
         g->graph_valid = false;
     });
 }

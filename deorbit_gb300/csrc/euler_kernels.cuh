@@ -37,6 +37,10 @@ __host__ __device__ __forceinline__ MatT<R> mat_as(const Mat& m) {
 struct P {
     Mat m;
     MatT<float> mf;  // the material rounded to FP32 once on the host (for the FP32 form)
+    // settings the FP32 form reads, rounded to FP32 once on the host (ymi: y_m - y_i0)
+    struct {
+        float y_i0, mu_i, ymi, y_d0, mu_d, y_m, y_bingham, c_reg, eps_act, dx, invdx, rho_vac;
+    } cf;
     double gz, tdec, eta_af, c_act, p_coh, p_act, rho_cfl, damp, rho_vac;
     double y_i0, mu_i, mu_d, y_d0, y_m, y_bingham, c_reg, af_sat;
     int32_t axisym, rock, af_reg, af_prel, af_seeddp;
@@ -62,6 +66,20 @@ __device__ __forceinline__ MatT<R> mat_of(const P& p) {
     if constexpr (sizeof(R) == 4) return p.mf;
     else return p.m;
 }
+
+// A setting in the compute type R: FP64 as given, FP32 as rounded on the host.
+#define EU_SETTING(R, name) (sizeof(R) == 4 ? R(p.cf.name) : R(p.name))
+
+// x in the compute type R (FP64: x itself) and back to FP64.  (Conversions by
+// integer operations instead of the hardware's were tried: bit-identical, but
+// the 256^3 mixed step went from 14.9 to 16.2 ms -- the conversions are not
+// what keeps the FP64 pipe busy; the FP64 state arithmetic is.)
+template <class R>
+__device__ __forceinline__ R narrow(double x) {
+    return R(x);
+}
+__device__ __forceinline__ double widen(float y) { return (double)y; }
+__device__ __forceinline__ double widen(double y) { return y; }
 
 template <class R> __device__ __forceinline__ R dmax2(R a, R b) { return a < b ? b : a; }  // std::max
 template <class R> __device__ __forceinline__ R dmin2(R a, R b) { return b < a ? b : a; }  // std::min
@@ -347,9 +365,10 @@ static __device__ __forceinline__ double eint_r(double r, double mu, double mv, 
 template <class R>
 static __device__ __forceinline__ double pcell_r(const P& p, const Fields& s, int64_t c) {
     const double r = s.q[F_R][c];
-    R pr = pressure(mat_of<R>(p), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
+    R pr = pressure(mat_of<R>(p), narrow<R>(r),
+                    narrow<R>(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])));
     if (pr < R(0)) pr = R(0);
-    return double(pr);
+    return widen(pr);
 }
 
 // A cell's Pcell formed at most once per state and shared by the damage
@@ -377,42 +396,45 @@ static __device__ void vonmises_cell(const P& p, const Fields& s, const double* 
     if (p.m.Y <= 0 && !p.rock) return;
     R Y;
     const double r = s.q[F_R][c];
-    const R afc = R(af[c]);
+    const R afc = narrow<R>(af[c]);
     if (p.rock) {
         R Pp = R(dmax2(pc.get(p, s, c), 0.0));
         R Peff = Pp;
         if (p.af_prel && s.q[F_VIB][c] > 0) {
             R p2, cs2;
-            eos_pc(mat_of<R>(p), R(r), R(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2,
-                   cs2);
-            Peff = dmax2(Pp - R(r) * cs2 * R(s.q[F_VIB][c]), R(0));
+            eos_pc(mat_of<R>(p), narrow<R>(r),
+                   narrow<R>(eint_r<R>(r, s.q[F_MU][c], s.q[F_MV][c], s.q[F_MW][c], s.q[F_E][c])), p2, cs2);
+            Peff = dmax2(Pp - narrow<R>(r) * cs2 * narrow<R>(s.q[F_VIB][c]), R(0));
         }
-        R Yi = R(p.y_i0) + R(p.mu_i) * Peff / (R(1) + R(p.mu_i) * Peff / dmax2(R(p.y_m - p.y_i0), R(1)));
-        R Yd = dmin2(R(p.y_d0) + R(p.mu_d) * Peff, R(p.y_m));
-        const R D = R(s.q[F_D][c]);
+        const R mu_i = EU_SETTING(R, mu_i);
+        const R ymi = sizeof(R) == 4 ? R(p.cf.ymi) : R(p.y_m - p.y_i0);
+        R Yi = EU_SETTING(R, y_i0) + mu_i * Peff / (R(1) + mu_i * Peff / dmax2(ymi, R(1)));
+        R Yd = dmin2(EU_SETTING(R, y_d0) + EU_SETTING(R, mu_d) * Peff, EU_SETTING(R, y_m));
+        const R D = narrow<R>(s.q[F_D][c]);
         R Yb = (R(1) - D) * Yi + D * Yd;
         Y = p.af_prel ? Yb : Yb * (R(1) - afc);
         if (p.y_bingham > 0 && afc > R(1e-3)) {
-            R Yf = dmin2(R(p.y_bingham), Yb);
+            R Yf = dmin2(EU_SETTING(R, y_bingham), Yb);
             if (Y < Yf) Y = Yf;
         }
     } else {
-        Y = (R(1) - R(s.q[F_D][c])) * (R(1) - afc) * R(p.m.Y);
+        Y = (R(1) - narrow<R>(s.q[F_D][c])) * (R(1) - afc) * mat_of<R>(p).Y;
     }
     const double sxx = s.q[F_SXX][c], syy = s.q[F_SYY][c], szz = s.q[F_SZZ][c], sxy = s.q[F_SXY][c],
                  sxz = s.q[F_SXZ][c], syz = s.q[F_SYZ][c];
-    const R xx = R(sxx), yy = R(syy), zz = R(szz), xy = R(sxy), xz = R(sxz), yz = R(syz);
+    const R xx = narrow<R>(sxx), yy = narrow<R>(syy), zz = narrow<R>(szz), xy = narrow<R>(sxy),
+            xz = narrow<R>(sxz), yz = narrow<R>(syz);
     R J2 = R(0.5) * (xx * xx + yy * yy + zz * zz) + xy * xy + xz * xz + yz * yz;
     R vm = sqrt(R(3) * J2);
     if (vm > Y) {
-        const double f = double(vm > R(0) ? Y / vm : R(0));
+        const double f = widen(vm > R(0) ? Y / vm : R(0));
         s.q[F_SXX][c] = sxx * f; s.q[F_SYY][c] = syy * f; s.q[F_SZZ][c] = szz * f;
         s.q[F_SXY][c] = sxy * f; s.q[F_SXZ][c] = sxz * f; s.q[F_SYZ][c] = syz * f;
         if (p.af_reg && reg && p.m.G > 0 && (p.rho_cfl <= 0 || r > p.rho_cfl)) {
-            R dW = (vm * vm - Y * Y) / (R(6) * R(p.m.G));
-            const R vb = R(s.q[F_VIB][c]);
-            s.q[F_VIB][c] = double(sqrt(vb * vb + R(2) * R(p.c_reg) * dW / R(r)));
-            s.q[F_E][c] -= double(R(p.c_reg) * dW);
+            R dW = (vm * vm - Y * Y) / (R(6) * mat_of<R>(p).G);
+            const R vb = narrow<R>(s.q[F_VIB][c]);
+            s.q[F_VIB][c] = widen(sqrt(vb * vb + R(2) * EU_SETTING(R, c_reg) * dW / narrow<R>(r)));
+            s.q[F_E][c] -= widen(EU_SETTING(R, c_reg) * dW);
         }
     }
 }
@@ -425,11 +447,13 @@ static __device__ void grow_damage_cell(const P& p, const Fields& g, int64_t c, 
     double* D = g.q[F_D];
     if (D[c] >= 1.0) return;
     const R Pp = R(pc.get(p, g, c));
-    const R sigmax = dmax2(-Pp + R(g.q[F_SXX][c]), dmax2(-Pp + R(g.q[F_SYY][c]), -Pp + R(g.q[F_SZZ][c])));
-    if (sigmax > R(0) && sigmax / R(p.m.Emod) > R(p.eps_act)) {
-        R cg = R(0.4) * sqrt(R(p.m.Emod) / dmax2(R(g.q[F_R][c]), R(1e-30))), Rs = R(0.5) * R(p.dx);
-        R d13 = pow(R(D[c]), R(1) / R(3)) + (cg / Rs) * R(dt);
-        D[c] = double(dmin2(R(1), d13 * d13 * d13));
+    const R sigmax = dmax2(-Pp + narrow<R>(g.q[F_SXX][c]),
+                           dmax2(-Pp + narrow<R>(g.q[F_SYY][c]), -Pp + narrow<R>(g.q[F_SZZ][c])));
+    if (sigmax > R(0) && sigmax / mat_of<R>(p).Emod > EU_SETTING(R, eps_act)) {
+        R cg = R(0.4) * sqrt(mat_of<R>(p).Emod / dmax2(narrow<R>(g.q[F_R][c]), R(1e-30))),
+          Rs = R(0.5) * EU_SETTING(R, dx);
+        R d13 = pow(narrow<R>(D[c]), R(1) / R(3)) + (cg / Rs) * R(dt);
+        D[c] = widen(dmin2(R(1), d13 * d13 * d13));
     }
 }
 
@@ -453,12 +477,13 @@ static __global__ void __launch_bounds__(256) k_maxspeed(P p, Fields g, Ctl* ctl
         const double r = g.q[F_R][c];
         if (!(r < p.rho_cfl)) {
             const double mu = g.q[F_MU][c], mv = g.q[F_MV][c], mw = g.q[F_MW][c];
-            const R rr = R(r);
+            const R rr = narrow<R>(r);
             R pr, cs;
-            eos_pc(mat_of<R>(p), rr, R(eint_r<R>(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
-            R cel = sqrt(cs * cs + (p.m.G > 0 ? R(4.0 / 3.0) * R(p.m.G) / rr : R(0)));
-            R v = sqrt(R(mu) * R(mu) + R(mv) * R(mv) + R(mw) * R(mw)) / rr;
-            s = dmax2(s, double(v + cel));
+            eos_pc(mat_of<R>(p), rr, narrow<R>(eint_r<R>(r, mu, mv, mw, g.q[F_E][c])), pr, cs);
+            R cel = sqrt(cs * cs + (p.m.G > 0 ? R(4.0 / 3.0) * mat_of<R>(p).G / rr : R(0)));
+            const R fu = narrow<R>(mu), fv = narrow<R>(mv), fw = narrow<R>(mw);
+            R v = sqrt(fu * fu + fv * fv + fw * fw) / rr;
+            s = dmax2(s, widen(v + cel));
         }
     }
     for (int o = 16; o > 0; o >>= 1) s = dmax2(s, __shfl_xor_sync(0xffffffffu, s, o));
@@ -507,21 +532,21 @@ static __global__ void k_prim(P p, Fields s, PrimT<R> W, const Ctl* ctl) {
     if constexpr (sizeof(R) == 4) {
         const double inv = 1.0 / r, vx = mu * inv, vy = mv * inv, vz = mw * inv;
         const double e = (E - 0.5 * (mu * vx + mv * vy + mw * vz)) * inv;
-        W.w[0][c] = R(r);
-        W.w[1][c] = R(vx);
-        W.w[2][c] = R(vy);
-        W.w[3][c] = R(vz);
-        W.w[4][c] = R(e);
-        W.w[5][c] = R(rc * inv);
+        W.w[0][c] = narrow<R>(r);
+        W.w[1][c] = narrow<R>(vx);
+        W.w[2][c] = narrow<R>(vy);
+        W.w[3][c] = narrow<R>(vz);
+        W.w[4][c] = narrow<R>(e);
+        W.w[5][c] = narrow<R>(rc * inv);
         if (p.ref_p0) {
             double pr = pressure(p.m, r, e);
             if (pr < 0) pr = 0;
-            W.w[6][c] = R(pr - p.ref_p0[c]);
+            W.w[6][c] = narrow<R>(pr - p.ref_p0[c]);
         }
 #pragma unroll
-        for (int q = 0; q < 6; q++) W.sq[q][c] = R(s.q[F_SXX + q][c]);
-        W.sq[6][c] = R(s.q[F_D][c]);
-        W.sq[7][c] = R(s.q[F_VIB][c]);
+        for (int q = 0; q < 6; q++) W.sq[q][c] = narrow<R>(s.q[F_SXX + q][c]);
+        W.sq[6][c] = narrow<R>(s.q[F_D][c]);
+        W.sq[7][c] = narrow<R>(s.q[F_VIB][c]);
         W.vd[c] = (p.rho_cfl > 0 && r < p.rho_cfl) ? 1 : 0;
         return;
     }
@@ -614,7 +639,7 @@ static __global__ void __launch_bounds__(256) k_face(P p, PrimT<R> W, FacesT<R> 
         fl = hllc_p(m, L[0], L[in], L[it1], L[it2], L[4], R(p0f) + dLf, Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4],
                     R(p0f) + dRf);
     } else {
-        fl = hllc(m, R(p.rho_vac), L[0], L[in], L[it1], L[it2], L[4], Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4]);
+        fl = hllc(m, EU_SETTING(R, rho_vac), L[0], L[in], L[it1], L[it2], L[4], Rr[0], Rr[in], Rr[it1], Rr[it2], Rr[4]);
     }
     F.q[DIR][0][id] = fl.r;
     F.q[DIR][1][id] = fl.mn;
@@ -675,7 +700,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
                 eos_pc(mat_of<R>(p), W.w[0][c], W.w[4][c], pr, cs);  // Pcell: EOS at the cell's internal energy
                 dmn += pr / R((i + 0.5) * p.dx);
             } else {  // face weights 1 (exact products)
-                const R inv = R(p.invdx);
+                const R inv = EU_SETTING(R, invdx);
                 vr = -(Fq[0][b] - Fq[0][a]) * inv;
                 vE = -(Fq[4][b] - Fq[4][a]) * inv;
                 vrc = -(Fq[5][b] - Fq[5][a]) * inv;
@@ -697,12 +722,12 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
     }
     if (p.gz != 0.0) {
         if (!p.ref_r0) {  // plain gravity body force, hydro_cpu.cpp:137-138
-            dmw += A(-p.gz * r[c]);
-            dE += A(-p.gz * mw[c]);
+            dmw += narrow<A>(-p.gz * r[c]);
+            dE += narrow<A>(-p.gz * mw[c]);
         } else {  // well-balanced source against the reference, hydro_cpu.cpp:139-143
             const double* R0 = p.ref_r0;
-            dmw += A(-p.gz * (r[c] - R0[c]) + p.ref_dp[c] * p.invdx);  // ref_dp: k_ref_dp
-            dE += A(-p.gz * mw[c]);
+            dmw += narrow<A>(-p.gz * (r[c] - R0[c]) + p.ref_dp[c] * p.invdx);  // ref_dp: k_ref_dp
+            dE += narrow<A>(-p.gz * mw[c]);
         }
     }
     A dS[6] = {A(0), A(0), A(0), A(0), A(0), A(0)}, dD = A(0), dvib = A(0);
@@ -712,7 +737,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
         else return p.rho_cfl > 0 && r[q] < p.rho_cfl;
     };
     if (p.m.G > 0 && !is_void(c)) {  // strength sources, hydro_cpu.cpp:145-213
-        const R G = R(p.m.G), dx = R(p.dx);
+        const R G = mat_of<R>(p).G, dx = EU_SETTING(R, dx);
         const int64_t xm = c - (i > 0 ? plane : 0), xp = c + (i < p.nx - 1 ? plane : 0);
         const int64_t ym = c - (j > 0 ? p.nz : 0), yp = c + (j < p.ny - 1 ? p.nz : 0);
         const int64_t zm = c - (k > 0 ? 1 : 0), zp = c + (k < p.nz - 1 ? 1 : 0);
@@ -803,16 +828,16 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? DEU_RHS_MINB_F32 
         dE += A((svx(xp) - svx(xm)) / hx + (svy(yp) - svy(ym)) / hy + (svz(zp) - svz(zm)) / hz);
         if (p.axisym) dE += A(svx(c) / rcyl);
     }
-    d.q[D_R][c] = dr;
-    d.q[D_MU][c] = dmu;
-    d.q[D_MV][c] = dmv;
-    d.q[D_MW][c] = dmw;
-    d.q[D_E][c] = dE;
+    d.q[D_R][c] = widen(dr);
+    d.q[D_MU][c] = widen(dmu);
+    d.q[D_MV][c] = widen(dmv);
+    d.q[D_MW][c] = widen(dmw);
+    d.q[D_E][c] = widen(dE);
 #pragma unroll
-    for (int q = 0; q < 6; q++) d.q[D_SXX + q][c] = dS[q];
-    d.q[D_D][c] = dD;
-    d.q[D_RC][c] = drc;
-    d.q[D_VIB][c] = dvib;
+    for (int q = 0; q < 6; q++) d.q[D_SXX + q][c] = widen(dS[q]);
+    d.q[D_D][c] = widen(dD);
+    d.q[D_RC][c] = widen(drc);
+    d.q[D_VIB][c] = widen(dvib);
 }
 
 // Near-void cell: momentum zeroed; with a reference state also reset to the
