@@ -111,6 +111,30 @@ class _Metrics:
         return float(np.cumsum(w)[-1])
 
 
+class Settling:
+    """The run-to-settling test (hydro_cpu.cpp:659-664): bowl-floor depths
+    sampled every 5 steps after t_auto are averaged over windows of 2 t_auto
+    (a window closes at the first sample at least that long after its first);
+    the run has settled when a window's mean agrees with the previous
+    window's to tol (relative to the newer mean)."""
+
+    def __init__(self, window, tol=0.02):
+        self.window, self.tol = window, tol
+        self.sum, self.count, self.start, self.prev = 0.0, 0, -1.0, -1.0
+
+    def sample(self, t, depth) -> bool:
+        if self.start < 0:
+            self.start = t
+        self.sum += depth
+        self.count += 1
+        if t - self.start >= self.window:
+            mean = self.sum / self.count
+            if self.prev > 0 and abs(mean - self.prev) < self.tol * mean:
+                return True
+            self.prev, self.sum, self.count, self.start = mean, 0.0, 0, t
+        return False
+
+
 def _next_event(n):
     """The step count after step n at which the loop next samples the floor
     (steps 1, 21, 41, ...: the reference samples before counting the step) or
@@ -137,10 +161,9 @@ def run(st: Setup, make_grid=None, form=0, device=0, log=None) -> dict:
     g.set_driver(case.pin_floor, case.sponge_from)
     ref_r0, _ = g.reference()
     M = _Metrics(st, ref_r0)
-    tol_m, w_win = 0.02, 2.0 * st.t_auto
+    settle = Settling(2.0 * st.t_auto)
     dmax_t, t, s = 0.0, 0.0, 0
     t_settled, next_log = -1.0, st.t_auto
-    sum_v, mean_prev, win_start, cnt_v = 0.0, -1.0, -1.0, 0
     while t < st.tend:
         want = _next_event(s) - s
         k, t = g.run(case.cfl, st.tend, want)
@@ -157,17 +180,9 @@ def run(st: Setup, make_grid=None, form=0, device=0, log=None) -> dict:
             next_log += 20.0
         if not st.fixed and t > st.t_auto and s % 5 == 0:  # run-to-settling test (hydro_cpu.cpp:659-664)
             r = g.read("r") if r is None else r
-            v = M.dfloor(r)
-            if win_start < 0:
-                win_start = t
-            sum_v += v
-            cnt_v += 1
-            if t - win_start >= w_win:
-                mean_now = sum_v / cnt_v
-                if mean_prev > 0 and abs(mean_now - mean_prev) < tol_m * mean_now:
-                    t_settled = t
-                    break
-                mean_prev, sum_v, cnt_v, win_start = mean_now, 0.0, 0, t
+            if settle.sample(t, M.dfloor(r)):
+                t_settled = t
+                break
     f = {k: g.read(k) for k in ("r", "mu", "mv", "mw")}
     P = g.pressure()
     out = _measure(st, M, f, P)

@@ -43,3 +43,21 @@ def test_arguments_read_as_the_reference_reads_them():
     st, _ = crater.setup_from_args(["500", "12000", "0", "0", "3.71", "2", "-1", "8", "8", "p", "1", "0", "0", "0",
                                     "0", "0", "-1"], env={})
     assert st.case.params["af_reg"] == 0 and st.case.params["c_reg"] == 0.0
+
+
+def test_settling_windows():
+    """hydro_cpu.cpp:659-664: window means of the floor depth over 2 t_auto;
+    settled when two consecutive means agree to 2 % of the newer one.  The
+    first window only opens the comparison; a window closes at its first
+    sample at least a window after its start, and the next window starts at
+    that sample's time."""
+    st = crater.Settling(window=10.0)
+    # first window: samples at t = 0..10 of depth 100 -> mean 100, no verdict
+    assert not any(st.sample(t, 100.0) for t in range(0, 11))
+    assert st.prev == 100.0 and st.count == 0 and st.start == 10
+    # second window: t = 11..20 (closes at 20 - 10 >= 10), mean 103 -- 3 % apart, not settled
+    assert not any(st.sample(t, 103.0) for t in range(11, 21))
+    assert st.prev == 103.0 and st.start == 20
+    # third window: mean 104 -- |104 - 103| < 0.02 * 104, settled when it closes at t = 30
+    assert not any(st.sample(t, 104.0) for t in range(21, 30))
+    assert st.sample(30, 104.0)
