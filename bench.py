@@ -589,6 +589,37 @@ def crater_visc_section(device, steps=20, warmup=3, cpu_steps=3):
     return out
 
 
+def crater_sweep_section(device, tend=3.0, form=0):
+    """The crater mode as a parameter sweep (impactor radius 300-600 m x speed
+    8 / 12 km/s at the mode's default domain of 30 x 22 radii and 5 cells per
+    radius, fixed end time): one run alone, then all eight at once through
+    crater.run_many (a grid, stream and host thread each).  Wall-clock times
+    of the whole driver loop, host measurements included."""
+    from deorbit_gb300 import crater
+
+    def setups():
+        return [crater.setup(a=a, U=U, tend=tend) for a in (300.0, 400.0, 500.0, 600.0) for U in (8000.0, 12000.0)]
+
+    one = setups()[5]
+    crater.run(crater.setup(a=one.a, U=one.U, tend=0.2), form=form, device=device)  # warm-up: library, graphs
+    t0 = time.perf_counter()
+    r1 = crater.run(one, form=form, device=device)
+    el1 = time.perf_counter() - t0
+    sts = setups()
+    t0 = time.perf_counter()
+    res = crater.run_many(sts, form=form, device=device)
+    el = time.perf_counter() - t0
+    cell_steps = sum(st.case.n * r["steps"] for st, r in zip(sts, res))
+    single = one.case.n * r1["steps"] / el1
+    return {"workload": f"crater mode sweep: a 300-600 m x U 8 / 12 km/s, default domain, t_end {tend} s, "
+                        + ("mixed" if form else "fp64") + " form",
+            "runs": len(sts), "cells": [st.case.n for st in sts], "steps": [r["steps"] for r in res],
+            "alone": {"cells": one.case.n, "steps": r1["steps"], "wall_s": el1, "value": single,
+                      "unit": "cell-steps/s"},
+            "concurrent": {"wall_s": el, "value": cell_steps / el, "unit": "cell-steps/s",
+                           "speedup_vs_alone": cell_steps / el / single}}
+
+
 def serving_section(device, rates=(4.0, 8.0, 16.0), count=200, steps=300):
     """Poisson request streams through the continuous-batching server."""
     from deorbit_gb300 import serve, sph
@@ -647,6 +678,7 @@ def main():
                                 acc=not args.no_acc, e2e=not args.no_e2e)
                for i, f in enumerate(("fp64", "mixed"))}
         out["crater_visc"] = crater_visc_section(local)
+        out["crater_sweep"] = crater_sweep_section(local)
         print(json.dumps(out), flush=True)
         return
 
@@ -759,7 +791,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_euler:
         euler = {"fp64": euler_section(device, args.steps, args.warmup, args.euler_n),
                  "mixed": euler_section(device, args.steps, args.warmup, args.euler_n, form=1, cpu=False),
-                 "crater_visc": crater_visc_section(device)}
+                 "crater_visc": crater_visc_section(device),
+                 "crater_sweep": crater_sweep_section(device)}
 
     # ---- accuracy of the mixed form against FP64 (same dt sequence), and of
     # both forms against the oracle on a bounded sample

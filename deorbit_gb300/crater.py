@@ -135,13 +135,14 @@ class Settling:
         return False
 
 
-def _next_event(n):
+def _next_event(n, settling):
     """The step count after step n at which the loop next samples the floor
-    (steps 1, 21, 41, ...: the reference samples before counting the step) or
-    may test settling (multiples of 5); the log is checked there too, so a
-    progress line can come up to four steps after its 20 s mark."""
+    (steps 1, 21, 41, ...: the reference samples before counting the step) or,
+    while the settling test is on, may test settling (multiples of 5).  The
+    log is checked there too, so a progress line can come a few steps after
+    its 20 s mark."""
     a = n + 1
-    while not (a % 5 == 0 or a % 20 == 1):
+    while not (a % 20 == 1 or (settling and a % 5 == 0)):
         a += 1
     return a
 
@@ -164,10 +165,16 @@ def run(st: Setup, make_grid=None, form=0, device=0, log=None) -> dict:
     settle = Settling(2.0 * st.t_auto)
     dmax_t, t, s = 0.0, 0.0, 0
     t_settled, next_log = -1.0, st.t_auto
+    dt_last = 0.0
     while t < st.tend:
-        want = _next_event(s) - s
+        # stop every 5 steps once t may pass t_auto within the next 20 steps
+        settling = not st.fixed and (t > st.t_auto or dt_last <= 0 or t + 25 * dt_last > st.t_auto)
+        want = _next_event(s, settling) - s
+        t_prev = t
         k, t = g.run(case.cfl, st.tend, want)
         s += k
+        if k:
+            dt_last = (t - t_prev) / k
         if k < want:  # t reached the end before the next sampling step
             break
         r = None
@@ -194,6 +201,21 @@ def run(st: Setup, make_grid=None, form=0, device=0, log=None) -> dict:
     if hasattr(g, "close"):
         g.close()
     return out
+
+
+def run_many(setups, form=0, device=0, workers=None, make_grid=None):
+    """Several crater runs at once (a parameter sweep, as the reference's
+    campaign scripts run the mode over impactor sizes and speeds): one grid,
+    CUDA stream and host thread per run, so the small grids' kernels overlap
+    on the device.  Returns the results in the order of `setups`; each equals
+    the same run made alone (the runs share nothing)."""
+    import concurrent.futures as cf
+
+    setups = list(setups)
+    n = workers or min(len(setups), 16)
+    with cf.ThreadPoolExecutor(max_workers=max(1, n)) as ex:
+        futs = [ex.submit(run, st, make_grid, form, device) for st in setups]
+        return [f.result() for f in futs]
 
 
 def _measure(st, M, f, P):

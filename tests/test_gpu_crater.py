@@ -55,3 +55,15 @@ def test_mixed_driver_matches_reference_mode(cuda_lib, mode):
     D = ref[1]
     for g, r in zip(got[1:4], ref[1:4]):  # diameter, depth, transient depth
         assert abs(g - r) <= 1e-3 * D, (got, ref)
+
+
+def test_sweep_runs_equal_alone(cuda_lib):
+    """crater.run_many: concurrent runs on their own grids and streams give
+    exactly the results of the same runs made one at a time."""
+    modes = [m["args"] for m in MODES[:4]]
+    setups = [crater.setup_from_args(a, env={})[0] for a in modes]
+    many = crater.run_many(setups, form=0)
+    for a, res in zip(modes, many):
+        alone = crater.run(crater.setup_from_args(a, env={})[0], form=0)
+        assert res["lines"] == alone["lines"]
+        assert np.array_equal(res["profile"], alone["profile"])
