@@ -434,6 +434,8 @@ struct Grid {
     bool graph_valid = false;
     int64_t graph_launches = 0;  // kernels per replay of the step graph
     Visc vw{};                   // implicit viscosity work arrays, allocated on first use
+    FaceFork fork{};             // side streams for the face passes (small grids)
+    bool fork_faces = false;
     int pin_floor = 0;           // driver adjustments after each step (eu_set_driver)
     int sponge_from = -1;
     int driver_flags = 0;
@@ -454,6 +456,10 @@ struct Grid {
         if (graph) cudaGraphExecDestroy(graph);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : {fork.fork, fork.join[0], fork.join[1]})
+            if (e) cudaEventDestroy(e);
+        for (cudaStream_t s2 : fork.side)
+            if (s2) cudaStreamDestroy(s2);
         for (void* a : allocs) cudaFree(a);
         allocs.clear();
         if (st) cudaStreamDestroy(st);
@@ -497,8 +503,9 @@ struct Grid {
     }
 
     void enqueue_lop(const Fields& s) {
-        if (mixed) enqueue_lop_f32(p, s, W32, g.q[F_AF], F32, d, ctl, st);
-        else enqueue_lop_t<double>(p, s, W, g.q[F_AF], F, d, ctl, st);
+        const FaceFork* fk = fork_faces ? &fork : nullptr;
+        EU_CUDA(mixed ? enqueue_lop_f32(p, s, W32, g.q[F_AF], F32, d, ctl, st, fk)
+                      : enqueue_lop_t<double>(p, s, W, g.q[F_AF], F, d, ctl, st, fk));
         launches += 5;
     }
 
@@ -706,6 +713,16 @@ int eu_create_form(int32_t nx, int32_t ny, int32_t nz, double dx, int32_t device
             g->ctl = (deu::Ctl*)c;
             EU_CUDA(cudaMemsetAsync(c, 0, sizeof(deu::Ctl), g->st));
             for (auto& ev : g->ev) EU_CUDA(cudaEventCreate(&ev));
+            // Small grids: the three face passes of a Lop fill the device only
+            // side by side (a pass of a 2-D grid is a few dozen blocks).
+            int nsm = 0;
+            EU_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+            g->fork_faces = n < (int64_t)nsm * 256 * 8;
+            if (g->fork_faces) {
+                for (auto& s2 : g->fork.side) EU_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+                EU_CUDA(cudaEventCreateWithFlags(&g->fork.fork, cudaEventDisableTiming));
+                for (auto& e : g->fork.join) EU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            }
             EU_CUDA(cudaStreamSynchronize(g->st));
         } catch (...) {
             g->release();

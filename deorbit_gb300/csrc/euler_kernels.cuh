@@ -1076,11 +1076,23 @@ static __global__ void k_maxspeed_begin(Ctl* ctl) {
 
 // ---------------------------------------------------------------- Lop launcher
 
+// Side streams and events that let the face passes of one Lop run side by side.
+struct FaceFork {
+    cudaStream_t side[2];
+    cudaEvent_t fork, join[2];
+};
+
 // One Lop (hydro_cpu.cpp:98-214) of state s in compute type R: primitives,
 // the three directions' face fluxes, the right-hand side.
 template <class R>
-inline void enqueue_lop_t(const P& p, const Fields& s, PrimT<R> W, const double* af, FacesT<R> F, Rhs d,
-                          const Ctl* ctl, cudaStream_t st) {
+// Returns the first error of the fork's event calls (kernel launch errors
+// are the caller's cudaGetLastError).
+inline cudaError_t enqueue_lop_t(const P& p, const Fields& s, PrimT<R> W, const double* af, FacesT<R> F, Rhs d,
+                                 const Ctl* ctl, cudaStream_t st, const FaceFork* fork) {
+    cudaError_t err = cudaSuccess;
+    auto fork_check = [&](cudaError_t e) {
+        if (err == cudaSuccess) err = e;
+    };
     auto blocks = [](int64_t count, int b) { return (unsigned)((count + b - 1) / b); };
     if constexpr (sizeof(R) == 8) {  // FP64: the right-hand side reads the state's own strength fields
 #pragma unroll
@@ -1090,10 +1102,28 @@ inline void enqueue_lop_t(const P& p, const Fields& s, PrimT<R> W, const double*
         W.vd = nullptr;
     }
     k_prim<R><<<blocks(p.n, 256), 256, 0, st>>>(p, s, W, ctl);
+    // the three directions' face passes are independent: with a fork, y and z
+    // run on side streams beside x (a small grid's passes then share the SMs;
+    // inside a captured graph they become parallel branches)
+    cudaStream_t sy = st, sz = st;
+    if (fork) {
+        fork_check(cudaEventRecord(fork->fork, st));
+        fork_check(cudaStreamWaitEvent(fork->side[0], fork->fork, 0));
+        fork_check(cudaStreamWaitEvent(fork->side[1], fork->fork, 0));
+        sy = fork->side[0];
+        sz = fork->side[1];
+    }
     k_face<0, R><<<blocks(face_count<0>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
-    k_face<1, R><<<blocks(face_count<1>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
-    k_face<2, R><<<blocks(face_count<2>(p.nx, p.ny, p.nz), 256), 256, 0, st>>>(p, W, F, ctl);
+    k_face<1, R><<<blocks(face_count<1>(p.nx, p.ny, p.nz), 256), 256, 0, sy>>>(p, W, F, ctl);
+    k_face<2, R><<<blocks(face_count<2>(p.nx, p.ny, p.nz), 256), 256, 0, sz>>>(p, W, F, ctl);
+    if (fork) {
+        fork_check(cudaEventRecord(fork->join[0], sy));
+        fork_check(cudaEventRecord(fork->join[1], sz));
+        fork_check(cudaStreamWaitEvent(st, fork->join[0], 0));
+        fork_check(cudaStreamWaitEvent(st, fork->join[1], 0));
+    }
     k_rhs<R><<<blocks(p.n, 128), 128, 0, st>>>(p, s, W, af, F, d, ctl);
+    return err;
 }
 
 // The CFL speed reduction, the predictor and the corrector in compute type R.
@@ -1119,8 +1149,8 @@ inline void enqueue_correct_t(const P& p, const Fields& g, const Fields& g1, Rhs
 
 // The FP32 instantiations live in euler_mixed.cu (compiled with fused
 // multiply-adds); the FP64 ones in euler.cu (compiled without).
-void enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* af, FacesT<float> F, Rhs d,
-                     const Ctl* ctl, cudaStream_t st);
+cudaError_t enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* af, FacesT<float> F, Rhs d,
+                            const Ctl* ctl, cudaStream_t st, const FaceFork* fork);
 void enqueue_maxspeed_f32(const P& p, const Fields& g, Ctl* ctl, cudaStream_t st);
 void enqueue_predict_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st);
 void enqueue_correct_f32(const P& p, const Fields& g, const Fields& g1, Rhs d, const Ctl* ctl, cudaStream_t st,

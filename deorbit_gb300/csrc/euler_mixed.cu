@@ -7,9 +7,9 @@
 
 namespace deu {
 
-void enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* af, FacesT<float> F, Rhs d,
-                     const Ctl* ctl, cudaStream_t st) {
-    enqueue_lop_t<float>(p, s, W, af, F, d, ctl, st);
+cudaError_t enqueue_lop_f32(const P& p, const Fields& s, PrimT<float> W, const double* af, FacesT<float> F, Rhs d,
+                            const Ctl* ctl, cudaStream_t st, const FaceFork* fork) {
+    return enqueue_lop_t<float>(p, s, W, af, F, d, ctl, st, fork);
 }
 
 void enqueue_maxspeed_f32(const P& p, const Fields& g, Ctl* ctl, cudaStream_t st) {
