@@ -331,6 +331,11 @@ def main(argv=None):
     import sys
 
     argv = sys.argv[1:] if argv is None else list(argv)
+    if "-h" in argv or "--help" in argv:
+        print("usage: python -m deorbit_gb300.crater [--mixed] [--log] [a U TDEC ETA_AF g cppr tend Rfac Zfac "
+              "profile ROCK Y_D0 VOID_AMB Y_BINGHAM VISC_IMP VOID_CONS C_REG AF_SAT]\n"
+              "The reference driver's crater mode (hydro_cpu.cpp crater) on the GPU; defaults as there.")
+        return 0
     form = 1 if "--mixed" in argv else 0
     log = (lambda line: print(line, file=sys.stderr, flush=True)) if "--log" in argv else None
     args = [a for a in argv if a not in ("--mixed", "--log")]
