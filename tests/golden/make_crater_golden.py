@@ -10,6 +10,11 @@ reproduce both with the crater driver (deorbit_gb300.crater) over the oracle
 exactly, and with the CUDA solver to the solver's tolerance.
 
     python tests/golden/make_crater_golden.py
+    python tests/golden/make_crater_golden.py --default   # also crater_default.json (~3 h)
+
+--default also runs the mode with no arguments (its default crater: a = 500 m,
+12 km/s, 150 x 110 cells, to the 763 s cap, 3 x 10^5 steps) into
+tests/golden/crater_default.json.
 """
 from __future__ import annotations
 
@@ -27,6 +32,7 @@ from oracle import euler as EO  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
 OUT = os.path.join(HERE, "crater_modes.json")
+OUT_DEFAULT = os.path.join(HERE, "crater_default.json")
 
 # the mode's arguments after "crater" (profile path inserted at position 10)
 MODES = [
@@ -52,8 +58,23 @@ def main():
     if not EO.ref_available():
         O.build(ref=True)
     out = []
+    modes = list(MODES) + ([None] if "--default" in sys.argv else [])
     with tempfile.TemporaryDirectory() as tmp:
-        for args in MODES:
+        for args in modes:
+            if args is None:  # the default crater: profile path only (argument 11 needs 2-10 given)
+                import time
+                prof = os.path.join(tmp, "profile.txt")
+                full = ["500", "12000", "0", "0", "3.71", "5", "-1", "30", "22", prof]
+                t0 = time.time()
+                r = subprocess.run([sys.executable, "-c", CHILD, EO.REF_SO] + full, capture_output=True, text=True,
+                                   cwd=tmp, check=True)
+                lines = [ln for ln in r.stdout.splitlines() if not ln.lstrip().startswith("voidzero:")]
+                with open(prof) as f:
+                    d = {"args": [], "lines": lines, "profile": f.read(), "reference_seconds": round(time.time() - t0)}
+                with open(OUT_DEFAULT, "w") as f:
+                    json.dump(d, f, indent=1)
+                print(lines[-1])
+                continue
             prof = os.path.join(tmp, "profile.txt")
             full = list(args[:9]) + [prof] + list(args[10:])
             r = subprocess.run([sys.executable, "-c", CHILD, EO.REF_SO] + full, capture_output=True, text=True,

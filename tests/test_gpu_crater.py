@@ -67,3 +67,21 @@ def test_sweep_runs_equal_alone(cuda_lib):
         alone = crater.run(crater.setup_from_args(a, env={})[0], form=0)
         assert res["lines"] == alone["lines"]
         assert np.array_equal(res["profile"], alone["profile"])
+
+
+def test_default_crater_mode_matches_reference(cuda_lib, tmp_path):
+    """The mode with no arguments -- the reference's default crater (a = 500 m,
+    12 km/s, 150 x 110 cells, run to the 763 s cap, ~3 x 10^5 steps) -- against
+    the reference's own run (tests/golden/crater_default.json): apparent
+    diameter, transient depth and d/D equal to the printed digits, final depth
+    within 2 %, step count within 2 % (over 3 x 10^5 steps of late-time
+    sloshing the device's exp / pow differences grow)."""
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "crater_default.json")))
+    st, _ = crater.setup_from_args([], env={})
+    res = crater.run(st, form=0)
+    got, ref = _result(res["result_line"]), _result(gold["lines"][-1])
+    assert got[1] == ref[1]                      # apparent diameter
+    assert abs(got[3] - ref[3]) <= 5e-5          # transient depth (printed to 1e-4 m)
+    assert abs(got[4] - ref[4]) <= 5e-5          # d/D
+    assert abs(got[2] - ref[2]) <= 0.02 * ref[2]  # final depth
+    assert abs(res["steps"] - _steps(gold["lines"])) <= 0.02 * _steps(gold["lines"])
