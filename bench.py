@@ -284,9 +284,11 @@ def accuracy_vs_oracle(sph, ic, sc, steps, device, tol=1e-4):
     return out
 
 
-def e2e_rate(sph, ctx, b, n, steps, warmup):
+def e2e_rate(sph, ctx, b, n, steps, warmup, fused=True):
     """Steps through the C ABI with the carried state crossing the boundary
-    from / to pinned host buffers every step."""
+    from / to pinned host buffers every step: one sph_step_fields call per
+    step (fused), or sph_write_fields + sph_timestep + sph_step +
+    sph_read_fields."""
     names = ["x", "y", "z", "vx", "vy", "vz", "u", "hh", "D", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"]
     pinned = True
     try:
@@ -299,6 +301,9 @@ def e2e_rate(sph, ctx, b, n, steps, warmup):
     ctx.read_many(b, names, outs)
 
     def one():
+        if fused:  # inputs and outputs are the same pinned buffers
+            ctx.step_fields(b, bufs, names, outs)
+            return
         ctx.write_many(b, bufs)          # the step's inputs, pinned host -> device
         dt = ctx.timestep(b)
         ctx.step(dt)
@@ -763,10 +768,15 @@ def main():
     if not args.no_e2e:
         r, el, nbytes, pinned = e2e_rate(sph, ctx, b, sc.n, args.steps, min(args.warmup, 2))
         el = max_over_ranks(el)
+        _, el_sep, _, _ = e2e_rate(sph, ctx, b, sc.n, args.steps, min(args.warmup, 2), fused=False)
+        el_sep = max_over_ranks(el_sep)
         e2e = {"value": world * sc.n * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes + 8, "pinned_host": pinned,
-               "host_path": "direct (kernels over the CPU-GPU link)" if ctx.get_option("host_direct")
-               else "device staging copies"}
+               "api": "sph_step_fields (one call per step; copies overlap the step)",
+               "separate_calls": {"value": world * sc.n * args.steps / el_sep,
+                                  "api": "sph_write_fields + sph_timestep + sph_step + sph_read_fields",
+                                  "host_path": "direct (kernels over the CPU-GPU link)"
+                                  if ctx.get_option("host_direct") else "device staging copies"}}
     ctx.close()
 
     # ---- plain FP64 form

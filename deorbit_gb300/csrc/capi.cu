@@ -466,6 +466,22 @@ int sph_write_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* 
     });
 }
 
+int sph_step_fields(sph_ctx* ctx, int32_t impact, double dt, int32_t nin, const char* const* in_names,
+                    const double* const* ins, int32_t nout, const char* const* out_names, double* const* outs,
+                    double* dt_used) {
+    return guard([&] {
+        if (!std::isfinite(dt)) throw SphError(SPH_ERR_ARG, "dt must be finite (< 0: the impact's CFL dt)");
+        if (nin < 0 || nout < 0) throw SphError(SPH_ERR_ARG, "nin < 0 or nout < 0");
+        if (nin > 0) { need(in_names, "in_names"); need(ins, "ins"); }
+        if (nout > 0) { need(out_names, "out_names"); need(outs, "outs"); }
+        for (int f = 0; f < nin; f++) { need(in_names[f], "in_names[f]"); need(ins[f], "ins[f]"); }
+        for (int f = 0; f < nout; f++) { need(out_names[f], "out_names[f]"); need(outs[f], "outs[f]"); }
+        CTX_SET();
+        const double d = E(ctx).step_fields(impact, dt, nin, in_names, ins, nout, out_names, outs);
+        if (dt_used) *dt_used = d;
+    });
+}
+
 int sph_read_mat(sph_ctx* ctx, int32_t impact, int32_t* out) {
     return guard([&] {
         need(out, "out");

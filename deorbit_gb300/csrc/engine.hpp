@@ -83,6 +83,8 @@ public:
     virtual void write_field(int b, const char* name, const double* in) = 0;
     virtual void read_fields(int b, int nf, const char* const* names, double* const* outs) = 0;
     virtual void write_fields(int b, int nf, const char* const* names, const double* const* ins) = 0;
+    virtual double step_fields(int b, double dt, int nin, const char* const* in_names, const double* const* ins,
+                               int nout, const char* const* out_names, double* const* outs) = 0;
     virtual void read_mat(int b, int32_t* out) = 0;
     virtual void read_fixed(int b, uint8_t* out) = 0;
     virtual void write_fixed(int b, const uint8_t* in) = 0;

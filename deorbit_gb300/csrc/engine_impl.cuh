@@ -7,6 +7,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -41,6 +42,34 @@ static __global__ void k_write_col(T* col, const int32_t* pos_of_gid, int64_t gi
     int64_t l = gtid();
     if (l >= n) return;
     col[pos_of_gid[gid_base + l]] = (T)in[l];
+}
+// Up to kColIo columns in one launch (step_fields): column c holds doubles,
+// or floats where f32[c] (the mixed form's FP32 columns), converted as
+// k_read_col / k_write_col convert them.
+constexpr int kColIo = 16;
+struct ColIo {
+    void* col[kColIo];
+    double* buf[kColIo];
+    int32_t f32[kColIo];
+    int32_t nc;
+};
+static __global__ void k_write_cols(ColIo s, const int32_t* pos_of_gid, int64_t gid_base, int64_t n) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    const int32_t k = pos_of_gid[gid_base + l];
+    for (int c = 0; c < s.nc; c++) {
+        const double v = s.buf[c][l];
+        if (s.f32[c]) static_cast<float*>(s.col[c])[k] = (float)v;
+        else static_cast<double*>(s.col[c])[k] = v;
+    }
+}
+static __global__ void k_read_cols(ColIo s, const int32_t* pos_of_gid, int64_t gid_base, int64_t n) {
+    int64_t l = gtid();
+    if (l >= n) return;
+    const int32_t k = pos_of_gid[gid_base + l];
+    for (int c = 0; c < s.nc; c++)
+        s.buf[c][l] = s.f32[c] ? (double)static_cast<const float*>(s.col[c])[k]
+                               : static_cast<const double*>(s.col[c])[k];
 }
 static __global__ void k_read_u8(const uint8_t* col, const int32_t* pos_of_gid, int64_t gid_base,
                           int64_t n, uint8_t* out) {
@@ -326,6 +355,9 @@ public:
         DSPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         DSPH_CUDA(cudaStreamCreateWithFlags(&copy_st_, cudaStreamNonBlocking));
         DSPH_CUDA(cudaEventCreateWithFlags(&copy_ev_, cudaEventDisableTiming));
+        DSPH_CUDA(cudaStreamCreateWithFlags(&out_st_, cudaStreamNonBlocking));
+        DSPH_CUDA(cudaEventCreateWithFlags(&out_ev_, cudaEventDisableTiming));
+        DSPH_CUDA(cudaEventCreateWithFlags(&late_ev_, cudaEventDisableTiming));
         DSPH_CUDA(cudaMalloc(&mats_d_, sizeof(MatT<R>) * kMaxMaterials));
         DSPH_CUDA(cudaMalloc(&flags_d_, sizeof(int32_t) * 4));
         DSPH_CUDA(cudaMalloc(&wait_err_d_, sizeof(int32_t)));
@@ -362,8 +394,12 @@ public:
                 if (graph_exec_[g][p]) cudaGraphExecDestroy(graph_exec_[g][p]);
         for (int i = 0; i < 16; i++) if (user_ev_[i]) cudaEventDestroy(user_ev_[i]);
         cudaStreamSynchronize(copy_st_);
+        cudaStreamSynchronize(out_st_);
         cudaEventDestroy(copy_ev_);
+        cudaEventDestroy(out_ev_);
+        cudaEventDestroy(late_ev_);
         cudaStreamDestroy(copy_st_);
+        cudaStreamDestroy(out_st_);
         cudaStreamDestroy(st_);
     }
 
@@ -693,8 +729,15 @@ public:
     // One KDK step of the masked impacts (sph.hpp:357-377).  host_sync: the
     // adaptive-h round loop reads its convergence flag back; otherwise all four
     // rounds are issued and converged impacts skip them on the device.
-    void one_step(bool host_sync) {
-        const int nimp = (int)imp_.size();
+    // before_eos (optional) runs between the head (kick, drift, sort, list,
+    // density rounds: x, y, z and h final, u, D and S not yet read) and the
+    // tail (EOS, forces, damage, finish, dt).
+    void one_step(bool host_sync, const std::function<void()>* before_eos = nullptr) {
+        step_head(host_sync);
+        if (before_eos) (*before_eos)();
+        step_tail();
+    }
+    void step_head(bool host_sync) {
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[0], st_));
         cls(KC_KICK);
         launch_n(k_kick_drift<R>, N_);
@@ -706,6 +749,9 @@ public:
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[2], st_));
         if (host_sync) refresh_list_if_needed();
         else refresh_list_device();
+    }
+    void step_tail() {
+        const int nimp = (int)imp_.size();
         cls(KC_EOS);
         launch_n(k_eos<R>, N_);
         if (profiling_) DSPH_CUDA(cudaEventRecord(ev_[3], st_));
@@ -814,6 +860,14 @@ public:
         const int64_t n0 = N_;
         DSPH_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         for (int k = 0; k < (kind == kGraphTwo ? 2 : 1); k++) {
+            if (kind == kGraphHead) {
+                step_head(false);
+                break;
+            }
+            if (kind == kGraphTail) {
+                step_tail();
+                break;
+            }
             if (kind != kGraphHostDt) launch_small(k_run_control, nimp, 0);
             one_step(false);
         }
@@ -1012,6 +1066,150 @@ public:
         }
         DSPH_CUDA(cudaStreamSynchronize(copy_st_));
         DSPH_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    // One step with the caller's host fields crossing the boundary inside it:
+    // the result of write_fields(ins); dt = timestep(b) when dt < 0; step(dt);
+    // read_fields(outs), bit for bit, with the copies overlapping the step.
+    // Inputs that no kernel of the step's head reads or writes (u, D, S, the
+    // old derivatives dudt and dS, eps_act) are copied up while the head
+    // (kick, drift, sort, list, density rounds) runs and are scattered, in the
+    // order the sort left, between the head and the tail (EOS, forces,
+    // damage, finish, dt); the other inputs go first.  Outputs
+    // final at the end of the head (x, y, z, mass, h0, hh) are gathered there
+    // and copied down while the tail runs, on a second copy stream, so both
+    // link directions carry data at once.  Head and tail replay captured
+    // graphs (one per buffer parity) unless graphs are off or profiling is on.
+    // Always through device staging slices.
+    double step_fields(int b, double dt, int nin, const char* const* in_names, const double* const* ins,
+                       int nout, const char* const* out_names, double* const* outs) override {
+        ImpactH& h = imp(b);
+        commit();
+        if (!h.committed) throw SphError(SPH_ERR_STATE, "impact has no device state yet (call sph_init)");
+        for (int f = 0; f < nin; f++)
+            if (!with_column(in_names[f], [](auto*) {}))
+                throw SphError(SPH_ERR_ARG, std::string("unknown field ") + in_names[f]);
+        for (int f = 0; f < nout; f++)
+            if (!with_column(out_names[f], [](auto*) {}))
+                throw SphError(SPH_ERR_ARG, std::string("unknown field ") + out_names[f]);
+        if (dt < 0) {
+            pull_table();
+            dt = bitsd_host(tab_[b].dt_bits);
+        }
+        const int64_t n = h.n;
+        if (n == 0 || N_ == 0) {
+            write_fields(b, nin, in_names, ins);
+            step(dt);
+            read_fields(b, nout, out_names, outs);
+            return dt;
+        }
+        std::vector<int32_t> mask(imp_.size(), 0);
+        std::vector<double> dts(imp_.size(), dt);
+        for (size_t i = 0; i < imp_.size(); i++)
+            if (imp_[i].used && imp_[i].alive && imp_[i].committed) mask[i] = 1;
+        set_masks(mask, &dts, nullptr);
+        ensure_stage((int64_t)(nin + nout) * n);
+        // carried fields that only the tail reads (EOS, forces, damage, finish)
+        auto is_late = [](const char* s) {
+            static const char* ln[] = {"u", "D", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz", "dudt",
+                                       "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz", "eps_act"};
+            for (const char* l : ln) if (!std::strcmp(s, l)) return true;
+            return false;
+        };
+        auto is_head_final = [](const char* s) {
+            static const char* ln[] = {"x", "y", "z", "mass", "h0", "hh"};
+            for (const char* l : ln) if (!std::strcmp(s, l)) return true;
+            return false;
+        };
+        auto in_slice = [&](int f) { return stage_d_ + (int64_t)f * n; };
+        auto out_slice = [&](int f) { return stage_d_ + (int64_t)(nin + f) * n; };
+        // one launch moves up to kColIo columns between staging slices and the
+        // columns of the current buffer parity
+        auto cols_io = [&](bool write, const std::vector<int>& fs) {
+            for (size_t at = 0; at < fs.size(); at += kColIo) {
+                ColIo s{};
+                for (size_t c = at; c < fs.size() && c < at + kColIo; c++) {
+                    const int f = fs[c];
+                    const char* nm = write ? in_names[f] : out_names[f];
+                    with_column(nm, [&](auto* col) {
+                        s.col[s.nc] = col;
+                        s.f32[s.nc] = sizeof(*col) == 4;
+                    });
+                    s.buf[s.nc++] = write ? in_slice(f) : out_slice(f);
+                }
+                if (write) launch_n_raw(k_write_cols, n, s, pos_of_gid_, h.gid_base, n);
+                else launch_n_raw(k_read_cols, n, s, pos_of_gid_, h.gid_base, n);
+            }
+        };
+        // the staging slices may still feed earlier work on the compute stream
+        DSPH_CUDA(cudaEventRecord(copy_ev_, st_));
+        DSPH_CUDA(cudaStreamWaitEvent(copy_st_, copy_ev_, 0));
+        // head inputs: each field's copy, then its scatter while the next copies
+        std::vector<int> late, head_out, tail_out;
+        for (int f = 0; f < nin; f++) {
+            if (is_late(in_names[f])) {
+                late.push_back(f);
+                continue;
+            }
+            DSPH_CUDA(cudaMemcpyAsync(in_slice(f), ins[f], sizeof(double) * n, cudaMemcpyHostToDevice, copy_st_));
+            DSPH_CUDA(cudaEventRecord(copy_ev_, copy_st_));
+            DSPH_CUDA(cudaStreamWaitEvent(st_, copy_ev_, 0));
+            cols_io(true, {f});
+            std::string nm(in_names[f]);
+            if (nm == "x" || nm == "y" || nm == "z" || nm == "hh") grid_valid_ = false;
+        }
+        for (int f : late)
+            DSPH_CUDA(cudaMemcpyAsync(in_slice(f), ins[f], sizeof(double) * n, cudaMemcpyHostToDevice, copy_st_));
+        DSPH_CUDA(cudaEventRecord(late_ev_, copy_st_));
+        // every input is read before any output is written, so the caller's
+        // input and output buffers may be the same memory
+        DSPH_CUDA(cudaStreamWaitEvent(out_st_, late_ev_, 0));
+        for (int f = 0; f < nout; f++) (is_head_final(out_names[f]) ? head_out : tail_out).push_back(f);
+        const std::function<void()> between = [&]() {
+            if (!late.empty()) {
+                DSPH_CUDA(cudaStreamWaitEvent(st_, late_ev_, 0));
+                cols_io(true, late);
+            }
+            if (!head_out.empty()) {
+                cols_io(false, head_out);
+                DSPH_CUDA(cudaEventRecord(out_ev_, st_));
+                DSPH_CUDA(cudaStreamWaitEvent(out_st_, out_ev_, 0));
+                for (int f : head_out)
+                    DSPH_CUDA(cudaMemcpyAsync(outs[f], out_slice(f), sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                              out_st_));
+            }
+        };
+        if (use_graphs_ && !profiling_) {
+            const int p = cur_;
+            DSPH_CUDA(cudaGraphLaunch(ensure_graph(kGraphHead), st_));
+            launches_ += graph_launches_[kGraphHead][p];
+            cur_ = p ^ 1;  // the head's sort moved the carried state
+            between();
+            DSPH_CUDA(cudaGraphLaunch(ensure_graph(kGraphTail), st_));
+            launches_ += graph_launches_[kGraphTail][cur_];
+        } else {
+            one_step(false, &between);
+        }
+        // tail outputs: each field's gather, then its copy while the next gathers
+        for (int f : tail_out) {
+            cols_io(false, {f});
+            DSPH_CUDA(cudaEventRecord(out_ev_, st_));
+            DSPH_CUDA(cudaStreamWaitEvent(out_st_, out_ev_, 0));
+            DSPH_CUDA(cudaMemcpyAsync(outs[f], out_slice(f), sizeof(double) * n, cudaMemcpyDeviceToHost, out_st_));
+        }
+        grow_lists_after_overflow();
+        pull_table();
+        for (size_t i = 0; i < imp_.size(); i++)
+            if (mask[i]) {
+                imp_[i].t = tab_[i].t;
+                imp_[i].steps = tab_[i].nsteps;
+                imp_[i].dt_last = dt;
+                imp_[i].initialized = true;
+            }
+        DSPH_CUDA(cudaStreamSynchronize(copy_st_));
+        DSPH_CUDA(cudaStreamSynchronize(out_st_));
+        check_async();
+        return dt;
     }
 
     void read_mat(int b, int32_t* out) override {
@@ -2339,6 +2537,9 @@ public:
     cudaStream_t st_{};
     cudaStream_t copy_st_{};   // host <-> device copies of the batched field I/O
     cudaEvent_t copy_ev_{};
+    cudaStream_t out_st_{};    // device -> host copies of step_fields (the other link direction)
+    cudaEvent_t out_ev_{};
+    cudaEvent_t late_ev_{};    // step_fields: the inputs first read by the EOS pass have landed
     std::vector<void*> allocs_, tmp_;
     std::vector<sph_material> mats_h_;
     MatT<R>* mats_d_ = nullptr;
@@ -2407,10 +2608,12 @@ public:
     int list_mode_ = 0;   // 0: thread per particle, 1: warp per column run
     bool use_graphs_ = true;
     uint64_t layout_epoch_ = 1;
-    enum { kGraphTwo = 0, kGraphOne = 1, kGraphHostDt = 2, kGraphKinds = 3 };
+    // kGraphHead / kGraphTail: the two halves of a host-dt step (step_head,
+    // step_tail), for step_fields' transfers between them
+    enum { kGraphTwo = 0, kGraphOne = 1, kGraphHostDt = 2, kGraphHead = 3, kGraphTail = 4, kGraphKinds = 5 };
     cudaGraphExec_t graph_exec_[kGraphKinds][2] = {};
     uint64_t graph_key_[kGraphKinds][2] = {};
-    int64_t graph_n_[kGraphKinds][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+    int64_t graph_n_[kGraphKinds][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
     int64_t graph_launches_[kGraphKinds][2] = {};
     int64_t launches_ = 0;
     bool profiling_ = false;

@@ -138,6 +138,8 @@ _SIGS = {
     "sph_write_field": (C.c_int, [_P, C.c_int32, C.c_char_p, _D]),
     "sph_read_fields": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(_D)]),
     "sph_write_fields": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(_D)]),
+    "sph_step_fields": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(_D),
+                                  C.c_int32, C.POINTER(C.c_char_p), C.POINTER(_D), _D]),
     "sph_read_mat": (C.c_int, [_P, C.c_int32, _I32]),
     "sph_read_fixed": (C.c_int, [_P, C.c_int32, _U8]),
     "sph_write_fixed": (C.c_int, [_P, C.c_int32, _U8]),
@@ -441,6 +443,23 @@ class Context:
         cn = (C.c_char_p * len(names))(*[k.encode() for k in names])
         ptrs = (_D * len(names))(*[_dp(v) for v in vals])
         check(lib().sph_write_fields(self.h, b, len(names), cn, ptrs))
+
+    def step_fields(self, b, fields, out_names, outs=None, dt=-1.0):
+        """write_many(b, fields); dt = timestep(b) when dt < 0; step(dt);
+        read_many(b, out_names) -- one call whose host copies overlap the
+        step (page-locked buffers copy fastest).  Returns (dt, {name: array})."""
+        n = self.n(b)
+        names = list(fields)
+        vals = [_f64(fields[k], n) for k in names]
+        outs = [np.zeros(n) for _ in out_names] if outs is None else [_out64(o, n) for o in outs]
+        cin = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        pin = (_D * max(1, len(names)))(*[_dp(v) for v in vals])
+        cout = (C.c_char_p * max(1, len(out_names)))(*[k.encode() for k in out_names])
+        pout = (_D * max(1, len(out_names)))(*[_dp(o) for o in outs])
+        used = C.c_double()
+        check(lib().sph_step_fields(self.h, b, float(dt), len(names), cin, pin, len(out_names), cout, pout,
+                                    C.byref(used)))
+        return used.value, dict(zip(out_names, outs))
 
     def mat(self, b) -> np.ndarray:
         out = np.zeros(self.n(b), np.int32)

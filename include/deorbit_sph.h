@@ -176,7 +176,7 @@ int sph_timestep(sph_ctx* ctx, int32_t impact, double* dt);
  * with the caller's dt. */
 int sph_step(sph_ctx* ctx, double dt);
 /* Batched run: nsteps KDK steps in which each impact uses its own CFL dt
- * (device-side, as run_ic.cpp:328-329), clipped at its t_end when t_end > 0.
+ * (device-side, as run_ic.cpp:178-180), clipped at its t_end when t_end > 0.
  * Impacts that reached t_end or their step limit stop advancing.  Unless the
  * "graphs" option is 0, steps run as a captured CUDA graph of two
  * device-controlled steps (no host round trips inside). */
@@ -199,6 +199,21 @@ int sph_read_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* c
                     double* const* outs);
 int sph_write_fields(sph_ctx* ctx, int32_t impact, int32_t nfields, const char* const* names,
                      const double* const* ins);
+/* One step with the state crossing the boundary inside it, for callers that
+ * own the particle state on the host (run_ic.cpp:177-190: a loop over
+ * System::timestep / step that reads the public vectors between steps).
+ * The result equals, bit for bit, sph_write_fields(ins); dt =
+ * sph_timestep(impact) when dt < 0 (else the given dt >= 0); sph_step(dt);
+ * sph_read_fields(outs) -- in one call whose host copies overlap the step's
+ * kernels (u, D, S, the old derivatives and eps_act go up while the sort,
+ * list and density passes run; x, y, z, mass, h0 and hh come down while the
+ * force pass runs).  Writes the dt used
+ * to *dt_used when dt_used is not null.  Every input is read before any
+ * output is written, so input and output buffers may be the same memory;
+ * the caller's buffers may be reused on return. */
+int sph_step_fields(sph_ctx* ctx, int32_t impact, double dt, int32_t nin, const char* const* in_names,
+                    const double* const* ins, int32_t nout, const char* const* out_names, double* const* outs,
+                    double* dt_used);
 int sph_read_mat(sph_ctx* ctx, int32_t impact, int32_t* out);
 int sph_read_fixed(sph_ctx* ctx, int32_t impact, uint8_t* out);
 int sph_write_fixed(sph_ctx* ctx, int32_t impact, const uint8_t* in);

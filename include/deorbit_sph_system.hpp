@@ -190,6 +190,20 @@ struct System {
 
     void step(double dt) {
         need();
+        if (sync && n && dt >= 0) {
+            // push, step and pull in one call whose host copies overlap the step
+            write_fixed_flags();
+            std::vector<std::vector<double>> in, out;
+            std::vector<const double*> ins;
+            std::vector<double*> outs;
+            pack_carried(in, ins);
+            pull_buffers(out, outs);
+            check(sph_step_fields(ctx_, b_, dt, (int32_t)ins.size(), kPushNames, ins.data(), (int32_t)outs.size(),
+                                  kPullNames, outs.data(), nullptr));
+            t += dt;
+            unpack_pulled(out);
+            return;
+        }
         if (sync) push();
         check(sph_step(ctx_, dt));
         t += dt;
@@ -225,16 +239,65 @@ struct System {
     // Copy every field from the device into the mirror (one batched call).
     void pull() {
         need();
-        static const char* names[] = {"x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az",
-                                      "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
-                                      "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz",
-                                      "mass", "rho", "u", "dudt", "P", "cs", "csig", "hh", "eps_work",
-                                      "D", "eps_act", "sigmax", "Pf", "Rart", "dscale"};
-        const int nf = (int)(sizeof(names) / sizeof(names[0]));
-        std::vector<std::vector<double>> buf(nf, std::vector<double>((size_t)n));
-        std::vector<double*> outs(nf);
-        for (int f = 0; f < nf; f++) outs[f] = buf[f].data();
-        if (n) check(sph_read_fields(ctx_, b_, nf, names, outs.data()));
+        std::vector<std::vector<double>> buf;
+        std::vector<double*> outs;
+        pull_buffers(buf, outs);
+        if (n) check(sph_read_fields(ctx_, b_, (int32_t)outs.size(), kPullNames, outs.data()));
+        unpack_pulled(buf);
+    }
+
+    // Copy the carried fields of the mirror to the device (the state a step
+    // reads: positions, velocities, old derivatives, u, h, mass, stress,
+    // damage, flaws, fixed flags), in one batched call.
+    void push() {
+        need();
+        std::vector<std::vector<double>> buf;
+        std::vector<const double*> ins;
+        pack_carried(buf, ins);
+        if (n) check(sph_write_fields(ctx_, b_, (int32_t)ins.size(), kPushNames, ins.data()));
+        write_fixed_flags();
+    }
+
+    sph_ctx* context() const { return ctx_; }
+    int32_t impact() const { return b_; }
+
+private:
+    sph_ctx* ctx_ = nullptr;
+    int32_t b_ = -1;
+
+    static constexpr int kNumPush = 27, kNumPull = 36;
+    static constexpr const char* kPushNames[kNumPush] = {
+        "x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
+        "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz", "mass", "u", "dudt", "hh", "D", "eps_act"};
+    static constexpr const char* kPullNames[kNumPull] = {
+        "x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
+        "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz", "mass", "rho", "u", "dudt", "P", "cs", "csig",
+        "hh", "eps_work", "D", "eps_act", "sigmax", "Pf", "Rart", "dscale"};
+
+    // the mirror's carried fields as kPushNames columns
+    void pack_carried(std::vector<std::vector<double>>& buf, std::vector<const double*>& ins) const {
+        buf.assign(kNumPush, std::vector<double>((size_t)n));
+        for (int i = 0; i < n; i++) {
+            buf[0][i] = pos[i].x; buf[1][i] = pos[i].y; buf[2][i] = pos[i].z;
+            buf[3][i] = vel[i].x; buf[4][i] = vel[i].y; buf[5][i] = vel[i].z;
+            buf[6][i] = acc[i].x; buf[7][i] = acc[i].y; buf[8][i] = acc[i].z;
+            for (int c = 0; c < 6; c++) {
+                buf[9 + c][i] = comp(S[i], c);
+                buf[15 + c][i] = comp(dSdt[i], c);
+            }
+        }
+        const std::vector<double>* scal[] = {&mass, &u, &dudt, &hh, &D, &eps_act};
+        for (int q = 0; q < 6; q++) buf[21 + q] = *scal[q];
+        ins.resize(kNumPush);
+        for (int f = 0; f < kNumPush; f++) ins[f] = buf[f].data();
+    }
+    void pull_buffers(std::vector<std::vector<double>>& buf, std::vector<double*>& outs) const {
+        buf.assign(kNumPull, std::vector<double>((size_t)n));
+        outs.resize(kNumPull);
+        for (int f = 0; f < kNumPull; f++) outs[f] = buf[f].data();
+    }
+    // kPullNames columns into the mirror, then the fixed flags and grid info
+    void unpack_pulled(const std::vector<std::vector<double>>& buf) {
         for (int i = 0; i < n; i++) {
             pos[i] = Vec3(buf[0][i], buf[1][i], buf[2][i]);
             vel[i] = Vec3(buf[3][i], buf[4][i], buf[5][i]);
@@ -255,43 +318,11 @@ struct System {
         for (int a = 0; a < 3; a++) nc[a] = inf.nc[a];
         h_max = inf.h_max;
     }
-
-    // Copy the carried fields of the mirror to the device (the state a step
-    // reads: positions, velocities, old derivatives, u, h, mass, stress,
-    // damage, flaws, fixed flags), in one batched call.
-    void push() {
-        need();
-        static const char* names[] = {"x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az",
-                                      "Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz",
-                                      "dSxx", "dSyy", "dSzz", "dSxy", "dSxz", "dSyz",
-                                      "mass", "u", "dudt", "hh", "D", "eps_act"};
-        const int nf = (int)(sizeof(names) / sizeof(names[0]));
-        std::vector<std::vector<double>> buf(nf, std::vector<double>((size_t)n));
-        for (int i = 0; i < n; i++) {
-            buf[0][i] = pos[i].x; buf[1][i] = pos[i].y; buf[2][i] = pos[i].z;
-            buf[3][i] = vel[i].x; buf[4][i] = vel[i].y; buf[5][i] = vel[i].z;
-            buf[6][i] = acc[i].x; buf[7][i] = acc[i].y; buf[8][i] = acc[i].z;
-            for (int c = 0; c < 6; c++) {
-                buf[9 + c][i] = comp(S[i], c);
-                buf[15 + c][i] = comp(dSdt[i], c);
-            }
-        }
-        const std::vector<double>* scal[] = {&mass, &u, &dudt, &hh, &D, &eps_act};
-        for (int q = 0; q < 6; q++) buf[21 + q] = *scal[q];
-        std::vector<const double*> ins(nf);
-        for (int f = 0; f < nf; f++) ins[f] = buf[f].data();
-        if (n) check(sph_write_fields(ctx_, b_, nf, names, ins.data()));
+    void write_fixed_flags() {
         std::vector<uint8_t> f(n);
         for (int i = 0; i < n; i++) f[i] = fixed[i] ? 1 : 0;
         if (n) check(sph_write_fixed(ctx_, b_, f.data()));
     }
-
-    sph_ctx* context() const { return ctx_; }
-    int32_t impact() const { return b_; }
-
-private:
-    sph_ctx* ctx_ = nullptr;
-    int32_t b_ = -1;
 
     static void check(int rc) {
         if (rc != SPH_OK) throw std::runtime_error(std::string("deorbit_sph: ") + sph_last_error());
@@ -327,6 +358,9 @@ private:
     }
 
     static double& comp(Sym3& s, int c) {
+        return c == 0 ? s.xx : c == 1 ? s.yy : c == 2 ? s.zz : c == 3 ? s.xy : c == 4 ? s.xz : s.yz;
+    }
+    static double comp(const Sym3& s, int c) {
         return c == 0 ? s.xx : c == 1 ? s.yy : c == 2 ? s.zz : c == 3 ? s.xy : c == 4 ? s.xz : s.yz;
     }
 };

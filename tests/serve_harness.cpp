@@ -101,6 +101,11 @@ struct Counting : dsph::EngineBase {
             for (int64_t i = 0; i < imps.at(b).n; i++) outs[f][i] = (double)(b * 1000 + f);
     }
     void write_fields(int, int, const char* const*, const double* const*) override { unused(__func__); }
+    double step_fields(int, double, int, const char* const*, const double* const*, int, const char* const*,
+                       double* const*) override {
+        unused(__func__);
+        return 0;
+    }
     void read_mat(int, int32_t*) override { unused(__func__); }
     void read_fixed(int, uint8_t*) override { unused(__func__); }
     void write_fixed(int, const uint8_t*) override { unused(__func__); }
