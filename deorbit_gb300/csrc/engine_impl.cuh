@@ -851,7 +851,7 @@ public:
     // no work; the parity the graph starts from is restored afterwards.
     cudaGraphExec_t ensure_graph(int kind) {
         const int p = cur_;
-        const int64_t shape = N_ * 65536 + (int64_t)imp_.size();
+        const int64_t shape = N_ * 65536 + (int64_t)imp_.size() + (any_periodic() ? (1ll << 62) : 0);
         cudaGraphExec_t& ge = graph_exec_[kind][p];
         if (ge && graph_key_[kind][p] == layout_epoch_ && graph_n_[kind][p] == shape) return ge;
         const int nimp = (int)imp_.size();
@@ -1605,6 +1605,13 @@ private:
         k_force<R, SE, SS, ASYNC><<<grid, FS::kBlock, FS::kSmemBytes, st_>>>(view(), wait_err_d_);
         launched((const void*)k_force<R, SE, SS, ASYNC>);
     }
+    // Some resident impact has a periodic axis: the pair kernels then take
+    // the minimum-image branches (the choice is part of a captured graph's key).
+    bool any_periodic() const {
+        for (const ImpactH& h : imp_)
+            if (h.used && h.alive && (h.per[0] | h.per[1] | h.per[2])) return true;
+        return false;
+    }
     void launch_force() {
         if (N_ <= 0) return;
         prof_begin();
@@ -1624,9 +1631,12 @@ private:
         if (levels_active_) {  // graded impacts resident: the level-aware pass (never staged)
             k_force<R, 0, 0, false, true><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
             launched((const void*)k_force<R, 0, 0, false, true>);
-        } else if (!done) {
-            k_force<R, 0, 0, false><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
-            launched((const void*)k_force<R, 0, 0, false>);
+        } else if (!done && any_periodic()) {
+            k_force<R, 0, 0, false, false, true><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
+            launched((const void*)k_force<R, 0, 0, false, false, true>);
+        } else if (!done) {  // no resident impact is periodic: pair loop without minimum image
+            k_force<R, 0, 0, false, false, false><<<grid, 128, 0, st_>>>(view(), wait_err_d_);
+            launched((const void*)k_force<R, 0, 0, false, false, false>);
         }
         prof_end();
         launches_++;
@@ -2416,9 +2426,12 @@ public:
         if (levels_active_) {
             k_list_thread<R, true><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
             launched((const void*)k_list_thread<R, true>);
+        } else if (any_periodic()) {
+            k_list_thread<R, false, true><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
+            launched((const void*)k_list_thread<R, false, true>);
         } else {
-            k_list_thread<R><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
-            launched((const void*)k_list_thread<R>);
+            k_list_thread<R, false, false><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, st_>>>(view(), refresh);
+            launched((const void*)k_list_thread<R, false, false>);
         }
         prof_end();
         launches_++;
@@ -2475,7 +2488,8 @@ public:
             cls(KC_DENSITY);
             if (iters > 0) {  // also reduces the new max h
                 if (levels_active_) launch_n_raw(k_density<R, true>, N_, view(), iters);
-                else launch_n_raw(k_density<R>, N_, view(), iters);
+                else if (any_periodic()) launch_n_raw(k_density<R, false, true>, N_, view(), iters);
+                else launch_n_raw(k_density<R, false, false>, N_, view(), iters);
             }
             else hmax_pass(1);
             cls(KC_GRID);

@@ -248,7 +248,9 @@ __device__ __forceinline__ void unpack_cell(uint32_t c, int& cx, int& cy, int& c
 }
 
 // FP32 separation i - j from cell-relative offsets (the "FP64 cell origin +
-// FP32 offset" representation), minimum image on periodic axes.
+// FP32 offset" representation), minimum image on periodic axes.  PER false:
+// the caller knows that no resident impact has a periodic axis.
+template <bool PER = true>
 __device__ __forceinline__ void sep_f32(const ImpactD& I, float4 pi, uint32_t ci, float4 pj,
                                         uint32_t cj, float& dx, float& dy, float& dz) {
     int ix, iy, iz, jx, jy, jz;
@@ -257,22 +259,26 @@ __device__ __forceinline__ void sep_f32(const ImpactD& I, float4 pi, uint32_t ci
     dx = (pi.x - pj.x) + (float)(ix - jx) * I.wf[0];
     dy = (pi.y - pj.y) + (float)(iy - jy) * I.wf[1];
     dz = (pi.z - pj.z) + (float)(iz - jz) * I.wf[2];
-    if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
-    if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
-    if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
+    if constexpr (PER) {
+        if (I.per[0]) dx -= I.Lf[0] * rintf(dx / I.Lf[0]);
+        if (I.per[1]) dy -= I.Lf[1] * rintf(dy / I.Lf[1]);
+        if (I.per[2]) dz -= I.Lf[2] * rintf(dz / I.Lf[2]);
+    }
 }
 
 // Exact FP64 separation and distance in the reference's operation order
 // (sph.hpp:130-136 and vec3.hpp norm): no contraction, IEEE divide and sqrt.
-template <class R>
+template <bool PER = true, class R>
 __device__ __forceinline__ double sep_exact(const View<R>& v, const ImpactD& I, int64_t i, int64_t j,
                                             double& dx, double& dy, double& dz) {
     dx = __dsub_rn(v.x[i], v.x[j]);
     dy = __dsub_rn(v.y[i], v.y[j]);
     dz = __dsub_rn(v.z[i], v.z[j]);
-    if (I.per[0]) { double L = __dsub_rn(I.dhi[0], I.dlo[0]); dx = __dsub_rn(dx, __dmul_rn(L, round(__ddiv_rn(dx, L)))); }
-    if (I.per[1]) { double L = __dsub_rn(I.dhi[1], I.dlo[1]); dy = __dsub_rn(dy, __dmul_rn(L, round(__ddiv_rn(dy, L)))); }
-    if (I.per[2]) { double L = __dsub_rn(I.dhi[2], I.dlo[2]); dz = __dsub_rn(dz, __dmul_rn(L, round(__ddiv_rn(dz, L)))); }
+    if constexpr (PER) {
+        if (I.per[0]) { double L = __dsub_rn(I.dhi[0], I.dlo[0]); dx = __dsub_rn(dx, __dmul_rn(L, round(__ddiv_rn(dx, L)))); }
+        if (I.per[1]) { double L = __dsub_rn(I.dhi[1], I.dlo[1]); dy = __dsub_rn(dy, __dmul_rn(L, round(__ddiv_rn(dy, L)))); }
+        if (I.per[2]) { double L = __dsub_rn(I.dhi[2], I.dlo[2]); dz = __dsub_rn(dz, __dmul_rn(L, round(__ddiv_rn(dz, L)))); }
+    }
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
 }
 
@@ -425,12 +431,14 @@ __device__ __forceinline__ void traverse(const View<R>& v, const ImpactD& I, flo
 // sphere and, per column, only the z-cells within the sphere's chord there
 // (non-periodic impacts; periodic ones use the full box).  Border columns are
 // never pruned by x / y because clamped particles may lie outside their cell.
-template <class R, bool LV = false, class F>
+template <class R, bool LV = false, bool PER = true, class F>
 __device__ __forceinline__ void traverse_sphere(const View<R>& v, const ImpactD& I, float4 pi,
                                                 uint32_t ci, float Rs, F&& f) {
-    if (I.per[0] | I.per[1] | I.per[2]) {
-        traverse(v, I, pi, ci, Rs, f);
-        return;
+    if constexpr (PER) {
+        if (I.per[0] | I.per[1] | I.per[2]) {
+            traverse(v, I, pi, ci, Rs, f);
+            return;
+        }
     }
     if constexpr (LV) {
         if (I.nlev > 1) {
@@ -928,12 +936,12 @@ __device__ __forceinline__ float list_r2(float4 a, float4 b) {
 
 // One particle's list by its own traversal (periodic impacts, and warps that
 // straddle two impacts).
-template <class R, bool LV = false>
+template <class R, bool LV = false, bool PER = true>
 __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int64_t k) {
     const float4 pi = v.pf[k];
     const uint32_t ci = v.cpk[k];
     const float4 li = v.lf[k];
-    const bool periodic = I.per[0] | I.per[1] | I.per[2];
+    const bool periodic = PER && (I.per[0] | I.per[1] | I.per[2]);
     const float m = (sizeof(R) == 8 ? I.margin : 0.0f) + I.lmargin;
     const float sl = 1.0f + I.slack;
     const float ri = 2.0f * pi.w * sl + m;
@@ -941,7 +949,7 @@ __device__ __forceinline__ void list_one(const View<R>& v, const ImpactD& I, int
     int cnt = 0;
     const int cap = v.cap;
     int32_t* out = v.nbr + 4 * k;  // entry t at out[nbr_slot(t, ls)]
-    traverse_sphere<R, LV>(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
+    traverse_sphere<R, LV, PER>(v, I, pi, ci, ri + m, [&](int32_t j, float dxc, float dyc, float dzc) {
         float r2, hj;
         if (!periodic) {
             const float4 lj = v.lf[j];
@@ -1070,7 +1078,7 @@ __device__ __forceinline__ void warp_walk_levels(const View<R>& v, const ImpactD
 //
 // refresh != 0: rebuild only the lists of impacts whose h outgrew the slack in
 // this step's density rounds (the others return at once).
-template <class R, bool LV = false>
+template <class R, bool LV = false, bool PER = true>
 static __global__ void k_list_thread(View<R> v, int refresh) {
     const unsigned full = 0xffffffffu;
     const int64_t k0 = gtid();
@@ -1080,8 +1088,8 @@ static __global__ void k_list_thread(View<R> v, int refresh) {
     const ImpactD& I = v.imps[ib];
     const bool wanted = I.mask && (!refresh || I.slack_flag);
     const bool one_impact = __all_sync(full, ib == __shfl_sync(full, ib, 0));
-    if (!one_impact || (I.per[0] | I.per[1] | I.per[2])) {
-        if (inb && wanted) list_one<R, LV>(v, I, k);
+    if (!one_impact || (PER && (I.per[0] | I.per[1] | I.per[2]))) {
+        if (inb && wanted) list_one<R, LV, PER>(v, I, k);
         return;
     }
     if (!wanted) return;  // warp-uniform: one impact
@@ -1549,7 +1557,7 @@ __device__ __forceinline__ bool list_covers(const View<R>& v, const ImpactD& I, 
 // compensated sum in the mixed form.  An iteration reads only the particle's
 // own h and the neighbours' positions and masses, so running the iterations
 // back to back per particle gives the same result as one launch per iteration.
-template <class R, bool LV = false>
+template <class R, bool LV = false, bool PER = true>
 static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_density(View<R> v, int iters) {
     int64_t k = gtid();
     if (k >= v.n) return;
@@ -1572,7 +1580,7 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_density(
         // mixed form: one entry's m_j W(r, h_i) from its offset record and (mass, cell)
         auto w_mixed = [&](int32_t j, float4 pj, float2 mk) -> float {
             float dx, dy, dz;
-            sep_f32(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
+            sep_f32<PER>(I, pi, ci, pj, __float_as_uint(mk.y), dx, dy, dz);
             const float r2 = dx * dx + dy * dy + dz * dz;
             // the kernel vanishes at q >= 2; only the stencil restriction needs a test
             const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;  // hardware 1/sqrt (2 ulp)
@@ -1583,10 +1591,10 @@ static __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_density(
         auto body = [&](int32_t j) {
             if constexpr (sizeof(R) == 8) {
                 float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
-                sep_f32(I, pi, ci, v.pf[j], v.cpk[j], fx, fy, fz);
+                sep_f32<PER>(I, pi, ci, v.pf[j], v.cpk[j], fx, fy, fz);
                 if (!(fx * fx + fy * fy + fz * fz < th2)) return;
                 double dx, dy, dz;
-                double rr = sep_exact(v, I, k, j, dx, dy, dz);
+                double rr = sep_exact<PER>(v, I, k, j, dx, dy, dz);
                 if (!(rr < 2.0 * (double)hi)) return;
                 if (need_member && !ref_member(bi, v.refbin[j], I)) return;
                 sum.add(v.mass[j] * kernel_W_ih<R>((R)rr, ihi));
@@ -1732,7 +1740,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // ASYNC selects the copy engine of the staging: false = one bulk copy per
 // entry (cp.async.bulk, TMA), true = six 16-byte cp.async per entry (the load
 // path through L1, completion tracked by cp.async.mbarrier.arrive).
-template <class R, int SE = 0, int SS = 0, bool ASYNC = false, bool LV = false>
+template <class R, int SE = 0, int SS = 0, bool ASYNC = false, bool LV = false, bool PER = true>
 static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(View<R> v, int32_t* wait_err) {
     using Acc = AccT<R>;
     constexpr bool kStaged = SS > 0 && sizeof(R) == 4;
@@ -1821,7 +1829,7 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
                         const float4 fb, const float4 fc) {
         const float mj = vhj.w;  // (mass, packed cell) ride in the .w lanes
         float dx, dy, dz;
-        sep_f32(I, pi, ci, pj, __float_as_uint(vlj.w), dx, dy, dz);
+        sep_f32<PER>(I, pi, ci, pj, __float_as_uint(vlj.w), dx, dy, dz);
         const float r2 = dx * dx + dy * dy + dz * dz;
         const float hif = (float)hi;
         const float hs = hif + pj.w;
@@ -1888,12 +1896,12 @@ static __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_force(Vi
             if (j == (int32_t)k) return;
             const float4 pjf = v.pf[j];
             float fx, fy, fz;  // FP32 pre-filter: skip entries that clearly fail
-            sep_f32(I, pi, ci, pjf, v.cpk[j], fx, fy, fz);
+            sep_f32<PER>(I, pi, ci, pjf, v.cpk[j], fx, fy, fz);
             const float lim = pi.w + pjf.w + hs_pad;
             if (!(fx * fx + fy * fy + fz * fz < lim * lim)) return;
             const R hj = v.hh[j];
             double dx, dy, dz;
-            double rr = sep_exact(v, I, k, j, dx, dy, dz);
+            double rr = sep_exact<PER>(v, I, k, j, dx, dy, dz);
             double hsum = __dadd_rn((double)hi, (double)hj);
             if (rr >= hsum || rr == 0.0) return;
             if (need_member && !ref_member(v.refbin[k], v.refbin[j], I)) return;
