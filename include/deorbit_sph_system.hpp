@@ -12,7 +12,9 @@
 // the device state.  With `sync` true (the default) every device call pushes
 // the mirror's carried fields to the device first and pulls every field back
 // afterwards, so a driver may read or modify any vector between calls exactly
-// as with the CPU solver (run_ic.cpp:36-38 writes D, eps_act and S after add()).
+// as with the CPU solver (run_ic.cpp:36-38 writes D, eps_act and S after add());
+// step(dt) does the push, the step and the pull in one sph_step_fields call,
+// whose host copies overlap the step's kernels.
 // A driver that only reads occasionally sets `sync = false` and calls pull()
 // when it needs the fields (and push() after changing them); run(nsteps) is the
 // batched device loop with each step's CFL dt taken on the device.
