@@ -102,3 +102,26 @@ def test_device_path_fails_loudly_without_gpu(cuda_lib):
     with pytest.raises(sph.SphError) as e:
         sph.Context(sph.FP64)
     assert e.value.code == -2
+
+
+def test_step_fields_rejects_bad_arguments_before_device_work(cuda_lib):
+    """sph_step_fields checks its arguments before it touches a device: a
+    non-finite dt, negative counts, missing name or buffer arrays and a null
+    context each return SPH_ERR_ARG with a message."""
+    from deorbit_gb300 import sph
+    L = sph.lib()
+    names = (C.c_char_p * 1)(b"x")
+    buf = np.zeros(4)
+    ptrs = (C.POINTER(C.c_double) * 1)(buf.ctypes.data_as(C.POINTER(C.c_double)))
+    cases = [
+        (float("inf"), 1, names, ptrs, 1, names, ptrs, b"dt"),
+        (float("nan"), 1, names, ptrs, 1, names, ptrs, b"dt"),
+        (-1.0, -1, names, ptrs, 1, names, ptrs, b"nin"),
+        (-1.0, 1, names, ptrs, -2, names, ptrs, b"nout"),
+        (-1.0, 1, None, ptrs, 1, names, ptrs, b"in_names"),
+        (-1.0, 1, names, ptrs, 1, names, None, b"outs"),
+        (0.5, 1, names, ptrs, 1, names, ptrs, b"null context"),
+    ]
+    for dt, nin, inn, ins, nout, outn, outs, msg in cases:
+        rc = L.sph_step_fields(None, 0, dt, nin, inn, ins, nout, outn, outs, None)
+        assert rc == -1 and msg in L.sph_last_error(), (dt, nin, nout, L.sph_last_error())
