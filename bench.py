@@ -13,7 +13,9 @@ value   particle-steps/s of the mixed form (FP32 pairs / EOS / stress, FP64
         engine stream around exactly K steps.
 e2e     the same metric through the C ABI with host buffers: every step
         writes the carried state from pinned host memory, steps, and reads it
-        back (a drop-in caller that keeps System's vectors on the host).
+        back (a drop-in caller that keeps System's vectors on the host), as
+        one sph_step_fields call per step; e2e.separate_calls times the same
+        steps as sph_write_fields + sph_timestep + sph_step + sph_read_fields.
 plain_fp64  the FP64 plain form on the same workload (the 4x comparison).
 accuracy_vs_oracle  both GPU forms against the FP64 CPU oracle on a bounded
         sample of the workload (per-field rel-L2, pass / fail at 1e-4).
