@@ -1158,14 +1158,15 @@ public:
             std::string nm(in_names[f]);
             if (nm == "x" || nm == "y" || nm == "z" || nm == "hh") grid_valid_ = false;
         }
-        for (int f : late)
-            DSPH_CUDA(cudaMemcpyAsync(in_slice(f), ins[f], sizeof(double) * n, cudaMemcpyHostToDevice, copy_st_));
-        DSPH_CUDA(cudaEventRecord(late_ev_, copy_st_));
-        // every input is read before any output is written, so the caller's
-        // input and output buffers may be the same memory
-        DSPH_CUDA(cudaStreamWaitEvent(out_st_, late_ev_, 0));
         for (int f = 0; f < nout; f++) (is_head_final(out_names[f]) ? head_out : tail_out).push_back(f);
+        // Host calls are ordered so that every copy is issued after the kernels
+        // it should overlap are queued: from pageable memory a copy holds the
+        // calling thread until it is done, from page-locked memory it does not.
         const std::function<void()> between = [&]() {
+            for (int f : late)
+                DSPH_CUDA(cudaMemcpyAsync(in_slice(f), ins[f], sizeof(double) * n, cudaMemcpyHostToDevice,
+                                          copy_st_));
+            DSPH_CUDA(cudaEventRecord(late_ev_, copy_st_));
             if (!late.empty()) {
                 DSPH_CUDA(cudaStreamWaitEvent(st_, late_ev_, 0));
                 cols_io(true, late);
@@ -1173,10 +1174,6 @@ public:
             if (!head_out.empty()) {
                 cols_io(false, head_out);
                 DSPH_CUDA(cudaEventRecord(out_ev_, st_));
-                DSPH_CUDA(cudaStreamWaitEvent(out_st_, out_ev_, 0));
-                for (int f : head_out)
-                    DSPH_CUDA(cudaMemcpyAsync(outs[f], out_slice(f), sizeof(double) * n, cudaMemcpyDeviceToHost,
-                                              out_st_));
             }
         };
         if (use_graphs_ && !profiling_) {
@@ -1189,6 +1186,15 @@ public:
             launches_ += graph_launches_[kGraphTail][cur_];
         } else {
             one_step(false, &between);
+        }
+        // every input is read before any output is written, so the caller's
+        // input and output buffers may be the same memory
+        DSPH_CUDA(cudaStreamWaitEvent(out_st_, late_ev_, 0));
+        if (!head_out.empty()) {
+            DSPH_CUDA(cudaStreamWaitEvent(out_st_, out_ev_, 0));
+            for (int f : head_out)
+                DSPH_CUDA(cudaMemcpyAsync(outs[f], out_slice(f), sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                          out_st_));
         }
         // tail outputs: each field's gather, then its copy while the next gathers
         for (int f : tail_out) {
